@@ -1,0 +1,174 @@
+// ref_harness.cpp -- drives the reference's own RayMarcher (Oracle A).
+//
+// TEST INFRASTRUCTURE ONLY.  Linked with the reference translation units
+// src/app/AdvancedRenderer/RayMarcher.cpp, src/app/Kernel.cpp,
+// src/app/ThreadPool.cpp and src/app/Dataset.cpp, compiled unmodified from the
+// reference tree against the stand-in headers in oracle/shim.  The result is
+// oracle/_ref/libfmref.so, which the tests load with ctypes to pin the CPU
+// restatement (fm_oracle.cpp) and to write golden vectors.
+//
+// The march is driven the way AdvancedRenderer::Render does it
+// (AdvancedRenderer.cpp:257-275): Prepare -> Start, then wait until the pool
+// reports done and join the workers with Exit() (ThreadPool.cpp:33-36 reports
+// done while a worker may still be writing its last pixel; Exit waits for it).
+// Pixel W*H-1 is never marched by the reference (ThreadPool.cpp:50); the
+// output buffers are zeroed first so that pixel reads as a miss.
+
+#include <engine/hzpch.h>
+
+#include "app/AdvancedRenderer/RayMarcher.h"
+#include "app/Dataset.h"
+
+#include <engine/renderer/Renderer.h>
+
+#include <chrono>
+#include <cstring>
+
+FmShimVulkan Vulkan;
+int fm_shim_box_mode = 0;
+
+float RandomFloat(float min, float max) { return min + (max - min) * 0.5f; }
+
+CameraController3D::CameraController3D(Camera3D& camera) : Camera(camera) {}
+
+namespace Partio
+{
+ParticlesDataMutable* read(const char*, bool, std::ostream&) { return nullptr; }
+}
+
+namespace
+{
+glm::mat4 MatFrom(const float* m)
+{
+    glm::mat4 r;
+    for (int c = 0; c < 4; ++c)
+        for (int k = 0; k < 4; ++k) r[c][k] = m[c * 4 + k];
+    return r;
+}
+}  // namespace
+
+extern "C" {
+
+// Build the reference Frame (search, AABB, density grid) for the particles.
+// Writes the sorted particle order (xyz, stride 3) when sorted_out is given
+// and the grid origin/dims when grid_out (min[3], cellwidth, dims[3] as float).
+// Then marches the whole W x H image with the reference's isotropic marcher.
+// box_mode: 0 = every skip flag true (skip off), 1 = own-cell counts.
+// Returns the wall time of Prepare -> Start -> Exit in seconds, or < 0 on error.
+double ref_march(const float* xyz, int64_t n, float radius, const float* inv_proj_view, const float* cam_pos,
+                 int32_t width, int32_t height, const float* depth_in, int32_t max_steps, float step_size,
+                 float iso, int32_t box_mode, float* out_pos, float* out_nrm, float* sorted_out, float* grid_out,
+                 double* build_seconds)
+{
+    if (n <= 0 || width <= 0 || height <= 0) return -1.0;
+    fm_shim_box_mode = box_mode;
+    Vulkan.SwapchainExtent.width = uint32_t(width);
+    Vulkan.SwapchainExtent.height = uint32_t(height);
+
+    auto t0 = std::chrono::steady_clock::now();
+    Dataset* ds = new Dataset();
+    ds->ParticleRadius = radius;
+    ds->ParticleRadiusExt = 2.0f * radius;
+    ds->ParticleRadiusInv = 1.0f / radius;
+    ds->ParticleRadiusExtInv = 1.0f / ds->ParticleRadiusExt;
+    ds->m_IsotropicKernel = CubicSplineKernel(radius);
+    ds->m_AnisotropicKernel = AnisotropicKernel(radius);
+    std::vector<Particle> particles(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) particles[i] = Particle(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+    ds->Frames.reserve(1);
+    ds->Frames.emplace_back(ds, particles, ds->ParticleRadius, ds->ParticleRadiusExt);
+    ds->MaxParticles = size_t(n);
+    ds->Loaded = true;
+    auto t1 = std::chrono::steady_clock::now();
+    if (build_seconds) *build_seconds = std::chrono::duration<double>(t1 - t0).count();
+
+    Frame& fr = ds->Frames[0];
+    if (sorted_out)
+        for (int64_t i = 0; i < n; ++i)
+        {
+            sorted_out[3 * i] = fr.m_Particles[i].x;
+            sorted_out[3 * i + 1] = fr.m_Particles[i].y;
+            sorted_out[3 * i + 2] = fr.m_Particles[i].z;
+        }
+    if (grid_out)
+    {
+        grid_out[0] = fr.m_Min.x; grid_out[1] = fr.m_Min.y; grid_out[2] = fr.m_Min.z;
+        grid_out[3] = fr.m_DensityGrid.m_CellWidth;
+        grid_out[4] = float(fr.m_DensityGrid.m_Width);
+        grid_out[5] = float(fr.m_DensityGrid.m_Height);
+        grid_out[6] = float(fr.m_DensityGrid.m_Depth);
+    }
+
+    Camera3D cam;
+    cam.InvProjectionView = MatFrom(inv_proj_view);
+    CameraController3D ctl(cam);
+    ctl.Position = glm::vec3(cam_pos[0], cam_pos[1], cam_pos[2]);
+
+    VisualizationSettings s{};
+    s.Frame = 0;
+    s.MaxSteps = max_steps;
+    s.StepSize = step_size;
+    s.IsoDensity = iso;
+    s.EnableAnisotropy = false;
+    s.k_n = 0.5f; s.k_r = 2.0f; s.k_s = 2000.0f; s.N_eps = 1;
+
+    const size_t npx = size_t(width) * size_t(height);
+    std::vector<glm::vec4> pos(npx, glm::vec4(0)), nrm(npx, glm::vec4(0));
+    std::vector<float> depth(depth_in, depth_in + npx);
+
+    auto t2 = std::chrono::steady_clock::now();
+    RayMarcher* rm = new RayMarcher();
+    rm->Prepare(s, ctl, ds, pos.data(), nrm.data(), depth.data());
+    rm->Start();
+    while (!rm->IsDone()) std::this_thread::sleep_for(std::chrono::microseconds(200));
+    rm->Exit();
+    auto t3 = std::chrono::steady_clock::now();
+
+    std::memcpy(out_pos, pos.data(), npx * sizeof(glm::vec4));
+    std::memcpy(out_nrm, nrm.data(), npx * sizeof(glm::vec4));
+    delete rm;
+    delete ds;
+    return std::chrono::duration<double>(t3 - t2).count();
+}
+
+// The reference kernel values (Kernel.cpp:16-52) for known-answer tests.
+float ref_W(float h, float rx, float ry, float rz)
+{
+    CubicSplineKernel k(h);
+    return k.W(glm::vec3(rx, ry, rz));
+}
+
+void ref_gradW(float h, float rx, float ry, float rz, float* out3)
+{
+    CubicSplineKernel k(h);
+    glm::vec3 g = k.gradW(glm::vec3(rx, ry, rz));
+    out3[0] = g.x; out3[1] = g.y; out3[2] = g.z;
+}
+
+// Frame::QueryDensityGrid (Dataset.cpp:26-47) on a built frame: linear cell
+// index of each query point (-1 when outside the grid).
+int ref_query_cells(const float* xyz, int64_t n, float radius, const float* queries, int64_t nq, int64_t* out)
+{
+    fm_shim_box_mode = 0;
+    Dataset* ds = new Dataset();
+    ds->ParticleRadius = radius;
+    ds->ParticleRadiusExt = 2.0f * radius;
+    ds->ParticleRadiusInv = 1.0f / radius;
+    ds->ParticleRadiusExtInv = 1.0f / ds->ParticleRadiusExt;
+    ds->m_IsotropicKernel = CubicSplineKernel(radius);
+    ds->m_AnisotropicKernel = AnisotropicKernel(radius);
+    std::vector<Particle> particles(static_cast<size_t>(n));
+    for (int64_t i = 0; i < n; ++i) particles[i] = Particle(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+    ds->Frames.reserve(1);
+    ds->Frames.emplace_back(ds, particles, ds->ParticleRadius, ds->ParticleRadiusExt);
+    Frame& fr = ds->Frames[0];
+    for (int64_t i = 0; i < nq; ++i)
+    {
+        OctreeNode* node = fr.QueryDensityGrid(glm::vec3(queries[3 * i], queries[3 * i + 1], queries[3 * i + 2]));
+        out[i] = node ? int64_t(node - fr.m_DensityGrid.m_Nodes.data()) : -1;
+    }
+    delete ds;
+    return 0;
+}
+
+}  // extern "C"
