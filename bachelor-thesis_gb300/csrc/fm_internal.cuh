@@ -1,0 +1,184 @@
+// fm_internal.cuh -- shared device structures and exact FP32 helpers.
+//
+// Every translation unit of libfluidmarch is compiled with --fmad=false, so a
+// plain expression `a * b + c` is two separately rounded operations, exactly
+// as the reference's /fp:precise build and glm 0.9.9 evaluate it.  That makes
+// the cell index, the march samples, the kernel sums and the shading
+// bit-identical to the reference formulas for the same summation order.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/fluidmarch.h"
+
+namespace fm {
+
+constexpr int kWarp = 32;
+
+// Uniform grid of a scene (Frame::m_Min, DensityGrid; Dataset.cpp:78-104).
+struct GridDev {
+    float min[3];
+    float inv;   // 1.0f / cell
+    float cell;  // cell width = support radius
+    int dims[3];
+    const float4* __restrict__ pts;       // cell-sorted particles (w = 0)
+    const uint32_t* __restrict__ start;   // n_cells + 1
+    const float* __restrict__ bound;      // per-cell density upper bound (FM_SKIP_EXACT) or null
+    const uint8_t* __restrict__ flag;     // per-cell reference skip flag (FM_SKIP_REFERENCE) or null
+};
+
+// Cubic spline constants, Kernel.cpp:8-14 (h = support radius).
+struct KernelDev {
+    float h, h2, hinv, sig;
+};
+
+// Host: constants evaluated in FP32 in the reference's order.
+inline KernelDev make_kernel(float h) {
+    KernelDev k;
+    k.h = h;
+    k.h2 = h * h;
+    k.hinv = 1.0f / h;
+    const float pi = 3.14159265358979323846f;
+    k.sig = 8.0f / (((pi * h) * h) * h);
+    return k;
+}
+
+// glm dot for vec3: (x*x' + y*y') + z*z'
+__device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, float by, float bz) {
+    return (ax * bx + ay * by) + az * bz;
+}
+
+// CubicSplineKernel::W for q2 = dot(r, r) < h2 (Kernel.cpp:16-32).
+__device__ __forceinline__ float w_in(const KernelDev& k, float q2) {
+    float q = sqrtf(q2) * k.hinv;
+    if (q >= 0.5f) {
+        float q_ = 1.0f - q;
+        return k.sig * (((2.0f * q_) * q_) * q_);
+    }
+    return k.sig * (6.0f * (((q * q) * q) - (q * q)) + 1.0f);
+}
+
+// CubicSplineKernel::gradW for 0 < rn < h2 (Kernel.cpp:34-52), accumulated
+// into g with glm's component order.
+__device__ __forceinline__ void gradw_acc(const KernelDev& k, float rx, float ry, float rz, float rn, float& gx,
+                                          float& gy, float& gz) {
+    float rl = sqrtf(rn);
+    float q = rl * k.hinv;
+    float inv = 1.0f / sqrtf(rn);  // normalize(r) = r * inversesqrt(dot(r, r))
+    float den = rl * k.h;
+    float nx = (rx * inv) / den, ny = (ry * inv) / den, nz = (rz * inv) / den;
+    float ax, ay, az, s;
+    if (q >= 0.5f) {
+        float q_ = 1.0f - q;
+        s = (6.0f * q_) * q_;
+        float ns = -k.sig;
+        ax = ns * nx; ay = ns * ny; az = ns * nz;
+    } else {
+        s = 6.0f * (((3.0f * q) * q) - (2.0f * q));
+        ax = k.sig * nx; ay = k.sig * ny; az = k.sig * nz;
+    }
+    gx = gx + ax * s;
+    gy = gy + ay * s;
+    gz = gz + az * s;
+}
+
+// Sample -> cell (QueryDensityGrid formula, Dataset.cpp:28-33).  false when
+// the sample is so far outside that its 27 neighbourhood misses the grid, or
+// non-finite.
+__device__ __forceinline__ bool sample_cell(const GridDev& g, float px, float py, float pz, int& cx, int& cy,
+                                            int& cz) {
+    float fx = floorf((px - g.min[0]) * g.inv);
+    float fy = floorf((py - g.min[1]) * g.inv);
+    float fz = floorf((pz - g.min[2]) * g.inv);
+    if (!(fx >= -2.0f && fx <= (float)g.dims[0] + 1.0f)) return false;
+    if (!(fy >= -2.0f && fy <= (float)g.dims[1] + 1.0f)) return false;
+    if (!(fz >= -2.0f && fz <= (float)g.dims[2] + 1.0f)) return false;
+    cx = (int)fx;
+    cy = (int)fy;
+    cz = (int)fz;
+    return true;
+}
+
+// ---- host-side objects ------------------------------------------------------
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+}  // namespace fm
+
+struct fm_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    int sm_count = 0;
+    // staging buffers for host in/outputs (grown on demand)
+    fm::DevBuf stage[6];
+    // device status word + stats accumulators
+    unsigned int* d_status = nullptr;
+    unsigned long long* d_stats = nullptr;  // 8 counters
+    int stats_enabled = 0;
+    fm_march_stats last_stats{};
+    // scratch for grid builds
+    fm::DevBuf scratch[8];
+    void* h_pinned_small = nullptr;  // 256 bytes of pinned memory for small readbacks
+};
+
+struct fm_scene {
+    fm_ctx* ctx = nullptr;
+    uint64_t n = 0;
+    uint64_t capacity = 0;
+    float support = 0.0f;
+    float min[3], max[3];
+    float inv = 0.0f;
+    int dims[3] = {0, 0, 0};
+    uint64_t ncells = 0;
+    uint64_t cell_capacity = 0;
+    float4* d_pts = nullptr;       // cell-sorted
+    uint32_t* d_cell = nullptr;    // cell of each input particle
+    uint32_t* d_perm = nullptr;    // input index of each sorted particle
+    uint32_t* d_start = nullptr;   // ncells + 1
+    float* d_bound = nullptr;      // per-cell density bound (lazy)
+    uint8_t* d_flag = nullptr;     // per-cell reference flag (lazy)
+    bool bound_valid = false;
+    bool flag_valid = false;
+};
+
+namespace fm {
+
+// Grid build (grid_build.cu).  Returns FM_* status, message in ctx->err.
+int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride);
+// Lazily built skip tables, launched on `st` (valid for every later launch
+// on that stream; other streams must order after it).
+int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
+int ensure_flags(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
+GridDev grid_dev(const fm_scene* s);
+
+// Splat (splat.cu): depth must be a device buffer of W*H floats.
+int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_depth, cudaStream_t st);
+
+// March (march.cu): all pointers device pointers.
+struct MarchOutDev {
+    float4* pos;
+    float4* nrm;
+    float* depth;
+    float4* col;
+    const float* start_depth;
+};
+int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
+                 const MarchOutDev& o, cudaStream_t st);
+
+int set_err(fm_ctx* ctx, int code, const std::string& msg);
+int cuda_err(fm_ctx* ctx, cudaError_t e, const char* what);
+
+}  // namespace fm
+
+#define FM_CUDA(ctx, call)                                  \
+    do {                                                    \
+        cudaError_t _e = (call);                            \
+        if (_e != cudaSuccess) return fm::cuda_err((ctx), _e, #call); \
+    } while (0)

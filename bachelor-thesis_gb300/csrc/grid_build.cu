@@ -1,0 +1,493 @@
+// grid_build.cu -- GPU uniform-grid build of a particle frame.
+//
+// Replaces Frame::BuildSearch / ComputeAABB / BuildDensityGrid
+// (src/app/Dataset.cpp:49-165) and the cell table inside the CompactNSearch
+// library the reference calls.  Integer results are bit-identical to the
+// reference formulas:
+//   AABB            min/max over all particles, padded by the support radius
+//                   (Dataset.cpp:78-92); min/max is exact, the padding is one
+//                   FP32 add/sub done on the host exactly as the reference does.
+//   dims            ceil((max - min) / cell) (Dataset.cpp:102-104).
+//   cell index      floor((p - min) * (1/cell)), x + y*W + z*W*H
+//                   (QueryDensityGrid, Dataset.cpp:28-40).
+//   order           stable counting sort by cell (an LSD radix sort of the
+//                   cell key, 8 bits per pass, input index as the value), so
+//                   particles of a cell keep their input order.
+//   cell table      start[c] = exclusive prefix sum of the cell counts.
+// Data layout in HBM: float4 cell-sorted positions (16 B, one coalesced
+// 128-bit load per particle), uint32 cell start table (n_cells + 1), uint32
+// cell and sorted->input index arrays.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "fm_internal.cuh"
+
+namespace fm {
+namespace {
+
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kScanTile = kScanThreads * kScanItems;
+
+constexpr int kSortThreads = 256;
+constexpr int kSortItems = 8;
+constexpr int kSortTile = kSortThreads * kSortItems;
+constexpr int kSortWarps = kSortThreads / kWarp;
+
+__device__ __forceinline__ uint32_t f2ord(float f) {
+    uint32_t b = __float_as_uint(f);
+    return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__host__ __device__ inline float ord2f(uint32_t k) {
+    uint32_t b = (k & 0x80000000u) ? (k & 0x7fffffffu) : ~k;
+    float f;
+    std::memcpy(&f, &b, 4);
+    return f;
+}
+
+// mm[0..2] = ordered min, mm[3..5] = ordered max, mm[6] = count of non-finite coordinates.
+__global__ void k_aabb(const float* __restrict__ xyz, uint64_t n, uint32_t stride, uint32_t* __restrict__ mm) {
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    uint32_t bad = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+        const float* p = xyz + i * stride;
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            float v = p[a];
+            if (!isfinite(v)) { bad++; continue; }
+            mn[a] = fminf(mn[a], v);
+            mx[a] = fmaxf(mx[a], v);
+        }
+    }
+    __shared__ uint32_t s[7][32];
+    uint32_t k[7];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { k[a] = f2ord(mn[a]); k[3 + a] = f2ord(mx[a]); }
+    k[6] = bad;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            k[a] = min(k[a], __shfl_xor_sync(0xffffffffu, k[a], o));
+            k[3 + a] = max(k[3 + a], __shfl_xor_sync(0xffffffffu, k[3 + a], o));
+        }
+        k[6] += __shfl_xor_sync(0xffffffffu, k[6], o);
+    }
+    int w = threadIdx.x / kWarp, l = threadIdx.x % kWarp;
+    if (l == 0)
+        for (int a = 0; a < 7; ++a) s[a][w] = k[a];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int nw = blockDim.x / kWarp;
+        for (int j = 1; j < nw; ++j) {
+            for (int a = 0; a < 3; ++a) {
+                k[a] = min(k[a], s[a][j]);
+                k[3 + a] = max(k[3 + a], s[3 + a][j]);
+            }
+            k[6] += s[6][j];
+        }
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(&mm[a], k[a]);
+            atomicMax(&mm[3 + a], k[3 + a]);
+        }
+        if (k[6]) atomicAdd(&mm[6], k[6]);
+    }
+}
+
+struct GridParams {
+    float min[3];
+    float inv;
+    int dims[3];
+};
+
+// Per-particle cell (QueryDensityGrid formula; coordinates clamped into the
+// grid, which the support-radius padding guarantees for finite input) and
+// the cell histogram.
+__global__ void k_cells(const float* __restrict__ xyz, uint64_t n, uint32_t stride, GridParams g,
+                        uint32_t* __restrict__ cell, uint32_t* __restrict__ count) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = xyz + i * stride;
+    int c[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float f = floorf((p[a] - g.min[a]) * g.inv);
+        int v = (int)f;
+        c[a] = min(max(v, 0), g.dims[a] - 1);
+    }
+    uint32_t lin = (uint32_t)c[0] + (uint32_t)c[1] * (uint32_t)g.dims[0] +
+                   (uint32_t)c[2] * (uint32_t)g.dims[0] * (uint32_t)g.dims[1];
+    cell[i] = lin;
+    atomicAdd(&count[lin], 1u);
+}
+
+// ---- exclusive scan (uint32), multi-level ---------------------------------
+// in and out may alias (in-place scan): each thread reads its items before any write.
+__global__ void k_scan_tile(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* __restrict__ tile_sums) {
+    __shared__ uint32_t s_warp[kScanThreads / kWarp];
+    uint64_t base = (uint64_t)blockIdx.x * kScanTile + (uint64_t)threadIdx.x * kScanItems;
+    uint32_t v[kScanItems];
+    uint32_t sum = 0;
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+        v[j] = (base + j < n) ? in[base + j] : 0u;
+        sum += v[j];
+    }
+    int l = threadIdx.x % kWarp, w = threadIdx.x / kWarp;
+    uint32_t inc = sum;
+#pragma unroll
+    for (int o = 1; o < kWarp; o <<= 1) {
+        uint32_t t = __shfl_up_sync(0xffffffffu, inc, o);
+        if (l >= o) inc += t;
+    }
+    if (l == kWarp - 1) s_warp[w] = inc;
+    __syncthreads();
+    if (w == 0) {
+        uint32_t x = s_warp[l];
+#pragma unroll
+        for (int o = 1; o < kWarp; o <<= 1) {
+            uint32_t t = __shfl_up_sync(0xffffffffu, x, o);
+            if (l >= o) x += t;
+        }
+        s_warp[l] = x;  // inclusive over warps
+    }
+    __syncthreads();
+    uint32_t run = (inc - sum) + (w > 0 ? s_warp[w - 1] : 0u);
+#pragma unroll
+    for (int j = 0; j < kScanItems; ++j) {
+        if (base + j < n) out[base + j] = run;
+        run += v[j];
+    }
+    if (threadIdx.x == kScanThreads - 1 && tile_sums) tile_sums[blockIdx.x] = s_warp[kScanThreads / kWarp - 1];
+}
+
+__global__ void k_scan_add(uint32_t* __restrict__ out, uint64_t n, const uint32_t* __restrict__ tile_offsets) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    out[i] += tile_offsets[i / kScanTile];
+}
+
+// out[i] = sum_{j<i} in[i]; in may equal out.  tmp needs scan_tmp_words(n).
+uint64_t scan_tmp_words(uint64_t n) {
+    uint64_t w = 0;
+    while (n > (uint64_t)kScanTile) {
+        n = (n + kScanTile - 1) / kScanTile;
+        w += 2 * n + 64;
+    }
+    return w + 64;
+}
+
+void exclusive_scan(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* tmp, cudaStream_t st) {
+    uint64_t tiles = (n + kScanTile - 1) / kScanTile;
+    if (tiles <= 1) {
+        k_scan_tile<<<1, kScanThreads, 0, st>>>(in, out, n, nullptr);
+        return;
+    }
+    uint32_t* sums = tmp;
+    uint32_t* offs = tmp + tiles + 32;
+    k_scan_tile<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, out, n, sums);
+    exclusive_scan(sums, offs, tiles, offs + tiles + 32, st);
+    k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, offs);
+}
+
+// ---- stable LSD radix sort pass (8-bit digit) -----------------------------
+__global__ void k_radix_hist(const uint32_t* __restrict__ keys, uint64_t n, int shift, uint32_t nblocks,
+                             uint32_t* __restrict__ hist) {
+    __shared__ uint32_t h[256];
+    h[threadIdx.x] = 0;
+    __syncthreads();
+    uint64_t base = (uint64_t)blockIdx.x * kSortTile;
+#pragma unroll
+    for (int it = 0; it < kSortItems; ++it) {
+        uint64_t e = base + (uint64_t)it * kSortThreads + threadIdx.x;
+        if (e < n) atomicAdd(&h[(keys[e] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
+}
+
+// vals_in == nullptr: the value is the element index (first pass).
+__global__ void k_radix_scatter(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
+                                uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint64_t n,
+                                int shift, uint32_t nblocks, const uint32_t* __restrict__ offs) {
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_tot[256];
+    __shared__ uint32_t s_w[kSortWarps][256];
+    const int t = threadIdx.x, l = t % kWarp, w = t / kWarp;
+    s_base[t] = offs[(uint64_t)t * nblocks + blockIdx.x];
+#pragma unroll
+    for (int j = 0; j < kSortWarps; ++j) s_w[j][t] = 0;
+    __syncthreads();
+    const uint32_t lt = (1u << l) - 1u;
+    uint64_t base = (uint64_t)blockIdx.x * kSortTile;
+    for (int it = 0; it < kSortItems; ++it) {
+        uint64_t e = base + (uint64_t)it * kSortThreads + t;
+        bool valid = e < n;
+        uint32_t key = valid ? keys_in[e] : 0u;
+        uint32_t val = valid ? (vals_in ? vals_in[e] : (uint32_t)e) : 0u;
+        uint32_t d = valid ? ((key >> shift) & 255u) : (0x10000u + l);
+        uint32_t peers = __match_any_sync(0xffffffffu, d);
+        uint32_t rank = __popc(peers & lt);
+        if (valid && rank == 0) s_w[w][d] = __popc(peers);
+        __syncthreads();
+        {
+            uint32_t run = 0;
+#pragma unroll
+            for (int j = 0; j < kSortWarps; ++j) {
+                uint32_t c = s_w[j][t];
+                s_w[j][t] = run;
+                run += c;
+            }
+            s_tot[t] = run;
+        }
+        __syncthreads();
+        if (valid) {
+            uint32_t pos = s_base[d] + s_w[w][d] + rank;
+            keys_out[pos] = key;
+            vals_out[pos] = val;
+        }
+        __syncthreads();
+        s_base[t] += s_tot[t];
+#pragma unroll
+        for (int j = 0; j < kSortWarps; ++j) s_w[j][t] = 0;
+        __syncthreads();
+    }
+}
+
+__global__ void k_gather(const float* __restrict__ xyz, uint64_t n, uint32_t stride, const uint32_t* __restrict__ perm,
+                         float4* __restrict__ out) {
+    uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const float* p = xyz + (uint64_t)perm[k] * stride;
+    out[k] = make_float4(p[0], p[1], p[2], 0.0f);
+}
+
+// Per-cell upper bound of the density any sample inside the cell can reach:
+// sum over the 27-neighbourhood particles of W at the particle's distance to
+// the (slightly enlarged) cell box, inflated by a rounding margin that covers
+// the FP32 summation error of up to n terms.  One warp per cell.
+__global__ void k_cell_bound(GridDev g, KernelDev k, float slack, float* __restrict__ bound) {
+    uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
+    uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
+    int l = threadIdx.x % kWarp;
+    if (c >= ncells) return;
+    int cx = (int)(c % (uint64_t)g.dims[0]);
+    int cy = (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]);
+    int cz = (int)(c / ((uint64_t)g.dims[0] * g.dims[1]));
+    float b0[3], b1[3];
+    int cc[3] = {cx, cy, cz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        b0[a] = g.min[a] + (float)cc[a] * g.cell;
+        b1[a] = b0[a] + g.cell;
+    }
+    float acc = 0.0f;
+    uint32_t cnt = 0;
+    int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.dims[0] - 1);
+    for (int z = max(cz - 1, 0); z <= min(cz + 1, g.dims[2] - 1); ++z)
+        for (int y = max(cy - 1, 0); y <= min(cy + 1, g.dims[1] - 1); ++y) {
+            uint64_t row = ((uint64_t)z * g.dims[1] + y) * g.dims[0];
+            uint32_t b = g.start[row + x0], e = g.start[row + x1 + 1];
+            cnt += e - b;
+            for (uint32_t j = b + l; j < e; j += kWarp) {
+                float4 q = g.pts[j];
+                float dx = fmaxf(fmaxf(b0[0] - q.x, q.x - b1[0]), 0.0f);
+                float dy = fmaxf(fmaxf(b0[1] - q.y, q.y - b1[1]), 0.0f);
+                float dz = fmaxf(fmaxf(b0[2] - q.z, q.z - b1[2]), 0.0f);
+                float d = fmaxf(sqrtf(dx * dx + dy * dy + dz * dz) - slack, 0.0f);
+                float q2 = d * d;
+                if (q2 < k.h2) acc += w_in(k, q2);
+            }
+        }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (l == 0) {
+        const float eps = 5.9604645e-8f;  // 2^-24
+        float n = (float)cnt;
+        float up = acc * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
+        bound[c] = (cnt == 0) ? 0.0f : up;
+    }
+}
+
+// Reference skip flags, Dataset.cpp:137-164, with each cell's own particle
+// count as the find_neighbors_box result.
+__global__ void k_ref_flags(GridDev g, float W0, uint8_t* __restrict__ flag) {
+    uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
+    uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    int x = (int)(c % (uint64_t)g.dims[0]);
+    int y = (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]);
+    int z = (int)(c / ((uint64_t)g.dims[0] * g.dims[1]));
+    float Nc = 0.0f;
+    for (int dx = -1; dx <= 1; ++dx)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dz = -1; dz <= 1; ++dz) {
+                int xx = x + dx, yy = y + dy, zz = z + dz;
+                if (xx < 0 || xx >= g.dims[0] || yy < 0 || yy >= g.dims[1] || zz < 0 || zz >= g.dims[2]) continue;
+                uint64_t cc = (uint64_t)xx + (uint64_t)yy * g.dims[0] + (uint64_t)zz * g.dims[0] * g.dims[1];
+                const float C = 1000.0f;
+                const float r = (float)(abs(dx) + abs(dy) + abs(dz));
+                const float wgt = expf(-C * r);
+                Nc = Nc + wgt * (float)(g.start[cc + 1] - g.start[cc]);
+            }
+    float rho = Nc * W0;
+    flag[c] = rho > 1.0f ? 1 : 0;
+}
+
+bool ensure_buf(DevBuf& b, size_t bytes) {
+    if (b.bytes >= bytes) return true;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    if (cudaMalloc(&b.p, bytes) != cudaSuccess) return false;
+    b.bytes = bytes;
+    return true;
+}
+
+}  // namespace
+
+GridDev grid_dev(const fm_scene* s) {
+    GridDev g;
+    for (int a = 0; a < 3; ++a) {
+        g.min[a] = s->min[a];
+        g.dims[a] = s->dims[a];
+    }
+    g.inv = s->inv;
+    g.cell = 1.0f * s->support;
+    g.pts = s->d_pts;
+    g.start = s->d_start;
+    g.bound = s->bound_valid ? s->d_bound : nullptr;
+    g.flag = s->flag_valid ? s->d_flag : nullptr;
+    return g;
+}
+
+int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
+    cudaStream_t st = ctx->stream;
+    const uint64_t n = s->n;
+    // 1. AABB (exact min/max) -> host
+    if (!ensure_buf(ctx->scratch[0], 64)) return set_err(ctx, FM_ERR_OOM, "scratch allocation failed");
+    uint32_t* mm = (uint32_t*)ctx->scratch[0].p;
+    FM_CUDA(ctx, cudaMemsetAsync(mm, 0xff, 3 * sizeof(uint32_t), st));
+    FM_CUDA(ctx, cudaMemsetAsync(mm + 3, 0, 4 * sizeof(uint32_t), st));
+    {
+        unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 8);
+        k_aabb<<<std::max(1u, blocks), 256, 0, st>>>(d_xyz, n, stride, mm);
+        FM_CUDA(ctx, cudaGetLastError());
+    }
+    uint32_t* h = (uint32_t*)ctx->h_pinned_small;
+    FM_CUDA(ctx, cudaMemcpyAsync(h, mm, 7 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
+    FM_CUDA(ctx, cudaStreamSynchronize(st));
+    if (h[6] != 0) return set_err(ctx, FM_ERR_INVALID, "particle positions contain non-finite values");
+    // 2. grid parameters, in the reference's FP32 order (Dataset.cpp:89-104)
+    const float H = s->support;
+    const float pad = 1.0f * H;
+    const float cell = 1.0f * H;
+    uint64_t ncells = 1;
+    for (int a = 0; a < 3; ++a) {
+        float mn = ord2f(h[a]), mx = ord2f(h[3 + a]);
+        s->max[a] = mx + pad;
+        s->min[a] = mn - pad;
+        float ext = s->max[a] - s->min[a];
+        float d = std::ceil(ext / cell);
+        if (!(d >= 1.0f && d < 1.0e6f)) return set_err(ctx, FM_ERR_INVALID, "grid extent / support radius out of range");
+        s->dims[a] = (int)d;
+        ncells *= (uint64_t)s->dims[a];
+    }
+    s->inv = 1.0f / cell;
+    if (ncells > (1ull << 28))
+        return set_err(ctx, FM_ERR_INVALID, "grid would exceed 2^28 cells: support radius too small for the extent");
+    s->ncells = ncells;
+    s->bound_valid = false;
+    s->flag_valid = false;
+    if (ncells > s->cell_capacity) {
+        cudaFree(s->d_start);
+        cudaFree(s->d_bound);
+        cudaFree(s->d_flag);
+        s->d_start = nullptr; s->d_bound = nullptr; s->d_flag = nullptr;
+        if (cudaMalloc(&s->d_start, (ncells + 1) * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&s->d_bound, ncells * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&s->d_flag, ncells) != cudaSuccess) {
+            s->cell_capacity = 0;
+            return set_err(ctx, FM_ERR_OOM, "cell table allocation failed");
+        }
+        s->cell_capacity = ncells;
+    }
+    // 3. cells + histogram
+    GridParams gp;
+    for (int a = 0; a < 3; ++a) { gp.min[a] = s->min[a]; gp.dims[a] = s->dims[a]; }
+    gp.inv = s->inv;
+    const uint64_t nblk = (n + kSortTile - 1) / kSortTile;
+    const uint64_t hist_n = 256 * nblk;
+    const uint64_t scan_n = std::max<uint64_t>(ncells + 1, hist_n);
+    if (!ensure_buf(ctx->scratch[1], (ncells + 1) * sizeof(uint32_t)) ||  // counts
+        !ensure_buf(ctx->scratch[2], n * sizeof(uint32_t)) ||            // keys b
+        !ensure_buf(ctx->scratch[3], n * sizeof(uint32_t)) ||            // vals b
+        !ensure_buf(ctx->scratch[4], n * sizeof(uint32_t)) ||            // keys a
+        !ensure_buf(ctx->scratch[5], hist_n * sizeof(uint32_t)) ||       // hist
+        !ensure_buf(ctx->scratch[6], scan_tmp_words(scan_n) * sizeof(uint32_t)))
+        return set_err(ctx, FM_ERR_OOM, "grid build scratch allocation failed");
+    uint32_t* counts = (uint32_t*)ctx->scratch[1].p;
+    FM_CUDA(ctx, cudaMemsetAsync(counts, 0, (ncells + 1) * sizeof(uint32_t), st));
+    k_cells<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_xyz, n, stride, gp, s->d_cell, counts);
+    FM_CUDA(ctx, cudaGetLastError());
+    uint32_t* tmp = (uint32_t*)ctx->scratch[6].p;
+    exclusive_scan(counts, s->d_start, ncells + 1, tmp, st);
+    FM_CUDA(ctx, cudaGetLastError());
+    // 4. stable LSD radix sort of (cell, index)
+    int bits = 1;
+    while (bits < 32 && (ncells - 1) >> bits) ++bits;
+    const uint32_t* kin = s->d_cell;
+    const uint32_t* vin = nullptr;
+    uint32_t* kbuf[2] = {(uint32_t*)ctx->scratch[4].p, (uint32_t*)ctx->scratch[2].p};
+    uint32_t* vbuf[2] = {s->d_perm, (uint32_t*)ctx->scratch[3].p};
+    uint32_t* hist = (uint32_t*)ctx->scratch[5].p;
+    int passes = (bits + 7) / 8;
+    // final pass must land its values in s->d_perm
+    int cur = (passes % 2 == 1) ? 0 : 1;
+    for (int p = 0; p < passes; ++p) {
+        int shift = 8 * p;
+        k_radix_hist<<<(unsigned)nblk, kSortThreads, 0, st>>>(kin, n, shift, (uint32_t)nblk, hist);
+        exclusive_scan(hist, hist, hist_n, tmp, st);
+        k_radix_scatter<<<(unsigned)nblk, kSortThreads, 0, st>>>(kin, vin, kbuf[cur], vbuf[cur], n, shift,
+                                                               (uint32_t)nblk, hist);
+        FM_CUDA(ctx, cudaGetLastError());
+        kin = kbuf[cur];
+        vin = vbuf[cur];
+        cur ^= 1;
+    }
+    // 5. gather cell-sorted float4 positions
+    k_gather<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_xyz, n, stride, s->d_perm, s->d_pts);
+    FM_CUDA(ctx, cudaGetLastError());
+    return FM_OK;
+}
+
+int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st) {
+    if (s->bound_valid) return FM_OK;
+    GridDev g = grid_dev(s);
+    KernelDev k = make_kernel(s->support);
+    float amax = 0.0f;
+    for (int a = 0; a < 3; ++a) amax = std::max(amax, std::max(std::fabs(s->min[a]), std::fabs(s->max[a])));
+    float slack = 1.0e-4f * s->support + 1.0e-6f * amax;
+    uint64_t threads = s->ncells * kWarp;
+    k_cell_bound<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, k, slack, s->d_bound);
+    FM_CUDA(ctx, cudaGetLastError());
+    s->bound_valid = true;
+    return FM_OK;
+}
+
+int ensure_flags(fm_ctx* ctx, fm_scene* s, cudaStream_t st) {
+    if (s->flag_valid) return FM_OK;
+    GridDev g = grid_dev(s);
+    KernelDev k = make_kernel(s->support);
+    k_ref_flags<<<(unsigned)((s->ncells + 255) / 256), 256, 0, st>>>(g, k.sig, s->d_flag);
+    FM_CUDA(ctx, cudaGetLastError());
+    s->flag_valid = true;
+    return FM_OK;
+}
+
+}  // namespace fm

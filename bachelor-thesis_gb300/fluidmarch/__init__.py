@@ -1,0 +1,313 @@
+"""Python binding of libfluidmarch (ctypes over the C ABI in include/fluidmarch.h).
+
+The classes mirror the reference's host interface for the march:
+
+* :class:`Context`      ~ ``RayMarcher`` (RayMarcher.h:28-77): owns a CUDA stream.
+* :class:`Scene`        ~ ``Frame`` (Dataset.h:37-65): particles + uniform grid.
+* :class:`RayMarcher`   ~ ``RayMarcher::Prepare/Start/IsDone/Exit`` on top of the
+                          two above, with the reference's ``VisualizationSettings``.
+
+Arrays are numpy (host memory) or any object exposing ``data_ptr()`` (device
+memory, e.g. a torch CUDA tensor).  Every call goes through the CUDA library;
+there is no CPU fallback: if the library or a GPU is missing, calls raise.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import scenes  # noqa: F401  (re-export)
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfluidmarch.so")
+
+FM_OK, FM_ERR_INVALID, FM_ERR_CUDA, FM_ERR_TIMEOUT, FM_ERR_OOM, FM_ERR_DEVICE = 0, 1, 2, 3, 4, 5
+FM_MEM_HOST, FM_MEM_DEVICE = 0, 1
+FM_SKIP_OFF, FM_SKIP_EXACT, FM_SKIP_REFERENCE = 0, 1, 2
+FM_MARCH_EXTERNAL_DEPTH = 1
+
+EXPORTS = [
+    "fm_version", "fm_create", "fm_destroy", "fm_last_error", "fm_stream", "fm_sync", "fm_query", "fm_host_alloc",
+    "fm_host_free", "fm_scene_create", "fm_scene_update", "fm_scene_destroy", "fm_scene_grid", "fm_scene_download",
+    "fm_splat_depth", "fm_march", "fm_set_stats", "fm_march_stats_get",
+]
+
+
+class FmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[fm error {code}] {msg}")
+        self.code = code
+
+
+class CCamera(C.Structure):
+    _fields_ = [("view", C.c_float * 16), ("proj", C.c_float * 16), ("inv_proj_view", C.c_float * 16),
+                ("position", C.c_float * 3), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class CMarchParams(C.Structure):
+    _fields_ = [("iso_density", C.c_float), ("step_size", C.c_float), ("max_steps", C.c_int32),
+                ("bisect_iters", C.c_int32), ("skip_mode", C.c_int32), ("flags", C.c_int32)]
+
+
+class CFrameOut(C.Structure):
+    _fields_ = [("position", C.c_void_p), ("normal", C.c_void_p), ("depth", C.c_void_p), ("colour", C.c_void_p),
+                ("start_depth", C.c_void_p)]
+
+
+class CGridInfo(C.Structure):
+    _fields_ = [("min", C.c_float * 3), ("max", C.c_float * 3), ("cell_width", C.c_float),
+                ("inv_cell_width", C.c_float), ("dims", C.c_int32 * 3), ("pad", C.c_int32),
+                ("n_particles", C.c_uint64), ("n_cells", C.c_uint64)]
+
+
+class CMarchStats(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("started", C.c_uint64), ("hits", C.c_uint64), ("evals", C.c_uint64),
+                ("candidates", C.c_uint64), ("skipped", C.c_uint64)]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH) -> C.CDLL:
+    """Load libfluidmarch.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} missing: run __graft_entry__.build() (the CUDA library is required)")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.fm_version.restype = C.c_int
+    L.fm_create.argtypes = [C.POINTER(vp), C.c_int]
+    L.fm_destroy.argtypes = [vp]
+    L.fm_destroy.restype = None
+    L.fm_last_error.argtypes = [vp]
+    L.fm_last_error.restype = C.c_char_p
+    L.fm_stream.argtypes = [vp]
+    L.fm_stream.restype = vp
+    L.fm_sync.argtypes = [vp, C.c_int]
+    L.fm_query.argtypes = [vp]
+    L.fm_host_alloc.argtypes = [vp, C.c_size_t, C.POINTER(vp)]
+    L.fm_host_free.argtypes = [vp, vp]
+    L.fm_host_free.restype = None
+    L.fm_scene_create.argtypes = [vp, vp, C.c_uint64, C.c_uint32, C.c_float, C.c_int, C.POINTER(vp)]
+    L.fm_scene_update.argtypes = [vp, vp, C.c_uint64, C.c_uint32, C.c_int]
+    L.fm_scene_destroy.argtypes = [vp]
+    L.fm_scene_destroy.restype = None
+    L.fm_scene_grid.argtypes = [vp, C.POINTER(CGridInfo)]
+    L.fm_scene_download.argtypes = [vp, vp, vp, vp, vp]
+    L.fm_splat_depth.argtypes = [vp, vp, C.POINTER(CCamera), vp, C.c_int, vp]
+    L.fm_march.argtypes = [vp, vp, C.POINTER(CCamera), C.POINTER(CMarchParams), C.POINTER(CFrameOut), C.c_int, vp]
+    L.fm_set_stats.argtypes = [vp, C.c_int]
+    L.fm_march_stats_get.argtypes = [vp, C.POINTER(CMarchStats)]
+    _lib = L
+    return L
+
+
+def _ptr(a):
+    """(address, memkind) of a numpy array or a device tensor."""
+    if a is None:
+        return None, None
+    if isinstance(a, np.ndarray):
+        if not a.flags["C_CONTIGUOUS"]:
+            raise ValueError("arrays must be C-contiguous")
+        return a.ctypes.data, FM_MEM_HOST
+    if hasattr(a, "data_ptr"):
+        dev = getattr(a, "is_cuda", True)
+        return a.data_ptr(), (FM_MEM_DEVICE if dev else FM_MEM_HOST)
+    raise TypeError(f"unsupported array type {type(a)}")
+
+
+def camera_struct(cam) -> CCamera:
+    c = CCamera()
+    c.view[:] = [float(x) for x in np.asarray(cam.view, np.float32)]
+    c.proj[:] = [float(x) for x in np.asarray(cam.proj, np.float32)]
+    c.inv_proj_view[:] = [float(x) for x in np.asarray(cam.inv_proj_view, np.float32)]
+    c.position[:] = [float(x) for x in np.asarray(cam.position, np.float32)]
+    c.width, c.height = int(cam.width), int(cam.height)
+    return c
+
+
+class Context:
+    """A device context (``RayMarcher()`` in the reference)."""
+
+    def __init__(self, device: int = 0):
+        self.L = load()
+        h = C.c_void_p()
+        rc = self.L.fm_create(C.byref(h), int(device))
+        if rc != FM_OK:
+            raise FmError(rc, f"fm_create(device={device}) failed")
+        self.h = h
+
+    def check(self, rc: int):
+        if rc != FM_OK:
+            raise FmError(rc, self.L.fm_last_error(self.h).decode())
+
+    @property
+    def stream(self) -> int:
+        return self.L.fm_stream(self.h) or 0
+
+    def sync(self, timeout_ms: int = -1):
+        self.check(self.L.fm_sync(self.h, int(timeout_ms)))
+
+    def query(self) -> bool:
+        r = self.L.fm_query(self.h)
+        if r < 0:
+            raise FmError(-r, self.L.fm_last_error(self.h).decode())
+        return r == 1
+
+    def set_stats(self, on: bool):
+        self.check(self.L.fm_set_stats(self.h, 1 if on else 0))
+
+    def stats(self) -> dict:
+        s = CMarchStats()
+        self.check(self.L.fm_march_stats_get(self.h, C.byref(s)))
+        return {k: int(getattr(s, k)) for k, _ in CMarchStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.L.fm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Scene:
+    """Particles plus their uniform grid (``Frame`` in the reference)."""
+
+    def __init__(self, ctx: Context, xyz, support: float, stride: int = 3):
+        self.ctx = ctx
+        p, mem = _ptr(xyz)
+        n = int(xyz.shape[0])
+        h = C.c_void_p()
+        ctx.check(ctx.L.fm_scene_create(ctx.h, p, n, int(stride), float(support), mem, C.byref(h)))
+        self.h = h
+        self.support = float(support)
+
+    def update(self, xyz, stride: int = 3):
+        p, mem = _ptr(xyz)
+        self.ctx.check(self.ctx.L.fm_scene_update(self.h, p, int(xyz.shape[0]), int(stride), mem))
+
+    def grid(self) -> dict:
+        g = CGridInfo()
+        self.ctx.check(self.ctx.L.fm_scene_grid(self.h, C.byref(g)))
+        return {"min": np.array(g.min[:], np.float32), "max": np.array(g.max[:], np.float32),
+                "cell_width": g.cell_width, "inv_cell_width": g.inv_cell_width, "dims": tuple(g.dims[:]),
+                "n_particles": int(g.n_particles), "n_cells": int(g.n_cells)}
+
+    def download(self) -> dict:
+        g = self.grid()
+        n, nc = g["n_particles"], g["n_cells"]
+        cell = np.empty(n, np.uint32)
+        perm = np.empty(n, np.uint32)
+        start = np.empty(nc + 1, np.uint32)
+        pts = np.empty((n, 4), np.float32)
+        self.ctx.check(self.ctx.L.fm_scene_download(self.h, cell.ctypes.data, perm.ctypes.data, start.ctypes.data,
+                                                    pts.ctypes.data))
+        return {"cell": cell, "perm": perm, "start": start, "sorted": pts}
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.L.fm_scene_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class MarchParams:
+    """``VisualizationSettings`` fields of the isotropic march, plus bisection and skip mode."""
+
+    iso: float
+    step: float
+    max_steps: int
+    bisect: int = 0
+    skip_mode: int = FM_SKIP_OFF
+    external_depth: bool = False
+
+    def cstruct(self) -> CMarchParams:
+        return CMarchParams(float(self.iso), float(self.step), int(self.max_steps), int(self.bisect),
+                            int(self.skip_mode), FM_MARCH_EXTERNAL_DEPTH if self.external_depth else 0)
+
+
+def splat_depth(scene: Scene, cam, out=None, stream=None):
+    """Depth pass: returns a (H*W,) float32 buffer cleared to 1.0 (numpy unless ``out`` is given)."""
+    ctx = scene.ctx
+    if out is None:
+        out = np.empty(cam.width * cam.height, np.float32)
+    p, mem = _ptr(out)
+    cs = camera_struct(cam)
+    ctx.check(ctx.L.fm_splat_depth(ctx.h, scene.h, C.byref(cs), p, mem, stream))
+    return out
+
+
+def march(scene: Scene, cam, params: MarchParams, position=None, normal=None, depth=None, colour=None,
+          start_depth=None, stream=None):
+    """Render one view.  Outputs are the given buffers (all host or all device)."""
+    ctx = scene.ctx
+    bufs = [position, normal, depth, colour, start_depth]
+    mems = {m for m in (_ptr(b)[1] for b in bufs) if m is not None}
+    if len(mems) > 1:
+        raise ValueError("outputs must all be host or all be device buffers")
+    mem = mems.pop() if mems else FM_MEM_HOST
+    o = CFrameOut(*[_ptr(b)[0] for b in bufs])
+    cs = camera_struct(cam)
+    ps = params.cstruct()
+    ctx.check(ctx.L.fm_march(ctx.h, scene.h, C.byref(cs), C.byref(ps), C.byref(o), mem, stream))
+
+
+def render(scene: Scene, cam, params: MarchParams, want_start: bool = True) -> dict:
+    """Convenience: march one view into fresh numpy buffers."""
+    npx = cam.width * cam.height
+    out = {"position": np.zeros((npx, 4), np.float32), "normal": np.zeros((npx, 4), np.float32),
+           "depth": np.zeros(npx, np.float32), "colour": np.zeros((npx, 4), np.float32)}
+    if want_start:
+        out["start_depth"] = np.zeros(npx, np.float32)
+    march(scene, cam, params, out["position"], out["normal"], out["depth"], out["colour"], out.get("start_depth"))
+    return out
+
+
+class RayMarcher:
+    """Mirror of the reference's ``RayMarcher`` host class (RayMarcher.h:28-77).
+
+    ``prepare(settings, camera, scene, positions, normals, depth)`` takes the
+    same arguments as ``RayMarcher::Prepare`` (RayMarcher.cpp:76-100): the
+    depth buffer is the ray-start (splat) depth the reference consumes; the
+    marcher writes positions and normals.  ``start()`` launches on the
+    context's stream, ``is_done()`` polls it, ``exit()`` waits.
+    """
+
+    def __init__(self, device: int = 0):
+        self.ctx = Context(device)
+        self._args = None
+
+    def prepare(self, settings: MarchParams, camera, scene: Scene, positions, normals, depth):
+        if positions is None or normals is None or depth is None:
+            raise ValueError("positions, normals and depth buffers are required")
+        self._args = (settings, camera, scene, positions, normals, depth)
+
+    def start(self):
+        if self._args is None:
+            raise RuntimeError("prepare() first")
+        settings, camera, scene, positions, normals, depth = self._args
+        p = MarchParams(settings.iso, settings.step, settings.max_steps, settings.bisect, settings.skip_mode, True)
+        march(scene, camera, p, position=positions, normal=normals, start_depth=depth,
+              stream=None)
+
+    def is_done(self) -> bool:
+        return self.ctx.query()
+
+    def exit(self):
+        self.ctx.sync()

@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Benchmark: rays/s of the GPU SPH iso-surface march (reference: the CPU
+RayMarcher, src/app/AdvancedRenderer/RayMarcher.cpp:256-344).
+
+Workload (one "step" = one rendered frame): the 1,000,000-particle sloshing
+scene (950k fluid below y = 0.4 + 0.08 sin(2 pi x) cos(3 pi z) + N(0, 0.005),
+50k spray above), support radius 0.04 (h = 0.02), iso = 0.5 x lattice rest
+density, 1920x1080, step 0.25 h, max 1024 steps, 8 bisection iterations.
+Synthetic, seeded particles; the scene stays resident in HBM for `value`.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+value  rays/s over all N GPUs (each rank renders its own frame: replicas,
+       weak scaling), device time of splat + march + shade per frame, CUDA
+       events on the launching stream, L2 flushed (512 MiB write) between
+       frames outside the events.
+e2e    the same frame through the C ABI with pinned HOST buffers: particle
+       upload + grid build + splat + march + shade + copy back of position,
+       normal, depth and colour, wall clock per frame.
+--impl reference times the CPU marcher (the oracle port of the reference's
+       loop, bisection 0, skipping off, all host threads but one as
+       RayMarcher.cpp:67 does) on a bounded random pixel sample per step.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import platform
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "bachelor-thesis_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "rays/s and 1080p frames/s: learned vs plain GPU march at fixed depth error"
+UNIT = "rays/s"
+L2_FLUSH_BYTES = 512 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip", default="exact", choices=["exact", "off"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the cpu_baseline sample")
+    return ap.parse_args()
+
+
+def workload_config(sc, cam, skip):
+    return {"workload": "sloshing surface, plain GPU march", "particles": sc.n, "support_radius": sc.support,
+            "h": sc.support / 2, "iso": sc.iso, "width": cam.width, "height": cam.height, "step": sc.step,
+            "max_steps": sc.max_steps, "bisect_iters": sc.bisect, "skip": skip,
+            "l2": "flushed between frames (512 MiB write)", "parallelism": "replicas"}
+
+
+def cpu_info():
+    model = platform.processor() or ""
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith(("model name", "cpu part")):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    return os.cpu_count() or 1, model or platform.machine()
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms during the timed region."""
+
+    FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "--query-gpu=" + ",".join(self.FIELDS),
+                                          "--format=csv,noheader,nounits", "-lms", "200", "-i", str(self.device)],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the march kernel from the committed ncu summary, if present."""
+    p = os.path.join(ROOT, "profiles", "march_sloshing_1080p.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("dram_bytes_per_launch")
+    except (OSError, ValueError):
+        return None
+
+
+def cpu_baseline_sample(sc, cam, depth, fr, target_s, threads):
+    """Time the oracle port (bisection 0, skip off) on a seeded random pixel sample."""
+    import oracle as O
+
+    rng = np.random.default_rng(1234)
+    npx = cam.width * cam.height
+    n = 2000
+    spent = 0.0
+    total_px = 0
+    while True:
+        pix = np.sort(rng.choice(npx, n, replace=False)).astype(np.int64)
+        t0 = time.perf_counter()
+        O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 0, depth, skip_mode=0, pixels=pix, threads=threads,
+                want_colour=False)
+        dt = time.perf_counter() - t0
+        spent += dt
+        total_px += n
+        if spent >= target_s or n >= npx:
+            break
+        n = int(min(npx, max(n * 2, n * (target_s - spent) / max(dt, 1e-3))))
+    return total_px / spent, total_px, spent
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import oracle as O
+    from fluidmarch import scenes
+
+    O.build_oracle(ref=False)
+    sc = scenes.sloshing()
+    cam = sc.cameras[0]
+    fr = O.build_frame(sc.xyz, sc.support)
+    depth = O.splat(sc.xyz, sc.support, cam)
+    cores, model = cpu_info()
+    threads = max(1, cores - 1)
+    rng = np.random.default_rng(77)
+    npx = cam.width * cam.height
+    per_step = 3000
+    times = []
+    for i in range(args.warmup + args.steps):
+        pix = np.sort(rng.choice(npx, per_step, replace=False)).astype(np.int64)
+        t0 = time.perf_counter()
+        O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 0, depth, skip_mode=0, pixels=pix, threads=threads,
+                want_colour=False)
+        dt = time.perf_counter() - t0
+        if i >= args.warmup:
+            times.append(dt)
+    total = sum(times)
+    v = per_step * len(times) / total
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded)",
+            "config": dict(workload_config(sc, cam, "off"), bisect_iters=0,
+                           sample=f"{per_step} random pixels of the 1920x1080 frame per step"),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{per_step} seeded random pixels per step, {len(times)} steps; "
+                                       f"CPU {model}, {cores} host cores"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import __graft_entry__ as ge
+
+    ge.build()
+    import fluidmarch as fm
+    from fluidmarch import scenes
+
+    sc = scenes.sloshing(seed=1000 + rank)
+    cam = sc.cameras[0]
+    npx = cam.width * cam.height
+    skip = fm.FM_SKIP_EXACT if args.skip == "exact" else fm.FM_SKIP_OFF
+    ctx = fm.Context(local)
+    xyz_d = torch.from_numpy(sc.xyz).cuda()
+    scene = fm.Scene(ctx, xyz_d, sc.support)
+    dev = torch.device("cuda", local)
+    out = {"position": torch.empty((npx, 4), device=dev), "normal": torch.empty((npx, 4), device=dev),
+           "depth": torch.empty(npx, device=dev), "colour": torch.empty((npx, 4), device=dev),
+           "start_depth": torch.empty(npx, device=dev)}
+    stream = torch.cuda.current_stream().cuda_stream
+    P_ext = fm.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, skip, external_depth=True)
+
+    def frame():
+        fm.splat_depth(scene, cam, out["start_depth"], stream=stream)
+        fm.march(scene, cam, P_ext, out["position"], out["normal"], out["depth"], out["colour"], out["start_depth"],
+                 stream=stream)
+
+    # counters for the algorithmic bytes (untimed run)
+    ctx.set_stats(True)
+    frame()
+    torch.cuda.synchronize()
+    st = ctx.stats()
+    ctx.set_stats(False)
+
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
+    for _ in range(args.warmup):
+        frame()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+           torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for e0, e1, e2 in ev:
+            flush.zero_()
+            e0.record()
+            fm.splat_depth(scene, cam, out["start_depth"], stream=stream)
+            e1.record()
+            fm.march(scene, cam, P_ext, out["position"], out["normal"], out["depth"], out["colour"],
+                     out["start_depth"], stream=stream)
+            e2.record()
+        torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    total_ms = sum(e0.elapsed_time(e2) for e0, _, e2 in ev)
+    march_ms = sum(e1.elapsed_time(e2) for _, e1, e2 in ev)
+    splat_ms = sum(e0.elapsed_time(e1) for e0, e1, _ in ev)
+    t_max = total_ms
+    if dist:
+        t = torch.tensor([total_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = npx * args.steps * world / (t_max / 1000.0)
+
+    # e2e through the C ABI with pinned host buffers
+    xyz_h = torch.from_numpy(sc.xyz).pin_memory()
+    host = {"position": torch.empty((npx, 4)).pin_memory(), "normal": torch.empty((npx, 4)).pin_memory(),
+            "depth": torch.empty(npx).pin_memory(), "colour": torch.empty((npx, 4)).pin_memory()}
+    P_full = fm.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, skip)
+    hp = {k: v.numpy() for k, v in host.items()}  # numpy views of the pinned buffers
+    xyz_np = xyz_h.numpy()
+
+    def e2e_frame():
+        scene.update(xyz_np)
+        fm.march(scene, cam, P_full, hp["position"], hp["normal"], hp["depth"], hp["colour"])
+
+    for _ in range(max(1, args.warmup // 2)):
+        e2e_frame()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_frame()
+    e2e_s = time.perf_counter() - t0
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e_value = npx * args.steps * world / e2e_s
+
+    if rank == 0:
+        peak, peak_kind = measured_peaks()
+        alg_bytes = 16 * st["candidates"] + 36 * npx
+        march_s = march_ms / args.steps / 1000.0
+        achieved = alg_bytes / march_s / 1e9
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded particles)",
+            "config": workload_config(sc, cam, args.skip),
+            "frames_per_s": 1000.0 * args.steps * world / t_max,
+            "stage_ms": {"splat": splat_ms / args.steps, "march": march_ms / args.steps},
+            "march_counters": st,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": profiled_traffic(),
+                         "kernel": "k_march", "peak_kind": peak_kind,
+                         "algorithmic_bytes_per_launch": alg_bytes,
+                         "note": "16 B x particles in the 27 cells of every density evaluation + 36 B/ray outputs; "
+                                 "served from L1/L2, so frac > 1 means on-chip reuse"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * sc.n,
+                    "d2h_bytes_per_step": npx * (16 + 16 + 4 + 16)},
+            "gpu_launches": 3 * args.steps,
+            "clocks": clk.summary(),
+        }
+        if world == 1 and not args.no_cpu_baseline:
+            import oracle as O
+
+            O.build_oracle(ref=False)
+            fr = O.build_frame(sc.xyz, sc.support)
+            depth = out["start_depth"].cpu().numpy()
+            cores, model = cpu_info()
+            threads = max(1, cores - 1)
+            v, npix, secs = cpu_baseline_sample(sc, cam, depth, fr, args.cpu_seconds, threads)
+            line["cpu_baseline"] = {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                                    "sample": f"{npix} seeded random pixels of the same 1920x1080 frame "
+                                              f"({secs:.1f} s), bisection 0, skipping off; CPU {model}, "
+                                              f"{cores} host cores"}
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

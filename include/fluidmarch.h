@@ -1,0 +1,194 @@
+/* fluidmarch.h -- C ABI of the GB300 SPH ray marcher (libfluidmarch.so).
+ *
+ * Drop-in for the reference's CPU ray marcher (Fruup/bachelor-thesis):
+ *   class RayMarcher  src/app/AdvancedRenderer/RayMarcher.h:28-77
+ *     RayMarcher()    RayMarcher.cpp:66-69   -> fm_create
+ *     Prepare(...)    RayMarcher.cpp:76-100  -> fm_scene_create + fm_march arguments
+ *     Start()         RayMarcher.cpp:102-112 -> fm_march (asynchronous on a CUDA stream)
+ *     IsDone()        RayMarcher.h:44        -> fm_query
+ *     Exit()          RayMarcher.cpp:71-74   -> fm_sync / fm_destroy
+ *   class Frame       src/app/Dataset.h:37-65 (search build, AABB, density grid,
+ *                     Dataset.cpp:9-165)     -> fm_scene_create
+ *   Frame::QueryDensityGrid Dataset.cpp:26-47 -> fm_scene_download (cell of each particle)
+ *
+ * All entry points are plain C: opaque handles, POD structs, int status.
+ * Matrices are float[16] in glm's column-major layout (m[col*4 + row]).
+ * Pointers are host or device memory as the FM_MEM_* argument says; host
+ * pointers are staged through device buffers the context owns.
+ * No entry point falls back to a CPU path: without a usable CUDA device every
+ * call that needs one returns FM_ERR_CUDA.
+ */
+#ifndef FLUIDMARCH_H
+#define FLUIDMARCH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes --------------------------------------------------------
+ * The reference has no status codes (SPDLOG_ERROR + continue, HZ_ASSERT);
+ * every fm_* call returns one of these and keeps a message for
+ * fm_last_error(). */
+#define FM_OK 0
+#define FM_ERR_INVALID 1  /* bad argument: null handle, N == 0, non-finite input, ... */
+#define FM_ERR_CUDA 2     /* a CUDA call failed, or no CUDA device */
+#define FM_ERR_TIMEOUT 3  /* fm_sync gave up waiting */
+#define FM_ERR_OOM 4      /* device or pinned allocation failed */
+#define FM_ERR_DEVICE 5   /* a kernel reported an error through its status word */
+
+#define FM_MEM_HOST 0     /* pointer is host memory (pageable or pinned) */
+#define FM_MEM_DEVICE 1   /* pointer is device memory of the context's device */
+
+/* skip modes (march parameter) */
+#define FM_SKIP_OFF 0        /* evaluate the density at every sample (reference parity gate) */
+#define FM_SKIP_EXACT 1      /* skip samples whose cell's density upper bound is below iso;
+                                same samples, same results as FM_SKIP_OFF */
+#define FM_SKIP_REFERENCE 2  /* the reference's skip: flag = own-cell count * W0 > 1, jump to the
+                                cell's exit plus one step (RayMarcher.cpp:281-306) */
+
+/* march flags */
+#define FM_MARCH_EXTERNAL_DEPTH 1 /* take ray-start depths from fm_frame_out.start_depth
+                                     instead of splatting them (reference signature mode) */
+
+typedef struct fm_ctx fm_ctx;
+typedef struct fm_scene fm_scene;
+
+/* Camera: what RayMarcher::Prepare reads from CameraController3D
+ * (RayMarcher.cpp:95-96: Position, InvProjectionView) plus what the depth
+ * pass (DepthRenderPass.cpp:245-247: View, Projection) and the composition
+ * pass (CompositionRenderPass.cpp:315-321: InvProjectionView, Position,
+ * System[2]) read.  The image size replaces Vulkan.SwapchainExtent
+ * (RayMarcher.cpp:86-89). */
+typedef struct fm_camera {
+    float view[16];
+    float proj[16];
+    float inv_proj_view[16];
+    float position[3];
+    int32_t width;
+    int32_t height;
+} fm_camera;
+
+/* March settings: VisualizationSettings (RayMarcher.h:12-26) fields used by
+ * the isotropic path, plus bisection and skip mode. */
+typedef struct fm_march_params {
+    float iso_density;    /* IsoDensity: hit when density >= iso_density */
+    float step_size;      /* StepSize (world units) */
+    int32_t max_steps;    /* MaxSteps */
+    int32_t bisect_iters; /* 0 = reference behaviour (first sample with rho >= iso) */
+    int32_t skip_mode;    /* FM_SKIP_* */
+    int32_t flags;        /* FM_MARCH_* */
+} fm_march_params;
+
+/* Per-pixel outputs (any pointer may be NULL to skip that output).  The
+ * reference writes glm::vec4 positions/normals (RayMarcher.cpp:330,338) into
+ * caller-owned W*H buffers; colour is the composition pass
+ * (composition.frag:132-184).  Pixel index = y * width + x, y = 0 at the top. */
+typedef struct fm_frame_out {
+    float* position;          /* 4 floats/pixel: (hit, 1) or 0 on miss */
+    float* normal;            /* 4 floats/pixel: (n, 1) or 0 on miss */
+    float* depth;             /* 1 float/pixel: |hit - camera| or 0 on miss */
+    float* colour;            /* 4 floats/pixel: shaded RGBA */
+    float* start_depth;       /* 1 float/pixel: splat depth written (or read with
+                                 FM_MARCH_EXTERNAL_DEPTH); clear value 1.0 = no particle */
+} fm_frame_out;
+
+/* Grid of a scene: Frame::m_Min/m_Max (Dataset.cpp:78-92) and
+ * DensityGrid (Dataset.cpp:94-104). */
+typedef struct fm_grid_info {
+    float min[3];
+    float max[3];
+    float cell_width;
+    float inv_cell_width;
+    int32_t dims[3];
+    int32_t pad;
+    uint64_t n_particles;
+    uint64_t n_cells;
+} fm_grid_info;
+
+/* Counters a march can accumulate (fm_march_stats). */
+typedef struct fm_march_stats {
+    uint64_t rays;          /* pixels marched */
+    uint64_t started;       /* rays whose start depth != 1.0 */
+    uint64_t hits;
+    uint64_t evals;         /* density evaluations (march samples + bisection + normal) */
+    uint64_t candidates;    /* particles in the 27 cells of every evaluation */
+    uint64_t skipped;       /* samples skipped by FM_SKIP_EXACT */
+} fm_march_stats;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* RayMarcher::RayMarcher (RayMarcher.cpp:66-69): create a context bound to a
+ * CUDA device, with its own non-blocking stream. */
+int fm_create(fm_ctx** out, int device);
+/* RayMarcher::Exit (RayMarcher.cpp:71-74): wait for work, free everything. */
+void fm_destroy(fm_ctx* ctx);
+/* Message of the last failing call on this context (never NULL). */
+const char* fm_last_error(const fm_ctx* ctx);
+/* The context's stream as a cudaStream_t. */
+void* fm_stream(fm_ctx* ctx);
+/* Wait for all work on the context's stream; FM_ERR_TIMEOUT after timeout_ms
+ * (< 0: wait forever).  Also reports kernel status words (FM_ERR_DEVICE). */
+int fm_sync(fm_ctx* ctx, int timeout_ms);
+/* RayMarcher::IsDone (RayMarcher.h:44, ThreadPool.cpp:33-36): 1 when the
+ * stream is idle, 0 when work is pending, < 0 on error.  Unlike the reference,
+ * "done" means every output has been written. */
+int fm_query(fm_ctx* ctx);
+/* Pinned host memory for staged, asynchronous copies. */
+int fm_host_alloc(fm_ctx* ctx, size_t bytes, void** out);
+void fm_host_free(fm_ctx* ctx, void* p);
+
+/* ---- scenes ------------------------------------------------------------- */
+
+/* Frame::Frame (Dataset.cpp:9-24): upload n particles (xyz at a stride of
+ * `stride` floats, >= 3) and build the uniform grid with cell width
+ * support_radius (Dataset::ParticleRadius): AABB, per-particle cell
+ * index (bit-identical to QueryDensityGrid), stable counting sort by cell,
+ * cell start table.  Synchronous.  Non-finite positions are rejected. */
+int fm_scene_create(fm_ctx* ctx, const float* xyz, uint64_t n, uint32_t stride, float support_radius,
+                    int mem, fm_scene** out);
+/* Rebuild an existing scene from new positions (same n or fewer, same
+ * radius): a new frame of the same dataset (Dataset::ReadFile adds one,
+ * Dataset.cpp:292-306). */
+int fm_scene_update(fm_scene* scene, const float* xyz, uint64_t n, uint32_t stride, int mem);
+void fm_scene_destroy(fm_scene* scene);
+int fm_scene_grid(const fm_scene* scene, fm_grid_info* out);
+/* Download the grid build (host pointers; any may be NULL):
+ *   cell[n]         linear cell of each input particle (QueryDensityGrid index)
+ *   sorted_index[n] input index of each cell-sorted particle
+ *   cell_start[n_cells + 1]
+ *   sorted_xyzw[4n] cell-sorted positions (w = 0) */
+int fm_scene_download(const fm_scene* scene, uint32_t* cell, uint32_t* sorted_index, uint32_t* cell_start,
+                      float* sorted_xyzw);
+
+/* ---- rendering ---------------------------------------------------------- */
+
+/* Depth pass (DepthRenderPass, depth.vert/depth.frag): splat every particle
+ * as a camera-facing sphere of radius support_radius into a W*H depth buffer
+ * cleared to 1.0 (LESS test).  Asynchronous on `stream` (NULL = context
+ * stream). */
+int fm_splat_depth(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, float* depth, int mem, void* stream);
+
+/* RayMarcher::Start + PerPixel_Isotropic (RayMarcher.cpp:102-112,256-344)
+ * plus the composition shading: splat (unless FM_MARCH_EXTERNAL_DEPTH),
+ * march every pixel, bisect, take the gradient normal, shade.  Asynchronous
+ * for device outputs; for host outputs the call returns once they are
+ * written. */
+int fm_march(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, const fm_march_params* params,
+             const fm_frame_out* out, int mem, void* stream);
+
+/* Counters of the last fm_march on this context (enable with
+ * fm_set_stats(ctx, 1); counting costs time, keep it off when timing). */
+int fm_set_stats(fm_ctx* ctx, int enable);
+int fm_march_stats_get(fm_ctx* ctx, fm_march_stats* out);
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int fm_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FLUIDMARCH_H */

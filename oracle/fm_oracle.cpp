@@ -426,15 +426,16 @@ constexpr float kHalfPi = 1.57079632679f;
 // Written out here and in the CUDA splat kernel with the same operation order,
 // so both produce the same bits.  |error| < 2e-7 on the interval.
 inline float cos_poly(float t) {
+    // coefficients 1/(2k)! rounded to float, written as exact hex literals
     float x = t * t;
-    float p = 1.0f / 20922789888000.0f;           // 1/16!
-    p = p * x - 1.0f / 87178291200.0f;            // 1/14!
-    p = p * x + 1.0f / 479001600.0f;              // 1/12!
-    p = p * x - 1.0f / 3628800.0f;                // 1/10!
-    p = p * x + 1.0f / 40320.0f;                  // 1/8!
-    p = p * x - 1.0f / 720.0f;                    // 1/6!
-    p = p * x + 1.0f / 24.0f;                     // 1/4!
-    p = p * x - 0.5f;                             // 1/2!
+    float p = 0x1.ae7f3ep-45f;   // 1/16!
+    p = p * x - 0x1.93974ap-37f; // 1/14!
+    p = p * x + 0x1.1eed8ep-29f; // 1/12!
+    p = p * x - 0x1.27e4fcp-22f; // 1/10!
+    p = p * x + 0x1.a01a02p-16f; // 1/8!
+    p = p * x - 0x1.6c16c2p-10f; // 1/6!
+    p = p * x + 0x1.555556p-5f;  // 1/4!
+    p = p * x - 0x1.0p-1f;       // 1/2!
     p = p * x + 1.0f;
     return p;
 }
@@ -495,9 +496,10 @@ int orc_grid_params(const float* xyz, int64_t n, int32_t stride, float H, OrcGri
 void orc_cells(const float* xyz, int64_t n, int32_t stride, const OrcGrid* g, uint32_t* cell) {
     for (int64_t i = 0; i < n; ++i) {
         const float* p = xyz + i * stride;
-        int x = int(std::floor((p[0] - g->min[0]) * g->inv));
-        int y = int(std::floor((p[1] - g->min[1]) * g->inv));
-        int z = int(std::floor((p[2] - g->min[2]) * g->inv));
+        // clamped into the grid; the support-radius padding keeps finite input inside
+        int x = std::min(std::max(int(std::floor((p[0] - g->min[0]) * g->inv)), 0), g->dims[0] - 1);
+        int y = std::min(std::max(int(std::floor((p[1] - g->min[1]) * g->inv)), 0), g->dims[1] - 1);
+        int z = std::min(std::max(int(std::floor((p[2] - g->min[2]) * g->inv)), 0), g->dims[2] - 1);
         cell[i] = uint32_t(x) + uint32_t(y) * uint32_t(g->dims[0]) +
                   uint32_t(z) * uint32_t(g->dims[0]) * uint32_t(g->dims[1]);
     }
@@ -590,6 +592,7 @@ void orc_splat(const float* xyz, int64_t n, int32_t stride, float R, const OrcCa
                 float zv = cz - R * off;
                 float d = (P22 * zv + P32) / (P23 * zv + P33);
                 if (!(d >= 0.0f && d < 1.0f)) continue;
+                d = d + 0.0f;  // -0 -> +0
                 float& dst = depth[int64_t(y) * W + x];
                 if (d < dst) dst = d;
             }

@@ -1,0 +1,98 @@
+"""GPU grid build: bit-exact against the oracle (cells, stable order, cell table)."""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from fluidmarch import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def check_grid(fm, ctx, xyz, H, stride=3):
+    fr = O.build_frame(xyz, H)
+    data = xyz if stride == 3 else np.ascontiguousarray(np.concatenate([xyz, np.ones((xyz.shape[0], stride - 3), np.float32)], 1))
+    sc = fm.Scene(ctx, data, H, stride=stride)
+    g = sc.grid()
+    assert g["dims"] == fr.dims
+    assert np.array_equal(g["min"].view(np.uint32), np.array(fr.grid.min[:], np.float32).view(np.uint32))
+    assert np.array_equal(g["max"].view(np.uint32), np.array(fr.grid.max[:], np.float32).view(np.uint32))
+    d = sc.download()
+    assert np.array_equal(d["cell"], fr.cells)
+    assert np.array_equal(d["perm"], fr.perm)
+    assert np.array_equal(d["start"], fr.start)
+    assert np.array_equal(d["sorted"].view(np.uint32), fr.sorted.view(np.uint32))
+    sc.close()
+    return g
+
+
+@pytest.mark.parametrize("n", [1, 2, 31, 2049, 5000])
+def test_grid_small(fmlib, ctx, n):
+    sc = scenes.small_scene(seed=n, n=max(n, 200))
+    check_grid(fmlib, ctx, np.ascontiguousarray(sc.xyz[:n]), sc.support)
+
+
+def test_grid_dam_break(fmlib, ctx):
+    sc = scenes.dam_break()
+    check_grid(fmlib, ctx, sc.xyz, sc.support)
+
+
+def test_grid_sloshing_1m(fmlib, ctx):
+    """The 1M-particle sloshing frame: every cell index and the sort order bit-exact."""
+    sc = scenes.sloshing()
+    g = check_grid(fmlib, ctx, sc.xyz, sc.support)
+    assert g["n_particles"] == 1_000_000
+
+
+def test_grid_stride4_negative_coordinates(fmlib, ctx):
+    rng = np.random.default_rng(1)
+    xyz = rng.uniform(-3.0, -1.0, size=(10000, 3)).astype(np.float32)
+    check_grid(fmlib, ctx, xyz, 0.13, stride=4)
+
+
+def test_grid_all_in_one_cell_and_duplicates(fmlib, ctx):
+    rng = np.random.default_rng(2)
+    xyz = np.repeat(rng.uniform(0.0, 0.01, size=(100, 3)).astype(np.float32), 50, axis=0)
+    check_grid(fmlib, ctx, xyz, 0.5)
+
+
+def test_grid_many_cells(fmlib, ctx):
+    """More than 2^16 cells: three radix passes."""
+    rng = np.random.default_rng(3)
+    xyz = rng.uniform(0.0, 1.0, size=(300000, 3)).astype(np.float32)
+    g = check_grid(fmlib, ctx, xyz, 0.012)
+    assert g["n_cells"] > (1 << 16)
+
+
+def test_scene_update_rebuilds(fmlib, ctx):
+    a = scenes.small_scene(seed=1, n=4000)
+    b = scenes.small_scene(seed=2, n=3500)
+    sc = fmlib.Scene(ctx, a.xyz, a.support)
+    sc.update(b.xyz)
+    fr = O.build_frame(b.xyz, a.support)
+    d = sc.download()
+    assert np.array_equal(d["perm"], fr.perm) and np.array_equal(d["start"], fr.start)
+
+
+def test_scene_from_device_memory(fmlib, ctx):
+    torch = pytest.importorskip("torch")
+    sc = scenes.small_scene(seed=6, n=6000)
+    t = torch.from_numpy(sc.xyz).cuda()
+    s = fmlib.Scene(ctx, t, sc.support)
+    fr = O.build_frame(sc.xyz, sc.support)
+    assert np.array_equal(s.download()["perm"], fr.perm)
+
+
+def test_rejects_bad_input(fmlib, ctx):
+    xyz = np.zeros((10, 3), np.float32)
+    xyz[3, 1] = np.nan
+    with pytest.raises(fmlib.FmError) as e:
+        fmlib.Scene(ctx, xyz, 0.1)
+    assert e.value.code == fmlib.FM_ERR_INVALID
+    with pytest.raises(fmlib.FmError):
+        fmlib.Scene(ctx, np.zeros((0, 3), np.float32), 0.1)
+    with pytest.raises(fmlib.FmError):
+        fmlib.Scene(ctx, np.zeros((4, 3), np.float32), -1.0)
+    xyz = np.array([[0, 0, 0], [1e6, 1e6, 1e6]], np.float32)
+    with pytest.raises(fmlib.FmError):  # 2^28 cell cap
+        fmlib.Scene(ctx, xyz, 1e-3)

@@ -1,0 +1,214 @@
+"""The CPU oracle, pinned against known answers, the reference's own code and
+the golden vectors the reference wrote (tests/golden).  No GPU needed."""
+
+import glob
+import math
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from fluidmarch import scenes
+
+GOLDEN = sorted(glob.glob(os.path.join(os.path.dirname(__file__), "golden", "*.npz")))
+
+
+def sigma(H):
+    return 8.0 / (math.pi * H ** 3)
+
+
+@pytest.fixture(scope="module")
+def L(oracle_lib):
+    return oracle_lib.lib()
+
+
+# ---- kernel known answers (Kernel.cpp:9-52) --------------------------------
+
+def test_w_known_answers(L):
+    H = 0.1
+    s = np.float32(8.0) / (np.float32(np.pi) * np.float32(H) * np.float32(H) * np.float32(H))
+    assert L.orc_sigma(H) == pytest.approx(sigma(H), rel=1e-6)
+    assert L.orc_W(H, 0, 0, 0) == pytest.approx(float(s), rel=1e-7)          # W(0) = sigma (Kernel.h W0)
+    assert L.orc_W(H, 0.01, 0, 0) == pytest.approx(2408.97, rel=2e-6)       # closed form at q = 0.1
+    # continuity at q = 0.5: both branches give sigma / 4
+    lo = L.orc_W(H, 0.5 * H * (1 - 1e-6), 0, 0)
+    hi = L.orc_W(H, 0.5 * H, 0, 0)
+    assert lo == pytest.approx(sigma(H) / 4, rel=1e-4)
+    assert hi == pytest.approx(sigma(H) / 4, rel=1e-4)
+    assert L.orc_W(H, H, 0, 0) == 0.0
+    assert L.orc_W(H, 0, 0, 0.2) == 0.0
+
+
+def test_gradw_reference_formula(L):
+    """gradQ = normalize(r) / (|r| H): the reference's extra 1/|r| factor is kept."""
+    H = 0.1
+    g = np.zeros(3, np.float32)
+    L.orc_gradW(H, 0.03, 0, 0, g)
+    q = 0.3
+    expect = sigma(H) * (1.0 / (0.03 * H)) * 6.0 * (3 * q * q - 2 * q)
+    assert g[0] == pytest.approx(expect, rel=1e-5)
+    assert g[1] == 0 and g[2] == 0
+    L.orc_gradW(H, 0, 0, -0.07, g)
+    q = 0.7
+    expect = -sigma(H) * (-1.0 / (0.07 * H)) * 6.0 * (1 - q) ** 2
+    assert g[2] == pytest.approx(expect, rel=1e-5)
+    L.orc_gradW(H, 0, 0, 0, g)  # r = 0 guarded (the reference would return NaN)
+    assert np.all(g == 0)
+
+
+def test_cos_poly_accuracy(L):
+    t = np.linspace(0, math.pi / 2, 2001, dtype=np.float32)
+    got = np.array([L.orc_cos_poly(float(x)) for x in t])
+    assert np.max(np.abs(got - np.cos(t.astype(np.float64)))) < 3e-7
+
+
+# ---- oracle vs the reference's compiled translation units ------------------
+
+needs_ref = pytest.mark.skipif(not O.ref_available(), reason="reference tree absent: oracle/_ref not built")
+
+
+@needs_ref
+def test_kernel_bitwise_vs_reference(L):
+    R = O.ref()
+    rng = np.random.default_rng(3)
+    g1 = np.zeros(3, np.float32)
+    g2 = np.zeros(3, np.float32)
+    for H in (0.1, 0.04, 0.0252):
+        r = rng.uniform(-1.1 * H, 1.1 * H, size=(500, 3)).astype(np.float32)
+        for x, y, z in r:
+            assert np.float32(L.orc_W(H, x, y, z)).view(np.uint32) == np.float32(R.ref_W(H, x, y, z)).view(np.uint32)
+            L.orc_gradW(H, x, y, z, g1)
+            R.ref_gradW(H, x, y, z, g2)
+            assert np.array_equal(g1.view(np.uint32), g2.view(np.uint32))
+
+
+@needs_ref
+def test_cells_match_query_density_grid():
+    """Per-particle cell = Frame::QueryDensityGrid index (Dataset.cpp:26-47), bit-exact."""
+    sc = scenes.small_scene(seed=5, n=5000)
+    fr = O.build_frame(sc.xyz, sc.support)
+    # query with the sorted particles (the reference's frame stores them z-sorted)
+    q = np.ascontiguousarray(fr.sorted[:, :3])
+    out = np.empty(q.shape[0], np.int64)
+    O.ref().ref_query_cells(np.ascontiguousarray(sc.xyz), sc.n, sc.support, q, q.shape[0], out)
+    assert np.array_equal(out.astype(np.uint32), fr.cells[fr.perm])
+
+
+@needs_ref
+@pytest.mark.parametrize("box_mode", [0, 1])
+@pytest.mark.parametrize("which", ["dam", "slosh"])
+def test_march_bitwise_vs_reference(which, box_mode):
+    if which == "dam":
+        sc = scenes.dam_break(width=96, height=72)
+    else:
+        sc = scenes.small_scene(seed=9, n=6000, width=96, height=72)
+    cam = sc.cameras[0]
+    fr = O.build_frame(sc.xyz, sc.support)
+    depth = O.splat(sc.xyz, sc.support, cam)
+    a = O.ref_march(sc.xyz, sc.support, cam, depth, sc.max_steps, sc.step, sc.iso, box_mode=box_mode)
+    b = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 0, depth, skip_mode=2 if box_mode else 0, threads=4)
+    assert np.array_equal(a["sorted"], fr.sorted[:, :3])
+    last = cam.width * cam.height - 1  # the reference never marches pixel W*H-1 (ThreadPool.cpp:50)
+    for k in ("position", "normal"):
+        x = b[k].copy()
+        x[last] = 0
+        assert np.array_equal(a[k].view(np.uint32), x.view(np.uint32)), k
+    assert (a["position"][:, 3] == 1).sum() > 100
+
+
+# ---- golden vectors written by the reference --------------------------------
+
+class _Cam:
+    def __init__(self, z):
+        self.view, self.proj, self.inv_proj_view = z["view"], z["proj"], z["inv_proj_view"]
+        self.position, self.width, self.height = z["cam_pos"], int(z["width"]), int(z["height"])
+
+
+def load_golden(path):
+    z = dict(np.load(path))
+    return z, _Cam(z)
+
+
+@pytest.mark.skipif(not GOLDEN, reason="no golden vectors")
+@pytest.mark.parametrize("path", GOLDEN, ids=[os.path.basename(p) for p in GOLDEN])
+def test_oracle_matches_golden(path):
+    z, cam = load_golden(path)
+    fr = O.build_frame(z["xyz"], float(z["support"]))
+    assert np.array_equal(fr.sorted[:, :3], z["ref_sorted"])
+    depth = O.splat(z["xyz"], float(z["support"]), cam)
+    assert np.array_equal(depth, z["start_depth"])
+    skip = 2 if int(z["box_mode"]) == 1 else 0
+    b = O.march(fr, cam, float(z["iso"]), float(z["step"]), int(z["max_steps"]), 0, z["start_depth"],
+                skip_mode=skip, threads=2)
+    last = cam.width * cam.height - 1
+    for k in ("position", "normal"):
+        x = b[k].copy()
+        x[last] = 0
+        assert np.array_equal(z["ref_" + k].view(np.uint32), x.view(np.uint32)), k
+
+
+# ---- self-made known answers --------------------------------------------------
+
+def test_lattice_rest_density():
+    assert scenes.lattice_rest_density(0.025, 0.1) == pytest.approx(64005, rel=1e-4)
+    assert scenes.lattice_rest_density((0.4 / 950000) ** (1 / 3), 0.04) == pytest.approx(2.376e6, rel=1e-3)
+
+
+def test_oracle_density_matches_lattice_sum():
+    s, H = 0.025, 0.1
+    i = np.arange(-6, 7) * s
+    x, y, z = np.meshgrid(i, i, i, indexing="ij")
+    xyz = np.stack([x.ravel(), y.ravel(), z.ravel()], 1).astype(np.float32)
+    fr = O.build_frame(xyz, H)
+    d64 = O.density(fr, np.zeros((1, 3), np.float32), precision=64)[0]
+    # positions are float32, so the sum differs from the exact lattice in the 8th digit
+    assert d64 == pytest.approx(scenes.lattice_rest_density(s, H), rel=1e-6)
+
+
+def test_single_particle_sphere_hit():
+    """One particle: the iso surface of W is a sphere; the bisected hit lies on it."""
+    H = 0.1
+    xyz = np.array([[0.0, 0.0, 0.0]], np.float32)
+    fr = O.build_frame(xyz, H)
+    iso = np.float32(sigma(H) * 0.25)  # W = sigma/4 at q = 0.5
+    cam = scenes.make_camera((0.0, 0.0, -1.0), (0.0, 0.0, 0.0), 129, 129)
+    depth = O.splat(xyz, H, cam)
+    out = O.march(fr, cam, float(iso), 0.002, 400, 12, depth, threads=1)
+    hit = out["position"][:, 3] == 1
+    # iso sphere radius 0.05 at distance 1 with a 60 degree view: about 5.6 pixels across
+    assert hit.sum() > 40
+    r = np.linalg.norm(out["position"][hit, :3], axis=1)
+    assert np.allclose(r, 0.5 * H, atol=2e-6)
+    centre = 64 * 129 + 64
+    assert hit[centre]
+    # the normal points away from the fluid (towards the camera at the centre pixel)
+    n = out["normal"][centre, :3]
+    assert n[2] < -0.99
+
+
+def test_splat_single_particle_centre_depth():
+    H = 0.1
+    xyz = np.array([[0.0, 0.0, 0.0]], np.float32)
+    cam = scenes.make_camera((0.0, 0.0, -1.0), (0.0, 0.0, 0.0), 31, 31)
+    depth = O.splat(xyz, H, cam).reshape(31, 31)
+    P = cam.proj.astype(np.float64)
+    zv = 1.0 - H
+    expect = (P[10] * zv + P[14]) / (P[11] * zv + P[15])
+    assert depth[15, 15] == pytest.approx(expect, abs=1e-6)
+    assert depth[0, 0] == 1.0
+
+
+def test_fp64_twin_close_to_fp32():
+    sc = scenes.small_scene(seed=4, n=4000, width=64, height=48)
+    cam = sc.cameras[0]
+    fr = O.build_frame(sc.xyz, sc.support)
+    depth = O.splat(sc.xyz, sc.support, cam)
+    # 12 bisections: the final interval (step / 4096) is well below the 1e-4 extent tolerance
+    a = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 12, depth, threads=4, precision=32)
+    b = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 12, depth, threads=4, precision=64)
+    ha, hb = a["position"][:, 3] == 1, b["position"][:, 3] == 1
+    assert (ha != hb).sum() <= 2
+    both = ha & hb
+    ext = float(np.max(sc.xyz.max(0) - sc.xyz.min(0)))
+    assert np.quantile(np.abs(a["depth"][both] - b["depth"][both]), 0.999) < 1e-4 * ext
