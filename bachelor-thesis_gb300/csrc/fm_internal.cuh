@@ -102,6 +102,23 @@ __device__ __forceinline__ bool sample_cell(const GridDev& g, float px, float py
     return true;
 }
 
+// True when sample p lies beyond the grid's evaluation range (the range in
+// which sample_cell succeeds) on some axis and the step s points further away
+// on that axis.  FP32 addition of a same-signed step is monotone, so every
+// later sample stays out there and has density exactly 0: the march can stop
+// with a miss and produce the same outputs as running to max_steps.
+__device__ __forceinline__ bool outside_forever(const GridDev& g, float px, float py, float pz, float sx, float sy,
+                                                float sz) {
+    const float p[3] = {px, py, pz}, s[3] = {sx, sy, sz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float f = floorf((p[a] - g.min[a]) * g.inv);
+        if (f > (float)g.dims[a] + 1.0f && s[a] >= 0.0f) return true;
+        if (f < -2.0f && s[a] <= 0.0f) return true;
+    }
+    return false;
+}
+
 // ---- host-side objects ------------------------------------------------------
 
 struct DevBuf {

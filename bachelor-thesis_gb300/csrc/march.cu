@@ -240,6 +240,7 @@ __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
                 int cx, cy, cz;
                 float rho;
                 if (!sample_cell(a.g, p0, p1, p2, cx, cy, cz)) {
+                    if (outside_forever(a.g, p0, p1, p2, sx, sy, sz)) break;
                     if (STATS) acc.evals++;
                     rho = 0.0f;
                 } else {

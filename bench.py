@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--skip", default="exact", choices=["exact", "off"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="target CPU time of the cpu_baseline sample")
+    ap.add_argument("--width", type=int, default=1920)
+    ap.add_argument("--height", type=int, default=1080)
+    ap.add_argument("--profile", action="store_true", help="short plain run of --steps frames for ncu")
     return ap.parse_args()
 
 
@@ -235,51 +238,61 @@ def run_ours(args):
     import fluidmarch as fm
     from fluidmarch import scenes
 
-    sc = scenes.sloshing(seed=1000 + rank)
+    sc = scenes.sloshing(seed=1000 + rank, width=args.width, height=args.height)
     cam = sc.cameras[0]
     npx = cam.width * cam.height
     skip = fm.FM_SKIP_EXACT if args.skip == "exact" else fm.FM_SKIP_OFF
     ctx = fm.Context(local)
+    # every launch, the L2 flush and the timing events go to the context's own stream
+    ext = torch.cuda.ExternalStream(ctx.stream, device=torch.device("cuda", local))
     xyz_d = torch.from_numpy(sc.xyz).cuda()
+    torch.cuda.synchronize()
     scene = fm.Scene(ctx, xyz_d, sc.support)
     dev = torch.device("cuda", local)
     out = {"position": torch.empty((npx, 4), device=dev), "normal": torch.empty((npx, 4), device=dev),
            "depth": torch.empty(npx, device=dev), "colour": torch.empty((npx, 4), device=dev),
            "start_depth": torch.empty(npx, device=dev)}
-    stream = torch.cuda.current_stream().cuda_stream
+    torch.cuda.synchronize()
     P_ext = fm.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, skip, external_depth=True)
 
     def frame():
-        fm.splat_depth(scene, cam, out["start_depth"], stream=stream)
-        fm.march(scene, cam, P_ext, out["position"], out["normal"], out["depth"], out["colour"], out["start_depth"],
-                 stream=stream)
+        fm.splat_depth(scene, cam, out["start_depth"])
+        fm.march(scene, cam, P_ext, out["position"], out["normal"], out["depth"], out["colour"], out["start_depth"])
 
     # counters for the algorithmic bytes (untimed run)
     ctx.set_stats(True)
     frame()
-    torch.cuda.synchronize()
+    ctx.sync()
     st = ctx.stats()
     ctx.set_stats(False)
 
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device=dev)
     for _ in range(args.warmup):
         frame()
-    torch.cuda.synchronize()
+    ctx.sync()
+    if args.profile:
+        # a short, plain run for ncu (no e2e, no CPU baseline)
+        for _ in range(args.steps):
+            frame()
+        ctx.sync()
+        print(json.dumps({"profile_run": True, "frames": args.steps, "march_counters": st}))
+        return
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
            torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    ctx.sync()
+    with ClockSampler(local) as clk, torch.cuda.stream(ext):
         for e0, e1, e2 in ev:
             flush.zero_()
-            e0.record()
-            fm.splat_depth(scene, cam, out["start_depth"], stream=stream)
-            e1.record()
+            e0.record(ext)
+            fm.splat_depth(scene, cam, out["start_depth"])
+            e1.record(ext)
             fm.march(scene, cam, P_ext, out["position"], out["normal"], out["depth"], out["colour"],
-                     out["start_depth"], stream=stream)
-            e2.record()
-        torch.cuda.synchronize()
+                     out["start_depth"])
+            e2.record(ext)
+        ext.synchronize()
     if dist:
         dist.barrier()
     total_ms = sum(e0.elapsed_time(e2) for e0, _, e2 in ev)
@@ -339,7 +352,7 @@ def run_ours(args):
                                  "served from L1/L2, so frac > 1 means on-chip reuse"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * sc.n,
                     "d2h_bytes_per_step": npx * (16 + 16 + 4 + 16)},
-            "gpu_launches": 3 * args.steps,
+            "gpu_launches": 3 * args.steps,  # fill + splat + march per frame
             "clocks": clk.summary(),
         }
         if world == 1 and not args.no_cpu_baseline:

@@ -183,6 +183,19 @@ template <typename T> inline bool sample_cell(const OrcGrid& g, V3<T> p, int& cx
 
 struct EvalStats { int64_t evals = 0; int64_t candidates = 0; };
 
+// floor((p - min) * inv) leaves [-2, dims + 1] on an axis and the step moves
+// further out on it (monotone FP addition): all later densities are 0.
+template <typename T> inline bool outside_forever(const OrcGrid& g, V3<T> p, V3<T> s) {
+    const T pa[3] = {p.x, p.y, p.z}, sa[3] = {s.x, s.y, s.z};
+    for (int a = 0; a < 3; ++a) {
+        T f = std::is_same<T, float>::value ? T(std::floor((float(pa[a]) - g.min[a]) * g.inv))
+                                            : std::floor((pa[a] - T(g.min[a])) * (T(1) / T(g.cell)));
+        if (f > T(g.dims[a]) + T(1) && sa[a] >= T(0)) return true;
+        if (f < T(-2) && sa[a] <= T(0)) return true;
+    }
+    return false;
+}
+
 // Visit the canonical neighbour list of cell (cx,cy,cz): rows (z, y) in
 // increasing order, each row a contiguous sorted range over x-1..x+1.
 template <typename F> inline void for_rows(const Scene& s, int cx, int cy, int cz, F&& f) {
@@ -370,6 +383,9 @@ void march_pixel(const Scene& s, const OrcCamera& cam, const OrcParams& P, const
                     p = V3<T>{T(pf.x), T(pf.y), T(pf.z)};
                 }
             }
+            // Past the grid's evaluation range on an axis the step moves away from:
+            // every later sample has density 0, so stop (same outputs as marching on).
+            if (outside_forever(s.g, p, step)) break;
             T rho = density(s, k, p, st);
             if (rho >= T(P.iso)) {
                 hit = true;
