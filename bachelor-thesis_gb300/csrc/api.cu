@@ -125,10 +125,23 @@ int fm_create(fm_ctx** out, int device) {
     return FM_OK;
 }
 
+static void scene_free(fm_scene* s) {
+    cudaFree(s->d_pts);
+    cudaFree(s->d_cell);
+    cudaFree(s->d_perm);
+    cudaFree(s->d_sub);
+    cudaFree(s->d_bound);
+    cudaFree(s->d_flag);
+    delete s;
+}
+
 void fm_destroy(fm_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    // scenes still alive die with their context (their handles become invalid)
+    for (fm_scene* s : ctx->scenes) scene_free(s);
+    ctx->scenes.clear();
     for (auto& b : ctx->stage) cudaFree(b.p);
     for (auto& b : ctx->scratch) cudaFree(b.p);
     cudaFree(ctx->d_status);
@@ -238,6 +251,7 @@ int fm_scene_create(fm_ctx* ctx, const float* xyz, uint64_t n, uint32_t stride, 
         fm_scene_destroy(s);
         return rc;
     }
+    ctx->scenes.push_back(s);
     *out = s;
     return FM_OK;
 }
@@ -255,15 +269,15 @@ int fm_scene_update(fm_scene* s, const float* xyz, uint64_t n, uint32_t stride, 
 
 void fm_scene_destroy(fm_scene* s) {
     if (!s) return;
-    cudaSetDevice(s->ctx->device);
-    cudaStreamSynchronize(s->ctx->stream);
-    cudaFree(s->d_pts);
-    cudaFree(s->d_cell);
-    cudaFree(s->d_perm);
-    cudaFree(s->d_start);
-    cudaFree(s->d_bound);
-    cudaFree(s->d_flag);
-    delete s;
+    fm_ctx* ctx = s->ctx;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    for (size_t i = 0; i < ctx->scenes.size(); ++i)
+        if (ctx->scenes[i] == s) {
+            ctx->scenes.erase(ctx->scenes.begin() + i);
+            break;
+        }
+    scene_free(s);
 }
 
 int fm_scene_grid(const fm_scene* s, fm_grid_info* out) {
@@ -289,7 +303,9 @@ int fm_scene_download(const fm_scene* s, uint32_t* cell, uint32_t* sorted_index,
     FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     if (cell) FM_CUDA(ctx, cudaMemcpy(cell, s->d_cell, s->n * 4, cudaMemcpyDeviceToHost));
     if (sorted_index) FM_CUDA(ctx, cudaMemcpy(sorted_index, s->d_perm, s->n * 4, cudaMemcpyDeviceToHost));
-    if (cell_start) FM_CUDA(ctx, cudaMemcpy(cell_start, s->d_start, (s->ncells + 1) * 4, cudaMemcpyDeviceToHost));
+    // every 8th sub-cell start is a cell start (the last one is n)
+    if (cell_start)
+        FM_CUDA(ctx, cudaMemcpy2D(cell_start, 4, s->d_sub, 32, 4, s->ncells + 1, cudaMemcpyDeviceToHost));
     if (sorted_xyzw) FM_CUDA(ctx, cudaMemcpy(sorted_xyzw, s->d_pts, s->n * 16, cudaMemcpyDeviceToHost));
     return FM_OK;
 }
@@ -335,6 +351,7 @@ int fm_march_stats_get(fm_ctx* ctx, fm_march_stats* out) {
     out->evals = h[3];
     out->candidates = h[4];
     out->skipped = h[5];
+    out->tested = h[6];
     return FM_OK;
 }
 

@@ -11,6 +11,7 @@
 #include <stdint.h>
 
 #include <string>
+#include <vector>
 
 #include "../../include/fluidmarch.h"
 
@@ -24,9 +25,9 @@ struct GridDev {
     float inv;   // 1.0f / cell
     float cell;  // cell width = support radius
     int dims[3];
-    const float4* __restrict__ pts;       // cell-sorted particles (w = 0)
-    const uint32_t* __restrict__ start;   // n_cells + 1
-    const float* __restrict__ bound;      // per-cell density upper bound (FM_SKIP_EXACT) or null
+    const float4* __restrict__ pts;       // sorted particles (w = 0): cell, 2x2x2 sub-cell, input index
+    const uint32_t* __restrict__ sub;     // 8 * n_cells + 1 sub-cell starts; cell c = [sub[8c], sub[8c+8])
+    const float* __restrict__ bound;      // per sub-cell density upper bound (FM_SKIP_EXACT) or null
     const uint8_t* __restrict__ flag;     // per-cell reference skip flag (FM_SKIP_REFERENCE) or null
 };
 
@@ -142,6 +143,8 @@ struct fm_ctx {
     fm_march_stats last_stats{};
     // scratch for grid builds
     fm::DevBuf scratch[8];
+    // live scenes of this context; fm_destroy frees the ones still alive
+    std::vector<fm_scene*> scenes;
     void* h_pinned_small = nullptr;  // 256 bytes of pinned memory for small readbacks
 };
 
@@ -155,11 +158,11 @@ struct fm_scene {
     int dims[3] = {0, 0, 0};
     uint64_t ncells = 0;
     uint64_t cell_capacity = 0;
-    float4* d_pts = nullptr;       // cell-sorted
+    float4* d_pts = nullptr;       // sorted by cell, sub-cell, input index
     uint32_t* d_cell = nullptr;    // cell of each input particle
     uint32_t* d_perm = nullptr;    // input index of each sorted particle
-    uint32_t* d_start = nullptr;   // ncells + 1
-    float* d_bound = nullptr;      // per-cell density bound (lazy)
+    uint32_t* d_sub = nullptr;     // 8 * ncells + 1 sub-cell starts
+    float* d_bound = nullptr;      // per sub-cell density bound (lazy)
     uint8_t* d_flag = nullptr;     // per-cell reference flag (lazy)
     bool bound_valid = false;
     bool flag_valid = false;

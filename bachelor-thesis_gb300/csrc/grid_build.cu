@@ -10,13 +10,17 @@
 //   dims            ceil((max - min) / cell) (Dataset.cpp:102-104).
 //   cell index      floor((p - min) * (1/cell)), x + y*W + z*W*H
 //                   (QueryDensityGrid, Dataset.cpp:28-40).
-//   order           stable counting sort by cell (an LSD radix sort of the
-//                   cell key, 8 bits per pass, input index as the value), so
-//                   particles of a cell keep their input order.
-//   cell table      start[c] = exclusive prefix sum of the cell counts.
-// Data layout in HBM: float4 cell-sorted positions (16 B, one coalesced
-// 128-bit load per particle), uint32 cell start table (n_cells + 1), uint32
-// cell and sorted->input index arrays.
+//   order           stable counting sort by key = cell * 8 + sub-cell, where
+//                   the sub-cell splits each cell into 2x2x2 half-width slabs
+//                   (sx = frac(f) >= 0.5, sub = sx + 2 sy + 4 sz); an LSD radix
+//                   sort of the key, 8 bits per pass, input index as the
+//                   value, so particles of a sub-cell keep their input order.
+//   tables          sub[k] = exclusive prefix sum of the key counts
+//                   (8 * n_cells + 1 entries); cell c spans [sub[8c], sub[8c+8]).
+// Data layout in HBM: float4 sorted positions (16 B, one 128-bit load per
+// particle), the uint32 sub-cell start table, uint32 cell and sorted->input
+// index arrays.  The march reads whole cell rows as contiguous ranges and
+// skips sub-cells out of reach of a sample.
 
 #include <cuda_runtime.h>
 
@@ -106,24 +110,28 @@ struct GridParams {
 };
 
 // Per-particle cell (QueryDensityGrid formula; coordinates clamped into the
-// grid, which the support-radius padding guarantees for finite input) and
-// the cell histogram.
+// grid, which the support-radius padding guarantees for finite input), the
+// sort key cell * 8 + sub-cell, and the key histogram.
 __global__ void k_cells(const float* __restrict__ xyz, uint64_t n, uint32_t stride, GridParams g,
-                        uint32_t* __restrict__ cell, uint32_t* __restrict__ count) {
+                        uint32_t* __restrict__ cell, uint32_t* __restrict__ key, uint32_t* __restrict__ count) {
     uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* p = xyz + i * stride;
     int c[3];
+    uint32_t sub = 0;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        float f = floorf((p[a] - g.min[a]) * g.inv);
-        int v = (int)f;
+        float f = (p[a] - g.min[a]) * g.inv;
+        int v = (int)floorf(f);
         c[a] = min(max(v, 0), g.dims[a] - 1);
+        if (f - (float)c[a] >= 0.5f) sub |= 1u << a;
     }
     uint32_t lin = (uint32_t)c[0] + (uint32_t)c[1] * (uint32_t)g.dims[0] +
                    (uint32_t)c[2] * (uint32_t)g.dims[0] * (uint32_t)g.dims[1];
     cell[i] = lin;
-    atomicAdd(&count[lin], 1u);
+    uint32_t k = lin * 8u + sub;
+    key[i] = k;
+    atomicAdd(&count[k], 1u);
 }
 
 // ---- exclusive scan (uint32), multi-level ---------------------------------
@@ -172,7 +180,7 @@ __global__ void k_scan_add(uint32_t* __restrict__ out, uint64_t n, const uint32_
     out[i] += tile_offsets[i / kScanTile];
 }
 
-// out[i] = sum_{j<i} in[i]; in may equal out.  tmp needs scan_tmp_words(n).
+// Words of temporary storage exclusive_scan needs for n items.
 uint64_t scan_tmp_words(uint64_t n) {
     uint64_t w = 0;
     while (n > (uint64_t)kScanTile) {
@@ -182,6 +190,7 @@ uint64_t scan_tmp_words(uint64_t n) {
     return w + 64;
 }
 
+// out[i] = sum_{j<i} in[j]; in may equal out.
 void exclusive_scan(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* tmp, cudaStream_t st) {
     uint64_t tiles = (n + kScanTile - 1) / kScanTile;
     if (tiles <= 1) {
@@ -211,7 +220,11 @@ __global__ void k_radix_hist(const uint32_t* __restrict__ keys, uint64_t n, int 
     hist[(uint64_t)threadIdx.x * nblocks + blockIdx.x] = h[threadIdx.x];
 }
 
-// vals_in == nullptr: the value is the element index (first pass).
+// Scatter one digit pass.  Elements keep their order within a digit: a tile
+// is walked in rounds of 256 consecutive elements, ranks inside a round come
+// from warp match masks plus per-warp digit counts, and blocks are ordered by
+// the digit-major scanned histogram.  vals_in == nullptr: the value is the
+// element index (first pass).
 __global__ void k_radix_scatter(const uint32_t* __restrict__ keys_in, const uint32_t* __restrict__ vals_in,
                                 uint32_t* __restrict__ keys_out, uint32_t* __restrict__ vals_out, uint64_t n,
                                 int shift, uint32_t nblocks, const uint32_t* __restrict__ offs) {
@@ -267,50 +280,70 @@ __global__ void k_gather(const float* __restrict__ xyz, uint64_t n, uint32_t str
     out[k] = make_float4(p[0], p[1], p[2], 0.0f);
 }
 
-// Per-cell upper bound of the density any sample inside the cell can reach:
-// sum over the 27-neighbourhood particles of W at the particle's distance to
-// the (slightly enlarged) cell box, inflated by a rounding margin that covers
-// the FP32 summation error of up to n terms.  One warp per cell.
+// Upper bound of the density any sample inside a sub-cell can reach: the sum
+// over the particles of the cell's 27-neighbourhood (the sample's candidate
+// set) of W at the particle's distance to the sub-cell box (shrunk by a slack
+// that covers the rounding of the sample's cell assignment), inflated by a
+// margin that covers the FP32 summation error of up to n terms.  One warp per
+// cell computes its 8 sub-cell bounds.
 __global__ void k_cell_bound(GridDev g, KernelDev k, float slack, float* __restrict__ bound) {
     uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
     uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
     int l = threadIdx.x % kWarp;
     if (c >= ncells) return;
-    int cx = (int)(c % (uint64_t)g.dims[0]);
-    int cy = (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]);
-    int cz = (int)(c / ((uint64_t)g.dims[0] * g.dims[1]));
-    float b0[3], b1[3];
-    int cc[3] = {cx, cy, cz};
+    int cc[3] = {(int)(c % (uint64_t)g.dims[0]), (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]),
+                 (int)(c / ((uint64_t)g.dims[0] * g.dims[1]))};
+    // slab edges: lo, mid, hi of the cell per axis
+    float e0[3], e1[3], e2[3];
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
-        b0[a] = g.min[a] + (float)cc[a] * g.cell;
-        b1[a] = b0[a] + g.cell;
+        e0[a] = g.min[a] + (float)cc[a] * g.cell;
+        e1[a] = g.min[a] + ((float)cc[a] + 0.5f) * g.cell;
+        e2[a] = e0[a] + g.cell;
     }
-    float acc = 0.0f;
+    float acc[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) acc[s] = 0.0f;
     uint32_t cnt = 0;
-    int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.dims[0] - 1);
-    for (int z = max(cz - 1, 0); z <= min(cz + 1, g.dims[2] - 1); ++z)
-        for (int y = max(cy - 1, 0); y <= min(cy + 1, g.dims[1] - 1); ++y) {
-            uint64_t row = ((uint64_t)z * g.dims[1] + y) * g.dims[0];
-            uint32_t b = g.start[row + x0], e = g.start[row + x1 + 1];
+    const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, g.dims[0] - 1);
+    for (int z = max(cc[2] - 1, 0); z <= min(cc[2] + 1, g.dims[2] - 1); ++z)
+        for (int y = max(cc[1] - 1, 0); y <= min(cc[1] + 1, g.dims[1] - 1); ++y) {
+            const uint64_t row = ((uint64_t)z * g.dims[1] + y) * g.dims[0];
+            const uint32_t b = g.sub[8 * (row + x0)], e = g.sub[8 * (row + x1) + 8];
             cnt += e - b;
             for (uint32_t j = b + l; j < e; j += kWarp) {
-                float4 q = g.pts[j];
-                float dx = fmaxf(fmaxf(b0[0] - q.x, q.x - b1[0]), 0.0f);
-                float dy = fmaxf(fmaxf(b0[1] - q.y, q.y - b1[1]), 0.0f);
-                float dz = fmaxf(fmaxf(b0[2] - q.z, q.z - b1[2]), 0.0f);
-                float d = fmaxf(sqrtf(dx * dx + dy * dy + dz * dz) - slack, 0.0f);
-                float q2 = d * d;
-                if (q2 < k.h2) acc += w_in(k, q2);
+                const float4 q = g.pts[j];
+                const float qa[3] = {q.x, q.y, q.z};
+                float dlo[3], dhi[3];  // distance per axis to the lower / upper half slab
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    dlo[a] = fmaxf(fmaxf(e0[a] - qa[a], qa[a] - e1[a]), 0.0f);
+                    dhi[a] = fmaxf(fmaxf(e1[a] - qa[a], qa[a] - e2[a]), 0.0f);
+                }
+#pragma unroll
+                for (int s = 0; s < 8; ++s) {
+                    float dx = (s & 1) ? dhi[0] : dlo[0];
+                    float dy = (s & 2) ? dhi[1] : dlo[1];
+                    float dz = (s & 4) ? dhi[2] : dlo[2];
+                    float d = fmaxf(sqrtf(dx * dx + dy * dy + dz * dz) - slack, 0.0f);
+                    float q2 = d * d;
+                    if (q2 < k.h2) acc[s] += w_in(k, q2);
+                }
             }
         }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (l == 0) {
+    for (int s = 0; s < 8; ++s)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
+    if (l < 8) {
         const float eps = 5.9604645e-8f;  // 2^-24
         float n = (float)cnt;
-        float up = acc * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
-        bound[c] = (cnt == 0) ? 0.0f : up;
+        float a = acc[0];
+#pragma unroll
+        for (int s = 1; s < 8; ++s)
+            if (l == s) a = acc[s];
+        float up = a * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
+        bound[8 * c + l] = (cnt == 0) ? 0.0f : up;
     }
 }
 
@@ -333,7 +366,7 @@ __global__ void k_ref_flags(GridDev g, float W0, uint8_t* __restrict__ flag) {
                 const float C = 1000.0f;
                 const float r = (float)(abs(dx) + abs(dy) + abs(dz));
                 const float wgt = expf(-C * r);
-                Nc = Nc + wgt * (float)(g.start[cc + 1] - g.start[cc]);
+                Nc = Nc + wgt * (float)(g.sub[8 * cc + 8] - g.sub[8 * cc]);
             }
     float rho = Nc * W0;
     flag[c] = rho > 1.0f ? 1 : 0;
@@ -360,7 +393,7 @@ GridDev grid_dev(const fm_scene* s) {
     g.inv = s->inv;
     g.cell = 1.0f * s->support;
     g.pts = s->d_pts;
-    g.start = s->d_start;
+    g.sub = s->d_sub;
     g.bound = s->bound_valid ? s->d_bound : nullptr;
     g.flag = s->flag_valid ? s->d_flag : nullptr;
     return g;
@@ -404,53 +437,56 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     s->ncells = ncells;
     s->bound_valid = false;
     s->flag_valid = false;
+    const uint64_t nkeys = 8 * ncells;
     if (ncells > s->cell_capacity) {
-        cudaFree(s->d_start);
+        cudaFree(s->d_sub);
         cudaFree(s->d_bound);
         cudaFree(s->d_flag);
-        s->d_start = nullptr; s->d_bound = nullptr; s->d_flag = nullptr;
-        if (cudaMalloc(&s->d_start, (ncells + 1) * sizeof(uint32_t)) != cudaSuccess ||
-            cudaMalloc(&s->d_bound, ncells * sizeof(float)) != cudaSuccess ||
+        s->d_sub = nullptr; s->d_bound = nullptr; s->d_flag = nullptr;
+        if (cudaMalloc(&s->d_sub, (nkeys + 1) * sizeof(uint32_t)) != cudaSuccess ||
+            cudaMalloc(&s->d_bound, nkeys * sizeof(float)) != cudaSuccess ||
             cudaMalloc(&s->d_flag, ncells) != cudaSuccess) {
             s->cell_capacity = 0;
             return set_err(ctx, FM_ERR_OOM, "cell table allocation failed");
         }
         s->cell_capacity = ncells;
     }
-    // 3. cells + histogram
+    // 3. cells, keys, key histogram
     GridParams gp;
     for (int a = 0; a < 3; ++a) { gp.min[a] = s->min[a]; gp.dims[a] = s->dims[a]; }
     gp.inv = s->inv;
     const uint64_t nblk = (n + kSortTile - 1) / kSortTile;
     const uint64_t hist_n = 256 * nblk;
-    const uint64_t scan_n = std::max<uint64_t>(ncells + 1, hist_n);
-    if (!ensure_buf(ctx->scratch[1], (ncells + 1) * sizeof(uint32_t)) ||  // counts
+    const uint64_t scan_n = std::max<uint64_t>(nkeys + 1, hist_n);
+    if (!ensure_buf(ctx->scratch[1], (nkeys + 1) * sizeof(uint32_t)) ||  // counts
         !ensure_buf(ctx->scratch[2], n * sizeof(uint32_t)) ||            // keys b
         !ensure_buf(ctx->scratch[3], n * sizeof(uint32_t)) ||            // vals b
         !ensure_buf(ctx->scratch[4], n * sizeof(uint32_t)) ||            // keys a
         !ensure_buf(ctx->scratch[5], hist_n * sizeof(uint32_t)) ||       // hist
-        !ensure_buf(ctx->scratch[6], scan_tmp_words(scan_n) * sizeof(uint32_t)))
+        !ensure_buf(ctx->scratch[6], scan_tmp_words(scan_n) * sizeof(uint32_t)) ||
+        !ensure_buf(ctx->scratch[7], n * sizeof(uint32_t)))              // keys (input order)
         return set_err(ctx, FM_ERR_OOM, "grid build scratch allocation failed");
     uint32_t* counts = (uint32_t*)ctx->scratch[1].p;
-    FM_CUDA(ctx, cudaMemsetAsync(counts, 0, (ncells + 1) * sizeof(uint32_t), st));
-    k_cells<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_xyz, n, stride, gp, s->d_cell, counts);
+    uint32_t* keys0 = (uint32_t*)ctx->scratch[7].p;
+    FM_CUDA(ctx, cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
+    k_cells<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_xyz, n, stride, gp, s->d_cell, keys0, counts);
     FM_CUDA(ctx, cudaGetLastError());
     uint32_t* tmp = (uint32_t*)ctx->scratch[6].p;
-    exclusive_scan(counts, s->d_start, ncells + 1, tmp, st);
+    exclusive_scan(counts, s->d_sub, nkeys + 1, tmp, st);
     FM_CUDA(ctx, cudaGetLastError());
-    // 4. stable LSD radix sort of (cell, index)
+    // 4. stable LSD radix sort of (key, index)
     int bits = 1;
-    while (bits < 32 && (ncells - 1) >> bits) ++bits;
-    const uint32_t* kin = s->d_cell;
+    while (bits < 32 && ((nkeys - 1) >> bits)) ++bits;
+    const uint32_t* kin = keys0;
     const uint32_t* vin = nullptr;
     uint32_t* kbuf[2] = {(uint32_t*)ctx->scratch[4].p, (uint32_t*)ctx->scratch[2].p};
     uint32_t* vbuf[2] = {s->d_perm, (uint32_t*)ctx->scratch[3].p};
     uint32_t* hist = (uint32_t*)ctx->scratch[5].p;
-    int passes = (bits + 7) / 8;
-    // final pass must land its values in s->d_perm
+    const int passes = (bits + 7) / 8;
+    // the last pass must land its values in s->d_perm
     int cur = (passes % 2 == 1) ? 0 : 1;
     for (int p = 0; p < passes; ++p) {
-        int shift = 8 * p;
+        const int shift = 8 * p;
         k_radix_hist<<<(unsigned)nblk, kSortThreads, 0, st>>>(kin, n, shift, (uint32_t)nblk, hist);
         exclusive_scan(hist, hist, hist_n, tmp, st);
         k_radix_scatter<<<(unsigned)nblk, kSortThreads, 0, st>>>(kin, vin, kbuf[cur], vbuf[cur], n, shift,
@@ -460,7 +496,7 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
         vin = vbuf[cur];
         cur ^= 1;
     }
-    // 5. gather cell-sorted float4 positions
+    // 5. gather sorted float4 positions
     k_gather<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_xyz, n, stride, s->d_perm, s->d_pts);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;

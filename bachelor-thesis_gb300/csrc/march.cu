@@ -9,20 +9,25 @@
 //                  p; hit at the first sample with rho >= iso      (:276-343)
 //   skip           FM_SKIP_REFERENCE: the reference's flag/jump loop
 //                  (:281-306, intersectAABB :51-62);  FM_SKIP_EXACT: samples in
-//                  cells whose density upper bound is below iso are stepped
+//                  sub-cells whose density upper bound is below iso are stepped
 //                  over without evaluating, so results equal skip-off exactly
 //   refinement     bisection between the last outside and first inside sample
 //   normal         normalize(sum_j gradW(x_j - p_hit)) (:332-338, Kernel.cpp:34-52)
 //   shading        composition.frag:132-184 fused into the epilogue
-// Summation order is the canonical order: cells in increasing linear index,
-// particles in cell-sorted order; every cell row (x-1..x+1 at fixed y, z) is
-// one contiguous range of the sorted float4 array.  With --fmad=false every
-// FP32 operation rounds like the reference's, so a pixel's result is
-// bit-identical to the CPU restatement.
 //
-// Launch shape: 128-thread blocks covering 16x8 pixels; each warp owns an 8x4
-// pixel tile, so the 32 rays of a warp sample neighbouring points and read the
-// same cell rows (their loads coalesce or broadcast in L1).
+// Summation order is the canonical order: the particles of the 27 cells in
+// sorted order (cell, 2x2x2 sub-cell, input index).  Sub-cells whose box is
+// out of reach of the sample (distance >= support radius, with a margin for
+// rounding) hold only particles with W = 0 and are skipped; every other
+// particle is added in order.  Since x + 0 = x exactly, a sum is bit-identical
+// to the reference loop over the same neighbour order.  With --fmad=false
+// every FP32 operation rounds like the reference's.
+//
+// Execution: each lane marches one ray as a small state machine (march,
+// bisect, normal, done); every loop iteration each live lane evaluates at most
+// one density, so lanes that march and lanes that bisect run the same code
+// path together.  128-thread blocks cover 16x8 pixels; a warp owns an 8x4
+// tile, so its rays read the same cell rows from L1.
 
 #include <cuda_runtime.h>
 
@@ -36,6 +41,7 @@ struct MarchArgs {
     KernelDev k;
     float iso, step;
     int max_steps, bisect, skip_mode;
+    float cull;  // squared reach in cell units (1 + margin)^2
     float ipv[16];
     float cam[3];
     float cdir[3];
@@ -51,68 +57,151 @@ struct MarchArgs {
 };
 
 constexpr int kTileW = 16, kTileH = 8, kThreads = 128;
+constexpr int kStats = 7;
 
 struct Acc {
     uint32_t evals = 0;
     uint64_t cand = 0;
+    uint64_t tested = 0;
     uint32_t skipped = 0;
 };
 
-// Density at p whose cell is (cx, cy, cz); canonical order.
-template <bool STATS>
-__device__ __forceinline__ float density_cell(const GridDev& g, const KernelDev& k, int cx, int cy, int cz,
-                                              float px, float py, float pz, Acc& acc) {
-    if (STATS) acc.evals++;
-    float rho = 0.0f;
-    const int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.dims[0] - 1);
-    if (x0 > x1) return rho;
-    const int z0 = max(cz - 1, 0), z1 = min(cz + 1, g.dims[2] - 1);
-    const int y0 = max(cy - 1, 0), y1 = min(cy + 1, g.dims[1] - 1);
-    for (int z = z0; z <= z1; ++z) {
-        for (int y = y0; y <= y1; ++y) {
-            const uint32_t row = ((uint32_t)z * (uint32_t)g.dims[1] + (uint32_t)y) * (uint32_t)g.dims[0];
-            const uint32_t b = __ldg(g.start + row + x0), e = __ldg(g.start + row + x1 + 1);
-            if (STATS) acc.cand += e - b;
-            for (uint32_t j = b; j < e; ++j) {
-                const float4 q = __ldg(g.pts + j);
-                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-                const float q2 = dot3(rx, ry, rz, rx, ry, rz);
-                if (q2 < k.h2) rho = rho + w_in(k, q2);
+// Location of a sample in the grid: cell and fractional position (cell units).
+struct Loc {
+    int c[3];
+    float u[3];
+};
+
+__device__ __forceinline__ bool locate(const GridDev& g, float px, float py, float pz, Loc& L) {
+    const float p[3] = {px, py, pz};
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        float f = (p[a] - g.min[a]) * g.inv;
+        float fl = floorf(f);
+        if (!(fl >= -2.0f && fl <= (float)g.dims[a] + 1.0f)) return false;
+        L.c[a] = (int)fl;
+        L.u[a] = f - fl;
+    }
+    return true;
+}
+
+__device__ __forceinline__ float slab_d2(float u, float lo) {
+    float d = fmaxf(fmaxf(lo - u, u - (lo + 0.5f)), 0.0f);
+    return d * d;
+}
+
+// Bit mask over the 24 sub-cells (3 cells x 8) of the row (cy+dy, cz+dz):
+// bit 8*i + sub for cell cx-1+i.  Set when the sub-cell box is within reach.
+__device__ __forceinline__ uint32_t row_mask(const float ax[6], float yz0, float yz1, float yz2, float yz3, float T) {
+    uint32_t m = 0;
+    const float yz[4] = {yz0, yz1, yz2, yz3};
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (ax[i] + yz[k] < T) m |= 1u << (8 * (i >> 1) + (i & 1) + 2 * k);
+    return m;
+}
+
+// Visit, in canonical order, the sorted ranges of every sub-cell within reach
+// of the sample; f(b, e) handles particles [b, e).
+template <bool STATS, typename F>
+__device__ __forceinline__ void for_ranges(const GridDev& g, const Loc& L, float T, Acc& acc, F&& f) {
+    float ax[6], ay[6], az[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) {
+        const float lo = -1.0f + 0.5f * (float)i;
+        ax[i] = slab_d2(L.u[0], lo);
+        ay[i] = slab_d2(L.u[1], lo);
+        az[i] = slab_d2(L.u[2], lo);
+    }
+    const int W = g.dims[0], Hd = g.dims[1], D = g.dims[2];
+    uint32_t xvalid = 0;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int x = L.c[0] - 1 + i;
+        if (x >= 0 && x < W) xvalid |= 0xffu << (8 * i);
+    }
+    if (!xvalid) return;
+#pragma unroll
+    for (int dz = 0; dz < 3; ++dz) {
+        const int z = L.c[2] - 1 + dz;
+        if (z < 0 || z >= D) continue;
+#pragma unroll
+        for (int dy = 0; dy < 3; ++dy) {
+            const int y = L.c[1] - 1 + dy;
+            if (y < 0 || y >= Hd) continue;
+            const float yz0 = ay[2 * dy] + az[2 * dz], yz1 = ay[2 * dy + 1] + az[2 * dz];
+            const float yz2 = ay[2 * dy] + az[2 * dz + 1], yz3 = ay[2 * dy + 1] + az[2 * dz + 1];
+            const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
+            // base may wrap below 0 when cx == 0; only bits >= 8 are used then
+            const uint32_t base = 8u * (row + (uint32_t)L.c[0]) - 8u;
+            if (STATS) {
+                const int x0 = max(L.c[0] - 1, 0), x1 = min(L.c[0] + 1, W - 1);
+                acc.cand += __ldg(g.sub + 8u * (row + x1) + 8u) - __ldg(g.sub + 8u * (row + x0));
+            }
+            uint32_t m = row_mask(ax, yz0, yz1, yz2, yz3, T) & xvalid;
+            while (m) {
+                const int s = __ffs(m) - 1;
+                const int t = __ffs(~(m >> s)) - 1;  // length of the run of set bits at s
+                const uint32_t b = __ldg(g.sub + base + s), e = __ldg(g.sub + base + s + t);
+                m &= ~(((1u << t) - 1u) << s);
+                if (STATS) acc.tested += e - b;
+                f(b, e);
             }
         }
     }
+}
+
+// Density at p (canonical order).
+template <bool STATS>
+__device__ __forceinline__ float density_at(const GridDev& g, const KernelDev& k, const Loc& L, float px, float py,
+                                            float pz, float T, Acc& acc) {
+    if (STATS) acc.evals++;
+    float rho = 0.0f;
+    for_ranges<STATS>(g, L, T, acc, [&](uint32_t b, uint32_t e) {
+        uint32_t j = b;
+        for (; j + 4 <= e; j += 4) {
+            const float4 q0 = __ldg(g.pts + j), q1 = __ldg(g.pts + j + 1);
+            const float4 q2 = __ldg(g.pts + j + 2), q3 = __ldg(g.pts + j + 3);
+            float r0x = q0.x - px, r0y = q0.y - py, r0z = q0.z - pz;
+            float r1x = q1.x - px, r1y = q1.y - py, r1z = q1.z - pz;
+            float r2x = q2.x - px, r2y = q2.y - py, r2z = q2.z - pz;
+            float r3x = q3.x - px, r3y = q3.y - py, r3z = q3.z - pz;
+            const float d0 = dot3(r0x, r0y, r0z, r0x, r0y, r0z);
+            const float d1 = dot3(r1x, r1y, r1z, r1x, r1y, r1z);
+            const float d2 = dot3(r2x, r2y, r2z, r2x, r2y, r2z);
+            const float d3 = dot3(r3x, r3y, r3z, r3x, r3y, r3z);
+            if (d0 < k.h2) rho = rho + w_in(k, d0);
+            if (d1 < k.h2) rho = rho + w_in(k, d1);
+            if (d2 < k.h2) rho = rho + w_in(k, d2);
+            if (d3 < k.h2) rho = rho + w_in(k, d3);
+        }
+        for (; j < e; ++j) {
+            const float4 q = __ldg(g.pts + j);
+            const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+            const float d = dot3(rx, ry, rz, rx, ry, rz);
+            if (d < k.h2) rho = rho + w_in(k, d);
+        }
+    });
     return rho;
 }
 
 template <bool STATS>
-__device__ __forceinline__ float density(const GridDev& g, const KernelDev& k, float px, float py, float pz,
-                                         Acc& acc) {
-    int cx, cy, cz;
-    if (!sample_cell(g, px, py, pz, cx, cy, cz)) {
-        if (STATS) acc.evals++;
-        return 0.0f;
-    }
-    return density_cell<STATS>(g, k, cx, cy, cz, px, py, pz, acc);
-}
-
-__device__ __forceinline__ void grad_sum(const GridDev& g, const KernelDev& k, float px, float py, float pz, float& gx, float& gy,
-                         float& gz) {
+__device__ __forceinline__ void grad_at(const GridDev& g, const KernelDev& k, float px, float py, float pz, float T,
+                                        Acc& acc, float& gx, float& gy, float& gz) {
     gx = gy = gz = 0.0f;
-    int cx, cy, cz;
-    if (!sample_cell(g, px, py, pz, cx, cy, cz)) return;
-    const int x0 = max(cx - 1, 0), x1 = min(cx + 1, g.dims[0] - 1);
-    if (x0 > x1) return;
-    for (int z = max(cz - 1, 0); z <= min(cz + 1, g.dims[2] - 1); ++z)
-        for (int y = max(cy - 1, 0); y <= min(cy + 1, g.dims[1] - 1); ++y) {
-            const uint32_t row = ((uint32_t)z * (uint32_t)g.dims[1] + (uint32_t)y) * (uint32_t)g.dims[0];
-            const uint32_t b = __ldg(g.start + row + x0), e = __ldg(g.start + row + x1 + 1);
-            for (uint32_t j = b; j < e; ++j) {
-                const float4 q = __ldg(g.pts + j);
-                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-                const float q2 = dot3(rx, ry, rz, rx, ry, rz);
-                if (q2 < k.h2 && q2 > 0.0f) gradw_acc(k, rx, ry, rz, q2, gx, gy, gz);
-            }
+    Loc L;
+    if (STATS) acc.evals++;
+    if (!locate(g, px, py, pz, L)) return;
+    for_ranges<STATS>(g, L, T, acc, [&](uint32_t b, uint32_t e) {
+        for (uint32_t j = b; j < e; ++j) {
+            const float4 q = __ldg(g.pts + j);
+            const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+            const float q2 = dot3(rx, ry, rz, rx, ry, rz);
+            if (q2 < k.h2 && q2 > 0.0f) gradw_acc(k, rx, ry, rz, q2, gx, gy, gz);
         }
+    });
 }
 
 // glm min/max semantics (func_common.inl): min(x,y) = y<x ? y : x, max(x,y) = x<y ? y : x
@@ -120,8 +209,8 @@ __device__ __forceinline__ float gmin(float x, float y) { return (y < x) ? y : x
 __device__ __forceinline__ float gmax(float x, float y) { return (x < y) ? y : x; }
 
 // The reference's empty-space skip loop (RayMarcher.cpp:284-306), capped.
-__device__ __forceinline__ void ref_skip(const GridDev& g, float& px, float& py, float& pz, float sx, float sy, float sz,
-                         unsigned int* status) {
+__device__ __forceinline__ void ref_skip(const GridDev& g, float& px, float& py, float& pz, float sx, float sy,
+                                         float sz, unsigned int* status) {
     for (int it = 0; it < (1 << 20); ++it) {
         float fx = floorf((px - g.min[0]) * g.inv);
         float fy = floorf((py - g.min[1]) * g.inv);
@@ -158,7 +247,6 @@ __device__ __forceinline__ float4 sample_floor(float ax, float ay, float az, flo
     float s = -1.0f - ay;
     float tx = (rx * s) / ry, tz = (rz * s) / ry;
     float bx = ax + tx, bz = az + tz;
-    (void)ry;
     float mx = bx - 2.0f * floorf(bx / 2.0f);
     float mz = bz - 2.0f * floorf(bz / 2.0f);
     float fx = (1.0f < mx) ? 0.0f : 1.0f;
@@ -168,8 +256,8 @@ __device__ __forceinline__ float4 sample_floor(float ax, float ay, float az, flo
 }
 
 // composition.frag:132-184, active branch.
-__device__ __forceinline__ float4 shade(const MarchArgs& a, int px, int py, bool hit, float hx, float hy, float hz, float nx, float ny,
-                        float nz) {
+__device__ __forceinline__ float4 shade(const MarchArgs& a, int px, int py, bool hit, float hx, float hy, float hz,
+                                        float nx, float ny, float nz) {
     float u = ((float)px + 0.5f) / (float)a.W;
     float v = ((float)py + 0.5f) / (float)a.Hh;
     float in0 = 2.0f * u - 1.0f, in1 = 2.0f * v - 1.0f;
@@ -204,20 +292,27 @@ __device__ __forceinline__ float4 shade(const MarchArgs& a, int px, int py, bool
                        f * fl.z + kd * (255.0f / 255.0f), f * fl.w + kd * (255.0f / 255.0f));
 }
 
+enum Phase : int { kMarch = 0, kBisect = 1, kNormal = 2, kDone = 3 };
+
 template <bool STATS>
 __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int px = blockIdx.x * kTileW + (warp & 1) * 8 + (lane & 7);
     const int py = blockIdx.y * kTileH + (warp >> 1) * 4 + (lane >> 3);
     const bool valid = px < a.W && py < a.Hh;
-    Acc acc;
-    bool hit = false, started = false;
-    float hx = 0.f, hy = 0.f, hz = 0.f, nx = 0.f, ny = 0.f, nz = 0.f;
     const uint64_t idx = (uint64_t)py * a.W + px;
+    Acc acc;
+    int phase = kDone;
+    bool hit = false, started = false;
+    float p0 = 0.f, p1 = 0.f, p2 = 0.f;        // current sample / upper bisection end
+    float q0 = 0.f, q1 = 0.f, q2 = 0.f;        // previous sample / lower bisection end
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    int i = 0, b = 0;
     if (valid) {
         const float z = a.zbuf[idx];
         if (z != 1.0f) {
             started = true;
+            phase = kMarch;
             const float cxp = (float)px * a.twoWinv - 1.0f;
             const float cyp = (float)py * a.twoHinv - 1.0f;
             float wh[4];
@@ -227,75 +322,107 @@ __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
                 float add1 = a.ipv[2 * 4 + r] * z + a.ipv[3 * 4 + r] * 1.0f;
                 wh[r] = add0 + add1;
             }
-            float p0 = wh[0] / wh[3], p1 = wh[1] / wh[3], p2 = wh[2] / wh[3];
+            p0 = wh[0] / wh[3];
+            p1 = wh[1] / wh[3];
+            p2 = wh[2] / wh[3];
             float dx = p0 - a.cam[0], dy = p1 - a.cam[1], dz = p2 - a.cam[2];
             float inv = 1.0f / sqrtf(dot3(dx, dy, dz, dx, dy, dz));
-            const float sx = a.step * (dx * inv), sy = a.step * (dy * inv), sz = a.step * (dz * inv);
-            float q0 = p0, q1 = p1, q2 = p2;  // previous sample
-            for (int i = 0; i < a.max_steps; ++i) {
-                p0 = p0 + sx;
-                p1 = p1 + sy;
-                p2 = p2 + sz;
+            sx = a.step * (dx * inv);
+            sy = a.step * (dy * inv);
+            sz = a.step * (dz * inv);
+            q0 = p0; q1 = p1; q2 = p2;
+        }
+    }
+    // one density evaluation per live lane per iteration
+    while (phase == kMarch || phase == kBisect) {
+        float e0, e1, e2;
+        bool eval = false, known = false;
+        float rho = 0.0f;
+        Loc L;
+        if (phase == kMarch) {
+            // advance to the next sample that needs its density
+            while (i < a.max_steps) {
+                p0 = p0 + sx; p1 = p1 + sy; p2 = p2 + sz;
+                ++i;
                 if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p0, p1, p2, sx, sy, sz, a.status);
-                int cx, cy, cz;
-                float rho;
-                if (!sample_cell(a.g, p0, p1, p2, cx, cy, cz)) {
-                    if (outside_forever(a.g, p0, p1, p2, sx, sy, sz)) break;
+                if (!locate(a.g, p0, p1, p2, L)) {
+                    if (outside_forever(a.g, p0, p1, p2, sx, sy, sz)) { i = a.max_steps; break; }
                     if (STATS) acc.evals++;
-                    rho = 0.0f;
-                } else {
-                    if (a.skip_mode == FM_SKIP_EXACT && cx >= 0 && cy >= 0 && cz >= 0 && cx < a.g.dims[0] &&
-                        cy < a.g.dims[1] && cz < a.g.dims[2]) {
-                        const uint32_t c = (uint32_t)cx + (uint32_t)cy * (uint32_t)a.g.dims[0] +
-                                           (uint32_t)cz * (uint32_t)a.g.dims[0] * (uint32_t)a.g.dims[1];
-                        if (__ldg(a.g.bound + c) < a.iso) {
-                            if (STATS) acc.skipped++;
-                            q0 = p0; q1 = p1; q2 = p2;
-                            continue;
-                        }
-                    }
-                    rho = density_cell<STATS>(a.g, a.k, cx, cy, cz, p0, p1, p2, acc);
-                }
-                if (rho >= a.iso) {
-                    hit = true;
+                    known = true;  // no particle within reach: density 0
                     break;
                 }
-                q0 = p0; q1 = p1; q2 = p2;
-            }
-            if (hit) {
-                float l0 = q0, l1 = q1, l2 = q2;
-                for (int b = 0; b < a.bisect; ++b) {
-                    float m0 = (l0 + p0) * 0.5f, m1 = (l1 + p1) * 0.5f, m2 = (l2 + p2) * 0.5f;
-                    float rho = density<STATS>(a.g, a.k, m0, m1, m2, acc);
-                    if (rho >= a.iso) { p0 = m0; p1 = m1; p2 = m2; }
-                    else { l0 = m0; l1 = m1; l2 = m2; }
+                if (a.skip_mode == FM_SKIP_EXACT && L.c[0] >= 0 && L.c[1] >= 0 && L.c[2] >= 0 &&
+                    L.c[0] < a.g.dims[0] && L.c[1] < a.g.dims[1] && L.c[2] < a.g.dims[2]) {
+                    const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)a.g.dims[0] +
+                                       (uint32_t)L.c[2] * (uint32_t)a.g.dims[0] * (uint32_t)a.g.dims[1];
+                    const uint32_t sc = (L.u[0] >= 0.5f ? 1u : 0u) | (L.u[1] >= 0.5f ? 2u : 0u) | (L.u[2] >= 0.5f ? 4u : 0u);
+                    if (__ldg(a.g.bound + 8u * c + sc) < a.iso) {
+                        if (STATS) acc.skipped++;
+                        q0 = p0; q1 = p1; q2 = p2;
+                        continue;
+                    }
                 }
-                hx = p0; hy = p1; hz = p2;
-                float gx, gy, gz;
-                grad_sum(a.g, a.k, hx, hy, hz, gx, gy, gz);
+                eval = true;
+                break;
+            }
+            if (!eval && !known) {  // march ended without a hit
+                phase = kDone;
+                break;
+            }
+            e0 = p0; e1 = p1; e2 = p2;
+        } else {
+            e0 = (q0 + p0) * 0.5f;
+            e1 = (q1 + p1) * 0.5f;
+            e2 = (q2 + p2) * 0.5f;
+            if (!locate(a.g, e0, e1, e2, L)) {
                 if (STATS) acc.evals++;
-                float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
-                nx = gx * gi; ny = gy * gi; nz = gz * gi;
+                known = true;
+            } else {
+                eval = true;
             }
         }
-        if (a.pos) a.pos[idx] = hit ? make_float4(hx, hy, hz, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (eval) rho = density_at<STATS>(a.g, a.k, L, e0, e1, e2, a.cull, acc);
+        const bool inside = rho >= a.iso;
+        if (phase == kMarch) {
+            if (inside) {
+                hit = true;
+                b = 0;
+                phase = a.bisect > 0 ? kBisect : kNormal;
+            } else {
+                q0 = p0; q1 = p1; q2 = p2;
+            }
+        } else {
+            if (inside) { p0 = e0; p1 = e1; p2 = e2; }
+            else { q0 = e0; q1 = e1; q2 = e2; }
+            if (++b >= a.bisect) phase = kNormal;
+        }
+    }
+    float nx = 0.f, ny = 0.f, nz = 0.f;
+    if (hit) {
+        float gx, gy, gz;
+        grad_at<STATS>(a.g, a.k, p0, p1, p2, a.cull, acc, gx, gy, gz);
+        float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+        nx = gx * gi; ny = gy * gi; nz = gz * gi;
+    }
+    if (valid) {
+        if (a.pos) a.pos[idx] = hit ? make_float4(p0, p1, p2, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
         if (a.nrm) a.nrm[idx] = hit ? make_float4(nx, ny, nz, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
         if (a.depth) {
             float d = 0.0f;
             if (hit) {
-                float rx = hx - a.cam[0], ry = hy - a.cam[1], rz = hz - a.cam[2];
+                float rx = p0 - a.cam[0], ry = p1 - a.cam[1], rz = p2 - a.cam[2];
                 d = sqrtf(dot3(rx, ry, rz, rx, ry, rz));
             }
             a.depth[idx] = d;
         }
-        if (a.col) a.col[idx] = shade(a, px, py, hit, hx, hy, hz, nx, ny, nz);
+        if (a.col) a.col[idx] = shade(a, px, py, hit, p0, p1, p2, nx, ny, nz);
     }
     if (STATS) {
-        unsigned long long v[6] = {valid ? 1ull : 0ull, started ? 1ull : 0ull, hit ? 1ull : 0ull,
-                                   (unsigned long long)acc.evals, (unsigned long long)acc.cand,
-                                   (unsigned long long)acc.skipped};
+        unsigned long long v[kStats] = {valid ? 1ull : 0ull, started ? 1ull : 0ull, hit ? 1ull : 0ull,
+                                        (unsigned long long)acc.evals, (unsigned long long)acc.cand,
+                                        (unsigned long long)acc.skipped, (unsigned long long)acc.tested};
 #pragma unroll
-        for (int j = 0; j < 6; ++j) {
+        for (int j = 0; j < kStats; ++j) {
             unsigned long long x = v[j];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
@@ -316,6 +443,12 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
     a.max_steps = p->max_steps;
     a.bisect = p->bisect_iters;
     a.skip_mode = p->skip_mode;
+    // reach of the support radius in cell units (cell width == support radius),
+    // widened to cover the rounding of (p - min) * inv on grids up to 10^6 cells
+    int maxdim = s->dims[0] > s->dims[1] ? s->dims[0] : s->dims[1];
+    maxdim = maxdim > s->dims[2] ? maxdim : s->dims[2];
+    const float reach = 1.0f + 1.0e-3f + 1.0e-6f * (float)maxdim;
+    a.cull = reach * reach;
     for (int i = 0; i < 16; ++i) a.ipv[i] = cam->inv_proj_view[i];
     for (int i = 0; i < 3; ++i) a.cam[i] = cam->position[i];
     a.cdir[0] = cam->view[2];

@@ -16,6 +16,7 @@ from __future__ import annotations
 
 import ctypes as C
 import os
+import weakref
 from dataclasses import dataclass
 
 import numpy as np
@@ -66,7 +67,7 @@ class CGridInfo(C.Structure):
 
 class CMarchStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("started", C.c_uint64), ("hits", C.c_uint64), ("evals", C.c_uint64),
-                ("candidates", C.c_uint64), ("skipped", C.c_uint64)]
+                ("candidates", C.c_uint64), ("skipped", C.c_uint64), ("tested", C.c_uint64)]
 
 
 _lib = None
@@ -142,6 +143,7 @@ class Context:
         if rc != FM_OK:
             raise FmError(rc, f"fm_create(device={device}) failed")
         self.h = h
+        self._scenes = weakref.WeakSet()
 
     def check(self, rc: int):
         if rc != FM_OK:
@@ -169,7 +171,10 @@ class Context:
         return {k: int(getattr(s, k)) for k, _ in CMarchStats._fields_}
 
     def close(self):
+        """Destroy the context; its scenes that are still open are closed first."""
         if getattr(self, "h", None):
+            for sc in list(self._scenes):
+                sc.close()
             self.L.fm_destroy(self.h)
             self.h = None
 
@@ -191,6 +196,7 @@ class Scene:
         ctx.check(ctx.L.fm_scene_create(ctx.h, p, n, int(stride), float(support), mem, C.byref(h)))
         self.h = h
         self.support = float(support)
+        ctx._scenes.add(self)
 
     def update(self, xyz, stride: int = 3):
         p, mem = _ptr(xyz)
@@ -216,7 +222,8 @@ class Scene:
 
     def close(self):
         if getattr(self, "h", None):
-            self.ctx.L.fm_scene_destroy(self.h)
+            if getattr(self.ctx, "h", None):  # a closed context already freed its scenes
+                self.ctx.L.fm_scene_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -296,6 +303,8 @@ class RayMarcher:
     def prepare(self, settings: MarchParams, camera, scene: Scene, positions, normals, depth):
         if positions is None or normals is None or depth is None:
             raise ValueError("positions, normals and depth buffers are required")
+        if scene.ctx is not self.ctx:
+            raise ValueError("the scene belongs to another context")
         self._args = (settings, camera, scene, positions, normals, depth)
 
     def start(self):

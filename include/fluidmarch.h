@@ -116,6 +116,7 @@ typedef struct fm_march_stats {
     uint64_t evals;         /* density evaluations (march samples + bisection + normal) */
     uint64_t candidates;    /* particles in the 27 cells of every evaluation */
     uint64_t skipped;       /* samples skipped by FM_SKIP_EXACT */
+    uint64_t tested;        /* particles actually tested: those of sub-cells within reach */
 } fm_march_stats;
 
 /* ---- context ------------------------------------------------------------ */
@@ -123,7 +124,9 @@ typedef struct fm_march_stats {
 /* RayMarcher::RayMarcher (RayMarcher.cpp:66-69): create a context bound to a
  * CUDA device, with its own non-blocking stream. */
 int fm_create(fm_ctx** out, int device);
-/* RayMarcher::Exit (RayMarcher.cpp:71-74): wait for work, free everything. */
+/* RayMarcher::Exit (RayMarcher.cpp:71-74): wait for work, free everything,
+ * including the scenes of this context that were not destroyed yet (their
+ * handles become invalid; destroy scenes first to keep them usable). */
 void fm_destroy(fm_ctx* ctx);
 /* Message of the last failing call on this context (never NULL). */
 const char* fm_last_error(const fm_ctx* ctx);

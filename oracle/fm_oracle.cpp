@@ -26,9 +26,10 @@
 // translation units compiled the same way, given the same neighbour order.
 //
 // Neighbour order (canonical order): the 27 cells around the sample's cell in
-// increasing linear cell index (z outer, y, x inner); inside a cell the
-// particles in the stable counting-sort order (increasing input index).  Because
-// particles are stored cell-sorted, this is the increasing sorted index.
+// increasing linear cell index (z outer, y, x inner); inside a cell by 2x2x2
+// sub-cell (sx + 2 sy + 4 sz), inside a sub-cell by increasing input index
+// (a stable counting sort).  Particles are stored in that order, so the
+// canonical order is the increasing sorted index.
 //
 // The FP64 twin runs the same march in double precision from the same inputs
 // (it keeps the FP32 cell table) and is the "FP64 re-evaluation" the parity
@@ -508,32 +509,40 @@ int orc_grid_params(const float* xyz, int64_t n, int32_t stride, float H, OrcGri
     return 0;
 }
 
-// Per-particle linear cell index, QueryDensityGrid formula (Dataset.cpp:28-40).
-void orc_cells(const float* xyz, int64_t n, int32_t stride, const OrcGrid* g, uint32_t* cell) {
+// Per-particle linear cell index, QueryDensityGrid formula (Dataset.cpp:28-40),
+// and the sort key cell * 8 + sub-cell: each cell is split into 2x2x2
+// sub-cells at half the cell width, sx = (f - floor(f) >= 0.5) per axis with
+// f = (p - min) * inv, sub = sx + 2 sy + 4 sz.  key may be null.
+void orc_cells(const float* xyz, int64_t n, int32_t stride, const OrcGrid* g, uint32_t* cell, uint32_t* key) {
     for (int64_t i = 0; i < n; ++i) {
         const float* p = xyz + i * stride;
-        // clamped into the grid; the support-radius padding keeps finite input inside
-        int x = std::min(std::max(int(std::floor((p[0] - g->min[0]) * g->inv)), 0), g->dims[0] - 1);
-        int y = std::min(std::max(int(std::floor((p[1] - g->min[1]) * g->inv)), 0), g->dims[1] - 1);
-        int z = std::min(std::max(int(std::floor((p[2] - g->min[2]) * g->inv)), 0), g->dims[2] - 1);
-        cell[i] = uint32_t(x) + uint32_t(y) * uint32_t(g->dims[0]) +
-                  uint32_t(z) * uint32_t(g->dims[0]) * uint32_t(g->dims[1]);
+        int c[3];
+        uint32_t sub = 0;
+        for (int a = 0; a < 3; ++a) {
+            float f = (p[a] - g->min[a]) * g->inv;
+            // clamped into the grid; the support-radius padding keeps finite input inside
+            c[a] = std::min(std::max(int(std::floor(f)), 0), g->dims[a] - 1);
+            if (f - float(c[a]) >= 0.5f) sub |= 1u << a;
+        }
+        cell[i] = uint32_t(c[0]) + uint32_t(c[1]) * uint32_t(g->dims[0]) +
+                  uint32_t(c[2]) * uint32_t(g->dims[0]) * uint32_t(g->dims[1]);
+        if (key) key[i] = cell[i] * 8u + sub;
     }
 }
 
-// Stable counting sort by cell: perm[k] = input index of the k-th sorted
-// particle, start[c] .. start[c+1] the sorted range of cell c.
-void orc_sort(const uint32_t* cell, int64_t n, int64_t ncells, uint32_t* perm, uint32_t* start) {
-    std::vector<uint32_t> cnt(size_t(ncells) + 1, 0);
-    for (int64_t i = 0; i < n; ++i) cnt[cell[i]]++;
+// Stable counting sort by key: perm[k] = input index of the k-th sorted
+// particle, start[c] .. start[c+1] the sorted range of key c.
+void orc_sort(const uint32_t* key, int64_t n, int64_t nkeys, uint32_t* perm, uint32_t* start) {
+    std::vector<uint32_t> cnt(size_t(nkeys) + 1, 0);
+    for (int64_t i = 0; i < n; ++i) cnt[key[i]]++;
     uint32_t acc = 0;
-    for (int64_t c = 0; c < ncells; ++c) {
+    for (int64_t c = 0; c < nkeys; ++c) {
         start[c] = acc;
         acc += cnt[c];
     }
-    start[ncells] = acc;
-    std::vector<uint32_t> cur(start, start + ncells);
-    for (int64_t i = 0; i < n; ++i) perm[cur[cell[i]]++] = uint32_t(i);
+    start[nkeys] = acc;
+    std::vector<uint32_t> cur(start, start + nkeys);
+    for (int64_t i = 0; i < n; ++i) perm[cur[key[i]]++] = uint32_t(i);
 }
 
 // Reference skip flags (Dataset.cpp:137-164) with each cell's particle count

@@ -63,7 +63,7 @@ def lib():
         L.orc_cos_poly.argtypes = [C.c_float]
         L.orc_gradW.argtypes = [C.c_float] * 4 + [_f32p]
         L.orc_grid_params.argtypes = [_f32p, C.c_int64, C.c_int32, C.c_float, C.POINTER(OrcGrid)]
-        L.orc_cells.argtypes = [_f32p, C.c_int64, C.c_int32, C.POINTER(OrcGrid), _u32p]
+        L.orc_cells.argtypes = [_f32p, C.c_int64, C.c_int32, C.POINTER(OrcGrid), _u32p, _u32p]
         L.orc_sort.argtypes = [_u32p, C.c_int64, C.c_int64, _u32p, _u32p]
         L.orc_ref_flags.argtypes = [_u32p, C.POINTER(OrcGrid), C.c_float, C.c_void_p]
         L.orc_splat.argtypes = [_f32p, C.c_int64, C.c_int32, C.c_float, C.POINTER(OrcCamera), _f32p]
@@ -114,9 +114,10 @@ class Frame:
     grid: OrcGrid
     cells: np.ndarray    # (N,) uint32 cell of each input particle
     perm: np.ndarray     # (N,) uint32 input index of each sorted particle
-    start: np.ndarray    # (ncells+1,) uint32
+    start: np.ndarray    # (ncells+1,) uint32 sorted range of each cell
     sorted: np.ndarray   # (N, 4) float32 cell-sorted xyz (w = 0)
     support: float
+    sub_start: np.ndarray = None
 
     @property
     def dims(self):
@@ -136,14 +137,16 @@ def build_frame(xyz: np.ndarray, support: float) -> Frame:
     if L.orc_grid_params(xyz, n, 3, support, C.byref(g)) != 0:
         raise ValueError("oracle grid: invalid input")
     cells = np.empty(n, np.uint32)
-    L.orc_cells(xyz, n, 3, C.byref(g), cells)
+    keys = np.empty(n, np.uint32)
+    L.orc_cells(xyz, n, 3, C.byref(g), cells, keys)
     ncells = int(g.dims[0]) * int(g.dims[1]) * int(g.dims[2])
     perm = np.empty(n, np.uint32)
-    start = np.empty(ncells + 1, np.uint32)
-    L.orc_sort(cells, n, ncells, perm, start)
+    sub_start = np.empty(8 * ncells + 1, np.uint32)
+    L.orc_sort(keys, n, 8 * ncells, perm, sub_start)
+    start = np.ascontiguousarray(sub_start[::8])
     srt = np.zeros((n, 4), np.float32)
     srt[:, :3] = xyz[perm]
-    return Frame(g, cells, perm, start, srt, float(support))
+    return Frame(g, cells, perm, start, srt, float(support), sub_start)
 
 
 def ref_flags(frame: Frame) -> np.ndarray:

@@ -11,8 +11,9 @@
 // Choices this stand-in makes (the real ordering is unpinned):
 //   * the spatial order is a stable counting sort by the linear cell index of
 //     the reference's density grid (origin = AABB min - r, width r, index
-//     x + y*W + z*W*H, Dataset.cpp:26-47,78-104), so point i of the sorted set
-//     is at sorted position i;
+//     x + y*W + z*W*H, Dataset.cpp:26-47,78-104), then by 2x2x2 sub-cell
+//     (half-width slabs, sx + 2 sy + 4 sz), so point i of the sorted set is at
+//     sorted position i;
 //   * find_neighbors lists the 27 cells around p in increasing linear index,
 //     each cell in sorted order (the canonical order of the CUDA path);
 //   * find_neighbors_box (a call of the reference's fork, Dataset.cpp:128)
@@ -72,12 +73,13 @@ public:
         for (auto& ps : m_Sets)
         {
             Build(ps);
-            std::vector<uint32_t> cnt(m_NumCells + 1, 0);
+            const std::size_t nkeys = 8 * m_NumCells;
+            std::vector<uint32_t> cnt(nkeys + 1, 0);
             std::vector<uint32_t> cell(ps.m_N);
-            for (std::size_t i = 0; i < ps.m_N; ++i) { cell[i] = CellOf(ps.m_X + 3 * i); cnt[cell[i]]++; }
-            std::vector<uint32_t> cur(m_NumCells + 1, 0);
+            for (std::size_t i = 0; i < ps.m_N; ++i) { cell[i] = KeyOf(ps.m_X + 3 * i); cnt[cell[i]]++; }
+            std::vector<uint32_t> cur(nkeys + 1, 0);
             uint32_t acc = 0;
-            for (std::size_t c = 0; c < m_NumCells; ++c) { cur[c] = acc; acc += cnt[c]; }
+            for (std::size_t c = 0; c < nkeys; ++c) { cur[c] = acc; acc += cnt[c]; }
             ps.m_Perm.assign(ps.m_N, 0);
             for (std::size_t i = 0; i < ps.m_N; ++i) ps.m_Perm[cur[cell[i]]++] = uint32_t(i);
         }
@@ -163,6 +165,22 @@ private:
         int y = int(std::floor((p[1] - m_Min[1]) * m_Inv));
         int z = int(std::floor((p[2] - m_Min[2]) * m_Inv));
         return uint32_t(x) + uint32_t(y) * uint32_t(m_Dims[0]) + uint32_t(z) * uint32_t(m_Dims[0]) * uint32_t(m_Dims[1]);
+    }
+
+    // cell * 8 + 2x2x2 sub-cell (sx + 2 sy + 4 sz, sx = frac >= 0.5)
+    uint32_t KeyOf(const float* p) const
+    {
+        int c[3];
+        uint32_t sub = 0;
+        for (int a = 0; a < 3; ++a)
+        {
+            float f = (p[a] - m_Min[a]) * m_Inv;
+            c[a] = std::min(std::max(int(std::floor(f)), 0), m_Dims[a] - 1);
+            if (f - float(c[a]) >= 0.5f) sub |= 1u << a;
+        }
+        uint32_t lin = uint32_t(c[0]) + uint32_t(c[1]) * uint32_t(m_Dims[0]) +
+                       uint32_t(c[2]) * uint32_t(m_Dims[0]) * uint32_t(m_Dims[1]);
+        return lin * 8u + sub;
     }
 
     bool SampleCell(const float* p, int& cx, int& cy, int& cz) const
