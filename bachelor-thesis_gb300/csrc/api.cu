@@ -177,7 +177,8 @@ int fm_sync(fm_ctx* ctx, int timeout_ms) {
         unsigned int code = h[0];
         cudaMemset(ctx->d_status, 0, sizeof(unsigned int));
         return set_err(ctx, FM_ERR_DEVICE, "kernel status word set: " + std::to_string(code) +
-                                               " (1 = reference skip loop reached its iteration cap)");
+                                               " (bit 1: reference skip loop reached its iteration cap;"
+                                               " bit 2: a march index guard fired)");
     }
     return FM_OK;
 }
@@ -421,7 +422,14 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
             if (user[i]) FM_CUDA(ctx, cudaMemcpyAsync(user[i], dev[i], npx * per[i], cudaMemcpyDeviceToHost, st));
         if (out->start_depth && !external)
             FM_CUDA(ctx, cudaMemcpyAsync(out->start_depth, z, npx * 4, cudaMemcpyDeviceToHost, st));
+        unsigned int* hs = (unsigned int*)ctx->h_pinned_small;
+        FM_CUDA(ctx, cudaMemcpyAsync(hs, ctx->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
         FM_CUDA(ctx, cudaStreamSynchronize(st));
+        if (hs[0] != 0) {
+            unsigned int code = hs[0];
+            cudaMemset(ctx->d_status, 0, sizeof(unsigned int));
+            return set_err(ctx, FM_ERR_DEVICE, "march kernel status word set: " + std::to_string(code));
+        }
     }
     return FM_OK;
 }

@@ -25,6 +25,7 @@ struct GridDev {
     float inv;   // 1.0f / cell
     float cell;  // cell width = support radius
     int dims[3];
+    uint32_t nsub;                        // 8 * n_cells + 1 (entries of sub)
     const float4* __restrict__ pts;       // sorted particles (w = 0): cell, 2x2x2 sub-cell, input index
     const uint32_t* __restrict__ sub;     // 8 * n_cells + 1 sub-cell starts; cell c = [sub[8c], sub[8c+8])
     const float* __restrict__ bound;      // per sub-cell density upper bound (FM_SKIP_EXACT) or null

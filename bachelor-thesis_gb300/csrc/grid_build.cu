@@ -394,6 +394,7 @@ GridDev grid_dev(const fm_scene* s) {
     g.cell = 1.0f * s->support;
     g.pts = s->d_pts;
     g.sub = s->d_sub;
+    g.nsub = (uint32_t)(8 * s->ncells + 1);
     g.bound = s->bound_valid ? s->d_bound : nullptr;
     g.flag = s->flag_valid ? s->d_flag : nullptr;
     return g;

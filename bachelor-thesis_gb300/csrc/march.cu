@@ -64,6 +64,7 @@ struct Acc {
     uint64_t cand = 0;
     uint64_t tested = 0;
     uint32_t skipped = 0;
+    bool bad = false;  // an index guard fired (reported through the status word, bit 2)
 };
 
 // Location of a sample in the grid: cell and fractional position (cell units).
@@ -134,7 +135,9 @@ __device__ __forceinline__ void for_ranges(const GridDev& g, const Loc& L, float
             const float yz0 = ay[2 * dy] + az[2 * dz], yz1 = ay[2 * dy + 1] + az[2 * dz];
             const float yz2 = ay[2 * dy] + az[2 * dz + 1], yz3 = ay[2 * dy + 1] + az[2 * dz + 1];
             const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
-            // base may wrap below 0 when cx == 0; only bits >= 8 are used then
+            // base wraps below 0 when row + cx == 0; then only bits >= 8 are set and
+            // base + s wraps back into range.  The index is always formed in uint32
+            // before it touches the pointer.
             const uint32_t base = 8u * (row + (uint32_t)L.c[0]) - 8u;
             if (STATS) {
                 const int x0 = max(L.c[0] - 1, 0), x1 = min(L.c[0] + 1, W - 1);
@@ -144,7 +147,12 @@ __device__ __forceinline__ void for_ranges(const GridDev& g, const Loc& L, float
             while (m) {
                 const int s = __ffs(m) - 1;
                 const int t = __ffs(~(m >> s)) - 1;  // length of the run of set bits at s
-                const uint32_t b = __ldg(g.sub + base + s), e = __ldg(g.sub + base + s + t);
+                const uint32_t i0 = base + (uint32_t)s, i1 = i0 + (uint32_t)t;
+                if (i1 >= g.nsub) {  // cannot happen for a consistent table; never read past it
+                    acc.bad = true;
+                    continue;
+                }
+                const uint32_t b = __ldg(g.sub + i0), e = __ldg(g.sub + i1);
                 m &= ~(((1u << t) - 1u) << s);
                 if (STATS) acc.tested += e - b;
                 f(b, e);
@@ -398,6 +406,7 @@ __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
         }
     }
     float nx = 0.f, ny = 0.f, nz = 0.f;
+    if (acc.bad) atomicOr(a.status, 2u);
     if (hit) {
         float gx, gy, gz;
         grad_at<STATS>(a.g, a.k, p0, p1, p2, a.cull, acc, gx, gy, gz);
