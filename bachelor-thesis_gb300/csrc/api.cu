@@ -114,6 +114,7 @@ int fm_create(fm_ctx** out, int device) {
         return FM_ERR_CUDA;
     }
     if (cudaMalloc(&ctx->d_status, 64) != cudaSuccess || cudaMalloc(&ctx->d_stats, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc(&ctx->d_work, fm::kWorkSlots * 32 * sizeof(unsigned int)) != cudaSuccess ||
         cudaHostAlloc(&ctx->h_pinned_small, 256, cudaHostAllocDefault) != cudaSuccess) {
         fm_destroy(ctx);
         return FM_ERR_OOM;
@@ -146,6 +147,7 @@ void fm_destroy(fm_ctx* ctx) {
     for (auto& b : ctx->scratch) cudaFree(b.p);
     cudaFree(ctx->d_status);
     cudaFree(ctx->d_stats);
+    cudaFree(ctx->d_work);
     if (ctx->h_pinned_small) cudaFreeHost(ctx->h_pinned_small);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

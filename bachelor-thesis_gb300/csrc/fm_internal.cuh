@@ -18,6 +18,7 @@
 namespace fm {
 
 constexpr int kWarp = 32;
+constexpr unsigned kWorkSlots = 64;
 
 // Uniform grid of a scene (Frame::m_Min, DensityGrid; Dataset.cpp:78-104).
 struct GridDev {
@@ -61,6 +62,29 @@ __device__ __forceinline__ float w_in(const KernelDev& k, float q2) {
         return k.sig * (((2.0f * q_) * q_) * q_);
     }
     return k.sig * (6.0f * (((q * q) * q) - (q * q)) + 1.0f);
+}
+
+// CubicSplineKernel::gradW for 0 < rn < h2 (Kernel.cpp:34-52): the term itself.
+__device__ __forceinline__ void gradw_term(const KernelDev& k, float rx, float ry, float rz, float rn, float& tx,
+                                           float& ty, float& tz) {
+    float rl = sqrtf(rn);
+    float q = rl * k.hinv;
+    float inv = 1.0f / sqrtf(rn);  // normalize(r) = r * inversesqrt(dot(r, r))
+    float den = rl * k.h;
+    float nx = (rx * inv) / den, ny = (ry * inv) / den, nz = (rz * inv) / den;
+    float ax, ay, az, s;
+    if (q >= 0.5f) {
+        float q_ = 1.0f - q;
+        s = (6.0f * q_) * q_;
+        float ns = -k.sig;
+        ax = ns * nx; ay = ns * ny; az = ns * nz;
+    } else {
+        s = 6.0f * (((3.0f * q) * q) - (2.0f * q));
+        ax = k.sig * nx; ay = k.sig * ny; az = k.sig * nz;
+    }
+    tx = ax * s;
+    ty = ay * s;
+    tz = az * s;
 }
 
 // CubicSplineKernel::gradW for 0 < rn < h2 (Kernel.cpp:34-52), accumulated
@@ -140,6 +164,10 @@ struct fm_ctx {
     // device status word + stats accumulators
     unsigned int* d_status = nullptr;
     unsigned long long* d_stats = nullptr;  // 8 counters
+    // work counters of persistent kernels: kWorkSlots slots of 32 words (one
+    // 128-byte line each), a fresh slot per launch
+    unsigned int* d_work = nullptr;
+    unsigned int work_slot = 0;
     int stats_enabled = 0;
     fm_march_stats last_stats{};
     // scratch for grid builds

@@ -16,18 +16,24 @@
 //   shading        composition.frag:132-184 fused into the epilogue
 //
 // Summation order is the canonical order: the particles of the 27 cells in
-// sorted order (cell, 2x2x2 sub-cell, input index).  Sub-cells whose box is
-// out of reach of the sample (distance >= support radius, with a margin for
-// rounding) hold only particles with W = 0 and are skipped; every other
-// particle is added in order.  Since x + 0 = x exactly, a sum is bit-identical
-// to the reference loop over the same neighbour order.  With --fmad=false
-// every FP32 operation rounds like the reference's.
+// sorted order (cell, 2x2x2 sub-cell, input index).  Sub-cells out of reach of
+// the sample (box distance >= support radius, with a margin for rounding) hold
+// only particles with W = 0 and are skipped; every other particle's W is added
+// in order.  x + 0 = x exactly, so each sum is bit-identical to the
+// reference's sequential loop over the same neighbour order; --fmad=false
+// makes every FP32 operation round as the reference's does.
 //
-// Execution: each lane marches one ray as a small state machine (march,
-// bisect, normal, done); every loop iteration each live lane evaluates at most
-// one density, so lanes that march and lanes that bisect run the same code
-// path together.  128-thread blocks cover 16x8 pixels; a warp owns an 8x4
-// tile, so its rays read the same cell rows from L1.
+// Execution (warp per ray): a persistent grid of warps takes 8x4-pixel tiles
+// from an atomic counter.  A warp first finishes the tile's pixels whose
+// splat depth is the clear value (misses) lane-parallel, then marches the
+// tile's remaining rays one at a time with all 32 lanes.  For each density
+// evaluation the lanes test the 24 sub-cells of a cell row against the sample
+// (one ballot gives the reach mask), walk the contiguous sorted ranges of the
+// reachable sub-cells 32 particles at a time (one coalesced 512-byte load),
+// compute W for in-support particles in parallel and add the terms to the
+// running sum in lane order through warp shuffles.  Every branch is
+// warp-uniform except the per-lane W evaluation, so no lane waits on another
+// ray's loop structure, and load balance is per tile.
 
 #include <cuda_runtime.h>
 
@@ -36,28 +42,32 @@
 namespace fm {
 namespace {
 
+constexpr unsigned kFull = 0xffffffffu;
+constexpr int kThreads = 256;  // 8 warps per block
+constexpr int kTileW = 8, kTileH = 4;
+constexpr int kStats = 7;
+
 struct MarchArgs {
     GridDev g;
     KernelDev k;
     float iso, step;
     int max_steps, bisect, skip_mode;
-    float cull;  // squared reach in cell units (1 + margin)^2
+    float cull;  // squared reach in cell units: (1 + margin)^2
     float ipv[16];
     float cam[3];
     float cdir[3];
     int W, Hh;
+    int tiles_x, ntiles;
     float twoWinv, twoHinv;
     const float* __restrict__ zbuf;
     float4* pos;
     float4* nrm;
     float* depth;
     float4* col;
+    unsigned int* tile_counter;
     unsigned long long* stats;
     unsigned int* status;
 };
-
-constexpr int kTileW = 16, kTileH = 8, kThreads = 128;
-constexpr int kStats = 7;
 
 struct Acc {
     uint32_t evals = 0;
@@ -86,74 +96,52 @@ __device__ __forceinline__ bool locate(const GridDev& g, float px, float py, flo
     return true;
 }
 
+// Squared distance (cell units) from fraction u to the half-cell slab [lo, lo + 0.5].
 __device__ __forceinline__ float slab_d2(float u, float lo) {
     float d = fmaxf(fmaxf(lo - u, u - (lo + 0.5f)), 0.0f);
     return d * d;
 }
 
-// Bit mask over the 24 sub-cells (3 cells x 8) of the row (cy+dy, cz+dz):
-// bit 8*i + sub for cell cx-1+i.  Set when the sub-cell box is within reach.
-__device__ __forceinline__ uint32_t row_mask(const float ax[6], float yz0, float yz1, float yz2, float yz3, float T) {
-    uint32_t m = 0;
-    const float yz[4] = {yz0, yz1, yz2, yz3};
-#pragma unroll
-    for (int i = 0; i < 6; ++i)
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            if (ax[i] + yz[k] < T) m |= 1u << (8 * (i >> 1) + (i & 1) + 2 * k);
-    return m;
-}
-
-// Visit, in canonical order, the sorted ranges of every sub-cell within reach
-// of the sample; f(b, e) handles particles [b, e).
+// Walk, in canonical order, the sorted ranges of the sub-cells within reach of
+// the sample at L.  Warp-uniform: every lane gets the same (b, e) sequence.
+// Lane l < 24 tests sub-cell (l & 7) of cell cx - 1 + (l >> 3) in each row.
 template <bool STATS, typename F>
-__device__ __forceinline__ void for_ranges(const GridDev& g, const Loc& L, float T, Acc& acc, F&& f) {
-    float ax[6], ay[6], az[6];
-#pragma unroll
-    for (int i = 0; i < 6; ++i) {
-        const float lo = -1.0f + 0.5f * (float)i;
-        ax[i] = slab_d2(L.u[0], lo);
-        ay[i] = slab_d2(L.u[1], lo);
-        az[i] = slab_d2(L.u[2], lo);
-    }
+__device__ __forceinline__ void for_ranges_warp(const GridDev& g, const Loc& L, float T, int lane, Acc& acc,
+                                                F&& f) {
     const int W = g.dims[0], Hd = g.dims[1], D = g.dims[2];
-    uint32_t xvalid = 0;
-#pragma unroll
-    for (int i = 0; i < 3; ++i) {
-        const int x = L.c[0] - 1 + i;
-        if (x >= 0 && x < W) xvalid |= 0xffu << (8 * i);
-    }
-    if (!xvalid) return;
-#pragma unroll
+    const int ci = lane >> 3, sb = lane & 7;
+    const int xl = L.c[0] - 1 + ci;
+    const bool lane_ok = lane < 24 && xl >= 0 && xl < W;
+    const float dx2 = slab_d2(L.u[0], -1.0f + 0.5f * (float)(2 * ci + (sb & 1)));
+#pragma unroll 1
     for (int dz = 0; dz < 3; ++dz) {
         const int z = L.c[2] - 1 + dz;
         if (z < 0 || z >= D) continue;
-#pragma unroll
+        const float dz2 = slab_d2(L.u[2], -1.0f + 0.5f * (float)(2 * dz + ((sb >> 2) & 1)));
+#pragma unroll 1
         for (int dy = 0; dy < 3; ++dy) {
             const int y = L.c[1] - 1 + dy;
             if (y < 0 || y >= Hd) continue;
-            const float yz0 = ay[2 * dy] + az[2 * dz], yz1 = ay[2 * dy + 1] + az[2 * dz];
-            const float yz2 = ay[2 * dy] + az[2 * dz + 1], yz3 = ay[2 * dy + 1] + az[2 * dz + 1];
+            const float dy2 = slab_d2(L.u[1], -1.0f + 0.5f * (float)(2 * dy + ((sb >> 1) & 1)));
+            uint32_t m = __ballot_sync(kFull, lane_ok && (dx2 + dy2 + dz2 < T));
             const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
             // base wraps below 0 when row + cx == 0; then only bits >= 8 are set and
-            // base + s wraps back into range.  The index is always formed in uint32
-            // before it touches the pointer.
+            // base + s wraps back into range.  Indices are formed in uint32 first.
             const uint32_t base = 8u * (row + (uint32_t)L.c[0]) - 8u;
             if (STATS) {
                 const int x0 = max(L.c[0] - 1, 0), x1 = min(L.c[0] + 1, W - 1);
-                acc.cand += __ldg(g.sub + 8u * (row + x1) + 8u) - __ldg(g.sub + 8u * (row + x0));
+                if (x0 <= x1) acc.cand += __ldg(g.sub + 8u * (row + (uint32_t)x1) + 8u) - __ldg(g.sub + 8u * (row + (uint32_t)x0));
             }
-            uint32_t m = row_mask(ax, yz0, yz1, yz2, yz3, T) & xvalid;
             while (m) {
                 const int s = __ffs(m) - 1;
                 const int t = __ffs(~(m >> s)) - 1;  // length of the run of set bits at s
+                m &= ~(((1u << t) - 1u) << s);
                 const uint32_t i0 = base + (uint32_t)s, i1 = i0 + (uint32_t)t;
                 if (i1 >= g.nsub) {  // cannot happen for a consistent table; never read past it
                     acc.bad = true;
                     continue;
                 }
                 const uint32_t b = __ldg(g.sub + i0), e = __ldg(g.sub + i1);
-                m &= ~(((1u << t) - 1u) << s);
                 if (STATS) acc.tested += e - b;
                 f(b, e);
             }
@@ -161,53 +149,63 @@ __device__ __forceinline__ void for_ranges(const GridDev& g, const Loc& L, float
     }
 }
 
-// Density at p (canonical order).
+// Density at p, identical on every lane (canonical order).
 template <bool STATS>
-__device__ __forceinline__ float density_at(const GridDev& g, const KernelDev& k, const Loc& L, float px, float py,
-                                            float pz, float T, Acc& acc) {
+__device__ __forceinline__ float density_warp(const GridDev& g, const KernelDev& k, const Loc& L, float px, float py,
+                                              float pz, float T, int lane, Acc& acc) {
     if (STATS) acc.evals++;
     float rho = 0.0f;
-    for_ranges<STATS>(g, L, T, acc, [&](uint32_t b, uint32_t e) {
-        uint32_t j = b;
-        for (; j + 4 <= e; j += 4) {
-            const float4 q0 = __ldg(g.pts + j), q1 = __ldg(g.pts + j + 1);
-            const float4 q2 = __ldg(g.pts + j + 2), q3 = __ldg(g.pts + j + 3);
-            float r0x = q0.x - px, r0y = q0.y - py, r0z = q0.z - pz;
-            float r1x = q1.x - px, r1y = q1.y - py, r1z = q1.z - pz;
-            float r2x = q2.x - px, r2y = q2.y - py, r2z = q2.z - pz;
-            float r3x = q3.x - px, r3y = q3.y - py, r3z = q3.z - pz;
-            const float d0 = dot3(r0x, r0y, r0z, r0x, r0y, r0z);
-            const float d1 = dot3(r1x, r1y, r1z, r1x, r1y, r1z);
-            const float d2 = dot3(r2x, r2y, r2z, r2x, r2y, r2z);
-            const float d3 = dot3(r3x, r3y, r3z, r3x, r3y, r3z);
-            if (d0 < k.h2) rho = rho + w_in(k, d0);
-            if (d1 < k.h2) rho = rho + w_in(k, d1);
-            if (d2 < k.h2) rho = rho + w_in(k, d2);
-            if (d3 < k.h2) rho = rho + w_in(k, d3);
-        }
-        for (; j < e; ++j) {
-            const float4 q = __ldg(g.pts + j);
-            const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-            const float d = dot3(rx, ry, rz, rx, ry, rz);
-            if (d < k.h2) rho = rho + w_in(k, d);
+    for_ranges_warp<STATS>(g, L, T, lane, acc, [&](uint32_t b, uint32_t e) {
+        for (uint32_t j0 = b; j0 < e; j0 += 32) {
+            const uint32_t j = j0 + (uint32_t)lane;
+            float w = 0.0f;
+            if (j < e) {
+                const float4 q = __ldg(g.pts + j);
+                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+                const float d2 = dot3(rx, ry, rz, rx, ry, rz);
+                if (d2 < k.h2) w = w_in(k, d2);
+            }
+            uint32_t bm = __ballot_sync(kFull, w != 0.0f);
+            while (bm) {
+                const int src = __ffs(bm) - 1;
+                bm &= bm - 1u;
+                rho = rho + __shfl_sync(kFull, w, src);
+            }
         }
     });
     return rho;
 }
 
+// Sum of gradW at p (canonical order), identical on every lane.
 template <bool STATS>
-__device__ __forceinline__ void grad_at(const GridDev& g, const KernelDev& k, float px, float py, float pz, float T,
-                                        Acc& acc, float& gx, float& gy, float& gz) {
+__device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, float px, float py, float pz, float T,
+                                          int lane, Acc& acc, float& gx, float& gy, float& gz) {
     gx = gy = gz = 0.0f;
     Loc L;
     if (STATS) acc.evals++;
     if (!locate(g, px, py, pz, L)) return;
-    for_ranges<STATS>(g, L, T, acc, [&](uint32_t b, uint32_t e) {
-        for (uint32_t j = b; j < e; ++j) {
-            const float4 q = __ldg(g.pts + j);
-            const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-            const float q2 = dot3(rx, ry, rz, rx, ry, rz);
-            if (q2 < k.h2 && q2 > 0.0f) gradw_acc(k, rx, ry, rz, q2, gx, gy, gz);
+    for_ranges_warp<STATS>(g, L, T, lane, acc, [&](uint32_t b, uint32_t e) {
+        for (uint32_t j0 = b; j0 < e; j0 += 32) {
+            const uint32_t j = j0 + (uint32_t)lane;
+            float tx = 0.0f, ty = 0.0f, tz = 0.0f;
+            bool in = false;
+            if (j < e) {
+                const float4 q = __ldg(g.pts + j);
+                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+                const float q2 = dot3(rx, ry, rz, rx, ry, rz);
+                if (q2 < k.h2 && q2 > 0.0f) {
+                    in = true;
+                    gradw_term(k, rx, ry, rz, q2, tx, ty, tz);
+                }
+            }
+            uint32_t bm = __ballot_sync(kFull, in);
+            while (bm) {
+                const int src = __ffs(bm) - 1;
+                bm &= bm - 1u;
+                gx = gx + __shfl_sync(kFull, tx, src);
+                gy = gy + __shfl_sync(kFull, ty, src);
+                gz = gz + __shfl_sync(kFull, tz, src);
+            }
         }
     });
 }
@@ -300,141 +298,139 @@ __device__ __forceinline__ float4 shade(const MarchArgs& a, int px, int py, bool
                        f * fl.z + kd * (255.0f / 255.0f), f * fl.w + kd * (255.0f / 255.0f));
 }
 
-enum Phase : int { kMarch = 0, kBisect = 1, kNormal = 2, kDone = 3 };
+__device__ __forceinline__ void write_pixel(const MarchArgs& a, uint64_t idx, int px, int py, bool hit, float hx,
+                                            float hy, float hz, float nx, float ny, float nz) {
+    if (a.pos) a.pos[idx] = hit ? make_float4(hx, hy, hz, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.nrm) a.nrm[idx] = hit ? make_float4(nx, ny, nz, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.depth) {
+        float d = 0.0f;
+        if (hit) {
+            float rx = hx - a.cam[0], ry = hy - a.cam[1], rz = hz - a.cam[2];
+            d = sqrtf(dot3(rx, ry, rz, rx, ry, rz));
+        }
+        a.depth[idx] = d;
+    }
+    if (a.col) a.col[idx] = shade(a, px, py, hit, hx, hy, hz, nx, ny, nz);
+}
+
+// March one ray with the whole warp.  Every lane holds the same state.
+template <bool STATS>
+__device__ __forceinline__ void march_ray(const MarchArgs& a, int lane, int px, int py, float z, Acc& acc, bool& hit,
+                                          float& h0, float& h1, float& h2, float& n0, float& n1, float& n2) {
+    const float cxp = (float)px * a.twoWinv - 1.0f;
+    const float cyp = (float)py * a.twoHinv - 1.0f;
+    float wh[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        float add0 = a.ipv[0 * 4 + r] * cxp + a.ipv[1 * 4 + r] * cyp;
+        float add1 = a.ipv[2 * 4 + r] * z + a.ipv[3 * 4 + r] * 1.0f;
+        wh[r] = add0 + add1;
+    }
+    float p0 = wh[0] / wh[3], p1 = wh[1] / wh[3], p2 = wh[2] / wh[3];
+    const float dx = p0 - a.cam[0], dy = p1 - a.cam[1], dz = p2 - a.cam[2];
+    const float inv = 1.0f / sqrtf(dot3(dx, dy, dz, dx, dy, dz));
+    const float sx = a.step * (dx * inv), sy = a.step * (dy * inv), sz = a.step * (dz * inv);
+    float q0 = p0, q1 = p1, q2 = p2;  // previous sample
+    hit = false;
+    for (int i = 0; i < a.max_steps; ++i) {
+        p0 = p0 + sx;
+        p1 = p1 + sy;
+        p2 = p2 + sz;
+        if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p0, p1, p2, sx, sy, sz, a.status);
+        Loc L;
+        float rho = 0.0f;
+        if (!locate(a.g, p0, p1, p2, L)) {
+            if (outside_forever(a.g, p0, p1, p2, sx, sy, sz)) break;
+            if (STATS) acc.evals++;  // no particle within reach: density 0
+        } else {
+            if (a.skip_mode == FM_SKIP_EXACT && L.c[0] >= 0 && L.c[1] >= 0 && L.c[2] >= 0 && L.c[0] < a.g.dims[0] &&
+                L.c[1] < a.g.dims[1] && L.c[2] < a.g.dims[2]) {
+                const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)a.g.dims[0] +
+                                   (uint32_t)L.c[2] * (uint32_t)a.g.dims[0] * (uint32_t)a.g.dims[1];
+                const uint32_t sc =
+                    (L.u[0] >= 0.5f ? 1u : 0u) | (L.u[1] >= 0.5f ? 2u : 0u) | (L.u[2] >= 0.5f ? 4u : 0u);
+                if (__ldg(a.g.bound + 8u * c + sc) < a.iso) {
+                    if (STATS) acc.skipped++;
+                    q0 = p0; q1 = p1; q2 = p2;
+                    continue;
+                }
+            }
+            rho = density_warp<STATS>(a.g, a.k, L, p0, p1, p2, a.cull, lane, acc);
+        }
+        if (rho >= a.iso) {
+            hit = true;
+            break;
+        }
+        q0 = p0; q1 = p1; q2 = p2;
+    }
+    n0 = n1 = n2 = 0.0f;
+    if (!hit) return;
+    for (int bi = 0; bi < a.bisect; ++bi) {
+        const float m0 = (q0 + p0) * 0.5f, m1 = (q1 + p1) * 0.5f, m2 = (q2 + p2) * 0.5f;
+        Loc L;
+        float rho = 0.0f;
+        if (locate(a.g, m0, m1, m2, L)) rho = density_warp<STATS>(a.g, a.k, L, m0, m1, m2, a.cull, lane, acc);
+        else if (STATS) acc.evals++;
+        if (rho >= a.iso) { p0 = m0; p1 = m1; p2 = m2; }
+        else { q0 = m0; q1 = m1; q2 = m2; }
+    }
+    h0 = p0; h1 = p1; h2 = p2;
+    float gx, gy, gz;
+    grad_warp<STATS>(a.g, a.k, h0, h1, h2, a.cull, lane, acc, gx, gy, gz);
+    const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+    n0 = gx * gi;
+    n1 = gy * gi;
+    n2 = gz * gi;
+}
 
 template <bool STATS>
 __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int px = blockIdx.x * kTileW + (warp & 1) * 8 + (lane & 7);
-    const int py = blockIdx.y * kTileH + (warp >> 1) * 4 + (lane >> 3);
-    const bool valid = px < a.W && py < a.Hh;
-    const uint64_t idx = (uint64_t)py * a.W + px;
-    Acc acc;
-    int phase = kDone;
-    bool hit = false, started = false;
-    float p0 = 0.f, p1 = 0.f, p2 = 0.f;        // current sample / upper bisection end
-    float q0 = 0.f, q1 = 0.f, q2 = 0.f;        // previous sample / lower bisection end
-    float sx = 0.f, sy = 0.f, sz = 0.f;
-    int i = 0, b = 0;
-    if (valid) {
-        const float z = a.zbuf[idx];
-        if (z != 1.0f) {
-            started = true;
-            phase = kMarch;
-            const float cxp = (float)px * a.twoWinv - 1.0f;
-            const float cyp = (float)py * a.twoHinv - 1.0f;
-            float wh[4];
-#pragma unroll
-            for (int r = 0; r < 4; ++r) {
-                float add0 = a.ipv[0 * 4 + r] * cxp + a.ipv[1 * 4 + r] * cyp;
-                float add1 = a.ipv[2 * 4 + r] * z + a.ipv[3 * 4 + r] * 1.0f;
-                wh[r] = add0 + add1;
+    const int lane = threadIdx.x & 31;
+    Acc acc;  // per-lane counters (lane 0 counts the rays, every lane the same evaluations)
+    uint64_t rays = 0, started_n = 0, hits = 0;
+    for (;;) {
+        unsigned int tile = 0;
+        if (lane == 0) tile = atomicAdd(a.tile_counter, 1u);
+        tile = __shfl_sync(kFull, tile, 0);
+        if (tile >= (unsigned)a.ntiles) break;
+        const int tx = (int)(tile % (unsigned)a.tiles_x), ty = (int)(tile / (unsigned)a.tiles_x);
+        const int px = tx * kTileW + (lane & (kTileW - 1));
+        const int py = ty * kTileH + (lane / kTileW);
+        const bool valid = px < a.W && py < a.Hh;
+        const uint64_t idx = (uint64_t)py * (uint64_t)a.W + (uint64_t)px;
+        const float z = valid ? a.zbuf[idx] : 1.0f;
+        const bool started = valid && z != 1.0f;
+        if (STATS && valid) { rays++; if (started) started_n++; }
+        // pixels without a splat are misses (RayMarcher.cpp:260-264): lane-parallel
+        if (valid && !started) write_pixel(a, idx, px, py, false, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+        uint32_t todo = __ballot_sync(kFull, started);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1u;
+            const int rpx = __shfl_sync(kFull, px, src), rpy = __shfl_sync(kFull, py, src);
+            const float rz = __shfl_sync(kFull, z, src);
+            bool hit;
+            float h0 = 0.f, h1 = 0.f, h2 = 0.f, n0, n1, n2;
+            march_ray<STATS>(a, lane, rpx, rpy, rz, acc, hit, h0, h1, h2, n0, n1, n2);
+            if (lane == src) {
+                write_pixel(a, idx, px, py, hit, h0, h1, h2, n0, n1, n2);
+                if (STATS && hit) hits++;
             }
-            p0 = wh[0] / wh[3];
-            p1 = wh[1] / wh[3];
-            p2 = wh[2] / wh[3];
-            float dx = p0 - a.cam[0], dy = p1 - a.cam[1], dz = p2 - a.cam[2];
-            float inv = 1.0f / sqrtf(dot3(dx, dy, dz, dx, dy, dz));
-            sx = a.step * (dx * inv);
-            sy = a.step * (dy * inv);
-            sz = a.step * (dz * inv);
-            q0 = p0; q1 = p1; q2 = p2;
         }
     }
-    // one density evaluation per live lane per iteration
-    while (phase == kMarch || phase == kBisect) {
-        float e0, e1, e2;
-        bool eval = false, known = false;
-        float rho = 0.0f;
-        Loc L;
-        if (phase == kMarch) {
-            // advance to the next sample that needs its density
-            while (i < a.max_steps) {
-                p0 = p0 + sx; p1 = p1 + sy; p2 = p2 + sz;
-                ++i;
-                if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p0, p1, p2, sx, sy, sz, a.status);
-                if (!locate(a.g, p0, p1, p2, L)) {
-                    if (outside_forever(a.g, p0, p1, p2, sx, sy, sz)) { i = a.max_steps; break; }
-                    if (STATS) acc.evals++;
-                    known = true;  // no particle within reach: density 0
-                    break;
-                }
-                if (a.skip_mode == FM_SKIP_EXACT && L.c[0] >= 0 && L.c[1] >= 0 && L.c[2] >= 0 &&
-                    L.c[0] < a.g.dims[0] && L.c[1] < a.g.dims[1] && L.c[2] < a.g.dims[2]) {
-                    const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)a.g.dims[0] +
-                                       (uint32_t)L.c[2] * (uint32_t)a.g.dims[0] * (uint32_t)a.g.dims[1];
-                    const uint32_t sc = (L.u[0] >= 0.5f ? 1u : 0u) | (L.u[1] >= 0.5f ? 2u : 0u) | (L.u[2] >= 0.5f ? 4u : 0u);
-                    if (__ldg(a.g.bound + 8u * c + sc) < a.iso) {
-                        if (STATS) acc.skipped++;
-                        q0 = p0; q1 = p1; q2 = p2;
-                        continue;
-                    }
-                }
-                eval = true;
-                break;
-            }
-            if (!eval && !known) {  // march ended without a hit
-                phase = kDone;
-                break;
-            }
-            e0 = p0; e1 = p1; e2 = p2;
-        } else {
-            e0 = (q0 + p0) * 0.5f;
-            e1 = (q1 + p1) * 0.5f;
-            e2 = (q2 + p2) * 0.5f;
-            if (!locate(a.g, e0, e1, e2, L)) {
-                if (STATS) acc.evals++;
-                known = true;
-            } else {
-                eval = true;
-            }
-        }
-        if (eval) rho = density_at<STATS>(a.g, a.k, L, e0, e1, e2, a.cull, acc);
-        const bool inside = rho >= a.iso;
-        if (phase == kMarch) {
-            if (inside) {
-                hit = true;
-                b = 0;
-                phase = a.bisect > 0 ? kBisect : kNormal;
-            } else {
-                q0 = p0; q1 = p1; q2 = p2;
-            }
-        } else {
-            if (inside) { p0 = e0; p1 = e1; p2 = e2; }
-            else { q0 = e0; q1 = e1; q2 = e2; }
-            if (++b >= a.bisect) phase = kNormal;
-        }
-    }
-    float nx = 0.f, ny = 0.f, nz = 0.f;
     if (acc.bad) atomicOr(a.status, 2u);
-    if (hit) {
-        float gx, gy, gz;
-        grad_at<STATS>(a.g, a.k, p0, p1, p2, a.cull, acc, gx, gy, gz);
-        float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
-        nx = gx * gi; ny = gy * gi; nz = gz * gi;
-    }
-    if (valid) {
-        if (a.pos) a.pos[idx] = hit ? make_float4(p0, p1, p2, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
-        if (a.nrm) a.nrm[idx] = hit ? make_float4(nx, ny, nz, 1.0f) : make_float4(0.f, 0.f, 0.f, 0.f);
-        if (a.depth) {
-            float d = 0.0f;
-            if (hit) {
-                float rx = p0 - a.cam[0], ry = p1 - a.cam[1], rz = p2 - a.cam[2];
-                d = sqrtf(dot3(rx, ry, rz, rx, ry, rz));
-            }
-            a.depth[idx] = d;
-        }
-        if (a.col) a.col[idx] = shade(a, px, py, hit, p0, p1, p2, nx, ny, nz);
-    }
     if (STATS) {
-        unsigned long long v[kStats] = {valid ? 1ull : 0ull, started ? 1ull : 0ull, hit ? 1ull : 0ull,
-                                        (unsigned long long)acc.evals, (unsigned long long)acc.cand,
-                                        (unsigned long long)acc.skipped, (unsigned long long)acc.tested};
+        // evaluation counters are identical on every lane: count them on lane 0 only
+        const bool l0 = lane == 0;
+        unsigned long long v[kStats] = {rays, started_n, hits, l0 ? (unsigned long long)acc.evals : 0ull,
+                                        l0 ? (unsigned long long)acc.cand : 0ull,
+                                        l0 ? (unsigned long long)acc.skipped : 0ull,
+                                        l0 ? (unsigned long long)acc.tested : 0ull};
 #pragma unroll
         for (int j = 0; j < kStats; ++j) {
             unsigned long long x = v[j];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
             if (lane == 0 && x) atomicAdd(a.stats + j, x);
         }
     }
@@ -465,6 +461,8 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
     a.cdir[2] = cam->view[10];
     a.W = cam->width;
     a.Hh = cam->height;
+    a.tiles_x = (cam->width + kTileW - 1) / kTileW;
+    a.ntiles = a.tiles_x * ((cam->height + kTileH - 1) / kTileH);
     a.twoWinv = 2.0f / (float)cam->width;
     a.twoHinv = 2.0f / (float)cam->height;
     a.zbuf = o.start_depth;
@@ -474,9 +472,20 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
     a.col = o.col;
     a.stats = ctx->stats_enabled ? ctx->d_stats : nullptr;
     a.status = ctx->d_status;
-    dim3 grid((cam->width + kTileW - 1) / kTileW, (cam->height + kTileH - 1) / kTileH);
-    if (a.stats) k_march<true><<<grid, kThreads, 0, st>>>(a);
-    else k_march<false><<<grid, kThreads, 0, st>>>(a);
+    // a fresh tile counter per launch (a ring of slots, so launches on
+    // different streams do not share one)
+    a.tile_counter = ctx->d_work + (ctx->work_slot++ % kWorkSlots) * 32;
+    FM_CUDA(ctx, cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned int), st));
+    int blocks_per_sm = 0;
+    if (a.stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<true>, kThreads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<false>, kThreads, 0);
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+    const int warps_needed = a.ntiles;
+    int blocks = ctx->sm_count * blocks_per_sm;
+    const int max_blocks = (warps_needed + kThreads / 32 - 1) / (kThreads / 32);
+    if (blocks > max_blocks) blocks = max_blocks;
+    if (a.stats) k_march<true><<<blocks, kThreads, 0, st>>>(a);
+    else k_march<false><<<blocks, kThreads, 0, st>>>(a);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }
