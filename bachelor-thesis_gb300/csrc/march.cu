@@ -106,7 +106,7 @@ __device__ __forceinline__ float slab_d2(float u, float lo) {
 // the sample at L.  Warp-uniform: every lane gets the same (b, e) sequence.
 // Lane l < 24 tests sub-cell (l & 7) of cell cx - 1 + (l >> 3) in each row.
 template <bool STATS, typename F>
-__device__ __forceinline__ void for_ranges_warp(const GridDev& g, const Loc& L, float T, int lane, Acc& acc,
+__device__ __forceinline__ void for_ranges_warp(const GridDev& g, const Loc& L, float T, int lane, Acc& acc, bool cnt,
                                                 F&& f) {
     const int W = g.dims[0], Hd = g.dims[1], D = g.dims[2];
     const int ci = lane >> 3, sb = lane & 7;
@@ -128,7 +128,7 @@ __device__ __forceinline__ void for_ranges_warp(const GridDev& g, const Loc& L, 
             // base wraps below 0 when row + cx == 0; then only bits >= 8 are set and
             // base + s wraps back into range.  Indices are formed in uint32 first.
             const uint32_t base = 8u * (row + (uint32_t)L.c[0]) - 8u;
-            if (STATS) {
+            if (STATS && cnt) {
                 const int x0 = max(L.c[0] - 1, 0), x1 = min(L.c[0] + 1, W - 1);
                 if (x0 <= x1) acc.cand += __ldg(g.sub + 8u * (row + (uint32_t)x1) + 8u) - __ldg(g.sub + 8u * (row + (uint32_t)x0));
             }
@@ -142,20 +142,20 @@ __device__ __forceinline__ void for_ranges_warp(const GridDev& g, const Loc& L, 
                     continue;
                 }
                 const uint32_t b = __ldg(g.sub + i0), e = __ldg(g.sub + i1);
-                if (STATS) acc.tested += e - b;
+                if (STATS && cnt) acc.tested += e - b;
                 f(b, e);
             }
         }
     }
 }
 
-// Density at p, identical on every lane (canonical order).
+// Density at p, identical on every lane (canonical order).  cnt: this lane counts the work.
 template <bool STATS>
 __device__ __forceinline__ float density_warp(const GridDev& g, const KernelDev& k, const Loc& L, float px, float py,
-                                              float pz, float T, int lane, Acc& acc) {
-    if (STATS) acc.evals++;
+                                              float pz, float T, int lane, Acc& acc, bool cnt) {
+    if (STATS && cnt) acc.evals++;
     float rho = 0.0f;
-    for_ranges_warp<STATS>(g, L, T, lane, acc, [&](uint32_t b, uint32_t e) {
+    for_ranges_warp<STATS>(g, L, T, lane, acc, cnt, [&](uint32_t b, uint32_t e) {
         for (uint32_t j0 = b; j0 < e; j0 += 32) {
             const uint32_t j = j0 + (uint32_t)lane;
             float w = 0.0f;
@@ -174,40 +174,6 @@ __device__ __forceinline__ float density_warp(const GridDev& g, const KernelDev&
         }
     });
     return rho;
-}
-
-// Sum of gradW at p (canonical order), identical on every lane.
-template <bool STATS>
-__device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, float px, float py, float pz, float T,
-                                          int lane, Acc& acc, float& gx, float& gy, float& gz) {
-    gx = gy = gz = 0.0f;
-    Loc L;
-    if (STATS) acc.evals++;
-    if (!locate(g, px, py, pz, L)) return;
-    for_ranges_warp<STATS>(g, L, T, lane, acc, [&](uint32_t b, uint32_t e) {
-        for (uint32_t j0 = b; j0 < e; j0 += 32) {
-            const uint32_t j = j0 + (uint32_t)lane;
-            float tx = 0.0f, ty = 0.0f, tz = 0.0f;
-            bool in = false;
-            if (j < e) {
-                const float4 q = __ldg(g.pts + j);
-                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-                const float q2 = dot3(rx, ry, rz, rx, ry, rz);
-                if (q2 < k.h2 && q2 > 0.0f) {
-                    in = true;
-                    gradw_term(k, rx, ry, rz, q2, tx, ty, tz);
-                }
-            }
-            uint32_t bm = __ballot_sync(kFull, in);
-            while (bm) {
-                const int src = __ffs(bm) - 1;
-                bm &= bm - 1u;
-                gx = gx + __shfl_sync(kFull, tx, src);
-                gy = gy + __shfl_sync(kFull, ty, src);
-                gz = gz + __shfl_sync(kFull, tz, src);
-            }
-        }
-    });
 }
 
 // glm min/max semantics (func_common.inl): min(x,y) = y<x ? y : x, max(x,y) = x<y ? y : x
@@ -313,36 +279,60 @@ __device__ __forceinline__ void write_pixel(const MarchArgs& a, uint64_t idx, in
     if (a.col) a.col[idx] = shade(a, px, py, hit, hx, hy, hz, nx, ny, nz);
 }
 
-// March one ray with the whole warp.  Every lane holds the same state.
-template <bool STATS>
-__device__ __forceinline__ void march_ray(const MarchArgs& a, int lane, int px, int py, float z, Acc& acc, bool& hit,
-                                          float& h0, float& h1, float& h2, float& n0, float& n1, float& n2) {
-    const float cxp = (float)px * a.twoWinv - 1.0f;
-    const float cyp = (float)py * a.twoHinv - 1.0f;
-    float wh[4];
-#pragma unroll
-    for (int r = 0; r < 4; ++r) {
-        float add0 = a.ipv[0 * 4 + r] * cxp + a.ipv[1 * 4 + r] * cyp;
-        float add1 = a.ipv[2 * 4 + r] * z + a.ipv[3 * 4 + r] * 1.0f;
-        wh[r] = add0 + add1;
-    }
-    float p0 = wh[0] / wh[3], p1 = wh[1] / wh[3], p2 = wh[2] / wh[3];
-    const float dx = p0 - a.cam[0], dy = p1 - a.cam[1], dz = p2 - a.cam[2];
-    const float inv = 1.0f / sqrtf(dot3(dx, dy, dz, dx, dy, dz));
-    const float sx = a.step * (dx * inv), sy = a.step * (dy * inv), sz = a.step * (dz * inv);
-    float q0 = p0, q1 = p1, q2 = p2;  // previous sample
-    hit = false;
-    for (int i = 0; i < a.max_steps; ++i) {
-        p0 = p0 + sx;
-        p1 = p1 + sy;
-        p2 = p2 + sz;
-        if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p0, p1, p2, sx, sy, sz, a.status);
-        Loc L;
-        float rho = 0.0f;
-        if (!locate(a.g, p0, p1, p2, L)) {
-            if (outside_forever(a.g, p0, p1, p2, sx, sy, sz)) break;
-            if (STATS) acc.evals++;  // no particle within reach: density 0
+// ---- per-lane ray state -------------------------------------------------------
+
+enum Phase : int { kMarch = 0, kBisect = 1, kNormal = 2, kDone = 3 };
+
+struct Ray {
+    int phase;
+    int i, b;             // march steps taken, bisection steps taken
+    float p[3];           // current sample (march) / inside end (bisection)
+    float q[3];           // previous sample (march) / outside end (bisection)
+    float s[3];           // step
+    float e[3];           // pending evaluation point
+};
+
+// Apply the density at the pending point (RayMarcher.cpp:327: hit when rho >= iso).
+__device__ __forceinline__ void apply(const MarchArgs& a, Ray& r, float rho) {
+    const bool inside = rho >= a.iso;
+    if (r.phase == kMarch) {
+        if (inside) {
+            r.b = 0;
+            r.phase = a.bisect > 0 ? kBisect : kNormal;
         } else {
+            r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
+        }
+    } else {
+        if (inside) { r.p[0] = r.e[0]; r.p[1] = r.e[1]; r.p[2] = r.e[2]; }
+        else { r.q[0] = r.e[0]; r.q[1] = r.e[1]; r.q[2] = r.e[2]; }
+        if (++r.b >= a.bisect) r.phase = kNormal;
+    }
+}
+
+// Advance a ray to its next density evaluation: march samples are stepped
+// (and, for FM_SKIP_EXACT, skipped while their sub-cell bound is below iso),
+// samples out of reach of every particle get density 0 without a sum.
+// Returns true with r.e / L set when a sum is needed, false when the ray left
+// the march or bisection phases.
+template <bool STATS>
+__device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc& acc, bool cnt) {
+    for (;;) {
+        if (r.phase == kMarch) {
+            if (r.i >= a.max_steps) { r.phase = kDone; return false; }
+            r.p[0] = r.p[0] + r.s[0];
+            r.p[1] = r.p[1] + r.s[1];
+            r.p[2] = r.p[2] + r.s[2];
+            ++r.i;
+            if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2], a.status);
+            if (!locate(a.g, r.p[0], r.p[1], r.p[2], L)) {
+                if (outside_forever(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2])) {
+                    r.phase = kDone;
+                    return false;
+                }
+                if (STATS && cnt) acc.evals++;
+                apply(a, r, 0.0f);
+                continue;
+            }
             if (a.skip_mode == FM_SKIP_EXACT && L.c[0] >= 0 && L.c[1] >= 0 && L.c[2] >= 0 && L.c[0] < a.g.dims[0] &&
                 L.c[1] < a.g.dims[1] && L.c[2] < a.g.dims[2]) {
                 const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)a.g.dims[0] +
@@ -350,43 +340,201 @@ __device__ __forceinline__ void march_ray(const MarchArgs& a, int lane, int px, 
                 const uint32_t sc =
                     (L.u[0] >= 0.5f ? 1u : 0u) | (L.u[1] >= 0.5f ? 2u : 0u) | (L.u[2] >= 0.5f ? 4u : 0u);
                 if (__ldg(a.g.bound + 8u * c + sc) < a.iso) {
-                    if (STATS) acc.skipped++;
-                    q0 = p0; q1 = p1; q2 = p2;
+                    if (STATS && cnt) acc.skipped++;
+                    r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
                     continue;
                 }
             }
-            rho = density_warp<STATS>(a.g, a.k, L, p0, p1, p2, a.cull, lane, acc);
+            r.e[0] = r.p[0]; r.e[1] = r.p[1]; r.e[2] = r.p[2];
+            return true;
+        } else if (r.phase == kBisect) {
+            r.e[0] = (r.q[0] + r.p[0]) * 0.5f;
+            r.e[1] = (r.q[1] + r.p[1]) * 0.5f;
+            r.e[2] = (r.q[2] + r.p[2]) * 0.5f;
+            if (!locate(a.g, r.e[0], r.e[1], r.e[2], L)) {
+                if (STATS && cnt) acc.evals++;
+                apply(a, r, 0.0f);
+                continue;
+            }
+            return true;
         }
-        if (rho >= a.iso) {
-            hit = true;
-            break;
+        return false;
+    }
+}
+
+// ---- shared candidate stream: lanes are rays ----------------------------------
+//
+// The lanes that need a sum are grouped so that a group's cells span at most
+// 2 per axis; for every cell row of the group's union neighbourhood (4x4 rows,
+// 4 cells = 32 sub-cells per row) each lane computes the mask of its own
+// reachable sub-cells (only cells within one of its own cell), the warp ORs
+// the masks, and all lanes walk the union's sub-cells in ascending order with
+// one broadcast load per particle.  A lane adds a particle only when the
+// particle's sub-cell is in its own mask, so its sum visits exactly its own
+// canonical sequence.
+
+// Own sub-cell reach mask of a lane for cell row (y, z), in union bit
+// positions (cell x - (gx - 1)) * 8 + sub, where gx is the group's min cell.
+__device__ __forceinline__ uint32_t own_row_mask(const GridDev& g, const Loc& L, const float ax[6], int y, int z, int gx,
+                                                 float T) {
+    const int dy = y - L.c[1], dz = z - L.c[2];
+    if (dy < -1 || dy > 1 || dz < -1 || dz > 1) return 0u;
+    const float y0 = slab_d2(L.u[1], (float)dy), y1 = slab_d2(L.u[1], (float)dy + 0.5f);
+    const float z0 = slab_d2(L.u[2], (float)dz), z1 = slab_d2(L.u[2], (float)dz + 0.5f);
+    const float yz[4] = {y0 + z0, y1 + z0, y0 + z1, y1 + z1};
+    uint32_t m = 0;
+#pragma unroll
+    for (int i = 0; i < 6; ++i)
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            if (ax[i] + yz[k] < T) m |= 1u << (8 * (i >> 1) + (i & 1) + 2 * k);
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+        const int x = L.c[0] - 1 + i;
+        if (x < 0 || x >= g.dims[0]) m &= ~(0xffu << (8 * i));
+    }
+    // own cells cx-1..cx+1 sit at union cells (cx - gx) .. (cx - gx + 2)
+    return m << (8 * (L.c[0] - gx));
+}
+
+// Visit the union stream.  f(pred, b, e): particles [b, e) of one sub-cell,
+// pred = this lane's own mask holds it.  `mine`: this lane takes part.
+template <bool STATS, typename F>
+__device__ __forceinline__ void union_stream(const GridDev& g, bool mine, const Loc& L, float T, Acc& acc, F&& f) {
+    float ax[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ax[i] = slab_d2(L.u[0], -1.0f + 0.5f * (float)i);
+    const int W = g.dims[0], Hd = g.dims[1], D = g.dims[2];
+    uint32_t pending = __ballot_sync(kFull, mine);
+    while (pending) {
+        const bool cand = (pending >> (threadIdx.x & 31)) & 1u;
+        const int gx = __reduce_min_sync(kFull, cand ? L.c[0] : 0x7fffffff);
+        const int gy = __reduce_min_sync(kFull, cand ? L.c[1] : 0x7fffffff);
+        const int gz = __reduce_min_sync(kFull, cand ? L.c[2] : 0x7fffffff);
+        const bool in = cand && L.c[0] - gx <= 1 && L.c[1] - gy <= 1 && L.c[2] - gz <= 1;
+        pending &= ~__ballot_sync(kFull, in);
+        if (STATS && in) {
+            const int x0 = max(L.c[0] - 1, 0), x1 = min(L.c[0] + 1, W - 1);
+            if (x0 <= x1)
+                for (int z = max(L.c[2] - 1, 0); z <= min(L.c[2] + 1, D - 1); ++z)
+                    for (int y = max(L.c[1] - 1, 0); y <= min(L.c[1] + 1, Hd - 1); ++y) {
+                        const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
+                        acc.cand += __ldg(g.sub + 8u * (row + (uint32_t)x1) + 8u) - __ldg(g.sub + 8u * (row + (uint32_t)x0));
+                    }
         }
-        q0 = p0; q1 = p1; q2 = p2;
+#pragma unroll 1
+        for (int zz = 0; zz < 4; ++zz) {
+            const int z = gz - 1 + zz;
+            if (z < 0 || z >= D) continue;
+#pragma unroll 1
+            for (int yy = 0; yy < 4; ++yy) {
+                const int y = gy - 1 + yy;
+                if (y < 0 || y >= Hd) continue;
+                const uint32_t own = in ? own_row_mask(g, L, ax, y, z, gx, T) : 0u;
+                uint32_t uni = __reduce_or_sync(kFull, own);
+                const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
+                // base wraps below 0 when row + gx == 0; then only bits >= 8 are set.
+                const uint32_t base = 8u * (row + (uint32_t)gx) - 8u;
+                while (uni) {
+                    const int u = __ffs(uni) - 1;
+                    uni &= uni - 1u;
+                    const uint32_t i0 = base + (uint32_t)u;
+                    if (i0 + 1u >= g.nsub) {  // cannot happen for a consistent table
+                        acc.bad = true;
+                        continue;
+                    }
+                    const uint32_t b = __ldg(g.sub + i0), e = __ldg(g.sub + i0 + 1u);
+                    const bool pred = (own >> u) & 1u;
+                    if (STATS && pred) acc.tested += e - b;
+                    f(pred, b, e);
+                }
+            }
+        }
     }
-    n0 = n1 = n2 = 0.0f;
-    if (!hit) return;
-    for (int bi = 0; bi < a.bisect; ++bi) {
-        const float m0 = (q0 + p0) * 0.5f, m1 = (q1 + p1) * 0.5f, m2 = (q2 + p2) * 0.5f;
-        Loc L;
-        float rho = 0.0f;
-        if (locate(a.g, m0, m1, m2, L)) rho = density_warp<STATS>(a.g, a.k, L, m0, m1, m2, a.cull, lane, acc);
-        else if (STATS) acc.evals++;
-        if (rho >= a.iso) { p0 = m0; p1 = m1; p2 = m2; }
-        else { q0 = m0; q1 = m1; q2 = m2; }
+}
+
+template <bool STATS>
+__device__ __forceinline__ float union_density(const MarchArgs& a, bool mine, const Loc& L, const float e[3], Acc& acc) {
+    if (STATS && mine) acc.evals++;
+    const float px = e[0], py = e[1], pz = e[2];
+    const KernelDev& k = a.k;
+    float rho = 0.0f;
+    union_stream<STATS>(a.g, mine, L, a.cull, acc, [&](bool pred, uint32_t b, uint32_t e_) {
+        uint32_t j = b;
+        for (; j + 2 <= e_; j += 2) {
+            const float4 q0 = __ldg(a.g.pts + j), q1 = __ldg(a.g.pts + j + 1);
+            if (pred) {
+                const float r0x = q0.x - px, r0y = q0.y - py, r0z = q0.z - pz;
+                const float r1x = q1.x - px, r1y = q1.y - py, r1z = q1.z - pz;
+                const float d0 = dot3(r0x, r0y, r0z, r0x, r0y, r0z);
+                const float d1 = dot3(r1x, r1y, r1z, r1x, r1y, r1z);
+                if (d0 < k.h2) rho = rho + w_in(k, d0);
+                if (d1 < k.h2) rho = rho + w_in(k, d1);
+            }
+        }
+        if (j < e_) {
+            const float4 q = __ldg(a.g.pts + j);
+            if (pred) {
+                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+                const float d = dot3(rx, ry, rz, rx, ry, rz);
+                if (d < k.h2) rho = rho + w_in(k, d);
+            }
+        }
+    });
+    return rho;
+}
+
+template <bool STATS>
+__device__ __forceinline__ void union_grad(const MarchArgs& a, bool mine, const Loc& L, const float e[3], Acc& acc,
+                                           float& gx, float& gy, float& gz) {
+    if (STATS && mine) acc.evals++;
+    const float px = e[0], py = e[1], pz = e[2];
+    const KernelDev& k = a.k;
+    gx = gy = gz = 0.0f;
+    union_stream<STATS>(a.g, mine, L, a.cull, acc, [&](bool pred, uint32_t b, uint32_t e_) {
+        for (uint32_t j = b; j < e_; ++j) {
+            const float4 q = __ldg(a.g.pts + j);
+            if (pred) {
+                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+                const float q2 = dot3(rx, ry, rz, rx, ry, rz);
+                if (q2 < k.h2 && q2 > 0.0f) gradw_acc(k, rx, ry, rz, q2, gx, gy, gz);
+            }
+        }
+    });
+}
+
+// ---- cooperative finish: the whole warp continues one lane's ray -----------------
+
+template <bool STATS>
+__device__ __forceinline__ void coop_finish(const MarchArgs& a, Ray& mine, int src, int lane, Acc& acc) {
+    Ray r;
+    r.phase = __shfl_sync(kFull, mine.phase, src);
+    r.i = __shfl_sync(kFull, mine.i, src);
+    r.b = __shfl_sync(kFull, mine.b, src);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        r.p[c] = __shfl_sync(kFull, mine.p[c], src);
+        r.q[c] = __shfl_sync(kFull, mine.q[c], src);
+        r.s[c] = __shfl_sync(kFull, mine.s[c], src);
+        r.e[c] = __shfl_sync(kFull, mine.e[c], src);
     }
-    h0 = p0; h1 = p1; h2 = p2;
-    float gx, gy, gz;
-    grad_warp<STATS>(a.g, a.k, h0, h1, h2, a.cull, lane, acc, gx, gy, gz);
-    const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
-    n0 = gx * gi;
-    n1 = gy * gi;
-    n2 = gz * gi;
+    const bool cnt = lane == src;
+    Loc L;
+    // the pending point was prepared already
+    bool need = locate(a.g, r.e[0], r.e[1], r.e[2], L);
+    for (;;) {
+        float rho = density_warp<STATS>(a.g, a.k, L, r.e[0], r.e[1], r.e[2], a.cull, lane, acc, cnt);
+        apply(a, r, rho);
+        need = prepare<STATS>(a, r, L, acc, cnt);
+        if (!need) break;
+    }
+    if (lane == src) mine = r;
 }
 
 template <bool STATS>
 __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
     const int lane = threadIdx.x & 31;
-    Acc acc;  // per-lane counters (lane 0 counts the rays, every lane the same evaluations)
+    Acc acc;
     uint64_t rays = 0, started_n = 0, hits = 0;
     for (;;) {
         unsigned int tile = 0;
@@ -399,33 +547,81 @@ __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
         const bool valid = px < a.W && py < a.Hh;
         const uint64_t idx = (uint64_t)py * (uint64_t)a.W + (uint64_t)px;
         const float z = valid ? a.zbuf[idx] : 1.0f;
-        const bool started = valid && z != 1.0f;
-        if (STATS && valid) { rays++; if (started) started_n++; }
-        // pixels without a splat are misses (RayMarcher.cpp:260-264): lane-parallel
-        if (valid && !started) write_pixel(a, idx, px, py, false, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
-        uint32_t todo = __ballot_sync(kFull, started);
-        while (todo) {
-            const int src = __ffs(todo) - 1;
-            todo &= todo - 1u;
-            const int rpx = __shfl_sync(kFull, px, src), rpy = __shfl_sync(kFull, py, src);
-            const float rz = __shfl_sync(kFull, z, src);
-            bool hit;
-            float h0 = 0.f, h1 = 0.f, h2 = 0.f, n0, n1, n2;
-            march_ray<STATS>(a, lane, rpx, rpy, rz, acc, hit, h0, h1, h2, n0, n1, n2);
-            if (lane == src) {
-                write_pixel(a, idx, px, py, hit, h0, h1, h2, n0, n1, n2);
-                if (STATS && hit) hits++;
+        Ray r;
+        r.phase = kDone;
+        r.i = r.b = 0;
+        if (valid && z != 1.0f) {
+            // RayMarcher.cpp:268-274
+            const float cxp = (float)px * a.twoWinv - 1.0f;
+            const float cyp = (float)py * a.twoHinv - 1.0f;
+            float wh[4];
+#pragma unroll
+            for (int rr = 0; rr < 4; ++rr) {
+                float add0 = a.ipv[0 * 4 + rr] * cxp + a.ipv[1 * 4 + rr] * cyp;
+                float add1 = a.ipv[2 * 4 + rr] * z + a.ipv[3 * 4 + rr] * 1.0f;
+                wh[rr] = add0 + add1;
             }
+            r.p[0] = wh[0] / wh[3];
+            r.p[1] = wh[1] / wh[3];
+            r.p[2] = wh[2] / wh[3];
+            const float dx = r.p[0] - a.cam[0], dy = r.p[1] - a.cam[1], dz = r.p[2] - a.cam[2];
+            const float inv = 1.0f / sqrtf(dot3(dx, dy, dz, dx, dy, dz));
+            r.s[0] = a.step * (dx * inv);
+            r.s[1] = a.step * (dy * inv);
+            r.s[2] = a.step * (dz * inv);
+            r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
+            r.phase = kMarch;
+        } else {
+            r.p[0] = r.p[1] = r.p[2] = 0.0f;
+            r.q[0] = r.q[1] = r.q[2] = 0.0f;
+            r.s[0] = r.s[1] = r.s[2] = 0.0f;
         }
+        r.e[0] = r.e[1] = r.e[2] = 0.0f;
+        if (STATS && valid) { rays++; if (z != 1.0f) started_n++; }
+        Loc L;
+        L.c[0] = L.c[1] = L.c[2] = 0;
+        L.u[0] = L.u[1] = L.u[2] = 0.0f;
+        for (;;) {
+            const bool need = (r.phase == kMarch || r.phase == kBisect) && prepare<STATS>(a, r, L, acc, true);
+            const uint32_t act = __ballot_sync(kFull, need);
+            if (!act) break;
+            if (__popc(act) <= 2) {
+                // too few rays left for a shared stream: finish them one by one with the whole warp
+                uint32_t m = act;
+                while (m) {
+                    const int src = __ffs(m) - 1;
+                    m &= m - 1u;
+                    coop_finish<STATS>(a, r, src, lane, acc);
+                }
+                break;
+            }
+            const float rho = union_density<STATS>(a, need, L, r.e, acc);
+            if (need) apply(a, r, rho);
+        }
+        // normals of the hit rays (all in phase kNormal), then outputs
+        const bool hit = r.phase == kNormal;
+        Loc Lh;
+        Lh.c[0] = Lh.c[1] = Lh.c[2] = 0;
+        Lh.u[0] = Lh.u[1] = Lh.u[2] = 0.0f;
+        const bool gn = hit && locate(a.g, r.p[0], r.p[1], r.p[2], Lh);
+        if (STATS && hit && !gn) acc.evals++;
+        float gx = 0.f, gy = 0.f, gz = 0.f;
+        if (__any_sync(kFull, gn)) union_grad<STATS>(a, gn, Lh, r.p, acc, gx, gy, gz);
+        float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+        if (hit) {
+            const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+            n0 = gx * gi;
+            n1 = gy * gi;
+            n2 = gz * gi;
+            if (STATS) hits++;
+        }
+        if (valid) write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
     }
     if (acc.bad) atomicOr(a.status, 2u);
     if (STATS) {
-        // evaluation counters are identical on every lane: count them on lane 0 only
-        const bool l0 = lane == 0;
-        unsigned long long v[kStats] = {rays, started_n, hits, l0 ? (unsigned long long)acc.evals : 0ull,
-                                        l0 ? (unsigned long long)acc.cand : 0ull,
-                                        l0 ? (unsigned long long)acc.skipped : 0ull,
-                                        l0 ? (unsigned long long)acc.tested : 0ull};
+        unsigned long long v[kStats] = {rays, started_n, hits, (unsigned long long)acc.evals,
+                                        (unsigned long long)acc.cand, (unsigned long long)acc.skipped,
+                                        (unsigned long long)acc.tested};
 #pragma unroll
         for (int j = 0; j < kStats; ++j) {
             unsigned long long x = v[j];
