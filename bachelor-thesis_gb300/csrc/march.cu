@@ -406,12 +406,19 @@ __device__ __forceinline__ void union_stream(const GridDev& g, bool mine, const 
     for (int i = 0; i < 6; ++i) ax[i] = slab_d2(L.u[0], -1.0f + 0.5f * (float)i);
     const int W = g.dims[0], Hd = g.dims[1], D = g.dims[2];
     uint32_t pending = __ballot_sync(kFull, mine);
-    while (pending) {
+    // Each pass takes the lowest pending lane as leader and groups the lanes
+    // whose cells lie in a 2x2x2 block that contains the leader's cell, so
+    // every pass retires at least the leader: at most 32 passes.
+    for (int pass = 0; pending && pass < 32; ++pass) {
         const bool cand = (pending >> (threadIdx.x & 31)) & 1u;
-        const int gx = __reduce_min_sync(kFull, cand ? L.c[0] : 0x7fffffff);
-        const int gy = __reduce_min_sync(kFull, cand ? L.c[1] : 0x7fffffff);
-        const int gz = __reduce_min_sync(kFull, cand ? L.c[2] : 0x7fffffff);
-        const bool in = cand && L.c[0] - gx <= 1 && L.c[1] - gy <= 1 && L.c[2] - gz <= 1;
+        const int lead = __ffs(pending) - 1;
+        const int lx = __shfl_sync(kFull, L.c[0], lead), ly = __shfl_sync(kFull, L.c[1], lead),
+                  lz = __shfl_sync(kFull, L.c[2], lead);
+        const bool near = cand && abs(L.c[0] - lx) <= 1 && abs(L.c[1] - ly) <= 1 && abs(L.c[2] - lz) <= 1;
+        const int gx = __reduce_min_sync(kFull, near ? L.c[0] : 0x7fffffff);
+        const int gy = __reduce_min_sync(kFull, near ? L.c[1] : 0x7fffffff);
+        const int gz = __reduce_min_sync(kFull, near ? L.c[2] : 0x7fffffff);
+        const bool in = near && L.c[0] - gx <= 1 && L.c[1] - gy <= 1 && L.c[2] - gz <= 1;
         pending &= ~__ballot_sync(kFull, in);
         if (STATS && in) {
             const int x0 = max(L.c[0] - 1, 0), x1 = min(L.c[0] + 1, W - 1);
@@ -451,6 +458,7 @@ __device__ __forceinline__ void union_stream(const GridDev& g, bool mine, const 
             }
         }
     }
+    if (pending) acc.bad = true;  // unreachable: every pass retires its leader
 }
 
 template <bool STATS>
