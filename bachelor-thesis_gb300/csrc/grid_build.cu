@@ -528,3 +528,151 @@ int ensure_flags(fm_ctx* ctx, fm_scene* s, cudaStream_t st) {
 }
 
 }  // namespace fm
+
+// ============================================================================
+// Grid build that allocates nothing: fm_grid_build_noalloc
+// ============================================================================
+//
+// For callers that must not allocate device memory: code that runs where
+// cudaMalloc is not allowed or not wanted (a renderer that reserves all of its
+// memory up front, a plugin living inside a host application's memory budget,
+// work recorded into a CUDA graph).  Same kernels and same results as the
+// grid build of fm_scene_create; the caller passes every output buffer, and
+// the scratch the build needs lives in one file-scope device array:
+//   * the AABB words, the radix-sort histograms and the scan temporaries in
+//     g_noalloc_scratch (kNoAllocWords words, about 1.1 MB, which every device
+//     that loads this library keeps until the process exits);
+//   * the sort keys and values in the caller's sorted_xyzw buffer (4n words),
+//     which holds them until the final gather writes the sorted positions.
+// Limits: n <= 2^21 particles and n_cells <= 2^21.  Every call shares the
+// scratch array, so calls that overlap on the GPU (other streams, other host
+// threads) race; serialise them.  The array keeps the last call's contents;
+// the AABB words are cleared at the start of each call and everything else is
+// fully rewritten before it is read.
+
+#include <mutex>
+
+namespace fm {
+namespace {
+
+constexpr uint64_t kNoAllocMaxParticles = 1ull << 21;
+constexpr uint64_t kNoAllocMaxCells = 1ull << 21;
+constexpr uint64_t kNoAllocAabbWords = 64;
+constexpr uint64_t kNoAllocHistWords = 256 * ((kNoAllocMaxParticles + kSortTile - 1) / kSortTile);
+constexpr uint64_t kNoAllocScanWords = 16384;  // >= scan_tmp_words(8 * kNoAllocMaxCells + 1)
+constexpr uint64_t kNoAllocWords = kNoAllocAabbWords + kNoAllocHistWords + kNoAllocScanWords;
+
+__device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
+
+// Device address of g_noalloc_scratch, looked up once per device with that
+// device current (a host-side reference to the symbol is not a device address).
+std::mutex g_noalloc_mu;
+uint32_t* g_noalloc_addr[256] = {};
+
+int noalloc_scratch(int dev, uint32_t** out) {
+    if (dev < 0 || dev >= 256) return FM_ERR_CUDA;
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void* p = nullptr;
+        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return FM_ERR_CUDA;
+        g_noalloc_addr[dev] = (uint32_t*)p;
+    }
+    *out = g_noalloc_addr[dev];
+    return FM_OK;
+}
+
+}  // namespace
+}  // namespace fm
+
+extern "C" int fm_grid_build_noalloc(const float* xyz, uint64_t n, uint32_t stride, float support_radius,
+                                     float* sorted_xyzw, uint32_t* cell, uint32_t* sorted_index, uint32_t* sub_start,
+                                     uint64_t sub_start_capacity, fm_grid_info* info, void* stream) {
+    using namespace fm;
+    if (!xyz || !sorted_xyzw || !cell || !sorted_index || !sub_start || !info) return FM_ERR_INVALID;
+    if (n == 0 || n > kNoAllocMaxParticles || stride < 3) return FM_ERR_INVALID;
+    if (!(support_radius > 0.0f) || !std::isfinite(support_radius)) return FM_ERR_INVALID;
+    if (((uintptr_t)sorted_xyzw & 15u) != 0) return FM_ERR_INVALID;
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return FM_ERR_CUDA;
+    uint32_t* scratch = nullptr;
+    if (noalloc_scratch(dev, &scratch) != FM_OK) return FM_ERR_CUDA;
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return FM_ERR_CUDA;
+    cudaStream_t st = (cudaStream_t)stream;
+    uint32_t* mm = scratch;
+    uint32_t* hist = scratch + kNoAllocAabbWords;
+    uint32_t* tmp = hist + kNoAllocHistWords;
+#define FM_NA(call)                                  \
+    do {                                             \
+        if ((call) != cudaSuccess) return FM_ERR_CUDA; \
+    } while (0)
+    // 1. AABB (exact min/max) -> host
+    FM_NA(cudaMemsetAsync(mm, 0xff, 3 * sizeof(uint32_t), st));
+    FM_NA(cudaMemsetAsync(mm + 3, 0, 4 * sizeof(uint32_t), st));
+    {
+        unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8);
+        k_aabb<<<std::max(1u, blocks), 256, 0, st>>>(xyz, n, stride, mm);
+        FM_NA(cudaGetLastError());
+    }
+    uint32_t h[7];
+    FM_NA(cudaMemcpyAsync(h, mm, sizeof(h), cudaMemcpyDeviceToHost, st));
+    FM_NA(cudaStreamSynchronize(st));
+    if (h[6] != 0) return FM_ERR_INVALID;  // non-finite positions
+    // 2. grid parameters, in the reference's FP32 order (Dataset.cpp:89-104)
+    const float pad = 1.0f * support_radius;
+    const float cellw = 1.0f * support_radius;
+    GridParams gp;
+    uint64_t ncells = 1;
+    for (int a = 0; a < 3; ++a) {
+        const float mn = ord2f(h[a]), mx = ord2f(h[3 + a]);
+        info->max[a] = mx + pad;
+        info->min[a] = mn - pad;
+        const float d = std::ceil((info->max[a] - info->min[a]) / cellw);
+        if (!(d >= 1.0f && d < 1.0e6f)) return FM_ERR_INVALID;
+        info->dims[a] = (int)d;
+        gp.min[a] = info->min[a];
+        gp.dims[a] = info->dims[a];
+        ncells *= (uint64_t)info->dims[a];
+    }
+    gp.inv = 1.0f / cellw;
+    info->cell_width = cellw;
+    info->inv_cell_width = gp.inv;
+    info->pad = 0;
+    info->n_particles = n;
+    info->n_cells = ncells;
+    const uint64_t nkeys = 8 * ncells;
+    if (ncells > kNoAllocMaxCells || sub_start_capacity < nkeys + 1) return FM_ERR_INVALID;
+    // 3. cells, keys, key histogram (the histogram is counted in sub_start)
+    uint32_t* keys0 = (uint32_t*)sorted_xyzw;
+    uint32_t* kbuf[2] = {keys0 + n, keys0 + 2 * n};
+    uint32_t* vbuf[2] = {sorted_index, keys0 + 3 * n};
+    FM_NA(cudaMemsetAsync(sub_start, 0, (nkeys + 1) * sizeof(uint32_t), st));
+    k_cells<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(xyz, n, stride, gp, cell, keys0, sub_start);
+    FM_NA(cudaGetLastError());
+    exclusive_scan(sub_start, sub_start, nkeys + 1, tmp, st);
+    // 4. stable LSD radix sort of (key, input index), the last pass landing in sorted_index
+    const uint64_t nblk = (n + kSortTile - 1) / kSortTile;
+    const uint64_t hist_n = 256 * nblk;
+    int bits = 1;
+    while (bits < 32 && ((nkeys - 1) >> bits)) ++bits;
+    const int passes = (bits + 7) / 8;
+    int cur = (passes % 2 == 1) ? 0 : 1;
+    const uint32_t* kin = keys0;
+    const uint32_t* vin = nullptr;
+    for (int p = 0; p < passes; ++p) {
+        const int shift = 8 * p;
+        k_radix_hist<<<(unsigned)nblk, kSortThreads, 0, st>>>(kin, n, shift, (uint32_t)nblk, hist);
+        exclusive_scan(hist, hist, hist_n, tmp, st);
+        k_radix_scatter<<<(unsigned)nblk, kSortThreads, 0, st>>>(kin, vin, kbuf[cur], vbuf[cur], n, shift,
+                                                               (uint32_t)nblk, hist);
+        FM_NA(cudaGetLastError());
+        kin = kbuf[cur];
+        vin = vbuf[cur];
+        cur ^= 1;
+    }
+    // 5. gather the sorted positions (overwrites the key/value temporaries)
+    k_gather<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(xyz, n, stride, sorted_index, (float4*)sorted_xyzw);
+    FM_NA(cudaGetLastError());
+#undef FM_NA
+    return FM_OK;
+}

@@ -34,7 +34,7 @@ FM_MARCH_EXTERNAL_DEPTH = 1
 EXPORTS = [
     "fm_version", "fm_create", "fm_destroy", "fm_last_error", "fm_stream", "fm_sync", "fm_query", "fm_host_alloc",
     "fm_host_free", "fm_scene_create", "fm_scene_update", "fm_scene_destroy", "fm_scene_grid", "fm_scene_download",
-    "fm_splat_depth", "fm_march", "fm_set_stats", "fm_march_stats_get",
+    "fm_splat_depth", "fm_march", "fm_set_stats", "fm_march_stats_get", "fm_grid_build_noalloc",
 ]
 
 
@@ -105,6 +105,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_march.argtypes = [vp, vp, C.POINTER(CCamera), C.POINTER(CMarchParams), C.POINTER(CFrameOut), C.c_int, vp]
     L.fm_set_stats.argtypes = [vp, C.c_int]
     L.fm_march_stats_get.argtypes = [vp, C.POINTER(CMarchStats)]
+    L.fm_grid_build_noalloc.argtypes = [vp, C.c_uint64, C.c_uint32, C.c_float, vp, vp, vp, vp, C.c_uint64,
+                                        C.POINTER(CGridInfo), vp]
     _lib = L
     return L
 
