@@ -148,6 +148,7 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->d_status);
     cudaFree(ctx->d_stats);
     cudaFree(ctx->d_work);
+    cudaFree(ctx->longq.p);
     if (ctx->h_pinned_small) cudaFreeHost(ctx->h_pinned_small);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

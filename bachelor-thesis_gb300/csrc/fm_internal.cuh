@@ -172,6 +172,8 @@ struct fm_ctx {
     fm_march_stats last_stats{};
     // scratch for grid builds
     fm::DevBuf scratch[8];
+    // long-ray queue of the march (64 B per pixel of the largest view so far)
+    fm::DevBuf longq;
     // live scenes of this context; fm_destroy frees the ones still alive
     std::vector<fm_scene*> scenes;
     void* h_pinned_small = nullptr;  // 256 bytes of pinned memory for small readbacks

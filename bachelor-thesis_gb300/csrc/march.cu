@@ -65,6 +65,11 @@ struct MarchArgs {
     float* depth;
     float4* col;
     unsigned int* tile_counter;
+    unsigned int* q_tail;  // long-ray queue: entries written by the shared-stream pass
+    unsigned int* q_head;  // entries taken by the long-ray pass
+    float4* longq;         // 4 float4 per entry (see push_long)
+    unsigned int q_cap;
+    int cap;               // shared-stream iterations per tile before the rays left are deferred
     unsigned long long* stats;
     unsigned int* status;
 };
@@ -511,32 +516,71 @@ __device__ __forceinline__ void union_grad(const MarchArgs& a, bool mine, const 
     });
 }
 
-// ---- cooperative finish: the whole warp continues one lane's ray -----------------
+// ---- long rays: the whole warp continues one ray ---------------------------------
 
-template <bool STATS>
-__device__ __forceinline__ void coop_finish(const MarchArgs& a, Ray& mine, int src, int lane, Acc& acc) {
-    Ray r;
-    r.phase = __shfl_sync(kFull, mine.phase, src);
-    r.i = __shfl_sync(kFull, mine.i, src);
-    r.b = __shfl_sync(kFull, mine.b, src);
+// Ray start and step of pixel (px, py) with splat depth z (RayMarcher.cpp:268-274).
+__device__ __forceinline__ void ray_setup(const MarchArgs& a, int px, int py, float z, float p[3], float s[3]) {
+    const float cxp = (float)px * a.twoWinv - 1.0f;
+    const float cyp = (float)py * a.twoHinv - 1.0f;
+    float wh[4];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        r.p[c] = __shfl_sync(kFull, mine.p[c], src);
-        r.q[c] = __shfl_sync(kFull, mine.q[c], src);
-        r.s[c] = __shfl_sync(kFull, mine.s[c], src);
-        r.e[c] = __shfl_sync(kFull, mine.e[c], src);
+    for (int rr = 0; rr < 4; ++rr) {
+        float add0 = a.ipv[0 * 4 + rr] * cxp + a.ipv[1 * 4 + rr] * cyp;
+        float add1 = a.ipv[2 * 4 + rr] * z + a.ipv[3 * 4 + rr] * 1.0f;
+        wh[rr] = add0 + add1;
     }
-    const bool cnt = lane == src;
+    p[0] = wh[0] / wh[3];
+    p[1] = wh[1] / wh[3];
+    p[2] = wh[2] / wh[3];
+    const float dx = p[0] - a.cam[0], dy = p[1] - a.cam[1], dz = p[2] - a.cam[2];
+    const float inv = 1.0f / sqrtf(dot3(dx, dy, dz, dx, dy, dz));
+    s[0] = a.step * (dx * inv);
+    s[1] = a.step * (dy * inv);
+    s[2] = a.step * (dz * inv);
+}
+
+// Long-ray queue entry: 4 float4 = {pixel, phase, i, b}, p, q, e (the pending
+// evaluation point).  The step is recomputed from the pixel.
+__device__ __forceinline__ void push_long(const MarchArgs& a, uint32_t slot, uint32_t idx, const Ray& r) {
+    float4* d = a.longq + 4ull * slot;
+    d[0] = make_float4(__uint_as_float(idx), __int_as_float(r.phase), __int_as_float(r.i), __int_as_float(r.b));
+    d[1] = make_float4(r.p[0], r.p[1], r.p[2], 0.0f);
+    d[2] = make_float4(r.q[0], r.q[1], r.q[2], 0.0f);
+    d[3] = make_float4(r.e[0], r.e[1], r.e[2], 0.0f);
+}
+
+// Sum of gradW at p (canonical order) with the whole warp, identical on every lane.
+template <bool STATS>
+__device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, float px, float py, float pz, float T,
+                                          int lane, Acc& acc, bool cnt, float& gx, float& gy, float& gz) {
+    gx = gy = gz = 0.0f;
     Loc L;
-    // the pending point was prepared already
-    bool need = locate(a.g, r.e[0], r.e[1], r.e[2], L);
-    for (;;) {
-        float rho = density_warp<STATS>(a.g, a.k, L, r.e[0], r.e[1], r.e[2], a.cull, lane, acc, cnt);
-        apply(a, r, rho);
-        need = prepare<STATS>(a, r, L, acc, cnt);
-        if (!need) break;
-    }
-    if (lane == src) mine = r;
+    if (STATS && cnt) acc.evals++;
+    if (!locate(g, px, py, pz, L)) return;
+    for_ranges_warp<STATS>(g, L, T, lane, acc, cnt, [&](uint32_t b, uint32_t e) {
+        for (uint32_t j0 = b; j0 < e; j0 += 32) {
+            const uint32_t j = j0 + (uint32_t)lane;
+            float tx = 0.0f, ty = 0.0f, tz = 0.0f;
+            bool in = false;
+            if (j < e) {
+                const float4 q = __ldg(g.pts + j);
+                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+                const float q2 = dot3(rx, ry, rz, rx, ry, rz);
+                if (q2 < k.h2 && q2 > 0.0f) {
+                    in = true;
+                    gradw_term(k, rx, ry, rz, q2, tx, ty, tz);
+                }
+            }
+            uint32_t bm = __ballot_sync(kFull, in);
+            while (bm) {
+                const int src = __ffs(bm) - 1;
+                bm &= bm - 1u;
+                gx = gx + __shfl_sync(kFull, tx, src);
+                gy = gy + __shfl_sync(kFull, ty, src);
+                gz = gz + __shfl_sync(kFull, tz, src);
+            }
+        }
+    });
 }
 
 template <bool STATS>
@@ -559,24 +603,7 @@ __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
         r.phase = kDone;
         r.i = r.b = 0;
         if (valid && z != 1.0f) {
-            // RayMarcher.cpp:268-274
-            const float cxp = (float)px * a.twoWinv - 1.0f;
-            const float cyp = (float)py * a.twoHinv - 1.0f;
-            float wh[4];
-#pragma unroll
-            for (int rr = 0; rr < 4; ++rr) {
-                float add0 = a.ipv[0 * 4 + rr] * cxp + a.ipv[1 * 4 + rr] * cyp;
-                float add1 = a.ipv[2 * 4 + rr] * z + a.ipv[3 * 4 + rr] * 1.0f;
-                wh[rr] = add0 + add1;
-            }
-            r.p[0] = wh[0] / wh[3];
-            r.p[1] = wh[1] / wh[3];
-            r.p[2] = wh[2] / wh[3];
-            const float dx = r.p[0] - a.cam[0], dy = r.p[1] - a.cam[1], dz = r.p[2] - a.cam[2];
-            const float inv = 1.0f / sqrtf(dot3(dx, dy, dz, dx, dy, dz));
-            r.s[0] = a.step * (dx * inv);
-            r.s[1] = a.step * (dy * inv);
-            r.s[2] = a.step * (dz * inv);
+            ray_setup(a, px, py, z, r.p, r.s);
             r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
             r.phase = kMarch;
         } else {
@@ -589,25 +616,35 @@ __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
         Loc L;
         L.c[0] = L.c[1] = L.c[2] = 0;
         L.u[0] = L.u[1] = L.u[2] = 0.0f;
+        int iters = 0;
+        bool deferred = false;
         for (;;) {
             const bool need = (r.phase == kMarch || r.phase == kBisect) && prepare<STATS>(a, r, L, acc, true);
             const uint32_t act = __ballot_sync(kFull, need);
             if (!act) break;
-            if (__popc(act) <= 2) {
-                // too few rays left for a shared stream: finish them one by one with the whole warp
-                uint32_t m = act;
-                while (m) {
-                    const int src = __ffs(m) - 1;
-                    m &= m - 1u;
-                    coop_finish<STATS>(a, r, src, lane, acc);
+            if (__popc(act) <= 2 || iters >= a.cap) {
+                // Few rays left, or rays that march long (grazing the surface): hand
+                // them to the long-ray pass, where each gets a whole warp, instead of
+                // keeping this warp busy while the rest of the grid idles.
+                const uint32_t base = (lane == 0) ? atomicAdd(a.q_tail, (unsigned)__popc(act)) : 0u;
+                const uint32_t slot = __shfl_sync(kFull, base, 0) + __popc(act & ((1u << lane) - 1u));
+                if (need) {
+                    if (slot < a.q_cap) {
+                        push_long(a, slot, (uint32_t)idx, r);
+                        deferred = true;
+                    } else {
+                        atomicOr(a.status, 4u);  // queue full: cannot happen (capacity = pixels)
+                    }
                 }
                 break;
             }
             const float rho = union_density<STATS>(a, need, L, r.e, acc);
             if (need) apply(a, r, rho);
+            ++iters;
         }
-        // normals of the hit rays (all in phase kNormal), then outputs
-        const bool hit = r.phase == kNormal;
+        // normals of the hit rays (all in phase kNormal), then outputs; deferred
+        // rays are finished (and written) by the long-ray pass
+        const bool hit = !deferred && r.phase == kNormal;
         Loc Lh;
         Lh.c[0] = Lh.c[1] = Lh.c[2] = 0;
         Lh.u[0] = Lh.u[1] = Lh.u[2] = 0.0f;
@@ -623,7 +660,7 @@ __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
             n2 = gz * gi;
             if (STATS) hits++;
         }
-        if (valid) write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
+        if (valid && !deferred) write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
     }
     if (acc.bad) atomicOr(a.status, 2u);
     if (STATS) {
@@ -637,6 +674,66 @@ __global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
             for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
             if (lane == 0 && x) atomicAdd(a.stats + j, x);
         }
+    }
+}
+
+// Long-ray pass: persistent warps take deferred rays one at a time and finish
+// them with all 32 lanes (density_warp / grad_warp), then write the pixel.
+template <bool STATS>
+__global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a) {
+    const int lane = threadIdx.x & 31;
+    Acc acc;
+    uint64_t hits = 0;
+    const unsigned total = min(*(volatile unsigned int*)a.q_tail, a.q_cap);
+    for (;;) {
+        unsigned k = 0;
+        if (lane == 0) k = atomicAdd(a.q_head, 1u);
+        k = __shfl_sync(kFull, k, 0);
+        if (k >= total) break;
+        const float4* d = a.longq + 4ull * k;
+        const float4 w0 = d[0], w1 = d[1], w2 = d[2], w3 = d[3];
+        const uint32_t idx = __float_as_uint(w0.x);
+        Ray r;
+        r.phase = __float_as_int(w0.y);
+        r.i = __float_as_int(w0.z);
+        r.b = __float_as_int(w0.w);
+        r.p[0] = w1.x; r.p[1] = w1.y; r.p[2] = w1.z;
+        r.q[0] = w2.x; r.q[1] = w2.y; r.q[2] = w2.z;
+        r.e[0] = w3.x; r.e[1] = w3.y; r.e[2] = w3.z;
+        const int px = (int)(idx % (uint32_t)a.W), py = (int)(idx / (uint32_t)a.W);
+        float p0[3];
+        ray_setup(a, px, py, a.zbuf[idx], p0, r.s);
+        const bool cnt = lane == 0;
+        Loc L;
+        bool need = locate(a.g, r.e[0], r.e[1], r.e[2], L);  // the pending point was prepared
+        while (need) {
+            const float rho = density_warp<STATS>(a.g, a.k, L, r.e[0], r.e[1], r.e[2], a.cull, lane, acc, cnt);
+            apply(a, r, rho);
+            need = prepare<STATS>(a, r, L, acc, cnt);
+        }
+        const bool hit = r.phase == kNormal;
+        float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+        if (hit) {
+            float gx, gy, gz;
+            grad_warp<STATS>(a.g, a.k, r.p[0], r.p[1], r.p[2], a.cull, lane, acc, cnt, gx, gy, gz);
+            const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+            n0 = gx * gi;
+            n1 = gy * gi;
+            n2 = gz * gi;
+        }
+        if (lane == 0) {
+            write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
+            if (STATS && hit) hits++;
+        }
+    }
+    if (acc.bad) atomicOr(a.status, 2u);
+    if (STATS && lane == 0) {
+        const unsigned long long v[kStats] = {0ull, 0ull, hits, (unsigned long long)acc.evals,
+                                              (unsigned long long)acc.cand, (unsigned long long)acc.skipped,
+                                              (unsigned long long)acc.tested};
+#pragma unroll
+        for (int j = 0; j < kStats; ++j)
+            if (v[j]) atomicAdd(a.stats + j, v[j]);
     }
 }
 
@@ -676,20 +773,42 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
     a.col = o.col;
     a.stats = ctx->stats_enabled ? ctx->d_stats : nullptr;
     a.status = ctx->d_status;
-    // a fresh tile counter per launch (a ring of slots, so launches on
-    // different streams do not share one)
-    a.tile_counter = ctx->d_work + (ctx->work_slot++ % kWorkSlots) * 32;
-    FM_CUDA(ctx, cudaMemsetAsync(a.tile_counter, 0, sizeof(unsigned int), st));
+    // fresh counters per launch (a ring of slots, so launches on different
+    // streams do not share them): word 0 tiles, word 1 queue tail, word 2 queue head
+    unsigned int* slot = ctx->d_work + (ctx->work_slot++ % kWorkSlots) * 32;
+    a.tile_counter = slot;
+    a.q_tail = slot + 1;
+    a.q_head = slot + 2;
+    FM_CUDA(ctx, cudaMemsetAsync(slot, 0, 3 * sizeof(unsigned int), st));
+    // long-ray queue: at most one entry per pixel
+    const uint64_t npx = (uint64_t)cam->width * (uint64_t)cam->height;
+    if (ctx->longq.bytes < npx * 64) {
+        FM_CUDA(ctx, cudaStreamSynchronize(st));  // the buffer may be in use by an earlier launch
+        if (ctx->longq.p) cudaFree(ctx->longq.p);
+        ctx->longq.p = nullptr;
+        ctx->longq.bytes = 0;
+        if (cudaMalloc(&ctx->longq.p, npx * 64) != cudaSuccess) return set_err(ctx, FM_ERR_OOM, "long-ray queue allocation failed");
+        ctx->longq.bytes = npx * 64;
+    }
+    a.longq = (float4*)ctx->longq.p;
+    a.q_cap = (unsigned int)npx;
+    a.cap = 32;
     int blocks_per_sm = 0;
     if (a.stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<true>, kThreads, 0);
     else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<false>, kThreads, 0);
     if (blocks_per_sm < 1) blocks_per_sm = 1;
-    const int warps_needed = a.ntiles;
     int blocks = ctx->sm_count * blocks_per_sm;
-    const int max_blocks = (warps_needed + kThreads / 32 - 1) / (kThreads / 32);
+    const int max_blocks = (a.ntiles + kThreads / 32 - 1) / (kThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
     if (a.stats) k_march<true><<<blocks, kThreads, 0, st>>>(a);
     else k_march<false><<<blocks, kThreads, 0, st>>>(a);
+    FM_CUDA(ctx, cudaGetLastError());
+    int long_per_sm = 0;
+    if (a.stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<true>, kThreads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<false>, kThreads, 0);
+    if (long_per_sm < 1) long_per_sm = 1;
+    if (a.stats) k_march_long<true><<<ctx->sm_count * long_per_sm, kThreads, 0, st>>>(a);
+    else k_march_long<false><<<ctx->sm_count * long_per_sm, kThreads, 0, st>>>(a);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }
