@@ -133,6 +133,7 @@ static void scene_free(fm_scene* s) {
     cudaFree(s->d_sub);
     cudaFree(s->d_bound);
     cudaFree(s->d_flag);
+    cudaFree(s->d_interior);
     delete s;
 }
 
@@ -149,6 +150,7 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->d_stats);
     cudaFree(ctx->d_work);
     cudaFree(ctx->longq.p);
+    cudaFree(ctx->hiz.p);
     if (ctx->h_pinned_small) cudaFreeHost(ctx->h_pinned_small);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

@@ -444,18 +444,24 @@ __device__ __forceinline__ void union_stream(const GridDev& g, bool mine, const 
                 if (y < 0 || y >= Hd) continue;
                 const uint32_t own = in ? own_row_mask(g, L, ax, y, z, gx, T) : 0u;
                 uint32_t uni = __reduce_or_sync(kFull, own);
+                if (!uni) continue;
                 const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
                 // base wraps below 0 when row + gx == 0; then only bits >= 8 are set.
                 const uint32_t base = 8u * (row + (uint32_t)gx) - 8u;
+                // the row's 33 sub-cell starts in one coalesced load: lane l holds
+                // start base + l, lane 0 also start base + 32 (indices past the
+                // table, including wrapped ones, are never used: their bits are clear)
+                const uint32_t il = base + (uint32_t)(threadIdx.x & 31);
+                const uint32_t mystart = il < g.nsub ? __ldg(g.sub + il) : 0u;
+                const uint32_t i32 = base + 32u;
+                const uint32_t start32 = i32 < g.nsub ? __ldg(g.sub + i32) : 0u;
+                if ((uni >> 31) && i32 >= g.nsub) acc.bad = true;  // cannot happen for a consistent table
                 while (uni) {
                     const int u = __ffs(uni) - 1;
                     uni &= uni - 1u;
-                    const uint32_t i0 = base + (uint32_t)u;
-                    if (i0 + 1u >= g.nsub) {  // cannot happen for a consistent table
-                        acc.bad = true;
-                        continue;
-                    }
-                    const uint32_t b = __ldg(g.sub + i0), e = __ldg(g.sub + i0 + 1u);
+                    const uint32_t b = __shfl_sync(kFull, mystart, u);
+                    const uint32_t enext = __shfl_sync(kFull, mystart, (u + 1) & 31);
+                    const uint32_t e = (u == 31) ? start32 : enext;
                     const bool pred = (own >> u) & 1u;
                     if (STATS && pred) acc.tested += e - b;
                     f(pred, b, e);
@@ -474,18 +480,25 @@ __device__ __forceinline__ float union_density(const MarchArgs& a, bool mine, co
     float rho = 0.0f;
     union_stream<STATS>(a.g, mine, L, a.cull, acc, [&](bool pred, uint32_t b, uint32_t e_) {
         uint32_t j = b;
-        for (; j + 2 <= e_; j += 2) {
+        for (; j + 4 <= e_; j += 4) {
             const float4 q0 = __ldg(a.g.pts + j), q1 = __ldg(a.g.pts + j + 1);
+            const float4 q2 = __ldg(a.g.pts + j + 2), q3 = __ldg(a.g.pts + j + 3);
             if (pred) {
                 const float r0x = q0.x - px, r0y = q0.y - py, r0z = q0.z - pz;
                 const float r1x = q1.x - px, r1y = q1.y - py, r1z = q1.z - pz;
+                const float r2x = q2.x - px, r2y = q2.y - py, r2z = q2.z - pz;
+                const float r3x = q3.x - px, r3y = q3.y - py, r3z = q3.z - pz;
                 const float d0 = dot3(r0x, r0y, r0z, r0x, r0y, r0z);
                 const float d1 = dot3(r1x, r1y, r1z, r1x, r1y, r1z);
+                const float d2 = dot3(r2x, r2y, r2z, r2x, r2y, r2z);
+                const float d3 = dot3(r3x, r3y, r3z, r3x, r3y, r3z);
                 if (d0 < k.h2) rho = rho + w_in(k, d0);
                 if (d1 < k.h2) rho = rho + w_in(k, d1);
+                if (d2 < k.h2) rho = rho + w_in(k, d2);
+                if (d3 < k.h2) rho = rho + w_in(k, d3);
             }
         }
-        if (j < e_) {
+        for (; j < e_; ++j) {
             const float4 q = __ldg(a.g.pts + j);
             if (pred) {
                 const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
@@ -584,7 +597,7 @@ __device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, 
 }
 
 template <bool STATS>
-__global__ void __launch_bounds__(kThreads) k_march(const MarchArgs a) {
+__global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a) {
     const int lane = threadIdx.x & 31;
     Acc acc;
     uint64_t rays = 0, started_n = 0, hits = 0;

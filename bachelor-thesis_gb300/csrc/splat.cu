@@ -7,15 +7,23 @@
 // into a D32 buffer cleared to 1.0 with a LESS test (DepthRenderPass.cpp:54,179).
 // The quad lies in the view-space plane z = view_z(p), so for a pixel centre
 // the quad point is (ndc * z / P00, ndc * z / P11) and UV follows directly.
-// This kernel evaluates exactly that per covered pixel centre, in the same
-// FP32 operation order as the CPU oracle, and keeps the minimum with an
-// atomicMin on the float bits (depths are in [0, 1), where the uint order is
-// the float order).  cos is a degree-16 Taylor polynomial (coefficients
+// Each covered pixel centre gets exactly that value, in the same FP32
+// operation order as the CPU oracle, and the buffer keeps the minimum through
+// an atomicMin on the float bits (depths are in [0, 1), where the uint order
+// is the float order).  cos is a degree-16 Taylor polynomial (coefficients
 // 1/(2k)! as exact float literals), identical in the oracle.
 //
-// Memory: reads 16 B per particle (cell-sorted float4), one 4 B atomic per
-// covered pixel.  Particles whose disc is not fully in front of the camera
-// (view z - R <= 0) and fragments outside [0, 1) are dropped.
+// Two passes keep the work near the visible surface without changing the
+// result (the buffer is a minimum, so skipping a particle that cannot lower
+// any pixel is exact):
+//   1. particles of boundary cells (cells with an empty or missing neighbour)
+//      are splatted in full;
+//   2. a max-depth pyramid level (8x8-pixel tiles) is built from the buffer;
+//   3. particles of interior cells are splatted only if some tile under
+//      their disc holds a depth above the nearest depth their disc can have
+//      (the depth at view z - R, lowered by a few ulps for rounding).
+// Memory: 16 B per particle, 4 B read (+ atomic) per covered pixel of a
+// splatted particle, 4 B per tile of the pyramid.
 
 #include <cuda_runtime.h>
 
@@ -24,12 +32,22 @@
 namespace fm {
 namespace {
 
+constexpr int kHizTile = 8;
+
 struct SplatArgs {
     float V[16];
     float P00, P11, P22, P32, P23, P33;
     float R, invR;
     float twoWinv, twoHinv;
     int W, Hh;
+    // grid, for the cell of a particle
+    float gmin[3];
+    float ginv;
+    int gdims[3];
+    const uint8_t* __restrict__ interior;  // per cell: all 26 neighbours exist and hold particles
+    const float* __restrict__ hiz;         // per 8x8 tile: max depth after pass 1
+    int hiz_w, hiz_h;
+    int hiz_ok;                            // depth grows with view z (pass 2 may cull)
 };
 
 __device__ __forceinline__ float cos_poly(float t) {
@@ -51,11 +69,45 @@ __global__ void k_fill(uint32_t* __restrict__ d, uint64_t n, uint32_t v) {
     if (i < n) d[i] = v;
 }
 
-__global__ void __launch_bounds__(256) k_splat(const float4* __restrict__ pts, uint64_t n, SplatArgs a,
-                                               uint32_t* __restrict__ depth) {
-    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 q = pts[i];
+// Interior cells: the cell and its 26 neighbours exist and hold particles.
+__global__ void k_interior(GridDev g, uint8_t* __restrict__ flag) {
+    const uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
+    const uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    const int x = (int)(c % (uint64_t)g.dims[0]);
+    const int y = (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]);
+    const int z = (int)(c / ((uint64_t)g.dims[0] * g.dims[1]));
+    bool in = true;
+    for (int dz = -1; dz <= 1 && in; ++dz)
+        for (int dy = -1; dy <= 1 && in; ++dy)
+            for (int dx = -1; dx <= 1 && in; ++dx) {
+                const int xx = x + dx, yy = y + dy, zz = z + dz;
+                if (xx < 0 || yy < 0 || zz < 0 || xx >= g.dims[0] || yy >= g.dims[1] || zz >= g.dims[2]) {
+                    in = false;
+                    break;
+                }
+                const uint64_t n = (uint64_t)xx + (uint64_t)yy * g.dims[0] + (uint64_t)zz * g.dims[0] * g.dims[1];
+                if (g.sub[8 * n + 8] == g.sub[8 * n]) in = false;
+            }
+    flag[c] = in ? 1 : 0;
+}
+
+__device__ __forceinline__ bool is_interior(const SplatArgs& a, const float4& q) {
+    const float p[3] = {q.x, q.y, q.z};
+    int c[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const int v = (int)floorf((p[k] - a.gmin[k]) * a.ginv);
+        c[k] = min(max(v, 0), a.gdims[k] - 1);
+    }
+    const uint64_t lin = (uint64_t)c[0] + (uint64_t)c[1] * a.gdims[0] + (uint64_t)c[2] * a.gdims[0] * a.gdims[1];
+    return a.interior[lin] != 0;
+}
+
+// View-space centre and conservative pixel box of a particle's disc.
+// Returns false when the disc is not entirely in front of the camera or off screen.
+__device__ __forceinline__ bool disc_box(const SplatArgs& a, const float4& q, float& cx, float& cy, float& cz, int& x0,
+                                         int& x1, int& y0, int& y1) {
     float c[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -63,9 +115,11 @@ __global__ void __launch_bounds__(256) k_splat(const float4* __restrict__ pts, u
         float add1 = a.V[2 * 4 + r] * q.z + a.V[3 * 4 + r] * 1.0f;
         c[r] = add0 + add1;
     }
-    const float cx = c[0] / c[3], cy = c[1] / c[3], cz = c[2] / c[3];
+    cx = c[0] / c[3];
+    cy = c[1] / c[3];
+    cz = c[2] / c[3];
     const float R = a.R;
-    if (!(cz - R > 0.0f)) return;
+    if (!(cz - R > 0.0f)) return false;
     float nx0 = a.P00 * (cx - R) / cz, nx1 = a.P00 * (cx + R) / cz;
     float ny0 = a.P11 * (cy - R) / cz, ny1 = a.P11 * (cy + R) / cz;
     float xa = fminf(nx0, nx1), xb = fmaxf(nx0, nx1);
@@ -74,9 +128,17 @@ __global__ void __launch_bounds__(256) k_splat(const float4* __restrict__ pts, u
     float fx1 = ceilf((xb + 1.0f) * 0.5f * (float)a.W - 0.5f) + 1.0f;
     float fy0 = floorf((ya + 1.0f) * 0.5f * (float)a.Hh - 0.5f) - 1.0f;
     float fy1 = ceilf((yb + 1.0f) * 0.5f * (float)a.Hh - 0.5f) + 1.0f;
-    if (fx1 < 0.0f || fy1 < 0.0f || fx0 > (float)(a.W - 1) || fy0 > (float)(a.Hh - 1)) return;
-    int x0 = max(0, (int)fmaxf(fx0, -1.0f)), x1 = min(a.W - 1, (int)fminf(fx1, (float)a.W));
-    int y0 = max(0, (int)fmaxf(fy0, -1.0f)), y1 = min(a.Hh - 1, (int)fminf(fy1, (float)a.Hh));
+    if (fx1 < 0.0f || fy1 < 0.0f || fx0 > (float)(a.W - 1) || fy0 > (float)(a.Hh - 1)) return false;
+    x0 = max(0, (int)fmaxf(fx0, -1.0f));
+    x1 = min(a.W - 1, (int)fminf(fx1, (float)a.W));
+    y0 = max(0, (int)fmaxf(fy0, -1.0f));
+    y1 = min(a.Hh - 1, (int)fminf(fy1, (float)a.Hh));
+    return true;
+}
+
+__device__ __forceinline__ void splat_disc(const SplatArgs& a, float cx, float cy, float cz, int x0, int x1, int y0,
+                                           int y1, uint32_t* __restrict__ depth) {
+    const float R = a.R;
     for (int y = y0; y <= y1; ++y) {
         float ny = ((float)y + 0.5f) * a.twoHinv - 1.0f;
         float vy = (ny * cz) / a.P11;
@@ -99,6 +161,71 @@ __global__ void __launch_bounds__(256) k_splat(const float4* __restrict__ pts, u
     }
 }
 
+// pass 1 (boundary particles) or the single pass (interior == null)
+__global__ void __launch_bounds__(256) k_splat(const float4* __restrict__ pts, uint64_t n, SplatArgs a,
+                                               uint32_t* __restrict__ depth) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 q = pts[i];
+    if (a.interior && is_interior(a, q)) return;
+    float cx, cy, cz;
+    int x0, x1, y0, y1;
+    if (!disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) return;
+    splat_disc(a, cx, cy, cz, x0, x1, y0, y1, depth);
+}
+
+// Max depth of each 8x8 tile of the buffer.
+__global__ void k_hiz(const float* __restrict__ depth, int W, int Hh, int tw, int th, float* __restrict__ hiz) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= tw * th) return;
+    const int tx = t % tw, ty = t / tw;
+    float m = 0.0f;
+    for (int y = ty * kHizTile; y < min(ty * kHizTile + kHizTile, Hh); ++y)
+        for (int x = tx * kHizTile; x < min(tx * kHizTile + kHizTile, W); ++x) m = fmaxf(m, depth[(uint64_t)y * W + x]);
+    hiz[t] = m;
+}
+
+// pass 3: interior particles, culled against the tile maxima.
+__global__ void __launch_bounds__(256) k_splat_interior(const float4* __restrict__ pts, uint64_t n, SplatArgs a,
+                                                        uint32_t* __restrict__ depth) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 q = pts[i];
+    if (!is_interior(a, q)) return;
+    float cx, cy, cz;
+    int x0, x1, y0, y1;
+    if (!disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) return;
+    if (a.hiz_ok) {
+        // nearest depth the disc can produce (view z - R; every fragment has
+        // view z >= that), lowered by 8 ulps so that rounding in the fragment
+        // formula cannot go below it
+        const float zv = cz - a.R;
+        const float d0 = (a.P22 * zv + a.P32) / (a.P23 * zv + a.P33);
+        uint32_t db = __float_as_uint(fmaxf(d0, 0.0f));  // NaN -> 0
+        db = db > 8u ? db - 8u : 0u;
+        const float dmin = __uint_as_float(db);
+        bool needed = false;
+        for (int ty = y0 / kHizTile; ty <= y1 / kHizTile && !needed; ++ty)
+            for (int tx = x0 / kHizTile; tx <= x1 / kHizTile; ++tx)
+                if (a.hiz[ty * a.hiz_w + tx] > dmin) {
+                    needed = true;
+                    break;
+                }
+        if (!needed) return;  // every pixel under the disc already holds a depth <= any of its fragments
+    }
+    splat_disc(a, cx, cy, cz, x0, x1, y0, y1, depth);
+}
+
+bool grow(DevBuf& b, size_t bytes) {
+    if (b.bytes >= bytes) return true;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    if (cudaMalloc(&b.p, bytes) != cudaSuccess) return false;
+    b.bytes = bytes;
+    return true;
+}
+
 }  // namespace
 
 int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_depth, cudaStream_t st) {
@@ -116,9 +243,39 @@ int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_
     a.Hh = cam->height;
     a.twoWinv = 2.0f / (float)cam->width;
     a.twoHinv = 2.0f / (float)cam->height;
-    uint64_t npx = (uint64_t)cam->width * cam->height;
+    for (int k = 0; k < 3; ++k) {
+        a.gmin[k] = s->min[k];
+        a.gdims[k] = s->dims[k];
+    }
+    a.ginv = s->inv;
+    a.interior = nullptr;
+    a.hiz = nullptr;
+    a.hiz_w = (cam->width + kHizTile - 1) / kHizTile;
+    a.hiz_h = (cam->height + kHizTile - 1) / kHizTile;
+    // the culling test needs depth to grow with view z: d(z) = (P22 z + P32) / (P23 z + P33)
+    a.hiz_ok = (a.P22 * a.P33 - a.P32 * a.P23) > 0.0f && a.P23 > 0.0f && a.P33 >= 0.0f;
+    const uint64_t npx = (uint64_t)cam->width * cam->height;
     k_fill<<<(unsigned)((npx + 255) / 256), 256, 0, st>>>((uint32_t*)d_depth, npx, 0x3f800000u);
-    if (s->n > 0) k_splat<<<(unsigned)((s->n + 255) / 256), 256, 0, st>>>(s->d_pts, s->n, a, (uint32_t*)d_depth);
+    if (s->n == 0) return FM_OK;
+    fm_scene* sm = const_cast<fm_scene*>(s);
+    if (!sm->interior_valid) {
+        if (!sm->d_interior && cudaMalloc(&sm->d_interior, sm->cell_capacity) != cudaSuccess)
+            return set_err(ctx, FM_ERR_OOM, "interior flag allocation failed");
+        k_interior<<<(unsigned)((s->ncells + 255) / 256), 256, 0, st>>>(grid_dev(s), sm->d_interior);
+        sm->interior_valid = true;
+    }
+    a.interior = sm->d_interior;
+    const unsigned blocks = (unsigned)((s->n + 255) / 256);
+    k_splat<<<blocks, 256, 0, st>>>(s->d_pts, s->n, a, (uint32_t*)d_depth);
+    const size_t hiz_bytes = (size_t)a.hiz_w * a.hiz_h * sizeof(float);
+    if (ctx->hiz.bytes < hiz_bytes) {
+        FM_CUDA(ctx, cudaStreamSynchronize(st));  // the old buffer may still be in use on this stream
+        if (!grow(ctx->hiz, hiz_bytes)) return set_err(ctx, FM_ERR_OOM, "depth tile allocation failed");
+    }
+    a.hiz = (const float*)ctx->hiz.p;
+    const int tiles = a.hiz_w * a.hiz_h;
+    k_hiz<<<(tiles + 255) / 256, 256, 0, st>>>(d_depth, a.W, a.Hh, a.hiz_w, a.hiz_h, (float*)ctx->hiz.p);
+    k_splat_interior<<<blocks, 256, 0, st>>>(s->d_pts, s->n, a, (uint32_t*)d_depth);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }
