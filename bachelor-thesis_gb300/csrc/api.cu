@@ -133,7 +133,6 @@ static void scene_free(fm_scene* s) {
     cudaFree(s->d_sub);
     cudaFree(s->d_bound);
     cudaFree(s->d_flag);
-    cudaFree(s->d_interior);
     delete s;
 }
 
@@ -151,6 +150,7 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->d_work);
     cudaFree(ctx->longq.p);
     cudaFree(ctx->hiz.p);
+    cudaFree(ctx->splat_list.p);
     if (ctx->h_pinned_small) cudaFreeHost(ctx->h_pinned_small);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;

@@ -174,9 +174,11 @@ struct fm_ctx {
     fm::DevBuf scratch[8];
     // long-ray queue of the march (64 B per pixel of the largest view so far)
     fm::DevBuf longq;
-    // splat depth tile maxima (4 B per 8x8 tile); renders of one context on
-    // different streams must not overlap
+    // splat depth tile maxima (4 B per 8x8 tile) and the list of particles that
+    // survive the tile test; renders of one context on different streams must
+    // not overlap
     fm::DevBuf hiz;
+    fm::DevBuf splat_list;
     // live scenes of this context; fm_destroy frees the ones still alive
     std::vector<fm_scene*> scenes;
     void* h_pinned_small = nullptr;  // 256 bytes of pinned memory for small readbacks
@@ -198,10 +200,8 @@ struct fm_scene {
     uint32_t* d_sub = nullptr;     // 8 * ncells + 1 sub-cell starts
     float* d_bound = nullptr;      // per sub-cell density bound (lazy)
     uint8_t* d_flag = nullptr;     // per-cell reference flag (lazy)
-    uint8_t* d_interior = nullptr; // per-cell: 26 neighbours all hold particles (lazy, splat culling)
     bool bound_valid = false;
     bool flag_valid = false;
-    bool interior_valid = false;
 };
 
 namespace fm {

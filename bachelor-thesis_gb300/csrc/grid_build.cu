@@ -438,14 +438,12 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     s->ncells = ncells;
     s->bound_valid = false;
     s->flag_valid = false;
-    s->interior_valid = false;
     const uint64_t nkeys = 8 * ncells;
     if (ncells > s->cell_capacity) {
         cudaFree(s->d_sub);
         cudaFree(s->d_bound);
         cudaFree(s->d_flag);
-        cudaFree(s->d_interior);
-        s->d_sub = nullptr; s->d_bound = nullptr; s->d_flag = nullptr; s->d_interior = nullptr;
+        s->d_sub = nullptr; s->d_bound = nullptr; s->d_flag = nullptr;
         if (cudaMalloc(&s->d_sub, (nkeys + 1) * sizeof(uint32_t)) != cudaSuccess ||
             cudaMalloc(&s->d_bound, nkeys * sizeof(float)) != cudaSuccess ||
             cudaMalloc(&s->d_flag, ncells) != cudaSuccess) {

@@ -13,20 +13,21 @@
 // is the float order).  cos is a degree-16 Taylor polynomial (coefficients
 // 1/(2k)! as exact float literals), identical in the oracle.
 //
-// Two passes keep the work near the visible surface without changing the
-// result (the buffer is a minimum, so skipping a particle that cannot lower
-// any pixel is exact):
-//   1. every 8th particle and every particle of a boundary cell (a cell with
-//      an empty or missing neighbour) is splatted in full: their discs, about
-//      five particle spacings wide, already cover the front surface;
-//   2. a max-depth pyramid level (8x8-pixel tiles) is built from the buffer;
-//   3. the other particles are splatted only if some tile under their disc
-//      holds a depth above the nearest depth their disc can have (the depth
-//      at view z - R, lowered by 8 ulps for rounding).  The buffer after pass
-//      1 is >= the final one, so the test never drops a fragment that would
-//      have won a pixel.
+// A warp splats one particle: its lanes walk the disc's pixel box 32 pixels
+// at a time.  Three passes keep the work near the visible surface without
+// changing the result (the buffer is a minimum, so leaving out a particle that
+// cannot lower any pixel is exact):
+//   1. every 8th particle is splatted: the discs, about five particle spacings
+//      wide, already form an opaque cover of the front surface;
+//   2. a max-depth tile level (8x8 pixels) is built from the buffer, and every
+//      other particle is tested against it: it is kept only if some tile
+//      under its disc holds a depth above the nearest depth the disc can have
+//      (the depth at view z - R, lowered by 8 ulps for rounding); the buffer
+//      after pass 1 is >= the final one, so no fragment that would win a
+//      pixel is dropped;
+//   3. the kept particles are splatted.
 // Memory: 16 B per particle, 4 B read (+ atomic) per covered pixel of a
-// splatted particle, 4 B per tile of the pyramid.
+// splatted particle, 4 B per tile.
 
 #include <cuda_runtime.h>
 
@@ -36,6 +37,8 @@ namespace fm {
 namespace {
 
 constexpr int kHizTile = 8;
+constexpr uint64_t kSample = 8;
+constexpr int kThreads = 256;
 
 struct SplatArgs {
     float V[16];
@@ -43,14 +46,8 @@ struct SplatArgs {
     float R, invR;
     float twoWinv, twoHinv;
     int W, Hh;
-    // grid, for the cell of a particle
-    float gmin[3];
-    float ginv;
-    int gdims[3];
-    const uint8_t* __restrict__ interior;  // per cell: all 26 neighbours exist and hold particles
-    const float* __restrict__ hiz;         // per 8x8 tile: max depth after pass 1
+    const float* __restrict__ hiz;  // per 8x8 tile: max depth after pass 1
     int hiz_w, hiz_h;
-    int hiz_ok;                            // depth grows with view z (pass 2 may cull)
 };
 
 __device__ __forceinline__ float cos_poly(float t) {
@@ -70,41 +67,6 @@ __device__ __forceinline__ float cos_poly(float t) {
 __global__ void k_fill(uint32_t* __restrict__ d, uint64_t n, uint32_t v) {
     uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i < n) d[i] = v;
-}
-
-// Interior cells: the cell and its 26 neighbours exist and hold particles.
-__global__ void k_interior(GridDev g, uint8_t* __restrict__ flag) {
-    const uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
-    const uint64_t c = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (c >= ncells) return;
-    const int x = (int)(c % (uint64_t)g.dims[0]);
-    const int y = (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]);
-    const int z = (int)(c / ((uint64_t)g.dims[0] * g.dims[1]));
-    bool in = true;
-    for (int dz = -1; dz <= 1 && in; ++dz)
-        for (int dy = -1; dy <= 1 && in; ++dy)
-            for (int dx = -1; dx <= 1 && in; ++dx) {
-                const int xx = x + dx, yy = y + dy, zz = z + dz;
-                if (xx < 0 || yy < 0 || zz < 0 || xx >= g.dims[0] || yy >= g.dims[1] || zz >= g.dims[2]) {
-                    in = false;
-                    break;
-                }
-                const uint64_t n = (uint64_t)xx + (uint64_t)yy * g.dims[0] + (uint64_t)zz * g.dims[0] * g.dims[1];
-                if (g.sub[8 * n + 8] == g.sub[8 * n]) in = false;
-            }
-    flag[c] = in ? 1 : 0;
-}
-
-__device__ __forceinline__ bool is_interior(const SplatArgs& a, const float4& q) {
-    const float p[3] = {q.x, q.y, q.z};
-    int c[3];
-#pragma unroll
-    for (int k = 0; k < 3; ++k) {
-        const int v = (int)floorf((p[k] - a.gmin[k]) * a.ginv);
-        c[k] = min(max(v, 0), a.gdims[k] - 1);
-    }
-    const uint64_t lin = (uint64_t)c[0] + (uint64_t)c[1] * a.gdims[0] + (uint64_t)c[2] * a.gdims[0] * a.gdims[1];
-    return a.interior[lin] != 0;
 }
 
 // View-space centre and conservative pixel box of a particle's disc.
@@ -139,52 +101,57 @@ __device__ __forceinline__ bool disc_box(const SplatArgs& a, const float4& q, fl
     return true;
 }
 
-__device__ __forceinline__ void splat_disc(const SplatArgs& a, float cx, float cy, float cz, int x0, int x1, int y0,
-                                           int y1, uint32_t* __restrict__ depth) {
+// One pixel centre of a disc (depth.frag:19-34 restated).
+__device__ __forceinline__ void splat_pixel(const SplatArgs& a, float cx, float cy, float cz, int x, int y,
+                                            uint32_t* __restrict__ depth) {
     const float R = a.R;
-    for (int y = y0; y <= y1; ++y) {
-        float ny = ((float)y + 0.5f) * a.twoHinv - 1.0f;
-        float vy = (ny * cz) / a.P11;
-        float vv = (vy - cy) * a.invR;
-        for (int x = x0; x <= x1; ++x) {
-            float nx = ((float)x + 0.5f) * a.twoWinv - 1.0f;
-            float vx = (nx * cz) / a.P00;
-            float uu = (vx - cx) * a.invR;
-            float l2 = uu * uu + vv * vv;
-            if (l2 > 1.0f) continue;
-            float off = cos_poly(1.57079632679f * sqrtf(l2));
-            float zv = cz - R * off;
-            float d = (a.P22 * zv + a.P32) / (a.P23 * zv + a.P33);
-            if (!(d >= 0.0f && d < 1.0f)) continue;
-            d = d + 0.0f;
-            uint32_t* dst = depth + (uint64_t)y * a.W + x;
-            uint32_t bits = __float_as_uint(d);
-            // plain (possibly stale) read first: the buffer only decreases, so a
-            // stale value is >= the current one and skipping on it is safe
-            if (bits < *dst) atomicMin(dst, bits);
-        }
+    float ny = ((float)y + 0.5f) * a.twoHinv - 1.0f;
+    float vy = (ny * cz) / a.P11;
+    float vv = (vy - cy) * a.invR;
+    float nx = ((float)x + 0.5f) * a.twoWinv - 1.0f;
+    float vx = (nx * cz) / a.P00;
+    float uu = (vx - cx) * a.invR;
+    float l2 = uu * uu + vv * vv;
+    if (l2 > 1.0f) return;
+    float off = cos_poly(1.57079632679f * sqrtf(l2));
+    float zv = cz - R * off;
+    float d = (a.P22 * zv + a.P32) / (a.P23 * zv + a.P33);
+    if (!(d >= 0.0f && d < 1.0f)) return;
+    d = d + 0.0f;
+    uint32_t* dst = depth + (uint64_t)y * a.W + x;
+    uint32_t bits = __float_as_uint(d);
+    // plain (possibly stale) read first: the buffer only decreases, so a
+    // stale value is >= the current one and skipping on it is safe
+    if (bits < *dst) atomicMin(dst, bits);
+}
+
+// The whole warp splats one disc: lane l starts at box pixel l and advances
+// 32 pixels per step.
+__device__ __forceinline__ void splat_disc_warp(const SplatArgs& a, float cx, float cy, float cz, int x0, int x1,
+                                                int y0, int y1, int lane, uint32_t* __restrict__ depth) {
+    const int bw = x1 - x0 + 1;
+    int x = x0 + lane, y = y0;
+    while (x > x1) { x -= bw; ++y; }
+    while (y <= y1) {
+        splat_pixel(a, cx, cy, cz, x, y, depth);
+        x += 32;
+        while (x > x1) { x -= bw; ++y; }
     }
 }
 
-// The first pass splats every kSample-th particle and every particle of a
-// boundary cell: a sparse but opaque cover of the front surface.
-constexpr uint64_t kSample = 8;
-
-__device__ __forceinline__ bool first_pass(const SplatArgs& a, uint64_t i, const float4& q) {
-    return (i % kSample) == 0 || !is_interior(a, q);
-}
-
-// pass 1 (interior != null) or the single pass (interior == null)
-__global__ void __launch_bounds__(256) k_splat(const float4* __restrict__ pts, uint64_t n, SplatArgs a,
-                                               uint32_t* __restrict__ depth) {
-    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 q = pts[i];
-    if (a.interior && !first_pass(a, i, q)) return;
-    float cx, cy, cz;
-    int x0, x1, y0, y1;
-    if (!disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) return;
-    splat_disc(a, cx, cy, cz, x0, x1, y0, y1, depth);
+// Pass 1 (stride = kSample) or the only pass (stride = 1): warp w splats
+// particle w * stride, for every warp of a persistent grid.
+__global__ void __launch_bounds__(kThreads) k_splat_warp(const float4* __restrict__ pts, uint64_t n, uint64_t stride,
+                                                        SplatArgs a, uint32_t* __restrict__ depth) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (kThreads / 32);
+    for (uint64_t w = (blockIdx.x * (uint64_t)kThreads + threadIdx.x) / 32; w * stride < n; w += warps) {
+        const float4 q = pts[w * stride];
+        float cx, cy, cz;
+        int x0, x1, y0, y1;
+        if (!disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) continue;
+        splat_disc_warp(a, cx, cy, cz, x0, x1, y0, y1, lane, depth);
+    }
 }
 
 // Max depth of each 8x8 tile of the buffer.
@@ -198,35 +165,56 @@ __global__ void k_hiz(const float* __restrict__ depth, int W, int Hh, int tw, in
     hiz[t] = m;
 }
 
-// pass 3: the particles pass 1 left out, culled against the tile maxima.
-__global__ void __launch_bounds__(256) k_splat_interior(const float4* __restrict__ pts, uint64_t n, SplatArgs a,
-                                                        uint32_t* __restrict__ depth) {
-    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float4 q = pts[i];
-    if (first_pass(a, i, q)) return;
-    float cx, cy, cz;
-    int x0, x1, y0, y1;
-    if (!disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) return;
-    if (a.hiz_ok) {
-        // nearest depth the disc can produce (view z - R; every fragment has
-        // view z >= that), lowered by 8 ulps so that rounding in the fragment
-        // formula cannot go below it
-        const float zv = cz - a.R;
-        const float d0 = (a.P22 * zv + a.P32) / (a.P23 * zv + a.P33);
-        uint32_t db = __float_as_uint(fmaxf(d0, 0.0f));  // NaN -> 0
-        db = db > 8u ? db - 8u : 0u;
-        const float dmin = __uint_as_float(db);
-        bool needed = false;
-        for (int ty = y0 / kHizTile; ty <= y1 / kHizTile && !needed; ++ty)
-            for (int tx = x0 / kHizTile; tx <= x1 / kHizTile; ++tx)
-                if (a.hiz[ty * a.hiz_w + tx] > dmin) {
-                    needed = true;
-                    break;
-                }
-        if (!needed) return;  // every pixel under the disc already holds a depth <= any of its fragments
+// Pass 2: the particles pass 1 left out, tested against the tile maxima; the
+// ones that may still lower a pixel are appended to `list`.
+__global__ void __launch_bounds__(kThreads) k_splat_cull(const float4* __restrict__ pts, uint64_t n, SplatArgs a,
+                                                        uint32_t* __restrict__ list, unsigned int* __restrict__ count) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    bool keep = false;
+    if (i < n && (i % kSample) != 0) {
+        const float4 q = pts[i];
+        float cx, cy, cz;
+        int x0, x1, y0, y1;
+        if (disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) {
+            // nearest depth the disc can produce (every fragment has view z >= z - R),
+            // lowered by 8 ulps so that rounding in the fragment formula cannot go below it
+            const float zv = cz - a.R;
+            const float d0 = (a.P22 * zv + a.P32) / (a.P23 * zv + a.P33);
+            uint32_t db = __float_as_uint(fmaxf(d0, 0.0f));  // NaN -> 0
+            db = db > 8u ? db - 8u : 0u;
+            const float dmin = __uint_as_float(db);
+            for (int ty = y0 / kHizTile; ty <= y1 / kHizTile && !keep; ++ty)
+                for (int tx = x0 / kHizTile; tx <= x1 / kHizTile; ++tx)
+                    if (a.hiz[ty * a.hiz_w + tx] > dmin) {
+                        keep = true;
+                        break;
+                    }
+        }
     }
-    splat_disc(a, cx, cy, cz, x0, x1, y0, y1, depth);
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    unsigned base = 0;
+    if (lane == 0) base = atomicAdd(count, (unsigned)__popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (keep) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+}
+
+// Pass 3: warp per kept particle.
+__global__ void __launch_bounds__(kThreads) k_splat_list(const float4* __restrict__ pts,
+                                                        const uint32_t* __restrict__ list,
+                                                        const unsigned int* __restrict__ count, SplatArgs a,
+                                                        uint32_t* __restrict__ depth) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (kThreads / 32);
+    const uint64_t total = *count;
+    for (uint64_t w = (blockIdx.x * (uint64_t)kThreads + threadIdx.x) / 32; w < total; w += warps) {
+        const float4 q = pts[list[w]];
+        float cx, cy, cz;
+        int x0, x1, y0, y1;
+        if (!disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) continue;
+        splat_disc_warp(a, cx, cy, cz, x0, x1, y0, y1, lane, depth);
+    }
 }
 
 bool grow(DevBuf& b, size_t bytes) {
@@ -256,39 +244,36 @@ int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_
     a.Hh = cam->height;
     a.twoWinv = 2.0f / (float)cam->width;
     a.twoHinv = 2.0f / (float)cam->height;
-    for (int k = 0; k < 3; ++k) {
-        a.gmin[k] = s->min[k];
-        a.gdims[k] = s->dims[k];
-    }
-    a.ginv = s->inv;
-    a.interior = nullptr;
     a.hiz = nullptr;
     a.hiz_w = (cam->width + kHizTile - 1) / kHizTile;
     a.hiz_h = (cam->height + kHizTile - 1) / kHizTile;
-    // the culling test needs depth to grow with view z: d(z) = (P22 z + P32) / (P23 z + P33)
-    a.hiz_ok = (a.P22 * a.P33 - a.P32 * a.P23) > 0.0f && a.P23 > 0.0f && a.P33 >= 0.0f;
     const uint64_t npx = (uint64_t)cam->width * cam->height;
     k_fill<<<(unsigned)((npx + 255) / 256), 256, 0, st>>>((uint32_t*)d_depth, npx, 0x3f800000u);
     if (s->n == 0) return FM_OK;
-    fm_scene* sm = const_cast<fm_scene*>(s);
-    if (!sm->interior_valid) {
-        if (!sm->d_interior && cudaMalloc(&sm->d_interior, sm->cell_capacity) != cudaSuccess)
-            return set_err(ctx, FM_ERR_OOM, "interior flag allocation failed");
-        k_interior<<<(unsigned)((s->ncells + 255) / 256), 256, 0, st>>>(grid_dev(s), sm->d_interior);
-        sm->interior_valid = true;
+    const unsigned persist = (unsigned)ctx->sm_count * 8;  // 64 warps per SM
+    // the culling test needs depth to grow with view z: d(z) = (P22 z + P32) / (P23 z + P33)
+    const bool cull = (a.P22 * a.P33 - a.P32 * a.P23) > 0.0f && a.P23 > 0.0f && a.P33 >= 0.0f;
+    if (!cull) {
+        k_splat_warp<<<persist, kThreads, 0, st>>>(s->d_pts, s->n, 1, a, (uint32_t*)d_depth);
+        FM_CUDA(ctx, cudaGetLastError());
+        return FM_OK;
     }
-    a.interior = sm->d_interior;
-    const unsigned blocks = (unsigned)((s->n + 255) / 256);
-    k_splat<<<blocks, 256, 0, st>>>(s->d_pts, s->n, a, (uint32_t*)d_depth);
     const size_t hiz_bytes = (size_t)a.hiz_w * a.hiz_h * sizeof(float);
-    if (ctx->hiz.bytes < hiz_bytes) {
-        FM_CUDA(ctx, cudaStreamSynchronize(st));  // the old buffer may still be in use on this stream
-        if (!grow(ctx->hiz, hiz_bytes)) return set_err(ctx, FM_ERR_OOM, "depth tile allocation failed");
+    if (ctx->hiz.bytes < hiz_bytes || ctx->splat_list.bytes < s->n * sizeof(uint32_t)) {
+        FM_CUDA(ctx, cudaStreamSynchronize(st));  // old buffers may still be in use on this stream
+        if (!grow(ctx->hiz, hiz_bytes) || !grow(ctx->splat_list, s->n * sizeof(uint32_t)))
+            return set_err(ctx, FM_ERR_OOM, "splat buffer allocation failed");
     }
     a.hiz = (const float*)ctx->hiz.p;
+    unsigned int* count = ctx->d_work + (ctx->work_slot++ % kWorkSlots) * 32;
+    FM_CUDA(ctx, cudaMemsetAsync(count, 0, sizeof(unsigned int), st));
+    k_splat_warp<<<persist, kThreads, 0, st>>>(s->d_pts, s->n, kSample, a, (uint32_t*)d_depth);
     const int tiles = a.hiz_w * a.hiz_h;
     k_hiz<<<(tiles + 255) / 256, 256, 0, st>>>(d_depth, a.W, a.Hh, a.hiz_w, a.hiz_h, (float*)ctx->hiz.p);
-    k_splat_interior<<<blocks, 256, 0, st>>>(s->d_pts, s->n, a, (uint32_t*)d_depth);
+    k_splat_cull<<<(unsigned)((s->n + kThreads - 1) / kThreads), kThreads, 0, st>>>(
+        s->d_pts, s->n, a, (uint32_t*)ctx->splat_list.p, count);
+    k_splat_list<<<persist, kThreads, 0, st>>>(s->d_pts, (const uint32_t*)ctx->splat_list.p, count, a,
+                                               (uint32_t*)d_depth);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }
