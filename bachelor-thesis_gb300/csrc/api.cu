@@ -113,14 +113,14 @@ int fm_create(fm_ctx** out, int device) {
         delete ctx;
         return FM_ERR_CUDA;
     }
-    if (cudaMalloc(&ctx->d_status, 64) != cudaSuccess || cudaMalloc(&ctx->d_stats, 8 * sizeof(unsigned long long)) != cudaSuccess ||
+    if (cudaMalloc(&ctx->d_status, 64) != cudaSuccess || cudaMalloc(&ctx->d_stats, fm::kStatSlots * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMalloc(&ctx->d_work, fm::kWorkSlots * 32 * sizeof(unsigned int)) != cudaSuccess ||
         cudaHostAlloc(&ctx->h_pinned_small, 256, cudaHostAllocDefault) != cudaSuccess) {
         fm_destroy(ctx);
         return FM_ERR_OOM;
     }
     cudaMemset(ctx->d_status, 0, 64);
-    cudaMemset(ctx->d_stats, 0, 8 * sizeof(unsigned long long));
+    cudaMemset(ctx->d_stats, 0, fm::kStatSlots * sizeof(unsigned long long));
     cudaDeviceSynchronize();
     *out = ctx;
     return FM_OK;
@@ -349,7 +349,7 @@ int fm_march_stats_get(fm_ctx* ctx, fm_march_stats* out) {
     if (!ctx || !out) return FM_ERR_INVALID;
     cudaSetDevice(ctx->device);
     FM_CUDA(ctx, cudaDeviceSynchronize());
-    unsigned long long h[8];
+    unsigned long long h[fm::kStatSlots];
     FM_CUDA(ctx, cudaMemcpy(h, ctx->d_stats, sizeof(h), cudaMemcpyDeviceToHost));
     out->rays = h[0];
     out->started = h[1];
@@ -358,6 +358,8 @@ int fm_march_stats_get(fm_ctx* ctx, fm_march_stats* out) {
     out->candidates = h[4];
     out->skipped = h[5];
     out->tested = h[6];
+    out->streamed = h[7];
+    out->deferred = h[8];
     return FM_OK;
 }
 
@@ -419,7 +421,7 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     o.nrm = (float4*)dev[1];
     o.depth = (float*)dev[2];
     o.col = (float4*)dev[3];
-    if (ctx->stats_enabled) FM_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, 8 * sizeof(unsigned long long), st));
+    if (ctx->stats_enabled) FM_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, fm::kStatSlots * sizeof(unsigned long long), st));
     rc = launch_march(ctx, s, cam, p, o, st);
     if (rc) return rc;
     if (host) {

@@ -19,6 +19,7 @@ namespace fm {
 
 constexpr int kWarp = 32;
 constexpr unsigned kWorkSlots = 64;
+constexpr int kStatSlots = 16;
 
 // Uniform grid of a scene (Frame::m_Min, DensityGrid; Dataset.cpp:78-104).
 struct GridDev {
@@ -163,7 +164,7 @@ struct fm_ctx {
     fm::DevBuf stage[6];
     // device status word + stats accumulators
     unsigned int* d_status = nullptr;
-    unsigned long long* d_stats = nullptr;  // 8 counters
+    unsigned long long* d_stats = nullptr;  // kStatSlots counters
     // work counters of persistent kernels: kWorkSlots slots of 32 words (one
     // 128-byte line each), a fresh slot per launch
     unsigned int* d_work = nullptr;

@@ -45,7 +45,7 @@ namespace {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 256;  // 8 warps per block
 constexpr int kTileW = 8, kTileH = 4;
-constexpr int kStats = 7;
+constexpr int kStats = 9;  // fm_march_stats field order
 
 struct MarchArgs {
     GridDev g;
@@ -78,6 +78,8 @@ struct Acc {
     uint32_t evals = 0;
     uint64_t cand = 0;
     uint64_t tested = 0;
+    uint64_t streamed = 0;   // shared-stream particles (counted by lane 0 of the warp)
+    uint32_t deferred = 0;   // rays handed to the long-ray pass
     uint32_t skipped = 0;
     bool bad = false;  // an index guard fired (reported through the status word, bit 2)
 };
@@ -464,6 +466,7 @@ __device__ __forceinline__ void union_stream(const GridDev& g, bool mine, const 
                     const uint32_t e = (u == 31) ? start32 : enext;
                     const bool pred = (own >> u) & 1u;
                     if (STATS && pred) acc.tested += e - b;
+                    if (STATS && (threadIdx.x & 31) == 0) acc.streamed += e - b;
                     f(pred, b, e);
                 }
             }
@@ -645,6 +648,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a) {
                     if (slot < a.q_cap) {
                         push_long(a, slot, (uint32_t)idx, r);
                         deferred = true;
+                        if (STATS) acc.deferred++;
                     } else {
                         atomicOr(a.status, 4u);  // queue full: cannot happen (capacity = pixels)
                     }
@@ -679,7 +683,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a) {
     if (STATS) {
         unsigned long long v[kStats] = {rays, started_n, hits, (unsigned long long)acc.evals,
                                         (unsigned long long)acc.cand, (unsigned long long)acc.skipped,
-                                        (unsigned long long)acc.tested};
+                                        (unsigned long long)acc.tested, (unsigned long long)acc.streamed,
+                                        (unsigned long long)acc.deferred};
 #pragma unroll
         for (int j = 0; j < kStats; ++j) {
             unsigned long long x = v[j];
@@ -743,7 +748,7 @@ __global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a) {
     if (STATS && lane == 0) {
         const unsigned long long v[kStats] = {0ull, 0ull, hits, (unsigned long long)acc.evals,
                                               (unsigned long long)acc.cand, (unsigned long long)acc.skipped,
-                                              (unsigned long long)acc.tested};
+                                              (unsigned long long)acc.tested, 0ull, 0ull};
 #pragma unroll
         for (int j = 0; j < kStats; ++j)
             if (v[j]) atomicAdd(a.stats + j, v[j]);

@@ -67,7 +67,8 @@ class CGridInfo(C.Structure):
 
 class CMarchStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("started", C.c_uint64), ("hits", C.c_uint64), ("evals", C.c_uint64),
-                ("candidates", C.c_uint64), ("skipped", C.c_uint64), ("tested", C.c_uint64)]
+                ("candidates", C.c_uint64), ("skipped", C.c_uint64), ("tested", C.c_uint64),
+                ("streamed", C.c_uint64), ("deferred", C.c_uint64)]
 
 
 _lib = None

@@ -117,6 +117,8 @@ typedef struct fm_march_stats {
     uint64_t candidates;    /* particles in the 27 cells of every evaluation */
     uint64_t skipped;       /* samples skipped by FM_SKIP_EXACT */
     uint64_t tested;        /* particles actually tested: those of sub-cells within reach */
+    uint64_t streamed;      /* particles a warp streamed for its lanes (shared candidate stream) */
+    uint64_t deferred;      /* rays finished by the long-ray pass */
 } fm_march_stats;
 
 /* ---- context ------------------------------------------------------------ */
