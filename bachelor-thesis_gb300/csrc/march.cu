@@ -23,17 +23,26 @@
 // reference's sequential loop over the same neighbour order; --fmad=false
 // makes every FP32 operation round as the reference's does.
 //
-// Execution (warp per ray): a persistent grid of warps takes 8x4-pixel tiles
-// from an atomic counter.  A warp first finishes the tile's pixels whose
-// splat depth is the clear value (misses) lane-parallel, then marches the
-// tile's remaining rays one at a time with all 32 lanes.  For each density
-// evaluation the lanes test the 24 sub-cells of a cell row against the sample
-// (one ballot gives the reach mask), walk the contiguous sorted ranges of the
-// reachable sub-cells 32 particles at a time (one coalesced 512-byte load),
-// compute W for in-support particles in parallel and add the terms to the
-// running sum in lane order through warp shuffles.  Every branch is
-// warp-uniform except the per-lane W evaluation, so no lane waits on another
-// ray's loop structure, and load balance is per tile.
+// Execution, two passes:
+//   k_march       a persistent grid of warps takes 8x4-pixel tiles from an
+//                 atomic counter; lane = ray.  Each lane runs a small state
+//                 machine (march / bisect / normal / done, `prepare` and
+//                 `apply`).  All lanes that need a density sum in the same
+//                 iteration share one candidate stream: lanes whose cells lie
+//                 in a 2x2x2 cell block are grouped, every cell row of the
+//                 group's 4x4x4-cell union is walked once in ascending sorted
+//                 order with one broadcast load per particle, and a lane adds
+//                 a particle only when its sub-cell is in the lane's own
+//                 reach mask, so every lane's sum visits exactly its own
+//                 canonical sequence.  When at most 2 lanes are still active,
+//                 or after 32 iterations, the remaining rays are pushed to a
+//                 long-ray queue with their full state.
+//   k_march_long  persistent warps pop queued rays and finish each with all
+//                 32 lanes: the reachable sub-cell ranges of the 27 cells are
+//                 walked 32 particles at a time (one coalesced load), W is
+//                 evaluated in parallel and added to the running sum in lane
+//                 order through warp shuffles.
+// The 4 float4 outputs are written by whichever pass finishes the ray.
 
 #include <cuda_runtime.h>
 
