@@ -43,7 +43,11 @@ bool grow(DevBuf& b, size_t bytes) {
     return true;
 }
 
-bool finite16(const float* m) {
+cudaStream_t pick(fm_ctx* ctx, void* stream) { return stream ? (cudaStream_t)stream : ctx->stream; }
+
+}  // namespace
+
+static bool finite16(const float* m) {
     for (int i = 0; i < 16; ++i)
         if (!std::isfinite(m[i])) return false;
     return true;
@@ -88,9 +92,6 @@ int check_params(fm_ctx* ctx, const fm_march_params* p) {
     return FM_OK;
 }
 
-cudaStream_t pick(fm_ctx* ctx, void* stream) { return stream ? (cudaStream_t)stream : ctx->stream; }
-
-}  // namespace
 }  // namespace fm
 
 using namespace fm;
@@ -140,7 +141,8 @@ void fm_destroy(fm_ctx* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    // scenes still alive die with their context (their handles become invalid)
+    // batches and scenes still alive die with their context (their handles become invalid)
+    destroy_batches(ctx);
     for (fm_scene* s : ctx->scenes) scene_free(s);
     ctx->scenes.clear();
     for (auto& b : ctx->stage) cudaFree(b.p);
@@ -223,9 +225,11 @@ static int scene_build(fm_scene* s, const float* xyz, uint64_t n, uint32_t strid
         d_xyz = (const float*)ctx->stage[0].p;
     }
     s->n = n;
+    s->gen = 0;  // a failed rebuild leaves no valid generation
     int rc = build_grid(ctx, s, d_xyz, stride);
     if (rc != FM_OK) return rc;
     FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    s->gen = ++ctx->gen_counter;
     return FM_OK;
 }
 

@@ -1,0 +1,468 @@
+// batch.cu -- many views of many scenes in one launch per pass, under a CUDA graph.
+//
+// The reference renders one view per RayMarcher::Start (RayMarcher.cpp:102-112)
+// with a thread pool over the pixels of that view (ThreadPool.cpp:5-55).  A
+// batch instead lays the views of any number of scenes (uneven particle
+// counts, resolutions, march settings) end to end: every pass of the frame
+// (depth fill, sampled splat, tile maxima, cull, survivor splat, march, long
+// rays) is one launch whose persistent warps walk the units of all views, and
+// a view is found from a unit by a binary search over per-view prefix sums.
+// The seven launches and the counter reset are captured once into a CUDA
+// graph; a frame is one cudaGraphLaunch.
+//
+// fm_batch_autotune times the batch under candidate work splits (tile shape,
+// tiles per claim, iterations before deferral) and keeps the fastest; results
+// do not depend on the split.
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "fm_internal.cuh"
+
+struct fm_batch {
+    fm_ctx* ctx = nullptr;
+    std::vector<fm_view> views;
+    std::vector<uint64_t> gens;  // scene generations the arguments were built from
+    fm::TileConfig cfg;
+    // device buffers
+    fm::DevBuf margs, tile_pfx, sviews, pfx64, pfx_tiles, depth, hiz, list, counters, longq;
+    uint32_t q_cap = 0;
+    fm::MarchArgs launch{};  // launch-wide march arguments
+    fm::SplatBatch sb{};
+    uint64_t pixels = 0, particles = 0, tiles = 0;
+    cudaStream_t cap_stream = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    int nodes = 0;
+};
+
+namespace fm {
+namespace {
+
+constexpr int kMaxViews = 1 << 16;
+
+void drop_graph(fm_batch* b) {
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    b->exec = nullptr;
+    b->graph = nullptr;
+    b->nodes = 0;
+}
+
+void free_batch(fm_batch* b) {
+    // a graph of this batch may still run on any stream
+    cudaDeviceSynchronize();
+    drop_graph(b);
+    DevBuf* bufs[] = {&b->margs, &b->tile_pfx, &b->sviews, &b->pfx64, &b->pfx_tiles,
+                      &b->depth, &b->hiz,      &b->list,   &b->counters, &b->longq};
+    for (DevBuf* d : bufs) cudaFree(d->p);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    delete b;
+}
+
+int check_config(fm_ctx* ctx, const fm_tile_config* c, TileConfig* out) {
+    if (!c) return set_err(ctx, FM_ERR_INVALID, "tile config is NULL");
+    int lg = -1;
+    for (int i = 0; i <= 5; ++i)
+        if (c->tile_width == (1 << i)) lg = i;
+    if (lg < 0) return set_err(ctx, FM_ERR_INVALID, "tile_width must be 1, 2, 4, 8, 16 or 32");
+    if (c->tiles_per_claim < 1 || c->tiles_per_claim > 16)
+        return set_err(ctx, FM_ERR_INVALID, "tiles_per_claim must be in [1, 16]");
+    if (c->defer_iters < 1 || c->defer_iters > 4096)
+        return set_err(ctx, FM_ERR_INVALID, "defer_iters must be in [1, 4096]");
+    if (c->long_queue < 0) return set_err(ctx, FM_ERR_INVALID, "long_queue must be >= 0");
+    out->tw_log2 = lg;
+    out->claim = c->tiles_per_claim;
+    out->cap = c->defer_iters;
+    out->qlimit = (uint32_t)c->long_queue;
+    return FM_OK;
+}
+
+fm_tile_config to_public(const TileConfig& c) {
+    fm_tile_config o{};
+    o.tile_width = 1 << c.tw_log2;
+    o.tiles_per_claim = c.claim;
+    o.defer_iters = c.cap;
+    o.long_queue = (int32_t)c.qlimit;
+    return o;
+}
+
+// Sizes, skip tables, buffers and argument blocks for the current scenes and
+// work split.  Synchronous.
+int prepare(fm_batch* b) {
+    fm_ctx* ctx = b->ctx;
+    const int n = (int)b->views.size();
+    // a run of this batch may still be reading the argument blocks
+    FM_CUDA(ctx, cudaDeviceSynchronize());
+    // skip tables of the scenes, built once on the context stream
+    for (const fm_view& v : b->views) {
+        fm_scene* s = const_cast<fm_scene*>(v.scene);
+        int rc = FM_OK;
+        if (v.params.skip_mode == FM_SKIP_EXACT) rc = ensure_bound(ctx, s, ctx->stream);
+        if (v.params.skip_mode == FM_SKIP_REFERENCE) rc = ensure_flags(ctx, s, ctx->stream);
+        if (rc) return rc;
+    }
+    FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    // prefix sums
+    std::vector<uint64_t> px(n + 1, 0), smp(n + 1, 0), pn(n + 1, 0);
+    std::vector<uint32_t> ht(n + 1, 0), tp(n + 1, 0);
+    const int tw = 1 << b->cfg.tw_log2, th = 32 >> b->cfg.tw_log2;
+    for (int i = 0; i < n; ++i) {
+        const fm_view& v = b->views[i];
+        const uint64_t w = (uint64_t)v.camera.width, h = (uint64_t)v.camera.height;
+        px[i + 1] = px[i] + w * h;
+        smp[i + 1] = smp[i] + (v.scene->n + kSplatSample - 1) / kSplatSample;
+        pn[i + 1] = pn[i] + v.scene->n;
+        const uint64_t hz = ((w + kSplatHizTile - 1) / kSplatHizTile) * ((h + kSplatHizTile - 1) / kSplatHizTile);
+        const uint64_t tl = ((w + tw - 1) / tw) * ((h + th - 1) / th);
+        if ((uint64_t)ht[i] + hz >= (1ull << 32) || (uint64_t)tp[i] + tl >= (1ull << 31))
+            return set_err(ctx, FM_ERR_INVALID, "batch has too many tiles");
+        ht[i + 1] = ht[i] + (uint32_t)hz;
+        tp[i + 1] = tp[i] + (uint32_t)tl;
+    }
+    if (pn[n] >= (1ull << 32)) return set_err(ctx, FM_ERR_INVALID, "batch has 2^32 or more particles");
+    const uint64_t entries = long_queue_entries(px[n], b->cfg.qlimit);
+    if (entries >= (1ull << 32)) return set_err(ctx, FM_ERR_INVALID, "batch has too many pixels");
+    b->pixels = px[n];
+    b->particles = pn[n];
+    b->tiles = tp[n];
+    // buffers (grown, never shrunk)
+    FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    if (!grow_buf(b->margs, sizeof(MarchArgs) * n) || !grow_buf(b->tile_pfx, 4ull * (n + 1)) ||
+        !grow_buf(b->sviews, sizeof(SplatView) * n) || !grow_buf(b->pfx64, 8ull * 3 * (n + 1)) ||
+        !grow_buf(b->pfx_tiles, 4ull * (n + 1)) || !grow_buf(b->depth, 4ull * std::max<uint64_t>(px[n], 1)) ||
+        !grow_buf(b->hiz, 4ull * std::max<uint32_t>(ht[n], 1)) ||
+        !grow_buf(b->list, 4ull * std::max<uint64_t>(pn[n], 1)) || !grow_buf(b->counters, 128) ||
+        !grow_buf(b->longq, 64ull * entries))
+        return set_err(ctx, FM_ERR_OOM, "batch buffer allocation failed");
+    b->q_cap = (uint32_t)entries;
+    unsigned int* cnt = (unsigned int*)b->counters.p;
+    // march arguments: per view, with the launch-wide fields in every block
+    std::vector<MarchArgs> ma(n);
+    std::vector<SplatView> sv(n);
+    float* depth = (float*)b->depth.p;
+    for (int i = 0; i < n; ++i) {
+        const fm_view& v = b->views[i];
+        float* z = v.out.start_depth ? v.out.start_depth : depth + px[i];
+        MarchOutDev o{};
+        o.pos = (float4*)v.out.position;
+        o.nrm = (float4*)v.out.normal;
+        o.depth = v.out.depth;
+        o.col = (float4*)v.out.colour;
+        o.start_depth = z;
+        MarchArgs a = march_view_args(v.scene, &v.camera, &v.params, o, b->cfg);
+        a.tile_counter = cnt;
+        a.q_tail = cnt + 1;
+        a.q_head = cnt + 2;
+        a.longq = (float4*)b->longq.p;
+        a.q_cap = b->q_cap;
+        a.status = ctx->d_status;
+        a.stats = nullptr;
+        ma[i] = a;
+        SplatView s{};
+        s.a = splat_args(v.scene, &v.camera);
+        s.a.hiz = (const float*)b->hiz.p + ht[i];
+        s.pts = v.scene->d_pts;
+        s.n = v.scene->n;
+        s.depth = (uint32_t*)z;
+        sv[i] = s;
+    }
+    b->launch = ma[0];
+    b->launch.ntiles = (int)tp[n];
+    b->gens.resize(n);
+    for (int i = 0; i < n; ++i) b->gens[i] = b->views[i].scene->gen;
+    FM_CUDA(ctx, cudaMemcpy(b->margs.p, ma.data(), sizeof(MarchArgs) * n, cudaMemcpyHostToDevice));
+    FM_CUDA(ctx, cudaMemcpy(b->tile_pfx.p, tp.data(), 4ull * (n + 1), cudaMemcpyHostToDevice));
+    FM_CUDA(ctx, cudaMemcpy(b->sviews.p, sv.data(), sizeof(SplatView) * n, cudaMemcpyHostToDevice));
+    uint64_t* p64 = (uint64_t*)b->pfx64.p;
+    FM_CUDA(ctx, cudaMemcpy(p64, px.data(), 8ull * (n + 1), cudaMemcpyHostToDevice));
+    FM_CUDA(ctx, cudaMemcpy(p64 + (n + 1), smp.data(), 8ull * (n + 1), cudaMemcpyHostToDevice));
+    FM_CUDA(ctx, cudaMemcpy(p64 + 2 * (n + 1), pn.data(), 8ull * (n + 1), cudaMemcpyHostToDevice));
+    FM_CUDA(ctx, cudaMemcpy(b->pfx_tiles.p, ht.data(), 4ull * (n + 1), cudaMemcpyHostToDevice));
+    SplatBatch& s = b->sb;
+    s.views = (const SplatView*)b->sviews.p;
+    s.nviews = n;
+    s.pfx_px = p64;
+    s.pfx_sample = p64 + (n + 1);
+    s.pfx_n = p64 + 2 * (n + 1);
+    s.pfx_tiles = (const uint32_t*)b->pfx_tiles.p;
+    s.hiz = (float*)b->hiz.p;
+    s.list = (uint32_t*)b->list.p;
+    s.count = cnt + 3;
+    s.tot_px = px[n];
+    s.tot_sample = smp[n];
+    s.tot_n = pn[n];
+    s.tot_tiles = ht[n];
+    return FM_OK;
+}
+
+// The frame's work on `st`: counter reset, depth pass, march.
+int enqueue(fm_batch* b, cudaStream_t st, bool stats) {
+    fm_ctx* ctx = b->ctx;
+    FM_CUDA(ctx, cudaMemsetAsync(b->counters.p, 0, 4 * sizeof(unsigned int), st));
+    int rc = launch_splat_batch(ctx, b->sb, st);
+    if (rc) return rc;
+    MarchArgs a = b->launch;
+    a.stats = stats ? ctx->d_stats : nullptr;
+    return launch_march_kernels(ctx, a, (const MarchArgs*)b->margs.p, (const uint32_t*)b->tile_pfx.p,
+                                (int)b->views.size(), st);
+}
+
+int capture(fm_batch* b) {
+    fm_ctx* ctx = b->ctx;
+    drop_graph(b);
+    FM_CUDA(ctx, cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = enqueue(b, b->cap_stream, false);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(b->cap_stream, &g);
+    if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaStreamEndCapture");
+    b->graph = g;
+    FM_CUDA(ctx, cudaGraphInstantiate(&b->exec, g, 0));
+    size_t nn = 0;
+    FM_CUDA(ctx, cudaGraphGetNodes(g, nullptr, &nn));
+    b->nodes = (int)nn;
+    return FM_OK;
+}
+
+}  // namespace
+
+void destroy_batches(fm_ctx* ctx) {
+    for (fm_batch* b : ctx->batches) free_batch(b);
+    ctx->batches.clear();
+}
+
+}  // namespace fm
+
+using namespace fm;
+
+extern "C" {
+
+int fm_set_tile_config(fm_ctx* ctx, const fm_tile_config* cfg) {
+    if (!ctx) return FM_ERR_INVALID;
+    TileConfig t;
+    const int rc = check_config(ctx, cfg, &t);
+    if (rc) return rc;
+    ctx->tile = t;
+    return FM_OK;
+}
+
+int fm_get_tile_config(const fm_ctx* ctx, fm_tile_config* out) {
+    if (!ctx || !out) return FM_ERR_INVALID;
+    *out = to_public(ctx->tile);
+    return FM_OK;
+}
+
+int fm_batch_create(fm_ctx* ctx, const fm_view* views, int32_t n_views, const fm_tile_config* cfg, fm_batch** out) {
+    if (!ctx) return FM_ERR_INVALID;
+    if (!out) return set_err(ctx, FM_ERR_INVALID, "output handle pointer is NULL");
+    *out = nullptr;
+    if (!views || n_views < 1 || n_views > kMaxViews)
+        return set_err(ctx, FM_ERR_INVALID, "a batch needs 1 to 65536 views");
+    TileConfig t = ctx->tile;
+    if (cfg) {
+        const int rc = check_config(ctx, cfg, &t);
+        if (rc) return rc;
+    }
+    for (int i = 0; i < n_views; ++i) {
+        const fm_view& v = views[i];
+        if (!v.scene || std::find(ctx->scenes.begin(), ctx->scenes.end(), v.scene) == ctx->scenes.end())
+            return set_err(ctx, FM_ERR_INVALID, "view scene is NULL or not a live scene of this context");
+        int rc = check_params(ctx, &v.params);
+        if (rc) return rc;
+        if (v.params.flags != 0) return set_err(ctx, FM_ERR_INVALID, "batched views are splatted: flags must be 0");
+        rc = check_camera(ctx, &v.camera, true);
+        if (rc) return rc;
+        if (v.scene->n == 0) return set_err(ctx, FM_ERR_INVALID, "view scene has no particles");
+    }
+    cudaSetDevice(ctx->device);
+    fm_batch* b = new (std::nothrow) fm_batch();
+    if (!b) return set_err(ctx, FM_ERR_OOM, "batch allocation failed");
+    b->ctx = ctx;
+    b->views.assign(views, views + n_views);
+    b->cfg = t;
+    if (cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        free_batch(b);
+        return set_err(ctx, FM_ERR_CUDA, "stream creation failed");
+    }
+    int rc = prepare(b);
+    if (!rc) rc = capture(b);
+    if (rc) {
+        free_batch(b);
+        return rc;
+    }
+    ctx->batches.push_back(b);
+    *out = b;
+    return FM_OK;
+}
+
+int fm_batch_run(fm_batch* b, void* stream) {
+    if (!b) return FM_ERR_INVALID;
+    fm_ctx* ctx = b->ctx;
+    // every scene must still be alive and unchanged since the arguments were built
+    for (size_t i = 0; i < b->views.size(); ++i) {
+        const fm_scene* s = b->views[i].scene;
+        if (std::find(ctx->scenes.begin(), ctx->scenes.end(), s) == ctx->scenes.end() || s->gen != b->gens[i])
+            return set_err(ctx, FM_ERR_INVALID, "a scene of the batch was destroyed or updated: fm_batch_refresh first");
+    }
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    if (ctx->stats_enabled) {
+        FM_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, kStatSlots * sizeof(unsigned long long), st));
+        return enqueue(b, st, true);
+    }
+    if (!b->exec) return set_err(ctx, FM_ERR_INVALID, "batch has no graph");
+    FM_CUDA(ctx, cudaGraphLaunch(b->exec, st));
+    return FM_OK;
+}
+
+int fm_batch_refresh(fm_batch* b) {
+    if (!b) return FM_ERR_INVALID;
+    fm_ctx* ctx = b->ctx;
+    cudaSetDevice(ctx->device);
+    for (const fm_view& v : b->views) {
+        if (std::find(ctx->scenes.begin(), ctx->scenes.end(), v.scene) == ctx->scenes.end())
+            return set_err(ctx, FM_ERR_INVALID, "a scene of the batch was destroyed");
+        if (v.scene->gen == 0) return set_err(ctx, FM_ERR_INVALID, "a scene of the batch has no valid grid");
+    }
+    int rc = prepare(b);
+    if (!rc) rc = capture(b);
+    return rc;
+}
+
+int fm_batch_autotune(fm_batch* b, const fm_tile_config* cands, int32_t n_cands, int32_t reps, fm_tile_config* best,
+                      float* best_ms) {
+    if (!b) return FM_ERR_INVALID;
+    fm_ctx* ctx = b->ctx;
+    if (reps < 1 || reps > 100) return set_err(ctx, FM_ERR_INVALID, "reps must be in [1, 100]");
+    if (cands && n_cands < 1) return set_err(ctx, FM_ERR_INVALID, "no candidates");
+    cudaSetDevice(ctx->device);
+    std::vector<TileConfig> list;
+    if (cands) {
+        for (int i = 0; i < n_cands; ++i) {
+            TileConfig t;
+            const int rc = check_config(ctx, &cands[i], &t);
+            if (rc) return rc;
+            list.push_back(t);
+        }
+    } else {
+        for (int lg : {2, 3, 4, 5})
+            for (int cap : {16, 32, 64}) {
+                TileConfig t;
+                t.tw_log2 = lg;
+                t.claim = 1;
+                t.cap = cap;
+                t.qlimit = b->cfg.qlimit;
+                list.push_back(t);
+            }
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+        if (e0) cudaEventDestroy(e0);
+        return set_err(ctx, FM_ERR_CUDA, "event creation failed");
+    }
+    const TileConfig keep = b->cfg;
+    TileConfig win = keep;
+    float win_ms = 0.0f;
+    bool have = false;
+    int rc = FM_OK;
+    // time one candidate: median of `reps` runs after one warm-up
+    auto time_one = [&](const TileConfig& t, float& ms) -> int {
+        b->cfg = t;
+        int r = prepare(b);
+        if (r) return r;
+        r = enqueue(b, ctx->stream, false);
+        if (r) return r;
+        std::vector<float> v;
+        for (int k = 0; k < reps; ++k) {
+            FM_CUDA(ctx, cudaEventRecord(e0, ctx->stream));
+            r = enqueue(b, ctx->stream, false);
+            if (r) return r;
+            FM_CUDA(ctx, cudaEventRecord(e1, ctx->stream));
+            FM_CUDA(ctx, cudaEventSynchronize(e1));
+            float x = 0.0f;
+            FM_CUDA(ctx, cudaEventElapsedTime(&x, e0, e1));
+            v.push_back(x);
+        }
+        std::sort(v.begin(), v.end());
+        ms = v[v.size() / 2];
+        return FM_OK;
+    };
+    for (const TileConfig& t : list) {
+        float ms = 0.0f;
+        if ((rc = time_one(t, ms)) != FM_OK) break;
+        if (!have || ms < win_ms) {
+            win = t;
+            win_ms = ms;
+            have = true;
+        }
+    }
+    if (!rc && !cands) {
+        // then coarser claims for the winning shape
+        const TileConfig base = win;
+        for (int claim : {2, 4}) {
+            TileConfig t = base;
+            t.claim = claim;
+            float ms = 0.0f;
+            if ((rc = time_one(t, ms)) != FM_OK) break;
+            if (ms < win_ms) {
+                win = t;
+                win_ms = ms;
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    b->cfg = rc ? keep : win;
+    const int rc2 = prepare(b);
+    const int rc3 = rc2 ? rc2 : capture(b);
+    if (rc) return rc;
+    if (rc3) return rc3;
+    if (best) *best = to_public(win);
+    if (best_ms) *best_ms = win_ms;
+    return FM_OK;
+}
+
+int fm_batch_info_get(const fm_batch* b, fm_batch_info* out) {
+    if (!b || !out) return FM_ERR_INVALID;
+    fm_batch_info i{};
+    i.n_views = (int32_t)b->views.size();
+    i.graph_nodes = b->nodes;
+    i.pixels = b->pixels;
+    i.particles = b->particles;
+    i.tiles = b->tiles;
+    i.config = to_public(b->cfg);
+    *out = i;
+    return FM_OK;
+}
+
+void fm_batch_destroy(fm_batch* b) {
+    if (!b) return;
+    fm_ctx* ctx = b->ctx;
+    cudaSetDevice(ctx->device);
+    auto& v = ctx->batches;
+    v.erase(std::remove(v.begin(), v.end(), b), v.end());
+    free_batch(b);
+}
+
+int fm_march_batch(fm_ctx* ctx, const fm_view* views, int32_t n_views, void* stream) {
+    fm_batch* b = nullptr;
+    int rc = fm_batch_create(ctx, views, n_views, nullptr, &b);
+    if (rc) return rc;
+    rc = fm_batch_run(b, stream);
+    cudaStream_t st = stream ? (cudaStream_t)stream : ctx->stream;
+    const cudaError_t e = cudaStreamSynchronize(st);
+    fm_batch_destroy(b);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_err(ctx, e, "cudaStreamSynchronize");
+    return FM_OK;
+}
+
+}  // extern "C"

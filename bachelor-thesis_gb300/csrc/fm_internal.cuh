@@ -153,7 +153,18 @@ struct DevBuf {
     size_t bytes = 0;
 };
 
+// Work split of the march: tile shape, tiles per claim, iterations before
+// the rays a warp has left are deferred to the long-ray pass.
+struct TileConfig {
+    int tw_log2 = 3;  // 8x4 pixels
+    int claim = 1;
+    int cap = 32;
+    uint32_t qlimit = 0;  // long-ray queue entries (0: long_queue_entries of the pixels)
+};
+
 }  // namespace fm
+
+struct fm_batch;
 
 struct fm_ctx {
     int device = 0;
@@ -173,7 +184,8 @@ struct fm_ctx {
     fm_march_stats last_stats{};
     // scratch for grid builds
     fm::DevBuf scratch[8];
-    // long-ray queue of the march (64 B per pixel of the largest view so far)
+    // long-ray queue of the march (64 B per entry, long_queue_entries(pixels)
+    // entries for the largest view so far)
     fm::DevBuf longq;
     // splat depth tile maxima (4 B per 8x8 tile) and the list of particles that
     // survive the tile test; renders of one context on different streams must
@@ -182,6 +194,12 @@ struct fm_ctx {
     fm::DevBuf splat_list;
     // live scenes of this context; fm_destroy frees the ones still alive
     std::vector<fm_scene*> scenes;
+    // live batches of this context; fm_destroy frees the ones still alive
+    std::vector<fm_batch*> batches;
+    // work split of single-view marches (fm_set_tile_config)
+    fm::TileConfig tile;
+    // source of scene generations (every successful build gets a new one)
+    uint64_t gen_counter = 0;
     void* h_pinned_small = nullptr;  // 256 bytes of pinned memory for small readbacks
 };
 
@@ -203,6 +221,7 @@ struct fm_scene {
     uint8_t* d_flag = nullptr;     // per-cell reference flag (lazy)
     bool bound_valid = false;
     bool flag_valid = false;
+    uint64_t gen = 0;              // build generation: batches bound to an older one refuse to run
 };
 
 namespace fm {
@@ -218,6 +237,46 @@ GridDev grid_dev(const fm_scene* s);
 // Splat (splat.cu): depth must be a device buffer of W*H floats.
 int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_depth, cudaStream_t st);
 
+// Camera-derived constants of the depth pass.
+struct SplatArgs {
+    float V[16];
+    float P00, P11, P22, P32, P23, P33;
+    float R, invR;
+    float twoWinv, twoHinv;
+    int W, Hh;
+    const float* __restrict__ hiz;  // per 8x8 tile: max depth after the sampled pass
+    int hiz_w, hiz_h;
+    int cull;                       // depth grows with view z: the tile test is valid
+};
+
+// One view of a batched splat.
+struct SplatView {
+    SplatArgs a;
+    const float4* pts;
+    uint64_t n;
+    uint32_t* depth;  // W*H floats (as bits)
+};
+
+// Batched splat: all views in one launch per pass.  Prefix arrays have
+// nviews + 1 entries: pixels, sampled particles, particles, hiz tiles.
+struct SplatBatch {
+    const SplatView* views;  // device
+    int nviews;
+    const uint64_t* pfx_px;
+    const uint64_t* pfx_sample;
+    const uint64_t* pfx_n;
+    const uint32_t* pfx_tiles;
+    float* hiz;              // all views' tiles
+    uint32_t* list;          // survivors: global particle index (pfx_n[v] + i)
+    unsigned int* count;     // survivor counter (zeroed by the caller)
+    uint64_t tot_px, tot_sample, tot_n;
+    uint32_t tot_tiles;
+};
+SplatArgs splat_args(const fm_scene* s, const fm_camera* cam);
+constexpr int kSplatHizTile = 8;
+constexpr uint64_t kSplatSample = 8;
+int launch_splat_batch(fm_ctx* ctx, const SplatBatch& b, cudaStream_t st);
+
 // March (march.cu): all pointers device pointers.
 struct MarchOutDev {
     float4* pos;
@@ -226,8 +285,62 @@ struct MarchOutDev {
     float4* col;
     const float* start_depth;
 };
+
+// Arguments of one view.  A batch holds one per view in device memory, with
+// the launch-wide fields (counters, queue, tile shape, stats, status) equal in
+// all of them.
+struct MarchArgs {
+    GridDev g;
+    KernelDev k;
+    float iso, step;
+    int max_steps, bisect, skip_mode;
+    float cull;  // squared reach in cell units: (1 + margin)^2
+    float ipv[16];
+    float cam[3];
+    float cdir[3];
+    int W, Hh;
+    int tiles_x, ntiles;   // ntiles: this view's tiles (launch argument: the launch's)
+    int tw_log2;           // tile = (1 << tw_log2) x (32 >> tw_log2) pixels
+    int claim;             // tiles a warp takes per atomic
+    float twoWinv, twoHinv;
+    const float* __restrict__ zbuf;
+    float4* pos;
+    float4* nrm;
+    float* depth;
+    float4* col;
+    unsigned int* tile_counter;
+    unsigned int* q_tail;  // long-ray queue: entries written by the shared-stream pass
+    unsigned int* q_head;  // entries taken by the long-ray pass
+    float4* longq;         // 4 float4 per entry
+    unsigned int q_cap;
+    int cap;               // shared-stream iterations per tile before the rays left are deferred
+    unsigned long long* stats;
+    unsigned int* status;
+};
+
+// Per-view fields of the march arguments (launch-wide fields left zero).
+MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_march_params* p, const MarchOutDev& o,
+                          const TileConfig& cfg);
+// Long-ray queue entries for `pixels` rays (deferred rays are a few percent;
+// a full queue only keeps rays in the first pass).
+inline uint64_t long_queue_entries(uint64_t pixels, uint32_t limit = 0) {
+    uint64_t q = limit ? (uint64_t)limit : pixels / 8 + 65536;
+    return q < pixels ? q : pixels;
+}
+// Both march passes.  nviews == 0: `launch` is the single view; otherwise
+// d_views / d_tile_pfx describe the batch and `launch` carries the
+// launch-wide fields with ntiles = total tiles.
+int launch_march_kernels(fm_ctx* ctx, const MarchArgs& launch, const MarchArgs* d_views, const uint32_t* d_tile_pfx,
+                         int nviews, cudaStream_t st);
 int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
                  const MarchOutDev& o, cudaStream_t st);
+
+// Argument checks shared by the single and batched entry points (api.cu).
+int check_camera(fm_ctx* ctx, const fm_camera* c, bool need_splat);
+int check_params(fm_ctx* ctx, const fm_march_params* p);
+bool grow_buf(DevBuf& b, size_t bytes);
+// Free the batches a context still holds (batch.cu).
+void destroy_batches(fm_ctx* ctx);
 
 int set_err(fm_ctx* ctx, int code, const std::string& msg);
 int cuda_err(fm_ctx* ctx, cudaError_t e, const char* what);

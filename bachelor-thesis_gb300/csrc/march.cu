@@ -53,35 +53,7 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 256;  // 8 warps per block
-constexpr int kTileW = 8, kTileH = 4;
 constexpr int kStats = 9;  // fm_march_stats field order
-
-struct MarchArgs {
-    GridDev g;
-    KernelDev k;
-    float iso, step;
-    int max_steps, bisect, skip_mode;
-    float cull;  // squared reach in cell units: (1 + margin)^2
-    float ipv[16];
-    float cam[3];
-    float cdir[3];
-    int W, Hh;
-    int tiles_x, ntiles;
-    float twoWinv, twoHinv;
-    const float* __restrict__ zbuf;
-    float4* pos;
-    float4* nrm;
-    float* depth;
-    float4* col;
-    unsigned int* tile_counter;
-    unsigned int* q_tail;  // long-ray queue: entries written by the shared-stream pass
-    unsigned int* q_head;  // entries taken by the long-ray pass
-    float4* longq;         // 4 float4 per entry (see push_long)
-    unsigned int q_cap;
-    int cap;               // shared-stream iterations per tile before the rays left are deferred
-    unsigned long long* stats;
-    unsigned int* status;
-};
 
 struct Acc {
     uint32_t evals = 0;
@@ -564,14 +536,26 @@ __device__ __forceinline__ void ray_setup(const MarchArgs& a, int px, int py, fl
     s[2] = a.step * (dz * inv);
 }
 
-// Long-ray queue entry: 4 float4 = {pixel, phase, i, b}, p, q, e (the pending
-// evaluation point).  The step is recomputed from the pixel.
-__device__ __forceinline__ void push_long(const MarchArgs& a, uint32_t slot, uint32_t idx, const Ray& r) {
+// Long-ray queue entry: 4 float4 = {pixel, phase, i, b}, p, q, {e, view}
+// (e: the pending evaluation point).  The step is recomputed from the pixel.
+__device__ __forceinline__ void push_long(const MarchArgs& a, uint32_t slot, uint32_t idx, uint32_t view,
+                                          const Ray& r) {
     float4* d = a.longq + 4ull * slot;
     d[0] = make_float4(__uint_as_float(idx), __int_as_float(r.phase), __int_as_float(r.i), __int_as_float(r.b));
     d[1] = make_float4(r.p[0], r.p[1], r.p[2], 0.0f);
     d[2] = make_float4(r.q[0], r.q[1], r.q[2], 0.0f);
-    d[3] = make_float4(r.e[0], r.e[1], r.e[2], 0.0f);
+    d[3] = make_float4(r.e[0], r.e[1], r.e[2], __uint_as_float(view));
+}
+
+// View of a batch tile: the largest v with pfx[v] <= t (pfx[0] = 0, ascending).
+__device__ __forceinline__ int find_view(const uint32_t* __restrict__ pfx, int nviews, uint32_t t) {
+    int lo = 0, hi = nviews - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(pfx + mid) <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
 }
 
 // Sum of gradW at p (canonical order) with the whole warp, identical on every lane.
@@ -608,106 +592,165 @@ __device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, 
     });
 }
 
+// One 32-pixel tile of view `a` (lane = ray).  `view` tags the rays this
+// warp defers to the long-ray queue.
 template <bool STATS>
-__global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a) {
+__device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, uint32_t view, int lane, Acc& acc,
+                                           uint64_t& rays, uint64_t& started_n, uint64_t& hits) {
+    const int tw = 1 << a.tw_log2;
+    const int tx = (int)(tile % (unsigned)a.tiles_x), ty = (int)(tile / (unsigned)a.tiles_x);
+    const int px = tx * tw + (lane & (tw - 1));
+    const int py = ty * (32 >> a.tw_log2) + (lane >> a.tw_log2);
+    const bool valid = px < a.W && py < a.Hh;
+    const uint64_t idx = (uint64_t)py * (uint64_t)a.W + (uint64_t)px;
+    const float z = valid ? a.zbuf[idx] : 1.0f;
+    Ray r;
+    r.phase = kDone;
+    r.i = r.b = 0;
+    if (valid && z != 1.0f) {
+        ray_setup(a, px, py, z, r.p, r.s);
+        r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
+        r.phase = kMarch;
+    } else {
+        r.p[0] = r.p[1] = r.p[2] = 0.0f;
+        r.q[0] = r.q[1] = r.q[2] = 0.0f;
+        r.s[0] = r.s[1] = r.s[2] = 0.0f;
+    }
+    r.e[0] = r.e[1] = r.e[2] = 0.0f;
+    if (STATS && valid) { rays++; if (z != 1.0f) started_n++; }
+    Loc L;
+    L.c[0] = L.c[1] = L.c[2] = 0;
+    L.u[0] = L.u[1] = L.u[2] = 0.0f;
+    int iters = 0;
+    bool deferred = false, keep = false;
+    for (;;) {
+        bool need = (r.phase == kMarch || r.phase == kBisect) && prepare<STATS>(a, r, L, acc, true);
+        uint32_t act = __ballot_sync(kFull, need);
+        if (!act) break;
+        if (!keep && (__popc(act) <= 2 || iters >= a.cap)) {
+            // Few rays left, or rays that march long (grazing the surface): hand
+            // them to the long-ray pass, where each gets a whole warp, instead of
+            // keeping this warp busy while the rest of the grid idles.  Rays that
+            // find the queue full stay here, and the warp stops deferring.
+            const uint32_t base = (lane == 0) ? atomicAdd(a.q_tail, (unsigned)__popc(act)) : 0u;
+            const uint32_t slot = __shfl_sync(kFull, base, 0) + __popc(act & ((1u << lane) - 1u));
+            if (need && slot < a.q_cap) {
+                push_long(a, slot, (uint32_t)idx, view, r);
+                deferred = true;
+                need = false;
+                r.phase = kDone;
+                if (STATS) acc.deferred++;
+            }
+            act = __ballot_sync(kFull, need);
+            if (!act) break;
+            keep = true;
+        }
+        const float rho = union_density<STATS>(a, need, L, r.e, acc);
+        if (need) apply(a, r, rho);
+        ++iters;
+    }
+    // normals of the hit rays (all in phase kNormal), then outputs; deferred
+    // rays are finished (and written) by the long-ray pass
+    const bool hit = !deferred && r.phase == kNormal;
+    Loc Lh;
+    Lh.c[0] = Lh.c[1] = Lh.c[2] = 0;
+    Lh.u[0] = Lh.u[1] = Lh.u[2] = 0.0f;
+    const bool gn = hit && locate(a.g, r.p[0], r.p[1], r.p[2], Lh);
+    if (STATS && hit && !gn) acc.evals++;
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    if (__any_sync(kFull, gn)) union_grad<STATS>(a, gn, Lh, r.p, acc, gx, gy, gz);
+    float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+    if (hit) {
+        const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+        n0 = gx * gi;
+        n1 = gy * gi;
+        n2 = gz * gi;
+        if (STATS) hits++;
+    }
+    if (valid && !deferred) write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
+}
+
+__device__ __forceinline__ void flush_stats(const MarchArgs& a, int lane, const Acc& acc, uint64_t rays,
+                                            uint64_t started_n, uint64_t hits, bool warp_sum) {
+    unsigned long long v[kStats] = {rays, started_n, hits, (unsigned long long)acc.evals,
+                                    (unsigned long long)acc.cand, (unsigned long long)acc.skipped,
+                                    (unsigned long long)acc.tested, (unsigned long long)acc.streamed,
+                                    (unsigned long long)acc.deferred};
+#pragma unroll
+    for (int j = 0; j < kStats; ++j) {
+        unsigned long long x = v[j];
+        if (warp_sum) {
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+        }
+        if (lane == 0 && x) atomicAdd(a.stats + j, x);
+    }
+}
+
+// Shared-stream pass.  Persistent warps take `a.claim` tiles per atomic from
+// the launch's counter.  BATCH: `a` holds the launch-wide fields and the total
+// tile count; tile t belongs to view find_view(tile_pfx, t) of `views`.
+template <bool STATS, bool BATCH>
+__global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a, const MarchArgs* __restrict__ views,
+                                                      const uint32_t* __restrict__ tile_pfx, int nviews) {
     const int lane = threadIdx.x & 31;
     Acc acc;
     uint64_t rays = 0, started_n = 0, hits = 0;
+    const unsigned total = (unsigned)a.ntiles, claim = (unsigned)a.claim;
     for (;;) {
-        unsigned int tile = 0;
-        if (lane == 0) tile = atomicAdd(a.tile_counter, 1u);
-        tile = __shfl_sync(kFull, tile, 0);
-        if (tile >= (unsigned)a.ntiles) break;
-        const int tx = (int)(tile % (unsigned)a.tiles_x), ty = (int)(tile / (unsigned)a.tiles_x);
-        const int px = tx * kTileW + (lane & (kTileW - 1));
-        const int py = ty * kTileH + (lane / kTileW);
-        const bool valid = px < a.W && py < a.Hh;
-        const uint64_t idx = (uint64_t)py * (uint64_t)a.W + (uint64_t)px;
-        const float z = valid ? a.zbuf[idx] : 1.0f;
-        Ray r;
-        r.phase = kDone;
-        r.i = r.b = 0;
-        if (valid && z != 1.0f) {
-            ray_setup(a, px, py, z, r.p, r.s);
-            r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
-            r.phase = kMarch;
-        } else {
-            r.p[0] = r.p[1] = r.p[2] = 0.0f;
-            r.q[0] = r.q[1] = r.q[2] = 0.0f;
-            r.s[0] = r.s[1] = r.s[2] = 0.0f;
-        }
-        r.e[0] = r.e[1] = r.e[2] = 0.0f;
-        if (STATS && valid) { rays++; if (z != 1.0f) started_n++; }
-        Loc L;
-        L.c[0] = L.c[1] = L.c[2] = 0;
-        L.u[0] = L.u[1] = L.u[2] = 0.0f;
-        int iters = 0;
-        bool deferred = false;
-        for (;;) {
-            const bool need = (r.phase == kMarch || r.phase == kBisect) && prepare<STATS>(a, r, L, acc, true);
-            const uint32_t act = __ballot_sync(kFull, need);
-            if (!act) break;
-            if (__popc(act) <= 2 || iters >= a.cap) {
-                // Few rays left, or rays that march long (grazing the surface): hand
-                // them to the long-ray pass, where each gets a whole warp, instead of
-                // keeping this warp busy while the rest of the grid idles.
-                const uint32_t base = (lane == 0) ? atomicAdd(a.q_tail, (unsigned)__popc(act)) : 0u;
-                const uint32_t slot = __shfl_sync(kFull, base, 0) + __popc(act & ((1u << lane) - 1u));
-                if (need) {
-                    if (slot < a.q_cap) {
-                        push_long(a, slot, (uint32_t)idx, r);
-                        deferred = true;
-                        if (STATS) acc.deferred++;
-                    } else {
-                        atomicOr(a.status, 4u);  // queue full: cannot happen (capacity = pixels)
-                    }
-                }
-                break;
+        unsigned t0 = 0;
+        if (lane == 0) t0 = atomicAdd(a.tile_counter, claim);
+        t0 = __shfl_sync(kFull, t0, 0);
+        if (t0 >= total) break;
+        const unsigned t1 = min(t0 + claim, total);
+        for (unsigned t = t0; t < t1; ++t) {
+            if (BATCH) {
+                const int v = find_view(tile_pfx, nviews, t);
+                march_tile<STATS>(views[v], t - __ldg(tile_pfx + v), (uint32_t)v, lane, acc, rays, started_n, hits);
+            } else {
+                march_tile<STATS>(a, t, 0u, lane, acc, rays, started_n, hits);
             }
-            const float rho = union_density<STATS>(a, need, L, r.e, acc);
-            if (need) apply(a, r, rho);
-            ++iters;
         }
-        // normals of the hit rays (all in phase kNormal), then outputs; deferred
-        // rays are finished (and written) by the long-ray pass
-        const bool hit = !deferred && r.phase == kNormal;
-        Loc Lh;
-        Lh.c[0] = Lh.c[1] = Lh.c[2] = 0;
-        Lh.u[0] = Lh.u[1] = Lh.u[2] = 0.0f;
-        const bool gn = hit && locate(a.g, r.p[0], r.p[1], r.p[2], Lh);
-        if (STATS && hit && !gn) acc.evals++;
-        float gx = 0.f, gy = 0.f, gz = 0.f;
-        if (__any_sync(kFull, gn)) union_grad<STATS>(a, gn, Lh, r.p, acc, gx, gy, gz);
-        float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-        if (hit) {
-            const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
-            n0 = gx * gi;
-            n1 = gy * gi;
-            n2 = gz * gi;
-            if (STATS) hits++;
-        }
-        if (valid && !deferred) write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
     }
     if (acc.bad) atomicOr(a.status, 2u);
-    if (STATS) {
-        unsigned long long v[kStats] = {rays, started_n, hits, (unsigned long long)acc.evals,
-                                        (unsigned long long)acc.cand, (unsigned long long)acc.skipped,
-                                        (unsigned long long)acc.tested, (unsigned long long)acc.streamed,
-                                        (unsigned long long)acc.deferred};
-#pragma unroll
-        for (int j = 0; j < kStats; ++j) {
-            unsigned long long x = v[j];
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
-            if (lane == 0 && x) atomicAdd(a.stats + j, x);
-        }
+    if (STATS) flush_stats(a, lane, acc, rays, started_n, hits, true);
+}
+
+// Finish one queued ray with the whole warp and write its pixel.
+template <bool STATS>
+__device__ __forceinline__ void finish_long(const MarchArgs& a, uint32_t idx, Ray& r, int lane, Acc& acc,
+                                            uint64_t& hits) {
+    const int px = (int)(idx % (uint32_t)a.W), py = (int)(idx / (uint32_t)a.W);
+    float p0[3];
+    ray_setup(a, px, py, a.zbuf[idx], p0, r.s);
+    const bool cnt = lane == 0;
+    Loc L;
+    bool need = locate(a.g, r.e[0], r.e[1], r.e[2], L);  // the pending point was prepared
+    while (need) {
+        const float rho = density_warp<STATS>(a.g, a.k, L, r.e[0], r.e[1], r.e[2], a.cull, lane, acc, cnt);
+        apply(a, r, rho);
+        need = prepare<STATS>(a, r, L, acc, cnt);
+    }
+    const bool hit = r.phase == kNormal;
+    float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+    if (hit) {
+        float gx, gy, gz;
+        grad_warp<STATS>(a.g, a.k, r.p[0], r.p[1], r.p[2], a.cull, lane, acc, cnt, gx, gy, gz);
+        const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+        n0 = gx * gi;
+        n1 = gy * gi;
+        n2 = gz * gi;
+    }
+    if (lane == 0) {
+        write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
+        if (STATS && hit) hits++;
     }
 }
 
 // Long-ray pass: persistent warps take deferred rays one at a time and finish
 // them with all 32 lanes (density_warp / grad_warp), then write the pixel.
-template <bool STATS>
-__global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a) {
+template <bool STATS, bool BATCH>
+__global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a, const MarchArgs* __restrict__ views) {
     const int lane = threadIdx.x & 31;
     Acc acc;
     uint64_t hits = 0;
@@ -727,48 +770,21 @@ __global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a) {
         r.p[0] = w1.x; r.p[1] = w1.y; r.p[2] = w1.z;
         r.q[0] = w2.x; r.q[1] = w2.y; r.q[2] = w2.z;
         r.e[0] = w3.x; r.e[1] = w3.y; r.e[2] = w3.z;
-        const int px = (int)(idx % (uint32_t)a.W), py = (int)(idx / (uint32_t)a.W);
-        float p0[3];
-        ray_setup(a, px, py, a.zbuf[idx], p0, r.s);
-        const bool cnt = lane == 0;
-        Loc L;
-        bool need = locate(a.g, r.e[0], r.e[1], r.e[2], L);  // the pending point was prepared
-        while (need) {
-            const float rho = density_warp<STATS>(a.g, a.k, L, r.e[0], r.e[1], r.e[2], a.cull, lane, acc, cnt);
-            apply(a, r, rho);
-            need = prepare<STATS>(a, r, L, acc, cnt);
-        }
-        const bool hit = r.phase == kNormal;
-        float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-        if (hit) {
-            float gx, gy, gz;
-            grad_warp<STATS>(a.g, a.k, r.p[0], r.p[1], r.p[2], a.cull, lane, acc, cnt, gx, gy, gz);
-            const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
-            n0 = gx * gi;
-            n1 = gy * gi;
-            n2 = gz * gi;
-        }
-        if (lane == 0) {
-            write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
-            if (STATS && hit) hits++;
-        }
+        if (BATCH) finish_long<STATS>(views[__float_as_uint(w3.w)], idx, r, lane, acc, hits);
+        else finish_long<STATS>(a, idx, r, lane, acc, hits);
     }
     if (acc.bad) atomicOr(a.status, 2u);
-    if (STATS && lane == 0) {
-        const unsigned long long v[kStats] = {0ull, 0ull, hits, (unsigned long long)acc.evals,
-                                              (unsigned long long)acc.cand, (unsigned long long)acc.skipped,
-                                              (unsigned long long)acc.tested, 0ull, 0ull};
-#pragma unroll
-        for (int j = 0; j < kStats; ++j)
-            if (v[j]) atomicAdd(a.stats + j, v[j]);
+    if (STATS) {
+        acc.streamed = 0;
+        acc.deferred = 0;
+        flush_stats(a, lane, acc, 0, 0, hits, false);
     }
 }
-
 }  // namespace
 
-int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
-                 const MarchOutDev& o, cudaStream_t st) {
-    MarchArgs a;
+MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_march_params* p, const MarchOutDev& o,
+                          const TileConfig& cfg) {
+    MarchArgs a{};
     a.g = grid_dev(s);
     a.k = make_kernel(s->support);
     a.iso = p->iso_density;
@@ -789,8 +805,12 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
     a.cdir[2] = cam->view[10];
     a.W = cam->width;
     a.Hh = cam->height;
-    a.tiles_x = (cam->width + kTileW - 1) / kTileW;
-    a.ntiles = a.tiles_x * ((cam->height + kTileH - 1) / kTileH);
+    a.tw_log2 = cfg.tw_log2;
+    a.claim = cfg.claim;
+    a.cap = cfg.cap;
+    const int tw = 1 << cfg.tw_log2, th = 32 >> cfg.tw_log2;
+    a.tiles_x = (cam->width + tw - 1) / tw;
+    a.ntiles = a.tiles_x * ((cam->height + th - 1) / th);
     a.twoWinv = 2.0f / (float)cam->width;
     a.twoHinv = 2.0f / (float)cam->height;
     a.zbuf = o.start_depth;
@@ -798,6 +818,58 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
     a.nrm = o.nrm;
     a.depth = o.depth;
     a.col = o.col;
+    return a;
+}
+
+int launch_march_kernels(fm_ctx* ctx, const MarchArgs& a, const MarchArgs* d_views, const uint32_t* d_tile_pfx,
+                         int nviews, cudaStream_t st) {
+    const bool stats = a.stats != nullptr, batch = nviews > 0;
+    int blocks_per_sm = 0;
+    if (batch) {
+        if (stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<true, true>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<false, true>, kThreads, 0);
+    } else {
+        if (stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<true, false>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<false, false>, kThreads, 0);
+    }
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+    int blocks = ctx->sm_count * blocks_per_sm;
+    const int warps_needed = (a.ntiles + a.claim - 1) / a.claim;
+    const int max_blocks = (warps_needed + kThreads / 32 - 1) / (kThreads / 32);
+    if (blocks > max_blocks) blocks = max_blocks;
+    if (blocks < 1) blocks = 1;
+    if (batch) {
+        if (stats) k_march<true, true><<<blocks, kThreads, 0, st>>>(a, d_views, d_tile_pfx, nviews);
+        else k_march<false, true><<<blocks, kThreads, 0, st>>>(a, d_views, d_tile_pfx, nviews);
+    } else {
+        if (stats) k_march<true, false><<<blocks, kThreads, 0, st>>>(a, nullptr, nullptr, 0);
+        else k_march<false, false><<<blocks, kThreads, 0, st>>>(a, nullptr, nullptr, 0);
+    }
+    FM_CUDA(ctx, cudaGetLastError());
+    int long_per_sm = 0;
+    if (batch) {
+        if (stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<true, true>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<false, true>, kThreads, 0);
+    } else {
+        if (stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<true, false>, kThreads, 0);
+        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<false, false>, kThreads, 0);
+    }
+    if (long_per_sm < 1) long_per_sm = 1;
+    const int lblocks = ctx->sm_count * long_per_sm;
+    if (batch) {
+        if (stats) k_march_long<true, true><<<lblocks, kThreads, 0, st>>>(a, d_views);
+        else k_march_long<false, true><<<lblocks, kThreads, 0, st>>>(a, d_views);
+    } else {
+        if (stats) k_march_long<true, false><<<lblocks, kThreads, 0, st>>>(a, nullptr);
+        else k_march_long<false, false><<<lblocks, kThreads, 0, st>>>(a, nullptr);
+    }
+    FM_CUDA(ctx, cudaGetLastError());
+    return FM_OK;
+}
+
+int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
+                 const MarchOutDev& o, cudaStream_t st) {
+    MarchArgs a = march_view_args(s, cam, p, o, ctx->tile);
     a.stats = ctx->stats_enabled ? ctx->d_stats : nullptr;
     a.status = ctx->d_status;
     // fresh counters per launch (a ring of slots, so launches on different
@@ -807,37 +879,14 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
     a.q_tail = slot + 1;
     a.q_head = slot + 2;
     FM_CUDA(ctx, cudaMemsetAsync(slot, 0, 3 * sizeof(unsigned int), st));
-    // long-ray queue: at most one entry per pixel
-    const uint64_t npx = (uint64_t)cam->width * (uint64_t)cam->height;
-    if (ctx->longq.bytes < npx * 64) {
+    const uint64_t entries = long_queue_entries((uint64_t)cam->width * (uint64_t)cam->height, ctx->tile.qlimit);
+    if (ctx->longq.bytes < entries * 64) {
         FM_CUDA(ctx, cudaStreamSynchronize(st));  // the buffer may be in use by an earlier launch
-        if (ctx->longq.p) cudaFree(ctx->longq.p);
-        ctx->longq.p = nullptr;
-        ctx->longq.bytes = 0;
-        if (cudaMalloc(&ctx->longq.p, npx * 64) != cudaSuccess) return set_err(ctx, FM_ERR_OOM, "long-ray queue allocation failed");
-        ctx->longq.bytes = npx * 64;
+        if (!grow_buf(ctx->longq, entries * 64)) return set_err(ctx, FM_ERR_OOM, "long-ray queue allocation failed");
     }
     a.longq = (float4*)ctx->longq.p;
-    a.q_cap = (unsigned int)npx;
-    a.cap = 32;
-    int blocks_per_sm = 0;
-    if (a.stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<true>, kThreads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<false>, kThreads, 0);
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
-    int blocks = ctx->sm_count * blocks_per_sm;
-    const int max_blocks = (a.ntiles + kThreads / 32 - 1) / (kThreads / 32);
-    if (blocks > max_blocks) blocks = max_blocks;
-    if (a.stats) k_march<true><<<blocks, kThreads, 0, st>>>(a);
-    else k_march<false><<<blocks, kThreads, 0, st>>>(a);
-    FM_CUDA(ctx, cudaGetLastError());
-    int long_per_sm = 0;
-    if (a.stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<true>, kThreads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<false>, kThreads, 0);
-    if (long_per_sm < 1) long_per_sm = 1;
-    if (a.stats) k_march_long<true><<<ctx->sm_count * long_per_sm, kThreads, 0, st>>>(a);
-    else k_march_long<false><<<ctx->sm_count * long_per_sm, kThreads, 0, st>>>(a);
-    FM_CUDA(ctx, cudaGetLastError());
-    return FM_OK;
+    a.q_cap = (unsigned int)entries;
+    return launch_march_kernels(ctx, a, nullptr, nullptr, 0, st);
 }
 
 }  // namespace fm

@@ -36,19 +36,9 @@
 namespace fm {
 namespace {
 
-constexpr int kHizTile = 8;
-constexpr uint64_t kSample = 8;
+constexpr int kHizTile = kSplatHizTile;
+constexpr uint64_t kSample = kSplatSample;
 constexpr int kThreads = 256;
-
-struct SplatArgs {
-    float V[16];
-    float P00, P11, P22, P32, P23, P33;
-    float R, invR;
-    float twoWinv, twoHinv;
-    int W, Hh;
-    const float* __restrict__ hiz;  // per 8x8 tile: max depth after pass 1
-    int hiz_w, hiz_h;
-};
 
 __device__ __forceinline__ float cos_poly(float t) {
     float x = t * t;
@@ -165,39 +155,44 @@ __global__ void k_hiz(const float* __restrict__ depth, int W, int Hh, int tw, in
     hiz[t] = m;
 }
 
-// Pass 2: the particles pass 1 left out, tested against the tile maxima; the
-// ones that may still lower a pixel are appended to `list`.
-__global__ void __launch_bounds__(kThreads) k_splat_cull(const float4* __restrict__ pts, uint64_t n, SplatArgs a,
-                                                        uint32_t* __restrict__ list, unsigned int* __restrict__ count) {
-    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    bool keep = false;
-    if (i < n && (i % kSample) != 0) {
-        const float4 q = pts[i];
-        float cx, cy, cz;
-        int x0, x1, y0, y1;
-        if (disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) {
-            // nearest depth the disc can produce (every fragment has view z >= z - R),
-            // lowered by 8 ulps so that rounding in the fragment formula cannot go below it
-            const float zv = cz - a.R;
-            const float d0 = (a.P22 * zv + a.P32) / (a.P23 * zv + a.P33);
-            uint32_t db = __float_as_uint(fmaxf(d0, 0.0f));  // NaN -> 0
-            db = db > 8u ? db - 8u : 0u;
-            const float dmin = __uint_as_float(db);
-            for (int ty = y0 / kHizTile; ty <= y1 / kHizTile && !keep; ++ty)
-                for (int tx = x0 / kHizTile; tx <= x1 / kHizTile; ++tx)
-                    if (a.hiz[ty * a.hiz_w + tx] > dmin) {
-                        keep = true;
-                        break;
-                    }
-        }
-    }
+// Cull test of pass 2: true when the disc of q may still lower a pixel.
+__device__ __forceinline__ bool cull_keep(const SplatArgs& a, const float4& q) {
+    float cx, cy, cz;
+    int x0, x1, y0, y1;
+    if (!disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) return false;
+    if (!a.cull) return true;
+    // nearest depth the disc can produce (every fragment has view z >= z - R),
+    // lowered by 8 ulps so that rounding in the fragment formula cannot go below it
+    const float zv = cz - a.R;
+    const float d0 = (a.P22 * zv + a.P32) / (a.P23 * zv + a.P33);
+    uint32_t db = __float_as_uint(fmaxf(d0, 0.0f));  // NaN -> 0
+    db = db > 8u ? db - 8u : 0u;
+    const float dmin = __uint_as_float(db);
+    for (int ty = y0 / kHizTile; ty <= y1 / kHizTile; ++ty)
+        for (int tx = x0 / kHizTile; tx <= x1 / kHizTile; ++tx)
+            if (a.hiz[ty * a.hiz_w + tx] > dmin) return true;
+    return false;
+}
+
+// Append the kept entries of a warp to list (one atomic per warp).
+__device__ __forceinline__ void append(bool keep, uint32_t value, uint32_t* __restrict__ list,
+                                       unsigned int* __restrict__ count) {
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     if (!m) return;
     const int lane = threadIdx.x & 31;
     unsigned base = 0;
     if (lane == 0) base = atomicAdd(count, (unsigned)__popc(m));
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (keep) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+    if (keep) list[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+// Pass 2: the particles pass 1 left out, tested against the tile maxima; the
+// ones that may still lower a pixel are appended to `list`.
+__global__ void __launch_bounds__(kThreads) k_splat_cull(const float4* __restrict__ pts, uint64_t n, SplatArgs a,
+                                                        uint32_t* __restrict__ list, unsigned int* __restrict__ count) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const bool keep = i < n && (i % kSample) != 0 && cull_keep(a, pts[i]);
+    append(keep, (uint32_t)i, list, count);
 }
 
 // Pass 3: warp per kept particle.
@@ -217,7 +212,88 @@ __global__ void __launch_bounds__(kThreads) k_splat_list(const float4* __restric
     }
 }
 
-bool grow(DevBuf& b, size_t bytes) {
+// ---- batched passes: one launch per pass over the units of all views --------
+
+// The largest v with pfx[v] <= u (pfx ascending, pfx[0] = 0).
+template <typename T>
+__device__ __forceinline__ int find_view(const T* __restrict__ pfx, int nviews, T u) {
+    int lo = 0, hi = nviews - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pfx[mid] <= u) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+__global__ void k_fill_b(SplatBatch b) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= b.tot_px) return;
+    const int v = find_view(b.pfx_px, b.nviews, i);
+    b.views[v].depth[i - b.pfx_px[v]] = 0x3f800000u;
+}
+
+// Pass 1: warp per sampled particle (every kSample-th of each view).
+__global__ void __launch_bounds__(kThreads) k_splat_warp_b(SplatBatch b) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (kThreads / 32);
+    for (uint64_t w = (blockIdx.x * (uint64_t)kThreads + threadIdx.x) / 32; w < b.tot_sample; w += warps) {
+        const int v = find_view(b.pfx_sample, b.nviews, w);
+        const SplatView& sv = b.views[v];
+        const float4 q = sv.pts[(w - b.pfx_sample[v]) * kSample];
+        float cx, cy, cz;
+        int x0, x1, y0, y1;
+        if (!disc_box(sv.a, q, cx, cy, cz, x0, x1, y0, y1)) continue;
+        splat_disc_warp(sv.a, cx, cy, cz, x0, x1, y0, y1, lane, sv.depth);
+    }
+}
+
+__global__ void k_hiz_b(SplatBatch b) {
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= b.tot_tiles) return;
+    const int v = find_view(b.pfx_tiles, b.nviews, t);
+    const SplatView& sv = b.views[v];
+    const int tl = (int)(t - b.pfx_tiles[v]);
+    const int tx = tl % sv.a.hiz_w, ty = tl / sv.a.hiz_w;
+    const float* depth = (const float*)sv.depth;
+    float m = 0.0f;
+    for (int y = ty * kHizTile; y < min(ty * kHizTile + kHizTile, sv.a.Hh); ++y)
+        for (int x = tx * kHizTile; x < min(tx * kHizTile + kHizTile, sv.a.W); ++x)
+            m = fmaxf(m, depth[(uint64_t)y * sv.a.W + x]);
+    b.hiz[t] = m;
+}
+
+__global__ void __launch_bounds__(kThreads) k_splat_cull_b(SplatBatch b) {
+    const uint64_t g = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    bool keep = false;
+    if (g < b.tot_n) {
+        const int v = find_view(b.pfx_n, b.nviews, g);
+        const SplatView& sv = b.views[v];
+        const uint64_t i = g - b.pfx_n[v];
+        keep = (i % kSample) != 0 && cull_keep(sv.a, sv.pts[i]);
+    }
+    append(keep, (uint32_t)g, b.list, b.count);
+}
+
+__global__ void __launch_bounds__(kThreads) k_splat_list_b(SplatBatch b) {
+    const int lane = threadIdx.x & 31;
+    const uint64_t warps = (uint64_t)gridDim.x * (kThreads / 32);
+    const uint64_t total = *b.count;
+    for (uint64_t w = (blockIdx.x * (uint64_t)kThreads + threadIdx.x) / 32; w < total; w += warps) {
+        const uint64_t g = b.list[w];
+        const int v = find_view(b.pfx_n, b.nviews, g);
+        const SplatView& sv = b.views[v];
+        const float4 q = sv.pts[g - b.pfx_n[v]];
+        float cx, cy, cz;
+        int x0, x1, y0, y1;
+        if (!disc_box(sv.a, q, cx, cy, cz, x0, x1, y0, y1)) continue;
+        splat_disc_warp(sv.a, cx, cy, cz, x0, x1, y0, y1, lane, sv.depth);
+    }
+}
+
+}  // namespace
+
+bool grow_buf(DevBuf& b, size_t bytes) {
     if (b.bytes >= bytes) return true;
     if (b.p) cudaFree(b.p);
     b.p = nullptr;
@@ -227,9 +303,7 @@ bool grow(DevBuf& b, size_t bytes) {
     return true;
 }
 
-}  // namespace
-
-int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_depth, cudaStream_t st) {
+SplatArgs splat_args(const fm_scene* s, const fm_camera* cam) {
     SplatArgs a;
     for (int i = 0; i < 16; ++i) a.V[i] = cam->view[i];
     a.P00 = cam->proj[0];
@@ -247,13 +321,18 @@ int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_
     a.hiz = nullptr;
     a.hiz_w = (cam->width + kHizTile - 1) / kHizTile;
     a.hiz_h = (cam->height + kHizTile - 1) / kHizTile;
+    // the culling test needs depth to grow with view z: d(z) = (P22 z + P32) / (P23 z + P33)
+    a.cull = ((a.P22 * a.P33 - a.P32 * a.P23) > 0.0f && a.P23 > 0.0f && a.P33 >= 0.0f) ? 1 : 0;
+    return a;
+}
+
+int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_depth, cudaStream_t st) {
+    SplatArgs a = splat_args(s, cam);
     const uint64_t npx = (uint64_t)cam->width * cam->height;
     k_fill<<<(unsigned)((npx + 255) / 256), 256, 0, st>>>((uint32_t*)d_depth, npx, 0x3f800000u);
     if (s->n == 0) return FM_OK;
     const unsigned persist = (unsigned)ctx->sm_count * 8;  // 64 warps per SM
-    // the culling test needs depth to grow with view z: d(z) = (P22 z + P32) / (P23 z + P33)
-    const bool cull = (a.P22 * a.P33 - a.P32 * a.P23) > 0.0f && a.P23 > 0.0f && a.P33 >= 0.0f;
-    if (!cull) {
+    if (!a.cull) {
         k_splat_warp<<<persist, kThreads, 0, st>>>(s->d_pts, s->n, 1, a, (uint32_t*)d_depth);
         FM_CUDA(ctx, cudaGetLastError());
         return FM_OK;
@@ -261,7 +340,7 @@ int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_
     const size_t hiz_bytes = (size_t)a.hiz_w * a.hiz_h * sizeof(float);
     if (ctx->hiz.bytes < hiz_bytes || ctx->splat_list.bytes < s->n * sizeof(uint32_t)) {
         FM_CUDA(ctx, cudaStreamSynchronize(st));  // old buffers may still be in use on this stream
-        if (!grow(ctx->hiz, hiz_bytes) || !grow(ctx->splat_list, s->n * sizeof(uint32_t)))
+        if (!grow_buf(ctx->hiz, hiz_bytes) || !grow_buf(ctx->splat_list, s->n * sizeof(uint32_t)))
             return set_err(ctx, FM_ERR_OOM, "splat buffer allocation failed");
     }
     a.hiz = (const float*)ctx->hiz.p;
@@ -274,6 +353,21 @@ int launch_splat(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* d_
         s->d_pts, s->n, a, (uint32_t*)ctx->splat_list.p, count);
     k_splat_list<<<persist, kThreads, 0, st>>>(s->d_pts, (const uint32_t*)ctx->splat_list.p, count, a,
                                                (uint32_t*)d_depth);
+    FM_CUDA(ctx, cudaGetLastError());
+    return FM_OK;
+}
+
+// Batched depth pass: fill, sampled pass, tile maxima, cull, survivors; one
+// launch each for all views.  Views whose projection does not allow the tile
+// test keep all their particles in the list (the result is the same).
+int launch_splat_batch(fm_ctx* ctx, const SplatBatch& b, cudaStream_t st) {
+    if (b.tot_px) k_fill_b<<<(unsigned)((b.tot_px + 255) / 256), 256, 0, st>>>(b);
+    if (b.tot_n == 0) return FM_OK;
+    const unsigned persist = (unsigned)ctx->sm_count * 8;
+    k_splat_warp_b<<<persist, kThreads, 0, st>>>(b);
+    if (b.tot_tiles) k_hiz_b<<<(b.tot_tiles + 255) / 256, 256, 0, st>>>(b);
+    k_splat_cull_b<<<(unsigned)((b.tot_n + kThreads - 1) / kThreads), kThreads, 0, st>>>(b);
+    k_splat_list_b<<<persist, kThreads, 0, st>>>(b);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }

@@ -35,6 +35,8 @@ EXPORTS = [
     "fm_version", "fm_create", "fm_destroy", "fm_last_error", "fm_stream", "fm_sync", "fm_query", "fm_host_alloc",
     "fm_host_free", "fm_scene_create", "fm_scene_update", "fm_scene_destroy", "fm_scene_grid", "fm_scene_download",
     "fm_splat_depth", "fm_march", "fm_set_stats", "fm_march_stats_get", "fm_grid_build_noalloc",
+    "fm_set_tile_config", "fm_get_tile_config", "fm_batch_create", "fm_batch_run", "fm_batch_refresh",
+    "fm_batch_autotune", "fm_batch_info_get", "fm_batch_destroy", "fm_march_batch",
 ]
 
 
@@ -69,6 +71,20 @@ class CMarchStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("started", C.c_uint64), ("hits", C.c_uint64), ("evals", C.c_uint64),
                 ("candidates", C.c_uint64), ("skipped", C.c_uint64), ("tested", C.c_uint64),
                 ("streamed", C.c_uint64), ("deferred", C.c_uint64)]
+
+
+class CTileConfig(C.Structure):
+    _fields_ = [("tile_width", C.c_int32), ("tiles_per_claim", C.c_int32), ("defer_iters", C.c_int32),
+                ("long_queue", C.c_int32)]
+
+
+class CView(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("camera", CCamera), ("params", CMarchParams), ("out", CFrameOut)]
+
+
+class CBatchInfo(C.Structure):
+    _fields_ = [("n_views", C.c_int32), ("graph_nodes", C.c_int32), ("pixels", C.c_uint64),
+                ("particles", C.c_uint64), ("tiles", C.c_uint64), ("config", CTileConfig)]
 
 
 _lib = None
@@ -108,6 +124,17 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_march_stats_get.argtypes = [vp, C.POINTER(CMarchStats)]
     L.fm_grid_build_noalloc.argtypes = [vp, C.c_uint64, C.c_uint32, C.c_float, vp, vp, vp, vp, C.c_uint64,
                                         C.POINTER(CGridInfo), vp]
+    L.fm_set_tile_config.argtypes = [vp, C.POINTER(CTileConfig)]
+    L.fm_get_tile_config.argtypes = [vp, C.POINTER(CTileConfig)]
+    L.fm_batch_create.argtypes = [vp, C.POINTER(CView), C.c_int32, C.POINTER(CTileConfig), C.POINTER(vp)]
+    L.fm_batch_run.argtypes = [vp, vp]
+    L.fm_batch_refresh.argtypes = [vp]
+    L.fm_batch_autotune.argtypes = [vp, C.POINTER(CTileConfig), C.c_int32, C.c_int32, C.POINTER(CTileConfig),
+                                    C.POINTER(C.c_float)]
+    L.fm_batch_info_get.argtypes = [vp, C.POINTER(CBatchInfo)]
+    L.fm_batch_destroy.argtypes = [vp]
+    L.fm_batch_destroy.restype = None
+    L.fm_march_batch.argtypes = [vp, C.POINTER(CView), C.c_int32, vp]
     _lib = L
     return L
 
@@ -147,6 +174,7 @@ class Context:
             raise FmError(rc, f"fm_create(device={device}) failed")
         self.h = h
         self._scenes = weakref.WeakSet()
+        self._batches = weakref.WeakSet()
 
     def check(self, rc: int):
         if rc != FM_OK:
@@ -173,9 +201,22 @@ class Context:
         self.check(self.L.fm_march_stats_get(self.h, C.byref(s)))
         return {k: int(getattr(s, k)) for k, _ in CMarchStats._fields_}
 
+    def set_tile_config(self, tile_width: int = 8, tiles_per_claim: int = 1, defer_iters: int = 32,
+                        long_queue: int = 0):
+        """Work split of single-view marches (results do not depend on it)."""
+        c = CTileConfig(int(tile_width), int(tiles_per_claim), int(defer_iters), int(long_queue))
+        self.check(self.L.fm_set_tile_config(self.h, C.byref(c)))
+
+    def tile_config(self) -> dict:
+        c = CTileConfig()
+        self.check(self.L.fm_get_tile_config(self.h, C.byref(c)))
+        return _tile_dict(c)
+
     def close(self):
-        """Destroy the context; its scenes that are still open are closed first."""
+        """Destroy the context; its batches and scenes that are still open are closed first."""
         if getattr(self, "h", None):
+            for b in list(self._batches):
+                b.close()
             for sc in list(self._scenes):
                 sc.close()
             self.L.fm_destroy(self.h)
@@ -287,6 +328,98 @@ def render(scene: Scene, cam, params: MarchParams, want_start: bool = True) -> d
         out["start_depth"] = np.zeros(npx, np.float32)
     march(scene, cam, params, out["position"], out["normal"], out["depth"], out["colour"], out.get("start_depth"))
     return out
+
+
+def _tile_dict(c: CTileConfig) -> dict:
+    return {"tile_width": int(c.tile_width), "tiles_per_claim": int(c.tiles_per_claim),
+            "defer_iters": int(c.defer_iters), "long_queue": int(c.long_queue)}
+
+
+def _tile_struct(d: dict) -> CTileConfig:
+    return CTileConfig(int(d["tile_width"]), int(d.get("tiles_per_claim", 1)), int(d.get("defer_iters", 32)),
+                       int(d.get("long_queue", 0)))
+
+
+@dataclass
+class View:
+    """One view of a batch: scene, camera, march settings and DEVICE output buffers."""
+
+    scene: Scene
+    camera: object
+    params: MarchParams
+    position: object = None
+    normal: object = None
+    depth: object = None
+    colour: object = None
+    start_depth: object = None
+
+    def cstruct(self) -> CView:
+        if self.params.external_depth:
+            raise ValueError("batched views are splatted: external_depth must be False")
+        ptrs = []
+        for b in (self.position, self.normal, self.depth, self.colour, self.start_depth):
+            p, mem = _ptr(b)
+            if p is not None and mem != FM_MEM_DEVICE:
+                raise ValueError("batch outputs must be device buffers")
+            ptrs.append(p)
+        return CView(self.scene.h, camera_struct(self.camera), self.params.cstruct(), CFrameOut(*ptrs))
+
+
+class Batch:
+    """Many views of many scenes rendered by one launch per pass under a CUDA graph."""
+
+    def __init__(self, ctx: Context, views: list, tile_config: dict | None = None):
+        self.ctx = ctx
+        self.views = list(views)  # keeps the scenes and buffers alive
+        arr = (CView * len(views))(*[v.cstruct() for v in views])
+        cfg = None
+        if tile_config is not None:
+            cfg = C.byref(_tile_struct(tile_config))
+        h = C.c_void_p()
+        ctx.check(ctx.L.fm_batch_create(ctx.h, arr, len(views), cfg, C.byref(h)))
+        self.h = h
+        ctx._batches.add(self)
+
+    def run(self, stream=None):
+        self.ctx.check(self.ctx.L.fm_batch_run(self.h, stream))
+
+    def refresh(self):
+        self.ctx.check(self.ctx.L.fm_batch_refresh(self.h))
+
+    def autotune(self, reps: int = 2, candidates: list | None = None) -> tuple:
+        best = CTileConfig()
+        ms = C.c_float()
+        if candidates:
+            arr = (CTileConfig * len(candidates))(*[_tile_struct(c) for c in candidates])
+            rc = self.ctx.L.fm_batch_autotune(self.h, arr, len(candidates), int(reps), C.byref(best), C.byref(ms))
+        else:
+            rc = self.ctx.L.fm_batch_autotune(self.h, None, 0, int(reps), C.byref(best), C.byref(ms))
+        self.ctx.check(rc)
+        return _tile_dict(best), float(ms.value)
+
+    def info(self) -> dict:
+        i = CBatchInfo()
+        self.ctx.check(self.ctx.L.fm_batch_info_get(self.h, C.byref(i)))
+        return {"n_views": int(i.n_views), "graph_nodes": int(i.graph_nodes), "pixels": int(i.pixels),
+                "particles": int(i.particles), "tiles": int(i.tiles), "config": _tile_dict(i.config)}
+
+    def close(self):
+        if getattr(self, "h", None):
+            if getattr(self.ctx, "h", None):  # a closed context already freed its batches
+                self.ctx.L.fm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def march_batch(ctx: Context, views: list, stream=None):
+    """One-shot batch: create, run, wait, destroy."""
+    arr = (CView * len(views))(*[v.cstruct() for v in views])
+    ctx.check(ctx.L.fm_march_batch(ctx.h, arr, len(views), stream))
 
 
 class RayMarcher:

@@ -210,10 +210,75 @@ int fm_splat_depth(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, flo
 int fm_march(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, const fm_march_params* params,
              const fm_frame_out* out, int mem, void* stream);
 
-/* Counters of the last fm_march on this context (enable with
+/* Counters of the last fm_march / fm_batch_run on this context (enable with
  * fm_set_stats(ctx, 1); counting costs time, keep it off when timing). */
 int fm_set_stats(fm_ctx* ctx, int enable);
 int fm_march_stats_get(fm_ctx* ctx, fm_march_stats* out);
+
+/* ---- work split and batches --------------------------------------------
+ * No counterpart in the reference, which renders one view per Start() with a
+ * thread pool over pixels (RayMarcher.cpp:102-112, ThreadPool.cpp:5-55).  */
+
+/* How the march splits an image among warps.  Results do not depend on it. */
+typedef struct fm_tile_config {
+    int32_t tile_width;      /* pixels per tile row: 1, 2, 4, 8, 16 or 32; a tile
+                                is tile_width x (32 / tile_width) pixels */
+    int32_t tiles_per_claim; /* tiles a warp takes at a time: 1..16 */
+    int32_t defer_iters;     /* density sums a warp runs for one tile before the
+                                rays it still has go to the long-ray pass: 1..4096 */
+    int32_t long_queue;      /* entries of the long-ray queue; 0 = pixels / 8 + 65536.
+                                Rays that find it full stay with their warp. */
+} fm_tile_config;
+
+/* Work split of fm_march on this context (default 8, 1, 32, 0). */
+int fm_set_tile_config(fm_ctx* ctx, const fm_tile_config* cfg);
+int fm_get_tile_config(const fm_ctx* ctx, fm_tile_config* out);
+
+/* One view of a batch: a scene seen from a camera with its own march
+ * settings.  Output pointers are DEVICE memory (NULL skips an output);
+ * start_depth may be NULL (the batch keeps the splat depths itself).
+ * params.flags must be 0: every view is splatted. */
+typedef struct fm_view {
+    const fm_scene* scene;
+    fm_camera camera;
+    fm_march_params params;
+    fm_frame_out out;
+} fm_view;
+
+typedef struct fm_batch fm_batch;
+
+typedef struct fm_batch_info {
+    int32_t n_views;
+    int32_t graph_nodes;     /* kernel and memset nodes of the captured graph */
+    uint64_t pixels;         /* sum of W * H over the views */
+    uint64_t particles;      /* sum of the views' particle counts */
+    uint64_t tiles;          /* march tiles of the whole batch */
+    fm_tile_config config;   /* work split in use */
+} fm_batch_info;
+
+/* Prepare a batch of views: all views are splatted and marched by one launch
+ * per pass (fill, sampled splat, tile maxima, cull, survivor splat, march,
+ * long rays), captured once into a CUDA graph.  The views' scenes and output
+ * buffers are bound at creation: after fm_scene_update of one of its scenes,
+ * call fm_batch_refresh.  cfg NULL: the context's work split.  Synchronous. */
+int fm_batch_create(fm_ctx* ctx, const fm_view* views, int32_t n_views, const fm_tile_config* cfg, fm_batch** out);
+/* Render every view: one graph launch on `stream` (NULL = context stream),
+ * asynchronous.  With counters enabled (fm_set_stats) the passes are launched
+ * without the graph and counted. */
+int fm_batch_run(fm_batch* batch, void* stream);
+/* Re-read the scenes' grids and re-capture the graph (synchronous). */
+int fm_batch_refresh(fm_batch* batch);
+/* Time the batch under candidate work splits (`reps` timed runs each after
+ * one warm-up; cands NULL: a built-in set of tile shapes, claims and defer
+ * limits), keep the fastest, re-capture.  best / best_ms may be NULL.
+ * Synchronous; the outputs hold the last run's results (identical for every
+ * split). */
+int fm_batch_autotune(fm_batch* batch, const fm_tile_config* cands, int32_t n_cands, int32_t reps,
+                      fm_tile_config* best, float* best_ms);
+int fm_batch_info_get(const fm_batch* batch, fm_batch_info* out);
+void fm_batch_destroy(fm_batch* batch);
+/* One-shot: create a batch, run it on `stream`, wait, destroy it. */
+int fm_march_batch(fm_ctx* ctx, const fm_view* views, int32_t n_views, void* stream);
 
 /* Library version (major * 10000 + minor * 100 + patch). */
 int fm_version(void);

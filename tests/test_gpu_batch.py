@@ -1,0 +1,217 @@
+"""Batched views and work splits against single-view marches and the oracle.
+
+A batch renders many views of many scenes (uneven particle counts,
+resolutions and march settings) with one launch per pass under a CUDA graph;
+every view must come out bit-identical to the same view rendered alone, and
+the single-view march must not depend on the work split (tile shape, tiles
+per claim, deferral limit, long-ray queue size).
+"""
+
+import numpy as np
+import pytest
+
+import oracle as O
+from fluidmarch import scenes
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+
+KEYS = ("position", "normal", "depth", "colour", "start_depth")
+SHAPE = {"position": 4, "normal": 4, "depth": 1, "colour": 4, "start_depth": 1}
+
+
+def bits(a):
+    return np.ascontiguousarray(a).view(np.uint32)
+
+
+def device_outputs(cam):
+    npx = cam.width * cam.height
+    return {k: torch.zeros((npx, SHAPE[k]) if SHAPE[k] > 1 else (npx,), dtype=torch.float32, device="cuda")
+            for k in KEYS}
+
+
+def host(out):
+    return {k: v.cpu().numpy() for k, v in out.items()}
+
+
+def single(fm, scene, cam, params):
+    npx = cam.width * cam.height
+    out = {"position": np.zeros((npx, 4), np.float32), "normal": np.zeros((npx, 4), np.float32),
+           "depth": np.zeros(npx, np.float32), "colour": np.zeros((npx, 4), np.float32),
+           "start_depth": np.zeros(npx, np.float32)}
+    fm.march(scene, cam, params, out["position"], out["normal"], out["depth"], out["colour"], out["start_depth"])
+    return out
+
+
+def assert_same(a, b, what=""):
+    for k in KEYS:
+        if k not in a or k not in b:
+            continue
+        x, y = bits(a[k]), bits(b[k])
+        bad = np.nonzero(np.any((x != y).reshape(x.shape[0], -1), axis=1))[0]
+        assert bad.size == 0, f"{what} {k}: {bad.size} pixels differ, first {bad[:5]}"
+
+
+@pytest.fixture(scope="module")
+def small_batch(fmlib, ctx):
+    """Six scenes of the sloshing family, 1-3 views each, mixed settings."""
+    specs = [(3000, 64, 48), (9000, 120, 90), (1500, 33, 17), (20000, 160, 96), (6000, 96, 64), (12000, 80, 120)]
+    rng = np.random.default_rng(5)
+    items = []
+    for i, (n, w, h) in enumerate(specs):
+        sc = scenes.small_scene(seed=100 + i, n=n, width=w, height=h, max_steps=200)
+        s = fmlib.Scene(ctx, sc.xyz, sc.support)
+        for k in range(1 + i % 3):
+            ang = rng.uniform(0, 2 * np.pi)
+            eye = (0.5 + 1.8 * np.cos(ang), 1.2, 0.5 + 1.8 * np.sin(ang))
+            cam = scenes.make_camera(eye, (0.5, 0.3, 0.5), w + 7 * k, h + 3 * k)
+            params = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, (0, 8, 3)[k % 3], (i + k) % 3)
+            items.append((sc, s, cam, params))
+    return items
+
+
+def make_views(fmlib, items):
+    views, outs = [], []
+    for sc, s, cam, params in items:
+        o = device_outputs(cam)
+        outs.append(o)
+        views.append(fmlib.View(s, cam, params, **o))
+    return views, outs
+
+
+def test_batch_matches_single_views(fmlib, ctx, small_batch):
+    views, outs = make_views(fmlib, small_batch)
+    b = fmlib.Batch(ctx, views)
+    info = b.info()
+    assert info["n_views"] == len(views)
+    assert info["graph_nodes"] >= 8  # counter reset, 5 depth-pass launches, 2 march launches
+    b.run()
+    ctx.sync()
+    for i, (sc, s, cam, params) in enumerate(small_batch):
+        assert_same(host(outs[i]), single(fmlib, s, cam, params), f"view {i}")
+    # a second graph launch gives the same frame
+    for o in outs:
+        for v in o.values():
+            v.zero_()
+    b.run()
+    ctx.sync()
+    for i, (sc, s, cam, params) in enumerate(small_batch):
+        assert_same(host(outs[i]), single(fmlib, s, cam, params), f"rerun view {i}")
+    b.close()
+
+
+def test_batch_view_matches_oracle(fmlib, ctx, small_batch, oracle_lib):
+    sc, s, cam, params = small_batch[3]
+    views, outs = make_views(fmlib, [small_batch[3]])
+    b = fmlib.Batch(ctx, views)
+    b.run()
+    ctx.sync()
+    g = host(outs[0])
+    fr = O.build_frame(sc.xyz, sc.support)
+    depth = O.splat(sc.xyz, sc.support, cam)
+    assert np.array_equal(bits(g["start_depth"]), bits(depth))
+    o = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, params.bisect, depth, skip_mode=params.skip_mode)
+    assert_same(g, o, "oracle")
+    b.close()
+
+
+@pytest.mark.parametrize("cfg", [
+    dict(tile_width=1), dict(tile_width=2), dict(tile_width=4), dict(tile_width=16), dict(tile_width=32),
+    dict(tile_width=8, tiles_per_claim=4), dict(tile_width=8, defer_iters=1), dict(tile_width=8, defer_iters=4096),
+    dict(tile_width=8, long_queue=3), dict(tile_width=16, defer_iters=2, long_queue=1),
+])
+def test_tile_config_does_not_change_results(fmlib, ctx, cfg):
+    sc = scenes.small_scene(seed=44, n=12000, width=130, height=70)
+    cam = sc.cameras[0]
+    s = fmlib.Scene(ctx, sc.xyz, sc.support)
+    p = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, 8, 1)
+    ref = single(fmlib, s, cam, p)
+    old = ctx.tile_config()
+    try:
+        ctx.set_tile_config(**cfg)
+        ctx.set_stats(True)
+        got = single(fmlib, s, cam, p)
+        st = ctx.stats()
+    finally:
+        ctx.set_stats(False)
+        ctx.set_tile_config(**old)
+    assert_same(got, ref, str(cfg))
+    if cfg.get("defer_iters") == 1 and "long_queue" not in cfg:
+        assert st["deferred"] > 0
+
+
+def test_batch_tile_configs_and_autotune(fmlib, ctx, small_batch):
+    views, outs = make_views(fmlib, small_batch[:5])
+    b = fmlib.Batch(ctx, views, tile_config=dict(tile_width=32, tiles_per_claim=2, defer_iters=8, long_queue=2))
+    b.run()
+    ctx.sync()
+    first = [host(o) for o in outs]
+    best, ms = b.autotune(reps=1, candidates=[dict(tile_width=4), dict(tile_width=8, defer_iters=64)])
+    assert best["tile_width"] in (4, 8) and ms > 0
+    assert b.info()["config"]["tile_width"] == best["tile_width"]
+    best, ms = b.autotune(reps=1)
+    assert best["tile_width"] in (4, 8, 16, 32) and ms > 0
+    for o in outs:
+        for v in o.values():
+            v.zero_()
+    b.run()
+    ctx.sync()
+    for i in range(len(outs)):
+        assert_same(host(outs[i]), first[i], f"view {i} after tuning")
+    b.close()
+
+
+def test_batch_counters(fmlib, ctx, small_batch):
+    views, outs = make_views(fmlib, small_batch)
+    b = fmlib.Batch(ctx, views)
+    ctx.set_stats(True)
+    try:
+        b.run()
+        ctx.sync()
+        st = ctx.stats()
+    finally:
+        ctx.set_stats(False)
+    assert st["rays"] == b.info()["pixels"]
+    assert st["hits"] == sum(int((o["depth"] > 0).sum()) for o in outs)
+    b.close()
+
+
+def test_batch_scene_update_needs_refresh(fmlib, ctx):
+    sc = scenes.small_scene(seed=61, n=6000, width=80, height=60)
+    cam = sc.cameras[0]
+    s = fmlib.Scene(ctx, sc.xyz, sc.support)
+    p = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, 8, 1)
+    views, outs = make_views(fmlib, [(sc, s, cam, p)])
+    b = fmlib.Batch(ctx, views)
+    moved = (sc.xyz + np.float32(0.01)).astype(np.float32)
+    s.update(moved)
+    with pytest.raises(fmlib.FmError):
+        b.run()
+    b.refresh()
+    b.run()
+    ctx.sync()
+    assert_same(host(outs[0]), single(fmlib, s, cam, p), "after refresh")
+    b.close()
+    s.close()
+
+
+def test_march_batch_one_shot(fmlib, ctx, small_batch):
+    views, outs = make_views(fmlib, small_batch[:3])
+    fmlib.march_batch(ctx, views)
+    for i, (sc, s, cam, params) in enumerate(small_batch[:3]):
+        assert_same(host(outs[i]), single(fmlib, s, cam, params), f"one-shot view {i}")
+
+
+def test_batch_rejects_bad_views(fmlib, ctx, small_batch):
+    sc, s, cam, params = small_batch[0]
+    o = device_outputs(cam)
+    with pytest.raises(fmlib.FmError):
+        fmlib.Batch(ctx, [])
+    bad = fmlib.MarchParams(params.iso, -1.0, params.max_steps)
+    with pytest.raises(fmlib.FmError):
+        fmlib.Batch(ctx, [fmlib.View(s, cam, bad, **o)])
+    with pytest.raises(fmlib.FmError):
+        fmlib.Batch(ctx, [fmlib.View(s, cam, params, **o)], tile_config=dict(tile_width=3))
+    with pytest.raises(ValueError):
+        fmlib.View(s, cam, params, position=np.zeros((cam.width * cam.height, 4), np.float32)).cstruct()
