@@ -88,7 +88,8 @@ int check_params(fm_ctx* ctx, const fm_march_params* p) {
     if (p->bisect_iters < 0 || p->bisect_iters > 64) return set_err(ctx, FM_ERR_INVALID, "bisect_iters must be in [0, 64]");
     if (p->skip_mode < FM_SKIP_OFF || p->skip_mode > FM_SKIP_REFERENCE)
         return set_err(ctx, FM_ERR_INVALID, "unknown skip mode");
-    if (p->flags & ~FM_MARCH_EXTERNAL_DEPTH) return set_err(ctx, FM_ERR_INVALID, "unknown march flags");
+    if (p->flags & ~(FM_MARCH_EXTERNAL_DEPTH | FM_MARCH_PROPOSAL))
+        return set_err(ctx, FM_ERR_INVALID, "unknown march flags");
     return FM_OK;
 }
 
@@ -134,6 +135,7 @@ static void scene_free(fm_scene* s) {
     cudaFree(s->d_sub);
     cudaFree(s->d_bound);
     cudaFree(s->d_flag);
+    cudaFree(s->d_occ);
     delete s;
 }
 
@@ -153,6 +155,10 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->longq.p);
     cudaFree(ctx->hiz.p);
     cudaFree(ctx->splat_list.p);
+    cudaFree(ctx->prop_ivl.p);
+    cudaFree(ctx->prop_scratch.p);
+    cudaFree(ctx->prop_low.p);
+    cudaFree(ctx->prop_judge.p);
     if (ctx->h_pinned_small) cudaFreeHost(ctx->h_pinned_small);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -364,6 +370,8 @@ int fm_march_stats_get(fm_ctx* ctx, fm_march_stats* out) {
     out->tested = h[6];
     out->streamed = h[7];
     out->deferred = h[8];
+    out->proposed = h[9];
+    out->fallbacks = h[10];
     return FM_OK;
 }
 
@@ -409,6 +417,14 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
         if (rc) return rc;
     }
     o.start_depth = z;
+    o.ivl = nullptr;
+    if (p->flags & FM_MARCH_PROPOSAL) {
+        if (!ctx->proposal) return set_err(ctx, FM_ERR_INVALID, "FM_MARCH_PROPOSAL needs a proposal (fm_set_proposal)");
+        if (!grow(ctx->prop_ivl, npx * sizeof(int2))) return set_err(ctx, FM_ERR_OOM, "interval buffer allocation failed");
+        rc = launch_propose(ctx, sm, cam, p, ctx->proposal, z, (int2*)ctx->prop_ivl.p, nullptr, st);
+        if (rc) return rc;
+        o.ivl = (const int2*)ctx->prop_ivl.p;
+    }
     float* user[4] = {out->position, out->normal, out->depth, out->colour};
     const size_t per[4] = {16, 16, 4, 16};
     void* dev[4] = {nullptr, nullptr, nullptr, nullptr};

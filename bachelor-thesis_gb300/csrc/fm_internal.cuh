@@ -18,6 +18,9 @@
 namespace fm {
 
 constexpr int kWarp = 32;
+constexpr int kProposalOcc = 64;        // occupancy grid resolution of the proposal
+constexpr int kProposalFeatures = FM_PROPOSAL_FEATURES;
+constexpr int kProposalParams = FM_PROPOSAL_PARAMS;
 constexpr unsigned kWorkSlots = 64;
 constexpr int kStatSlots = 16;
 
@@ -192,6 +195,10 @@ struct fm_ctx {
     // not overlap
     fm::DevBuf hiz;
     fm::DevBuf splat_list;
+    // learned proposal: the one fm_march uses with FM_MARCH_PROPOSAL, per-pixel
+    // intervals, occupancy counts, low-resolution depth, judge counters
+    fm_proposal* proposal = nullptr;
+    fm::DevBuf prop_ivl, prop_scratch, prop_low, prop_judge;
     // live scenes of this context; fm_destroy frees the ones still alive
     std::vector<fm_scene*> scenes;
     // live batches of this context; fm_destroy frees the ones still alive
@@ -222,6 +229,8 @@ struct fm_scene {
     bool bound_valid = false;
     bool flag_valid = false;
     uint64_t gen = 0;              // build generation: batches bound to an older one refuse to run
+    uint16_t* d_occ = nullptr;     // 64^3 FP16 occupancy of the proposal (lazy)
+    bool occ_valid = false;
 };
 
 namespace fm {
@@ -284,6 +293,7 @@ struct MarchOutDev {
     float* depth;
     float4* col;
     const float* start_depth;
+    const int2* ivl;  // proposed intervals (learned march) or null
 };
 
 // Arguments of one view.  A batch holds one per view in device memory, with
@@ -304,6 +314,7 @@ struct MarchArgs {
     int claim;             // tiles a warp takes per atomic
     float twoWinv, twoHinv;
     const float* __restrict__ zbuf;
+    const int2* __restrict__ ivl;  // proposed intervals per pixel (learned march) or null
     float4* pos;
     float4* nrm;
     float* depth;
@@ -341,6 +352,13 @@ int check_params(fm_ctx* ctx, const fm_march_params* p);
 bool grow_buf(DevBuf& b, size_t bytes);
 // Free the batches a context still holds (batch.cu).
 void destroy_batches(fm_ctx* ctx);
+
+// Learned proposal (proposal.cu).
+int ensure_occupancy(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
+int launch_features(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const float* zbuf, float* feat, float* t0,
+                    cudaStream_t st);
+int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const fm_proposal* pr,
+                   const float* zbuf, int2* ivl, float2* raw, cudaStream_t st);
 
 int set_err(fm_ctx* ctx, int code, const std::string& msg);
 int cuda_err(fm_ctx* ctx, cudaError_t e, const char* what);

@@ -438,6 +438,7 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     s->ncells = ncells;
     s->bound_valid = false;
     s->flag_valid = false;
+    s->occ_valid = false;
     const uint64_t nkeys = 8 * ncells;
     if (ncells > s->cell_capacity) {
         cudaFree(s->d_sub);

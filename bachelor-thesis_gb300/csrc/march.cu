@@ -53,7 +53,7 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 256;  // 8 warps per block
-constexpr int kStats = 9;  // fm_march_stats field order
+constexpr int kStats = 11;  // fm_march_stats field order
 
 struct Acc {
     uint32_t evals = 0;
@@ -62,6 +62,8 @@ struct Acc {
     uint64_t streamed = 0;   // shared-stream particles (counted by lane 0 of the warp)
     uint32_t deferred = 0;   // rays handed to the long-ray pass
     uint32_t skipped = 0;
+    uint32_t proposed = 0;   // rays that started inside a proposed interval
+    uint32_t fallbacks = 0;  // of those, rays restarted as full marches
     bool bad = false;  // an index guard fired (reported through the status word, bit 2)
 };
 
@@ -269,7 +271,7 @@ __device__ __forceinline__ void write_pixel(const MarchArgs& a, uint64_t idx, in
 
 // ---- per-lane ray state -------------------------------------------------------
 
-enum Phase : int { kMarch = 0, kBisect = 1, kNormal = 2, kDone = 3 };
+enum Phase : int { kMarch = 0, kBisect = 1, kNormal = 2, kDone = 3, kRestart = 4 };
 
 struct Ray {
     int phase;
@@ -278,13 +280,20 @@ struct Ray {
     float q[3];           // previous sample (march) / outside end (bisection)
     float s[3];           // step
     float e[3];           // pending evaluation point
+    int ks, kf;           // proposed interval: samples ks+1 .. kf (kf < 0: full march)
 };
 
 // Apply the density at the pending point (RayMarcher.cpp:327: hit when rho >= iso).
+// LEARNED: a ray marching a proposed interval whose first sample is already
+// inside cannot tell whether the crossing lies before the interval: it restarts
+// as a full march.
+template <bool LEARNED>
 __device__ __forceinline__ void apply(const MarchArgs& a, Ray& r, float rho) {
     const bool inside = rho >= a.iso;
     if (r.phase == kMarch) {
-        if (inside) {
+        if (LEARNED && inside && r.kf >= 0 && r.i == r.ks + 1) {
+            r.phase = kRestart;
+        } else if (inside) {
             r.b = 0;
             r.phase = a.bisect > 0 ? kBisect : kNormal;
         } else {
@@ -302,10 +311,13 @@ __device__ __forceinline__ void apply(const MarchArgs& a, Ray& r, float rho) {
 // samples out of reach of every particle get density 0 without a sum.
 // Returns true with r.e / L set when a sum is needed, false when the ray left
 // the march or bisection phases.
-template <bool STATS>
+// LEARNED: a ray in a proposed interval that reaches the interval's end (or
+// leaves the grid) without a crossing restarts as a full march (kRestart).
+template <bool STATS, bool LEARNED>
 __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc& acc, bool cnt) {
     for (;;) {
         if (r.phase == kMarch) {
+            if (LEARNED && r.kf >= 0 && r.i >= r.kf) { r.phase = kRestart; return false; }
             if (r.i >= a.max_steps) { r.phase = kDone; return false; }
             r.p[0] = r.p[0] + r.s[0];
             r.p[1] = r.p[1] + r.s[1];
@@ -314,11 +326,11 @@ __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc&
             if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2], a.status);
             if (!locate(a.g, r.p[0], r.p[1], r.p[2], L)) {
                 if (outside_forever(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2])) {
-                    r.phase = kDone;
+                    r.phase = (LEARNED && r.kf >= 0) ? kRestart : kDone;
                     return false;
                 }
                 if (STATS && cnt) acc.evals++;
-                apply(a, r, 0.0f);
+                apply<LEARNED>(a, r, 0.0f);
                 continue;
             }
             if (a.skip_mode == FM_SKIP_EXACT && L.c[0] >= 0 && L.c[1] >= 0 && L.c[2] >= 0 && L.c[0] < a.g.dims[0] &&
@@ -341,7 +353,7 @@ __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc&
             r.e[2] = (r.q[2] + r.p[2]) * 0.5f;
             if (!locate(a.g, r.e[0], r.e[1], r.e[2], L)) {
                 if (STATS && cnt) acc.evals++;
-                apply(a, r, 0.0f);
+                apply<LEARNED>(a, r, 0.0f);
                 continue;
             }
             return true;
@@ -536,14 +548,14 @@ __device__ __forceinline__ void ray_setup(const MarchArgs& a, int px, int py, fl
     s[2] = a.step * (dz * inv);
 }
 
-// Long-ray queue entry: 4 float4 = {pixel, phase, i, b}, p, q, {e, view}
+// Long-ray queue entry: 4 float4 = {pixel, phase, i, b}, {p, ks}, {q, kf}, {e, view}
 // (e: the pending evaluation point).  The step is recomputed from the pixel.
 __device__ __forceinline__ void push_long(const MarchArgs& a, uint32_t slot, uint32_t idx, uint32_t view,
                                           const Ray& r) {
     float4* d = a.longq + 4ull * slot;
     d[0] = make_float4(__uint_as_float(idx), __int_as_float(r.phase), __int_as_float(r.i), __int_as_float(r.b));
-    d[1] = make_float4(r.p[0], r.p[1], r.p[2], 0.0f);
-    d[2] = make_float4(r.q[0], r.q[1], r.q[2], 0.0f);
+    d[1] = make_float4(r.p[0], r.p[1], r.p[2], __int_as_float(r.ks));
+    d[2] = make_float4(r.q[0], r.q[1], r.q[2], __int_as_float(r.kf));
     d[3] = make_float4(r.e[0], r.e[1], r.e[2], __uint_as_float(view));
 }
 
@@ -594,7 +606,32 @@ __device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, 
 
 // One 32-pixel tile of view `a` (lane = ray).  `view` tags the rays this
 // warp defers to the long-ray queue.
+// LEARNED: restart a ray as a full march from its start (the proposal missed).
 template <bool STATS>
+__device__ __forceinline__ void restart(const MarchArgs& a, Ray& r, int px, int py, uint64_t idx, Acc& acc, bool cnt) {
+    ray_setup(a, px, py, a.zbuf[idx], r.p, r.s);
+    r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
+    r.i = 0;
+    r.b = 0;
+    r.kf = -1;
+    r.phase = kMarch;
+    if (STATS && cnt) acc.fallbacks++;
+}
+
+// Advance to the next sum, restarting rays whose proposed interval failed.
+template <bool STATS, bool LEARNED>
+__device__ __forceinline__ bool advance(const MarchArgs& a, Ray& r, Loc& L, int px, int py, uint64_t idx, Acc& acc,
+                                        bool cnt) {
+    if (LEARNED && r.phase == kRestart) restart<STATS>(a, r, px, py, idx, acc, cnt);
+    bool need = (r.phase == kMarch || r.phase == kBisect) && prepare<STATS, LEARNED>(a, r, L, acc, cnt);
+    if (LEARNED && !need && r.phase == kRestart) {
+        restart<STATS>(a, r, px, py, idx, acc, cnt);
+        need = prepare<STATS, LEARNED>(a, r, L, acc, cnt);
+    }
+    return need;
+}
+
+template <bool STATS, bool LEARNED>
 __device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, uint32_t view, int lane, Acc& acc,
                                            uint64_t& rays, uint64_t& started_n, uint64_t& hits) {
     const int tw = 1 << a.tw_log2;
@@ -607,8 +644,26 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, ui
     Ray r;
     r.phase = kDone;
     r.i = r.b = 0;
+    r.ks = 0;
+    r.kf = -1;
     if (valid && z != 1.0f) {
         ray_setup(a, px, py, z, r.p, r.s);
+        if (LEARNED) {
+            // start at sample ks of the plain march (the same FP32 additions),
+            // evaluate samples ks+1 .. kf
+            const int2 iv = a.ivl[idx];
+            if (iv.x >= 1 && iv.x < iv.y && iv.y <= a.max_steps) {
+                for (int k = 0; k < iv.x; ++k) {
+                    r.p[0] = r.p[0] + r.s[0];
+                    r.p[1] = r.p[1] + r.s[1];
+                    r.p[2] = r.p[2] + r.s[2];
+                }
+                r.i = iv.x;
+                r.ks = iv.x;
+                r.kf = iv.y;
+                if (STATS) acc.proposed++;
+            }
+        }
         r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
         r.phase = kMarch;
     } else {
@@ -624,7 +679,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, ui
     int iters = 0;
     bool deferred = false, keep = false;
     for (;;) {
-        bool need = (r.phase == kMarch || r.phase == kBisect) && prepare<STATS>(a, r, L, acc, true);
+        bool need = advance<STATS, LEARNED>(a, r, L, px, py, idx, acc, true);
         uint32_t act = __ballot_sync(kFull, need);
         if (!act) break;
         if (!keep && (__popc(act) <= 2 || iters >= a.cap)) {
@@ -646,7 +701,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, ui
             keep = true;
         }
         const float rho = union_density<STATS>(a, need, L, r.e, acc);
-        if (need) apply(a, r, rho);
+        if (need) apply<LEARNED>(a, r, rho);
         ++iters;
     }
     // normals of the hit rays (all in phase kNormal), then outputs; deferred
@@ -675,7 +730,8 @@ __device__ __forceinline__ void flush_stats(const MarchArgs& a, int lane, const 
     unsigned long long v[kStats] = {rays, started_n, hits, (unsigned long long)acc.evals,
                                     (unsigned long long)acc.cand, (unsigned long long)acc.skipped,
                                     (unsigned long long)acc.tested, (unsigned long long)acc.streamed,
-                                    (unsigned long long)acc.deferred};
+                                    (unsigned long long)acc.deferred, (unsigned long long)acc.proposed,
+                                    (unsigned long long)acc.fallbacks};
 #pragma unroll
     for (int j = 0; j < kStats; ++j) {
         unsigned long long x = v[j];
@@ -690,7 +746,7 @@ __device__ __forceinline__ void flush_stats(const MarchArgs& a, int lane, const 
 // Shared-stream pass.  Persistent warps take `a.claim` tiles per atomic from
 // the launch's counter.  BATCH: `a` holds the launch-wide fields and the total
 // tile count; tile t belongs to view find_view(tile_pfx, t) of `views`.
-template <bool STATS, bool BATCH>
+template <bool STATS, bool BATCH, bool LEARNED>
 __global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a, const MarchArgs* __restrict__ views,
                                                       const uint32_t* __restrict__ tile_pfx, int nviews) {
     const int lane = threadIdx.x & 31;
@@ -706,9 +762,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a, const 
         for (unsigned t = t0; t < t1; ++t) {
             if (BATCH) {
                 const int v = find_view(tile_pfx, nviews, t);
-                march_tile<STATS>(views[v], t - __ldg(tile_pfx + v), (uint32_t)v, lane, acc, rays, started_n, hits);
+                march_tile<STATS, LEARNED>(views[v], t - __ldg(tile_pfx + v), (uint32_t)v, lane, acc, rays,
+                                           started_n, hits);
             } else {
-                march_tile<STATS>(a, t, 0u, lane, acc, rays, started_n, hits);
+                march_tile<STATS, LEARNED>(a, t, 0u, lane, acc, rays, started_n, hits);
             }
         }
     }
@@ -717,7 +774,7 @@ __global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a, const 
 }
 
 // Finish one queued ray with the whole warp and write its pixel.
-template <bool STATS>
+template <bool STATS, bool LEARNED>
 __device__ __forceinline__ void finish_long(const MarchArgs& a, uint32_t idx, Ray& r, int lane, Acc& acc,
                                             uint64_t& hits) {
     const int px = (int)(idx % (uint32_t)a.W), py = (int)(idx / (uint32_t)a.W);
@@ -728,8 +785,8 @@ __device__ __forceinline__ void finish_long(const MarchArgs& a, uint32_t idx, Ra
     bool need = locate(a.g, r.e[0], r.e[1], r.e[2], L);  // the pending point was prepared
     while (need) {
         const float rho = density_warp<STATS>(a.g, a.k, L, r.e[0], r.e[1], r.e[2], a.cull, lane, acc, cnt);
-        apply(a, r, rho);
-        need = prepare<STATS>(a, r, L, acc, cnt);
+        apply<LEARNED>(a, r, rho);
+        need = advance<STATS, LEARNED>(a, r, L, px, py, idx, acc, cnt);
     }
     const bool hit = r.phase == kNormal;
     float n0 = 0.f, n1 = 0.f, n2 = 0.f;
@@ -749,7 +806,7 @@ __device__ __forceinline__ void finish_long(const MarchArgs& a, uint32_t idx, Ra
 
 // Long-ray pass: persistent warps take deferred rays one at a time and finish
 // them with all 32 lanes (density_warp / grad_warp), then write the pixel.
-template <bool STATS, bool BATCH>
+template <bool STATS, bool BATCH, bool LEARNED>
 __global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a, const MarchArgs* __restrict__ views) {
     const int lane = threadIdx.x & 31;
     Acc acc;
@@ -770,13 +827,16 @@ __global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a, cons
         r.p[0] = w1.x; r.p[1] = w1.y; r.p[2] = w1.z;
         r.q[0] = w2.x; r.q[1] = w2.y; r.q[2] = w2.z;
         r.e[0] = w3.x; r.e[1] = w3.y; r.e[2] = w3.z;
-        if (BATCH) finish_long<STATS>(views[__float_as_uint(w3.w)], idx, r, lane, acc, hits);
-        else finish_long<STATS>(a, idx, r, lane, acc, hits);
+        r.ks = __float_as_int(w1.w);
+        r.kf = __float_as_int(w2.w);
+        if (BATCH) finish_long<STATS, LEARNED>(views[__float_as_uint(w3.w)], idx, r, lane, acc, hits);
+        else finish_long<STATS, LEARNED>(a, idx, r, lane, acc, hits);
     }
     if (acc.bad) atomicOr(a.status, 2u);
     if (STATS) {
         acc.streamed = 0;
         acc.deferred = 0;
+        acc.proposed = 0;
         flush_stats(a, lane, acc, 0, 0, hits, false);
     }
 }
@@ -814,6 +874,7 @@ MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_marc
     a.twoWinv = 2.0f / (float)cam->width;
     a.twoHinv = 2.0f / (float)cam->height;
     a.zbuf = o.start_depth;
+    a.ivl = o.ivl;
     a.pos = o.pos;
     a.nrm = o.nrm;
     a.depth = o.depth;
@@ -821,50 +882,45 @@ MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_marc
     return a;
 }
 
-int launch_march_kernels(fm_ctx* ctx, const MarchArgs& a, const MarchArgs* d_views, const uint32_t* d_tile_pfx,
-                         int nviews, cudaStream_t st) {
-    const bool stats = a.stats != nullptr, batch = nviews > 0;
-    int blocks_per_sm = 0;
-    if (batch) {
-        if (stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<true, true>, kThreads, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<false, true>, kThreads, 0);
-    } else {
-        if (stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<true, false>, kThreads, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, k_march<false, false>, kThreads, 0);
-    }
-    if (blocks_per_sm < 1) blocks_per_sm = 1;
-    int blocks = ctx->sm_count * blocks_per_sm;
+namespace {
+
+template <bool STATS, bool BATCH, bool LEARNED>
+int launch_variant(fm_ctx* ctx, const MarchArgs& a, const MarchArgs* d_views, const uint32_t* d_tile_pfx, int nviews,
+                   cudaStream_t st) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march<STATS, BATCH, LEARNED>, kThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+    int blocks = ctx->sm_count * per_sm;
     const int warps_needed = (a.ntiles + a.claim - 1) / a.claim;
     const int max_blocks = (warps_needed + kThreads / 32 - 1) / (kThreads / 32);
     if (blocks > max_blocks) blocks = max_blocks;
     if (blocks < 1) blocks = 1;
-    if (batch) {
-        if (stats) k_march<true, true><<<blocks, kThreads, 0, st>>>(a, d_views, d_tile_pfx, nviews);
-        else k_march<false, true><<<blocks, kThreads, 0, st>>>(a, d_views, d_tile_pfx, nviews);
-    } else {
-        if (stats) k_march<true, false><<<blocks, kThreads, 0, st>>>(a, nullptr, nullptr, 0);
-        else k_march<false, false><<<blocks, kThreads, 0, st>>>(a, nullptr, nullptr, 0);
-    }
+    k_march<STATS, BATCH, LEARNED><<<blocks, kThreads, 0, st>>>(a, d_views, d_tile_pfx, nviews);
     FM_CUDA(ctx, cudaGetLastError());
     int long_per_sm = 0;
-    if (batch) {
-        if (stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<true, true>, kThreads, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<false, true>, kThreads, 0);
-    } else {
-        if (stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<true, false>, kThreads, 0);
-        else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<false, false>, kThreads, 0);
-    }
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<STATS, BATCH, LEARNED>, kThreads, 0);
     if (long_per_sm < 1) long_per_sm = 1;
-    const int lblocks = ctx->sm_count * long_per_sm;
-    if (batch) {
-        if (stats) k_march_long<true, true><<<lblocks, kThreads, 0, st>>>(a, d_views);
-        else k_march_long<false, true><<<lblocks, kThreads, 0, st>>>(a, d_views);
-    } else {
-        if (stats) k_march_long<true, false><<<lblocks, kThreads, 0, st>>>(a, nullptr);
-        else k_march_long<false, false><<<lblocks, kThreads, 0, st>>>(a, nullptr);
-    }
+    k_march_long<STATS, BATCH, LEARNED><<<ctx->sm_count * long_per_sm, kThreads, 0, st>>>(a, d_views);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
+}
+
+}  // namespace
+
+int launch_march_kernels(fm_ctx* ctx, const MarchArgs& a, const MarchArgs* d_views, const uint32_t* d_tile_pfx,
+                         int nviews, cudaStream_t st) {
+    const bool stats = a.stats != nullptr, batch = nviews > 0, learned = a.ivl != nullptr;
+    const int k = (stats ? 4 : 0) | (batch ? 2 : 0) | (learned ? 1 : 0);
+    switch (k) {
+        case 0: return launch_variant<false, false, false>(ctx, a, d_views, d_tile_pfx, nviews, st);
+        case 1: return launch_variant<false, false, true>(ctx, a, d_views, d_tile_pfx, nviews, st);
+        case 2: return launch_variant<false, true, false>(ctx, a, d_views, d_tile_pfx, nviews, st);
+        case 3: return launch_variant<false, true, true>(ctx, a, d_views, d_tile_pfx, nviews, st);
+        case 4: return launch_variant<true, false, false>(ctx, a, d_views, d_tile_pfx, nviews, st);
+        case 5: return launch_variant<true, false, true>(ctx, a, d_views, d_tile_pfx, nviews, st);
+        case 6: return launch_variant<true, true, false>(ctx, a, d_views, d_tile_pfx, nviews, st);
+        default: return launch_variant<true, true, true>(ctx, a, d_views, d_tile_pfx, nviews, st);
+    }
 }
 
 int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,

@@ -30,6 +30,9 @@ FM_OK, FM_ERR_INVALID, FM_ERR_CUDA, FM_ERR_TIMEOUT, FM_ERR_OOM, FM_ERR_DEVICE = 
 FM_MEM_HOST, FM_MEM_DEVICE = 0, 1
 FM_SKIP_OFF, FM_SKIP_EXACT, FM_SKIP_REFERENCE = 0, 1, 2
 FM_MARCH_EXTERNAL_DEPTH = 1
+FM_MARCH_PROPOSAL = 2
+FM_PROPOSAL_FEATURES = 32
+FM_PROPOSAL_PARAMS = 6402
 
 EXPORTS = [
     "fm_version", "fm_create", "fm_destroy", "fm_last_error", "fm_stream", "fm_sync", "fm_query", "fm_host_alloc",
@@ -37,6 +40,9 @@ EXPORTS = [
     "fm_splat_depth", "fm_march", "fm_set_stats", "fm_march_stats_get", "fm_grid_build_noalloc",
     "fm_set_tile_config", "fm_get_tile_config", "fm_batch_create", "fm_batch_run", "fm_batch_refresh",
     "fm_batch_autotune", "fm_batch_info_get", "fm_batch_destroy", "fm_march_batch",
+    "fm_proposal_create", "fm_proposal_destroy", "fm_set_proposal", "fm_proposal_features", "fm_proposal_intervals",
+    "fm_judge", "fm_trainer_create", "fm_trainer_destroy", "fm_trainer_step", "fm_trainer_predict",
+    "fm_trainer_params",
 ]
 
 
@@ -70,7 +76,13 @@ class CGridInfo(C.Structure):
 class CMarchStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("started", C.c_uint64), ("hits", C.c_uint64), ("evals", C.c_uint64),
                 ("candidates", C.c_uint64), ("skipped", C.c_uint64), ("tested", C.c_uint64),
-                ("streamed", C.c_uint64), ("deferred", C.c_uint64)]
+                ("streamed", C.c_uint64), ("deferred", C.c_uint64), ("proposed", C.c_uint64),
+                ("fallbacks", C.c_uint64)]
+
+
+class CJudge(C.Structure):
+    _fields_ = [("pixels", C.c_uint64), ("hits_ref", C.c_uint64), ("hits_test", C.c_uint64),
+                ("mask_mismatch", C.c_uint64), ("within_tol", C.c_uint64), ("max_err", C.c_float), ("tol", C.c_float)]
 
 
 class CTileConfig(C.Structure):
@@ -135,6 +147,19 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_batch_destroy.argtypes = [vp]
     L.fm_batch_destroy.restype = None
     L.fm_march_batch.argtypes = [vp, C.POINTER(CView), C.c_int32, vp]
+    L.fm_proposal_create.argtypes = [vp, vp, C.c_float, C.c_float, C.POINTER(vp)]
+    L.fm_proposal_destroy.argtypes = [vp]
+    L.fm_proposal_destroy.restype = None
+    L.fm_set_proposal.argtypes = [vp, vp]
+    L.fm_proposal_features.argtypes = [vp, vp, C.POINTER(CCamera), vp, vp, vp, vp]
+    L.fm_proposal_intervals.argtypes = [vp, vp, C.POINTER(CCamera), C.POINTER(CMarchParams), vp, vp, vp, vp]
+    L.fm_judge.argtypes = [vp, vp, vp, C.c_uint64, C.c_float, C.POINTER(CJudge), vp]
+    L.fm_trainer_create.argtypes = [vp, C.c_uint64, vp, C.POINTER(vp)]
+    L.fm_trainer_destroy.argtypes = [vp]
+    L.fm_trainer_destroy.restype = None
+    L.fm_trainer_step.argtypes = [vp, vp, vp, C.c_uint32, C.c_float, C.c_float, C.c_float, C.POINTER(C.c_float)]
+    L.fm_trainer_predict.argtypes = [vp, vp, C.c_uint32, vp]
+    L.fm_trainer_params.argtypes = [vp, vp]
     _lib = L
     return L
 
@@ -175,6 +200,8 @@ class Context:
         self.h = h
         self._scenes = weakref.WeakSet()
         self._batches = weakref.WeakSet()
+        self._proposals = weakref.WeakSet()
+        self._trainers = weakref.WeakSet()
 
     def check(self, rc: int):
         if rc != FM_OK:
@@ -217,6 +244,10 @@ class Context:
         if getattr(self, "h", None):
             for b in list(self._batches):
                 b.close()
+            for t in list(self._trainers):
+                t.close()
+            for p in list(self._proposals):
+                p.close()
             for sc in list(self._scenes):
                 sc.close()
             self.L.fm_destroy(self.h)
@@ -287,10 +318,12 @@ class MarchParams:
     bisect: int = 0
     skip_mode: int = FM_SKIP_OFF
     external_depth: bool = False
+    proposal: bool = False
 
     def cstruct(self) -> CMarchParams:
+        flags = (FM_MARCH_EXTERNAL_DEPTH if self.external_depth else 0) | (FM_MARCH_PROPOSAL if self.proposal else 0)
         return CMarchParams(float(self.iso), float(self.step), int(self.max_steps), int(self.bisect),
-                            int(self.skip_mode), FM_MARCH_EXTERNAL_DEPTH if self.external_depth else 0)
+                            int(self.skip_mode), flags)
 
 
 def splat_depth(scene: Scene, cam, out=None, stream=None):
@@ -407,6 +440,104 @@ class Batch:
         if getattr(self, "h", None):
             if getattr(self.ctx, "h", None):  # a closed context already freed its batches
                 self.ctx.L.fm_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Proposal:
+    """Learned hit-interval proposal (MLP parameters on the device)."""
+
+    def __init__(self, ctx: Context, params, margin_lo: float = 0.0, margin_hi: float = 0.0):
+        self.ctx = ctx
+        p = np.ascontiguousarray(params, np.float32).reshape(-1)
+        if p.size != FM_PROPOSAL_PARAMS:
+            raise ValueError(f"expected {FM_PROPOSAL_PARAMS} parameters, got {p.size}")
+        h = C.c_void_p()
+        ctx.check(ctx.L.fm_proposal_create(ctx.h, p.ctypes.data, float(margin_lo), float(margin_hi), C.byref(h)))
+        self.h = h
+        self.params = p
+        ctx._proposals.add(self)
+
+    def close(self):
+        if getattr(self, "h", None):
+            if getattr(self.ctx, "h", None):
+                self.ctx.L.fm_proposal_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def set_proposal(ctx: Context, p):
+    ctx.check(ctx.L.fm_set_proposal(ctx.h, p.h if p is not None else None))
+    ctx._active_proposal = p
+
+
+def proposal_features(scene: Scene, cam, start_depth, features, t0=None, stream=None):
+    """Features of every pixel's ray into device buffers (W*H x 32 floats, W*H floats)."""
+    ctx = scene.ctx
+    cs = camera_struct(cam)
+    ctx.check(ctx.L.fm_proposal_features(ctx.h, scene.h, C.byref(cs), _ptr(start_depth)[0], _ptr(features)[0],
+                                         _ptr(t0)[0], stream))
+
+
+def proposal_intervals(scene: Scene, cam, params: MarchParams, start_depth, intervals, near_far=None, stream=None):
+    ctx = scene.ctx
+    cs = camera_struct(cam)
+    ps = params.cstruct()
+    ctx.check(ctx.L.fm_proposal_intervals(ctx.h, scene.h, C.byref(cs), C.byref(ps), _ptr(start_depth)[0],
+                                          _ptr(intervals)[0], _ptr(near_far)[0], stream))
+
+
+def judge(ctx: Context, depth_ref, depth_test, tol: float, stream=None) -> dict:
+    """Hit-mask mismatches and depth errors of depth_test against depth_ref (device buffers)."""
+    r = CJudge()
+    n = int(depth_ref.numel()) if hasattr(depth_ref, "numel") else int(depth_ref.size)
+    ctx.check(ctx.L.fm_judge(ctx.h, _ptr(depth_ref)[0], _ptr(depth_test)[0], n, float(tol), C.byref(r), stream))
+    return {k: (float(getattr(r, k)) if k in ("max_err", "tol") else int(getattr(r, k))) for k, _ in CJudge._fields_}
+
+
+class Trainer:
+    """FP32 trainer of the proposal MLP (forward, backward, Adam kernels)."""
+
+    def __init__(self, ctx: Context, seed: int = 0, init=None):
+        self.ctx = ctx
+        h = C.c_void_p()
+        ip = None
+        if init is not None:
+            self._init = np.ascontiguousarray(init, np.float32).reshape(-1)
+            ip = self._init.ctypes.data
+        ctx.check(ctx.L.fm_trainer_create(ctx.h, int(seed), ip, C.byref(h)))
+        self.h = h
+        ctx._trainers.add(self)
+
+    def step(self, features, targets, n: int, lr: float, tau_lo: float, tau_hi: float, want_loss: bool = False):
+        loss = C.c_float()
+        self.ctx.check(self.ctx.L.fm_trainer_step(self.h, _ptr(features)[0], _ptr(targets)[0], int(n), float(lr),
+                                                  float(tau_lo), float(tau_hi),
+                                                  C.byref(loss) if want_loss else None))
+        return float(loss.value) if want_loss else None
+
+    def predict(self, features, n: int, out):
+        self.ctx.check(self.ctx.L.fm_trainer_predict(self.h, _ptr(features)[0], int(n), _ptr(out)[0]))
+
+    def params(self) -> np.ndarray:
+        p = np.empty(FM_PROPOSAL_PARAMS, np.float32)
+        self.ctx.check(self.ctx.L.fm_trainer_params(self.h, p.ctypes.data))
+        return p
+
+    def close(self):
+        if getattr(self, "h", None):
+            if getattr(self.ctx, "h", None):
+                self.ctx.L.fm_trainer_destroy(self.h)
             self.h = None
 
     def __del__(self):

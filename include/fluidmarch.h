@@ -52,6 +52,13 @@ extern "C" {
 /* march flags */
 #define FM_MARCH_EXTERNAL_DEPTH 1 /* take ray-start depths from fm_frame_out.start_depth
                                      instead of splatting them (reference signature mode) */
+#define FM_MARCH_PROPOSAL 2       /* march only inside the intervals the context's learned
+                                     proposal (fm_set_proposal) predicts, restarting as the
+                                     full march where an interval holds no crossing */
+
+/* learned proposal: features per ray and MLP parameter count */
+#define FM_PROPOSAL_FEATURES 32
+#define FM_PROPOSAL_PARAMS 6402
 
 typedef struct fm_ctx fm_ctx;
 typedef struct fm_scene fm_scene;
@@ -119,6 +126,8 @@ typedef struct fm_march_stats {
     uint64_t tested;        /* particles actually tested: those of sub-cells within reach */
     uint64_t streamed;      /* particles a warp streamed for its lanes (shared candidate stream) */
     uint64_t deferred;      /* rays finished by the long-ray pass */
+    uint64_t proposed;      /* rays that started inside a proposed interval (FM_MARCH_PROPOSAL) */
+    uint64_t fallbacks;     /* of those, rays restarted as full marches */
 } fm_march_stats;
 
 /* ---- context ------------------------------------------------------------ */
@@ -279,6 +288,66 @@ int fm_batch_info_get(const fm_batch* batch, fm_batch_info* out);
 void fm_batch_destroy(fm_batch* batch);
 /* One-shot: create a batch, run it on `stream`, wait, destroy it. */
 int fm_march_batch(fm_ctx* ctx, const fm_view* views, int32_t n_views, void* stream);
+
+/* ---- learned hit-interval proposal -------------------------------------
+ * No counterpart in the reference.  A 3-layer MLP (width 64, GELU) maps the
+ * FM_PROPOSAL_FEATURES features of a ray (16 samples of a 64^3 occupancy grid
+ * along the ray, the 1/8-resolution splat depth, the direction, the start
+ * point in the scene box) to an interval (near, far), in support radii past
+ * the ray start.  With FM_MARCH_PROPOSAL the march evaluates only the samples
+ * of its own sample lattice inside [near - margin_lo, far + margin_hi] and
+ * restarts as the full march when that interval holds no crossing or its first
+ * sample is already inside: hit masks equal the full march's, a depth differs
+ * only where the fluid is crossed before near.  Inference runs on the BF16
+ * tensor cores with FP32 accumulation.
+ *
+ * Parameters: FM_PROPOSAL_PARAMS floats, W1[64][32], b1[64], W2[64][64],
+ * b2[64], W3[2][64], b3[2] (W[out][in]). */
+typedef struct fm_proposal fm_proposal;
+int fm_proposal_create(fm_ctx* ctx, const float* params, float margin_lo, float margin_hi, fm_proposal** out);
+void fm_proposal_destroy(fm_proposal* p);
+/* The proposal FM_MARCH_PROPOSAL uses on this context (NULL clears). */
+int fm_set_proposal(fm_ctx* ctx, fm_proposal* p);
+/* Features of every pixel's ray (training data), device buffers:
+ *   start_depth  W*H splat depths (as fm_march writes them)
+ *   features     W*H*FM_PROPOSAL_FEATURES floats (0 for pixels without a ray)
+ *   t0           W*H ray-start distances from the camera (may be NULL) */
+int fm_proposal_features(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, const float* start_depth,
+                         float* features, float* t0, void* stream);
+/* Intervals the march would use, device buffers: intervals = W*H pairs
+ * (first sample - 1, last sample) of the march's sample index, (0, -1) for a
+ * full march; near_far = W*H raw (near, far) outputs (may be NULL). */
+int fm_proposal_intervals(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, const fm_march_params* params,
+                          const float* start_depth, int32_t* intervals, float* near_far, void* stream);
+
+/* Judge: compare a march's per-pixel hit distances (fm_frame_out.depth, 0 =
+ * miss) with a reference march's, device buffers, synchronous. */
+typedef struct fm_judge_result {
+    uint64_t pixels;
+    uint64_t hits_ref;
+    uint64_t hits_test;
+    uint64_t mask_mismatch;  /* pixels hit in one and missed in the other */
+    uint64_t within_tol;     /* pixels hit in both with |depth difference| <= tol */
+    float max_err;           /* largest |depth difference| over pixels hit in both */
+    float tol;
+} fm_judge_result;
+int fm_judge(fm_ctx* ctx, const float* depth_ref, const float* depth_test, uint64_t n, float tol,
+             fm_judge_result* out, void* stream);
+
+/* Training of the proposal: FP32 forward, backward and Adam kernels.  Loss:
+ * pinball (quantile) loss of near at quantile tau_lo and of far at tau_hi
+ * against the first-hit distance (support radii past the ray start). */
+typedef struct fm_trainer fm_trainer;
+/* init NULL: seeded uniform initialisation (biases 0). */
+int fm_trainer_create(fm_ctx* ctx, uint64_t seed, const float* init, fm_trainer** out);
+void fm_trainer_destroy(fm_trainer* t);
+/* One Adam step on a batch of n rays (device buffers: n*FM_PROPOSAL_FEATURES
+ * features, n targets); loss (host, may be NULL) = mean loss before the step. */
+int fm_trainer_step(fm_trainer* t, const float* features, const float* targets, uint32_t n, float lr, float tau_lo,
+                    float tau_hi, float* loss);
+/* FP32 outputs (near, far) of the current parameters: out = n*2 floats (device). */
+int fm_trainer_predict(fm_trainer* t, const float* features, uint32_t n, float* out);
+int fm_trainer_params(fm_trainer* t, float* host_params);
 
 /* Library version (major * 10000 + minor * 100 + patch). */
 int fm_version(void);

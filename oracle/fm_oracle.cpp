@@ -352,9 +352,13 @@ struct MarchOut {
     double* rho;     // per pixel density at the reported hit point or null
 };
 
+// ivl (optional, 2 per pixel): a proposed interval (ks, kf) of the learned
+// march: start at sample ks of this ray's lattice (ks additions of the step),
+// evaluate samples ks+1 .. kf, and restart as the full march when the first of
+// them is already inside or none of them is (the GPU's FM_MARCH_PROPOSAL).
 template <typename T>
 void march_pixel(const Scene& s, const OrcCamera& cam, const OrcParams& P, const float* depth_in, int64_t idx,
-                 const MarchOut& o) {
+                 const MarchOut& o, const int32_t* ivl = nullptr) {
     const int W = cam.width, Hh = cam.height;
     const int px = int(idx % W), py = int(idx / W);
     Cubic<T> k(s.H);
@@ -373,8 +377,23 @@ void march_pixel(const Scene& s, const OrcCamera& cam, const OrcParams& P, const
         V3<T> p{wh[0] / wh[3], wh[1] / wh[3], wh[2] / wh[3]};
         V3<T> cam_pos{T(cam.position[0]), T(cam.position[1]), T(cam.position[2])};
         V3<T> step = mul(T(P.step), normalize(sub(p, cam_pos)));
+        const V3<T> p0 = p;
+        int ks = 0, kf = -1;
+        if (ivl) {
+            ks = ivl[2 * idx];
+            kf = ivl[2 * idx + 1];
+            if (!(ks >= 1 && ks < kf && kf <= P.max_steps)) { ks = 0; kf = -1; }
+        }
+    attempt:
+        p = p0;
+        int i0 = 0;
+        if (kf >= 0) {
+            for (int k = 0; k < ks; ++k) p = add(p, step);
+            i0 = ks;
+        }
         V3<T> prev = p;
-        for (int i = 0; i < P.max_steps; ++i) {
+        bool restart = false;
+        for (int i = i0; i < (kf >= 0 ? kf : P.max_steps); ++i) {
             p = add(p, step);
             if (P.skip_mode == 2 && s.ref_flag) {
                 if (std::is_same<T, float>::value) {
@@ -389,11 +408,18 @@ void march_pixel(const Scene& s, const OrcCamera& cam, const OrcParams& P, const
             if (outside_forever(s.g, p, step)) break;
             T rho = density(s, k, p, st);
             if (rho >= T(P.iso)) {
+                if (kf >= 0 && i == ks) { restart = true; break; }
                 hit = true;
                 hit_rho = rho;
                 break;
             }
             prev = p;
+        }
+        if (kf >= 0 && !hit) restart = true;
+        if (restart) {
+            kf = -1;
+            ks = 0;
+            goto attempt;
         }
         if (hit) {
             V3<T> lo = prev, hi = p;
@@ -628,10 +654,10 @@ void orc_splat(const float* xyz, int64_t n, int32_t stride, float R, const OrcCa
 // March the given pixels (or all when pixels == null) on `threads` threads
 // (<= 0: hardware_concurrency - 1, as RayMarcher.cpp:67).  precision 32 or 64.
 // sorted: cell-sorted xyz with stride 4; start: ncells + 1 offsets.
-int orc_march(const float* sorted, const uint32_t* start, const OrcGrid* g, float H, const uint8_t* ref_flag,
-              const OrcCamera* cam, const OrcParams* P, const float* depth_in, const int64_t* pixels, int64_t npix,
-              int32_t threads, int32_t precision, float* out_pos, float* out_nrm, float* out_depth, float* out_col,
-              int32_t* out_evals, int64_t* out_cand, double* out_rho) {
+int orc_march_ivl(const float* sorted, const uint32_t* start, const OrcGrid* g, float H, const uint8_t* ref_flag,
+                  const OrcCamera* cam, const OrcParams* P, const float* depth_in, const int64_t* pixels, int64_t npix,
+                  int32_t threads, int32_t precision, float* out_pos, float* out_nrm, float* out_depth,
+                  float* out_col, int32_t* out_evals, int64_t* out_cand, double* out_rho, const int32_t* ivl) {
     Scene s{sorted, start, *g, H, ref_flag};
     MarchOut o{out_pos, out_nrm, out_depth, out_col, out_evals, out_cand, out_rho};
     const int64_t total = pixels ? npix : int64_t(cam->width) * cam->height;
@@ -642,8 +668,8 @@ int orc_march(const float* sorted, const uint32_t* start, const OrcGrid* g, floa
             int64_t k = next.fetch_add(1);
             if (k >= total) break;
             int64_t idx = pixels ? pixels[k] : k;
-            if (precision == 64) march_pixel<double>(s, *cam, *P, depth_in, idx, o);
-            else march_pixel<float>(s, *cam, *P, depth_in, idx, o);
+            if (precision == 64) march_pixel<double>(s, *cam, *P, depth_in, idx, o, ivl);
+            else march_pixel<float>(s, *cam, *P, depth_in, idx, o, ivl);
         }
     };
     if (nt == 1) { worker(); return 0; }
@@ -651,6 +677,14 @@ int orc_march(const float* sorted, const uint32_t* start, const OrcGrid* g, floa
     for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
     for (auto& t : pool) t.join();
     return 0;
+}
+
+int orc_march(const float* sorted, const uint32_t* start, const OrcGrid* g, float H, const uint8_t* ref_flag,
+              const OrcCamera* cam, const OrcParams* P, const float* depth_in, const int64_t* pixels, int64_t npix,
+              int32_t threads, int32_t precision, float* out_pos, float* out_nrm, float* out_depth, float* out_col,
+              int32_t* out_evals, int64_t* out_cand, double* out_rho) {
+    return orc_march_ivl(sorted, start, g, H, ref_flag, cam, P, depth_in, pixels, npix, threads, precision, out_pos,
+                         out_nrm, out_depth, out_col, out_evals, out_cand, out_rho, nullptr);
 }
 
 // Density at arbitrary points (FP32 canonical order, or FP64).

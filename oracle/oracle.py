@@ -70,6 +70,7 @@ def lib():
         L.orc_march.argtypes = [_f32p, _u32p, C.POINTER(OrcGrid), C.c_float, C.c_void_p, C.POINTER(OrcCamera),
                                 C.POINTER(OrcParams), _f32p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32,
                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
+        L.orc_march_ivl.argtypes = L.orc_march.argtypes + [C.c_void_p]
         L.orc_density.argtypes = [_f32p, _u32p, C.POINTER(OrcGrid), C.c_float, _f32p, C.c_int64, C.c_int32,
                                   np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")]
         _lib = L
@@ -164,8 +165,12 @@ def splat(xyz: np.ndarray, support: float, cam) -> np.ndarray:
 
 
 def march(frame: Frame, cam, iso: float, step: float, max_steps: int, bisect: int, depth: np.ndarray,
-          skip_mode: int = 0, pixels=None, threads: int = 0, precision: int = 32, want_colour: bool = True):
-    """March all pixels (or the given pixel indices).  Returns a dict of arrays."""
+          skip_mode: int = 0, pixels=None, threads: int = 0, precision: int = 32, want_colour: bool = True,
+          intervals=None):
+    """March all pixels (or the given pixel indices).  Returns a dict of arrays.
+
+    intervals: optional (W*H, 2) int32 proposed intervals (ks, kf) of the
+    learned march (fm_oracle.cpp march_pixel)."""
     L = lib()
     npx = cam.width * cam.height
     P = OrcParams(float(iso), float(step), int(max_steps), int(bisect), int(skip_mode), 0)
@@ -183,11 +188,13 @@ def march(frame: Frame, cam, iso: float, step: float, max_steps: int, bisect: in
     if pixels is not None:
         pix = np.ascontiguousarray(pixels, np.int64)
         npix = pix.shape[0]
-    L.orc_march(np.ascontiguousarray(frame.sorted.reshape(-1)), frame.start, C.byref(frame.grid), frame.support,
-                flags.ctypes.data if flags is not None else None, C.byref(cs), C.byref(P),
-                np.ascontiguousarray(depth, np.float32), pix.ctypes.data if pix is not None else None, npix,
-                int(threads), int(precision), pos.ctypes.data, nrm.ctypes.data, dep.ctypes.data,
-                col.ctypes.data if want_colour else None, evals.ctypes.data, cand.ctypes.data, rho.ctypes.data)
+    ivl = None if intervals is None else np.ascontiguousarray(intervals, np.int32).reshape(npx, 2)
+    L.orc_march_ivl(np.ascontiguousarray(frame.sorted.reshape(-1)), frame.start, C.byref(frame.grid), frame.support,
+                    flags.ctypes.data if flags is not None else None, C.byref(cs), C.byref(P),
+                    np.ascontiguousarray(depth, np.float32), pix.ctypes.data if pix is not None else None, npix,
+                    int(threads), int(precision), pos.ctypes.data, nrm.ctypes.data, dep.ctypes.data,
+                    col.ctypes.data if want_colour else None, evals.ctypes.data, cand.ctypes.data, rho.ctypes.data,
+                    ivl.ctypes.data if ivl is not None else None)
     return {"position": pos, "normal": nrm, "depth": dep, "colour": col, "evals": evals, "candidates": cand,
             "rho": rho}
 

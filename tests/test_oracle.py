@@ -212,3 +212,36 @@ def test_fp64_twin_close_to_fp32():
     both = ha & hb
     ext = float(np.max(sc.xyz.max(0) - sc.xyz.min(0)))
     assert np.quantile(np.abs(a["depth"][both] - b["depth"][both]), 0.999) < 1e-4 * ext
+
+
+# ---- the learned march's interval semantics --------------------------------
+
+def test_interval_march_semantics():
+    """A proposed interval (ks, kf) never changes a hit mask; a hit only moves
+    deeper, and only when the plain march crosses at or before sample ks."""
+    sc = scenes.small_scene(seed=33, n=6000, width=96, height=72, max_steps=160)
+    cam = sc.cameras[0]
+    fr = O.build_frame(sc.xyz, sc.support)
+    depth = O.splat(sc.xyz, sc.support, cam)
+    npx = cam.width * cam.height
+    plain = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 0, depth)
+    rng = np.random.default_rng(4)
+    ks = rng.integers(1, 12, npx).astype(np.int32)
+    kf = (ks + rng.integers(1, 30, npx)).astype(np.int32)
+    ivl = np.stack([ks, kf], axis=1)
+    got = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 0, depth, intervals=ivl)
+    hit_p, hit_g = plain["depth"] > 0, got["depth"] > 0
+    assert np.array_equal(hit_p, hit_g)
+    # with bisection 0 and skipping off, a hit ray's evaluations = its hit sample number
+    h = plain["evals"]
+    later = hit_p & (h > ks)
+    assert np.array_equal(got["position"][later], plain["position"][later])
+    early = hit_p & (h <= ks)
+    same = np.all(got["position"] == plain["position"], axis=1)
+    moved = early & ~same
+    assert np.all(got["depth"][moved] > plain["depth"][moved])
+    assert later.sum() > 100 and early.sum() > 20
+    # intervals that are not usable (ks < 1, kf <= ks, kf > max_steps) mean the full march
+    bad = np.stack([np.zeros(npx, np.int32), np.full(npx, 5, np.int32)], axis=1)
+    got0 = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 0, depth, intervals=bad)
+    assert np.array_equal(got0["position"], plain["position"])
