@@ -419,6 +419,8 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     o.start_depth = z;
     o.ivl = nullptr;
     if (p->flags & FM_MARCH_PROPOSAL) {
+        if (p->skip_mode == FM_SKIP_REFERENCE)
+            return set_err(ctx, FM_ERR_INVALID, "FM_MARCH_PROPOSAL marches the plain sample lattice: skip mode must be off or exact");
         if (!ctx->proposal) return set_err(ctx, FM_ERR_INVALID, "FM_MARCH_PROPOSAL needs a proposal (fm_set_proposal)");
         if (!grow(ctx->prop_ivl, npx * sizeof(int2))) return set_err(ctx, FM_ERR_OOM, "interval buffer allocation failed");
         rc = launch_propose(ctx, sm, cam, p, ctx->proposal, z, (int2*)ctx->prop_ivl.p, nullptr, st);

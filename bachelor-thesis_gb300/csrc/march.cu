@@ -273,6 +273,14 @@ __device__ __forceinline__ void write_pixel(const MarchArgs& a, uint64_t idx, in
 
 enum Phase : int { kMarch = 0, kBisect = 1, kNormal = 2, kDone = 3, kRestart = 4 };
 
+// LEARNED march modes.  kInterval: samples ks+1 .. kf of the plain lattice.
+// When that finds no crossing, or its first sample is already inside, the ray
+// goes back to its start and marches the prefix 1 .. ks (kPrefixClear /
+// kPrefixInside); after the prefix it resumes exactly where the plain march
+// would be, without evaluating any sample twice: after kf (samples ks+1 .. kf
+// are known outside) or with the crossing at ks+1 (known inside).
+enum Mode : int { kWhole = 0, kInterval = 1, kPrefixInside = 2, kPrefixClear = 3 };
+
 struct Ray {
     int phase;
     int i, b;             // march steps taken, bisection steps taken
@@ -280,19 +288,21 @@ struct Ray {
     float q[3];           // previous sample (march) / outside end (bisection)
     float s[3];           // step
     float e[3];           // pending evaluation point
-    int ks, kf;           // proposed interval: samples ks+1 .. kf (kf < 0: full march)
+    int ks, kf;           // proposed interval: samples ks+1 .. kf
+    int mode;             // Mode (LEARNED)
 };
 
 // Apply the density at the pending point (RayMarcher.cpp:327: hit when rho >= iso).
 // LEARNED: a ray marching a proposed interval whose first sample is already
-// inside cannot tell whether the crossing lies before the interval: it restarts
-// as a full march.
+// inside cannot tell whether the crossing lies before the interval: it goes
+// back for the prefix.
 template <bool LEARNED>
 __device__ __forceinline__ void apply(const MarchArgs& a, Ray& r, float rho) {
     const bool inside = rho >= a.iso;
     if (r.phase == kMarch) {
-        if (LEARNED && inside && r.kf >= 0 && r.i == r.ks + 1) {
+        if (LEARNED && inside && r.mode == kInterval && r.i == r.ks + 1) {
             r.phase = kRestart;
+            r.mode = kPrefixInside;
         } else if (inside) {
             r.b = 0;
             r.phase = a.bisect > 0 ? kBisect : kNormal;
@@ -312,12 +322,41 @@ __device__ __forceinline__ void apply(const MarchArgs& a, Ray& r, float rho) {
 // Returns true with r.e / L set when a sum is needed, false when the ray left
 // the march or bisection phases.
 // LEARNED: a ray in a proposed interval that reaches the interval's end (or
-// leaves the grid) without a crossing restarts as a full march (kRestart).
+// leaves the grid) without a crossing goes back for the prefix (kRestart); a
+// ray that finished its prefix resumes the plain march (see Mode).
 template <bool STATS, bool LEARNED>
 __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc& acc, bool cnt) {
     for (;;) {
         if (r.phase == kMarch) {
-            if (LEARNED && r.kf >= 0 && r.i >= r.kf) { r.phase = kRestart; return false; }
+            if (LEARNED && r.mode == kInterval && r.i >= r.kf) {
+                r.phase = kRestart;
+                r.mode = kPrefixClear;
+                return false;
+            }
+            if (LEARNED && r.mode >= kPrefixInside && r.i >= r.ks) {
+                if (r.mode == kPrefixInside) {
+                    // sample ks+1 is inside: it is the plain march's first crossing
+                    r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
+                    r.p[0] = r.p[0] + r.s[0];
+                    r.p[1] = r.p[1] + r.s[1];
+                    r.p[2] = r.p[2] + r.s[2];
+                    r.i = r.ks + 1;
+                    r.mode = kWhole;
+                    r.b = 0;
+                    r.phase = a.bisect > 0 ? kBisect : kNormal;
+                    continue;
+                }
+                // samples ks+1 .. kf are outside: go on after kf
+                for (int k = r.ks; k < r.kf; ++k) {
+                    r.p[0] = r.p[0] + r.s[0];
+                    r.p[1] = r.p[1] + r.s[1];
+                    r.p[2] = r.p[2] + r.s[2];
+                }
+                r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
+                r.i = r.kf;
+                r.mode = kWhole;
+                continue;
+            }
             if (r.i >= a.max_steps) { r.phase = kDone; return false; }
             r.p[0] = r.p[0] + r.s[0];
             r.p[1] = r.p[1] + r.s[1];
@@ -326,7 +365,12 @@ __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc&
             if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2], a.status);
             if (!locate(a.g, r.p[0], r.p[1], r.p[2], L)) {
                 if (outside_forever(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2])) {
-                    r.phase = (LEARNED && r.kf >= 0) ? kRestart : kDone;
+                    // every later sample has density 0; an interval still needs its prefix
+                    r.phase = kDone;
+                    if (LEARNED && r.mode == kInterval) {
+                        r.phase = kRestart;
+                        r.mode = kPrefixClear;
+                    }
                     return false;
                 }
                 if (STATS && cnt) acc.evals++;
@@ -548,12 +592,13 @@ __device__ __forceinline__ void ray_setup(const MarchArgs& a, int px, int py, fl
     s[2] = a.step * (dz * inv);
 }
 
-// Long-ray queue entry: 4 float4 = {pixel, phase, i, b}, {p, ks}, {q, kf}, {e, view}
+// Long-ray queue entry: 4 float4 = {pixel, phase | mode << 8, i, b}, {p, ks}, {q, kf}, {e, view}
 // (e: the pending evaluation point).  The step is recomputed from the pixel.
 __device__ __forceinline__ void push_long(const MarchArgs& a, uint32_t slot, uint32_t idx, uint32_t view,
                                           const Ray& r) {
     float4* d = a.longq + 4ull * slot;
-    d[0] = make_float4(__uint_as_float(idx), __int_as_float(r.phase), __int_as_float(r.i), __int_as_float(r.b));
+    d[0] = make_float4(__uint_as_float(idx), __int_as_float(r.phase | (r.mode << 8)), __int_as_float(r.i),
+                       __int_as_float(r.b));
     d[1] = make_float4(r.p[0], r.p[1], r.p[2], __int_as_float(r.ks));
     d[2] = make_float4(r.q[0], r.q[1], r.q[2], __int_as_float(r.kf));
     d[3] = make_float4(r.e[0], r.e[1], r.e[2], __uint_as_float(view));
@@ -606,14 +651,13 @@ __device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, 
 
 // One 32-pixel tile of view `a` (lane = ray).  `view` tags the rays this
 // warp defers to the long-ray queue.
-// LEARNED: restart a ray as a full march from its start (the proposal missed).
+// LEARNED: send a ray back to its start for the prefix of its interval.
 template <bool STATS>
 __device__ __forceinline__ void restart(const MarchArgs& a, Ray& r, int px, int py, uint64_t idx, Acc& acc, bool cnt) {
     ray_setup(a, px, py, a.zbuf[idx], r.p, r.s);
     r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
     r.i = 0;
     r.b = 0;
-    r.kf = -1;
     r.phase = kMarch;
     if (STATS && cnt) acc.fallbacks++;
 }
@@ -646,6 +690,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, ui
     r.i = r.b = 0;
     r.ks = 0;
     r.kf = -1;
+    r.mode = kWhole;
     if (valid && z != 1.0f) {
         ray_setup(a, px, py, z, r.p, r.s);
         if (LEARNED) {
@@ -661,6 +706,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, ui
                 r.i = iv.x;
                 r.ks = iv.x;
                 r.kf = iv.y;
+                r.mode = kInterval;
                 if (STATS) acc.proposed++;
             }
         }
@@ -821,7 +867,8 @@ __global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a, cons
         const float4 w0 = d[0], w1 = d[1], w2 = d[2], w3 = d[3];
         const uint32_t idx = __float_as_uint(w0.x);
         Ray r;
-        r.phase = __float_as_int(w0.y);
+        r.phase = __float_as_int(w0.y) & 0xff;
+        r.mode = __float_as_int(w0.y) >> 8;
         r.i = __float_as_int(w0.z);
         r.b = __float_as_int(w0.w);
         r.p[0] = w1.x; r.p[1] = w1.y; r.p[2] = w1.z;

@@ -46,6 +46,7 @@ struct fm_proposal {
     void* d_weights = nullptr;  // BF16 W1 | W2 | W3 in k_propose's shared-memory image
     float* d_bias = nullptr;    // b1 | b2 | b3
     float margin_lo = 0.0f, margin_hi = 0.0f;
+    float min_near = 0.0f;  // intervals starting closer than this (support radii) are not used
 };
 
 struct fm_trainer {
@@ -232,14 +233,15 @@ __device__ __forceinline__ float gelu_grad(float x) {
 struct IvlArgs {
     float H, step;
     int max_steps;
-    float margin_lo, margin_hi;
+    float margin_lo, margin_hi, min_near;
 };
 
 // (near, far) in support radii -> march samples (ks, kf): evaluate ks+1 .. kf.
 // (0, -1): no usable interval, the ray runs the full march.
 __device__ __forceinline__ int2 to_interval(const IvlArgs& v, float y0, float y1) {
     const float near = y0 - v.margin_lo, far = y1 + v.margin_hi;
-    if (!(near == near) || !(far == far) || !(far > near) || !(far > 0.0f)) return make_int2(0, -1);
+    if (!(near == near) || !(far == far) || !(far > near) || !(far > 0.0f) || !(near >= v.min_near))
+        return make_int2(0, -1);
     const float s0 = fmaxf(near, 0.0f) * v.H / v.step, s1 = far * v.H / v.step;
     if (!(s0 < 1.0e6f)) return make_int2(0, -1);
     const int ks = (int)floorf(s0);
@@ -740,6 +742,7 @@ int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_marc
     a.v.max_steps = p->max_steps;
     a.v.margin_lo = pr->margin_lo;
     a.v.margin_hi = pr->margin_hi;
+    a.v.min_near = pr->min_near;
     a.weights = (const uint8_t*)pr->d_weights;
     a.bias = pr->d_bias;
     a.ivl = ivl;
@@ -782,14 +785,16 @@ void init_params(uint64_t seed, float* P) {
 
 extern "C" {
 
-int fm_proposal_create(fm_ctx* ctx, const float* params, float margin_lo, float margin_hi, fm_proposal** out) {
+int fm_proposal_create(fm_ctx* ctx, const float* params, float margin_lo, float margin_hi, float min_near,
+                       fm_proposal** out) {
     if (!ctx) return FM_ERR_INVALID;
     if (!out || !params) return set_err(ctx, FM_ERR_INVALID, "parameters or output handle pointer are NULL");
     *out = nullptr;
     for (int i = 0; i < kProposalParams; ++i)
         if (!std::isfinite(params[i])) return set_err(ctx, FM_ERR_INVALID, "proposal parameters are not finite");
-    if (!std::isfinite(margin_lo) || !std::isfinite(margin_hi) || margin_lo < 0.0f || margin_hi < 0.0f)
-        return set_err(ctx, FM_ERR_INVALID, "margins must be finite and >= 0");
+    if (!std::isfinite(margin_lo) || !std::isfinite(margin_hi) || margin_lo < 0.0f || margin_hi < 0.0f ||
+        !std::isfinite(min_near) || min_near < 0.0f)
+        return set_err(ctx, FM_ERR_INVALID, "margins and min_near must be finite and >= 0");
     std::vector<uint8_t> img(kWeightBytes, 0);
     auto put = [&](uint32_t base, int n, int K, int rows, const float* W) {
         for (int r = 0; r < rows; ++r)
@@ -812,6 +817,7 @@ int fm_proposal_create(fm_ctx* ctx, const float* params, float margin_lo, float 
     p->ctx = ctx;
     p->margin_lo = margin_lo;
     p->margin_hi = margin_hi;
+    p->min_near = min_near;
     if (cudaMalloc(&p->d_weights, kWeightBytes) != cudaSuccess ||
         cudaMalloc(&p->d_bias, bias.size() * sizeof(float)) != cudaSuccess ||
         cudaMemcpy(p->d_weights, img.data(), kWeightBytes, cudaMemcpyHostToDevice) != cudaSuccess ||

@@ -147,7 +147,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_batch_destroy.argtypes = [vp]
     L.fm_batch_destroy.restype = None
     L.fm_march_batch.argtypes = [vp, C.POINTER(CView), C.c_int32, vp]
-    L.fm_proposal_create.argtypes = [vp, vp, C.c_float, C.c_float, C.POINTER(vp)]
+    L.fm_proposal_create.argtypes = [vp, vp, C.c_float, C.c_float, C.c_float, C.POINTER(vp)]
     L.fm_proposal_destroy.argtypes = [vp]
     L.fm_proposal_destroy.restype = None
     L.fm_set_proposal.argtypes = [vp, vp]
@@ -452,13 +452,14 @@ class Batch:
 class Proposal:
     """Learned hit-interval proposal (MLP parameters on the device)."""
 
-    def __init__(self, ctx: Context, params, margin_lo: float = 0.0, margin_hi: float = 0.0):
+    def __init__(self, ctx: Context, params, margin_lo: float = 0.0, margin_hi: float = 0.0, min_near: float = 0.0):
         self.ctx = ctx
         p = np.ascontiguousarray(params, np.float32).reshape(-1)
         if p.size != FM_PROPOSAL_PARAMS:
             raise ValueError(f"expected {FM_PROPOSAL_PARAMS} parameters, got {p.size}")
         h = C.c_void_p()
-        ctx.check(ctx.L.fm_proposal_create(ctx.h, p.ctypes.data, float(margin_lo), float(margin_hi), C.byref(h)))
+        ctx.check(ctx.L.fm_proposal_create(ctx.h, p.ctypes.data, float(margin_lo), float(margin_hi), float(min_near),
+                                           C.byref(h)))
         self.h = h
         self.params = p
         ctx._proposals.add(self)

@@ -20,6 +20,12 @@ e2e    the same frame through the C ABI with pinned HOST buffers: particle
 --impl reference times the CPU marcher (the oracle port of the reference's
        loop, bisection 0, skipping off, all host threads but one as
        RayMarcher.cpp:67 does) on a bounded random pixel sample per step.
+learned  the same frame with the learned hit-interval proposal
+       (FM_MARCH_PROPOSAL, weights fluidmarch/proposal_sloshing.npz), timed the
+       same way, and its depth error judged against the plain march of the
+       same frame (hit masks, |depth difference| <= 1e-4 x scene extent).
+batch  64 scenes of the sloshing family (50k..2M particles, 1-4 views each
+       at 640x480 / 1280x720 / 1920x1080) in one graph launch per frame.
 """
 
 from __future__ import annotations
@@ -56,6 +62,9 @@ def parse():
     ap.add_argument("--width", type=int, default=1920)
     ap.add_argument("--height", type=int, default=1080)
     ap.add_argument("--profile", action="store_true", help="short plain run of --steps frames for ncu")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal comparison")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-scene measurement")
+    ap.add_argument("--autotune", action="store_true", help="autotune the batch's work split first")
     return ap.parse_args()
 
 
@@ -219,6 +228,117 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, plain_ms):
+    """The learned-proposal march of the same frame, timed like the plain one, judged against it."""
+    from fluidmarch import proposal as PR
+
+    params, meta = PR.load()
+    margin_lo, margin_hi, min_near = 0.5, 0.5, 8.0
+    prop = fm.Proposal(ctx, params, margin_lo, margin_hi, min_near)
+    fm.set_proposal(ctx, prop)
+    npx = cam.width * cam.height
+    dev = out["depth"].device
+    lo = {k: torch.empty_like(v) for k, v in out.items()}
+    P_l = fm.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, skip, external_depth=True, proposal=True)
+
+    def frame():
+        fm.splat_depth(scene, cam, lo["start_depth"])
+        fm.march(scene, cam, P_l, lo["position"], lo["normal"], lo["depth"], lo["colour"], lo["start_depth"])
+
+    ctx.set_stats(True)
+    frame()
+    ctx.sync()
+    st = ctx.stats()
+    ctx.set_stats(False)
+    for _ in range(args.warmup):
+        frame()
+    ctx.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    with torch.cuda.stream(ext):
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(ext)
+            frame()
+            e1.record(ext)
+        ext.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
+    extent = float((sc.xyz.max(0) - sc.xyz.min(0)).max())
+    tol = 1e-4 * extent
+    j = fm.judge(ctx, out["depth"], lo["depth"], tol)
+    # the plain march without empty-space skipping, for reference (a few frames)
+    P_off = fm.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, fm.FM_SKIP_OFF, external_depth=True)
+    off = []
+    for k in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(ext):
+            flush.zero_()
+            e0.record(ext)
+            fm.splat_depth(scene, cam, lo["start_depth"])
+            fm.march(scene, cam, P_off, lo["position"], lo["normal"], lo["depth"], lo["colour"], lo["start_depth"])
+            e1.record(ext)
+            ext.synchronize()
+        if k > 0:
+            off.append(e0.elapsed_time(e1))
+    fm.set_proposal(ctx, None)
+    prop.close()
+    return {"rays_per_s": npx / (ms / 1e3), "frames_per_s": 1e3 / ms, "ms_per_frame": ms,
+            "vs_plain": plain_ms / ms, "plain_ms_per_frame": plain_ms,
+            "plain_skip_off_ms_per_frame": float(np.mean(off)), "vs_plain_skip_off": float(np.mean(off)) / ms,
+            "depth_tol": tol, "judge": j, "hits_within_tol": j["within_tol"] / max(1, j["hits_ref"]),
+            "mask_identical": j["mask_mismatch"] == 0,
+            "margins_support_radii": [margin_lo, margin_hi], "min_near_support_radii": min_near,
+            "counters": {k: st[k] for k in ("evals", "proposed", "fallbacks", "deferred")},
+            "proposal": {"weights": "fluidmarch/proposal_sloshing.npz", "train_scenes": meta.get("train_scenes"),
+                         "heldout_scenes": meta.get("heldout_scenes"), "heldout": meta.get("heldout")}}
+
+
+def run_batch(args, fm, torch, ctx, ext, dev):
+    """The batched configuration: 64 sloshing-family scenes, 1-4 views each, one graph launch per frame."""
+    from fluidmarch import scenes
+
+    t0 = time.perf_counter()
+    bs = scenes.batch_scenes()
+    gen_s = time.perf_counter() - t0
+    views, keep = [], []
+    for sc in bs:
+        s = fm.Scene(ctx, sc.xyz, sc.support)
+        keep.append(s)
+        p = fm.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, fm.FM_SKIP_EXACT)
+        for cam in sc.cameras:
+            npx = cam.width * cam.height
+            o = {"position": torch.empty((npx, 4), device=dev), "normal": torch.empty((npx, 4), device=dev),
+                 "depth": torch.empty(npx, device=dev), "colour": torch.empty((npx, 4), device=dev)}
+            keep.append(o)
+            views.append(fm.View(s, cam, p, **o))
+    torch.cuda.synchronize()
+    b = fm.Batch(ctx, views, tile_config=dict(tile_width=8, tiles_per_claim=1, defer_iters=64))
+    tuned = None
+    if args.autotune:
+        best, ms = b.autotune(reps=1)
+        tuned = {"best": best, "ms": ms}
+    b.run()
+    ctx.sync()
+    steps = max(3, min(args.steps, 5))
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(ext):
+        for e0, e1 in ev:
+            e0.record(ext)
+            b.run(ext.cuda_stream)
+            e1.record(ext)
+        ext.synchronize()
+    ms = sum(a.elapsed_time(c) for a, c in ev) / steps
+    info = b.info()
+    b.close()
+    for s in keep:
+        if hasattr(s, "close"):
+            s.close()
+    return {"workload": "64 sloshing-family scenes, 50k..2M particles, 1-4 views at 640x480/1280x720/1920x1080",
+            "views": info["n_views"], "pixels": info["pixels"], "particles": info["particles"],
+            "graph_nodes": info["graph_nodes"], "config": info["config"], "autotune": tuned,
+            "ms_per_frame": ms, "rays_per_s": info["pixels"] / (ms / 1e3), "frames_per_s": info["n_views"] / (ms / 1e3),
+            "steps": steps, "scene_generation_s": gen_s}
+
+
 def run_ours(args):
     import torch
 
@@ -331,6 +451,13 @@ def run_ours(args):
         e2e_s = float(t.item())
     e2e_value = npx * args.steps * world / e2e_s
 
+    learned = None
+    if rank == 0 and not args.no_learned:
+        learned = run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, total_ms / args.steps)
+    batch = None
+    if rank == 0 and not args.no_batch:
+        batch = run_batch(args, fm, torch, ctx, ext, dev)
+
     if rank == 0:
         peak, peak_kind = measured_peaks()
         alg_bytes = 16 * st["candidates"] + 36 * npx
@@ -352,9 +479,14 @@ def run_ours(args):
                                  "served from L1/L2, so frac > 1 means on-chip reuse"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * sc.n,
                     "d2h_bytes_per_step": npx * (16 + 16 + 4 + 16)},
-            "gpu_launches": 3 * args.steps,  # fill + splat + march per frame
+            # per frame: fill, sampled splat, tile maxima, cull, survivor splat, march, long rays
+            "gpu_launches": 7 * args.steps,
             "clocks": clk.summary(),
         }
+        if learned:
+            line["learned"] = learned
+        if batch:
+            line["batch"] = batch
         if world == 1 and not args.no_cpu_baseline:
             import oracle as O
 

@@ -52,9 +52,10 @@ extern "C" {
 /* march flags */
 #define FM_MARCH_EXTERNAL_DEPTH 1 /* take ray-start depths from fm_frame_out.start_depth
                                      instead of splatting them (reference signature mode) */
-#define FM_MARCH_PROPOSAL 2       /* march only inside the intervals the context's learned
-                                     proposal (fm_set_proposal) predicts, restarting as the
-                                     full march where an interval holds no crossing */
+#define FM_MARCH_PROPOSAL 2       /* march first inside the interval the context's learned
+                                     proposal (fm_set_proposal) predicts; where it holds no
+                                     crossing, march the rest of the ray (skip mode off or
+                                     exact only) */
 
 /* learned proposal: features per ray and MLP parameter count */
 #define FM_PROPOSAL_FEATURES 32
@@ -127,7 +128,7 @@ typedef struct fm_march_stats {
     uint64_t streamed;      /* particles a warp streamed for its lanes (shared candidate stream) */
     uint64_t deferred;      /* rays finished by the long-ray pass */
     uint64_t proposed;      /* rays that started inside a proposed interval (FM_MARCH_PROPOSAL) */
-    uint64_t fallbacks;     /* of those, rays restarted as full marches */
+    uint64_t fallbacks;     /* of those, rays that went back for the samples before the interval */
 } fm_march_stats;
 
 /* ---- context ------------------------------------------------------------ */
@@ -304,7 +305,10 @@ int fm_march_batch(fm_ctx* ctx, const fm_view* views, int32_t n_views, void* str
  * Parameters: FM_PROPOSAL_PARAMS floats, W1[64][32], b1[64], W2[64][64],
  * b2[64], W3[2][64], b3[2] (W[out][in]). */
 typedef struct fm_proposal fm_proposal;
-int fm_proposal_create(fm_ctx* ctx, const float* params, float margin_lo, float margin_hi, fm_proposal** out);
+/* margin_lo / margin_hi widen every interval (support radii); rays whose
+ * widened near is below min_near (support radii) run the full march. */
+int fm_proposal_create(fm_ctx* ctx, const float* params, float margin_lo, float margin_hi, float min_near,
+                       fm_proposal** out);
 void fm_proposal_destroy(fm_proposal* p);
 /* The proposal FM_MARCH_PROPOSAL uses on this context (NULL clears). */
 int fm_set_proposal(fm_ctx* ctx, fm_proposal* p);

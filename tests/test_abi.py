@@ -91,3 +91,14 @@ def test_camera_matrices_are_consistent():
     # y is flipped (Camera3D.cpp:9): a point above the target has negative NDC y
     u = P @ V @ np.array([0.5, 0.5, 0.5, 1.0])
     assert u[1] / u[3] < 0
+
+
+def test_committed_proposal_weights():
+    """The trained proposal ships with its training record (no GPU needed to read it)."""
+    from fluidmarch import proposal as PR
+
+    params, meta = PR.load()
+    assert params.dtype == np.float32 and params.size == 6402
+    assert np.all(np.isfinite(params))
+    assert meta["train_scenes"] >= 2000 and meta["heldout_scenes"] >= 200
+    assert meta["heldout"]["covered"] > 0.9
