@@ -349,6 +349,27 @@ int fm_splat_depth(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, float* 
     return FM_OK;
 }
 
+int fm_density(fm_ctx* ctx, const fm_scene* s, const float* xyz, uint64_t n, uint32_t stride, float* out, int mem,
+               void* stream) {
+    if (!ctx) return FM_ERR_INVALID;
+    if (!s || (n && (!xyz || !out))) return set_err(ctx, FM_ERR_INVALID, "NULL argument");
+    if (stride < 3) return set_err(ctx, FM_ERR_INVALID, "stride must be >= 3 floats");
+    if (mem != FM_MEM_HOST && mem != FM_MEM_DEVICE) return set_err(ctx, FM_ERR_INVALID, "unknown memory kind");
+    if (n == 0) return FM_OK;
+    cudaSetDevice(ctx->device);
+    cudaStream_t st = pick(ctx, stream);
+    if (mem == FM_MEM_DEVICE) return launch_density(ctx, s, xyz, n, stride, out, st);
+    const size_t in_bytes = (size_t)n * stride * sizeof(float), out_bytes = (size_t)n * sizeof(float);
+    if (!grow(ctx->stage[0], in_bytes) || !grow(ctx->stage[1], out_bytes))
+        return set_err(ctx, FM_ERR_OOM, "staging allocation failed");
+    FM_CUDA(ctx, cudaMemcpyAsync(ctx->stage[0].p, xyz, in_bytes, cudaMemcpyHostToDevice, st));
+    int rc = launch_density(ctx, s, (const float*)ctx->stage[0].p, n, stride, (float*)ctx->stage[1].p, st);
+    if (rc) return rc;
+    FM_CUDA(ctx, cudaMemcpyAsync(out, ctx->stage[1].p, out_bytes, cudaMemcpyDeviceToHost, st));
+    FM_CUDA(ctx, cudaStreamSynchronize(st));
+    return FM_OK;
+}
+
 int fm_set_stats(fm_ctx* ctx, int enable) {
     if (!ctx) return FM_ERR_INVALID;
     ctx->stats_enabled = enable ? 1 : 0;

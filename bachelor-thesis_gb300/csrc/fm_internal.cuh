@@ -345,6 +345,9 @@ int launch_march_kernels(fm_ctx* ctx, const MarchArgs& launch, const MarchArgs* 
                          int nviews, cudaStream_t st);
 int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
                  const MarchOutDev& o, cudaStream_t st);
+// Density at n points (xyz at a stride of `stride` floats), device pointers.
+int launch_density(fm_ctx* ctx, const fm_scene* s, const float* d_xyz, uint64_t n, uint32_t stride, float* d_out,
+                   cudaStream_t st);
 
 // Argument checks shared by the single and batched entry points (api.cu).
 int check_camera(fm_ctx* ctx, const fm_camera* c, bool need_splat);

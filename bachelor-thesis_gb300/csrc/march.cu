@@ -970,6 +970,48 @@ int launch_march_kernels(fm_ctx* ctx, const MarchArgs& a, const MarchArgs* d_vie
     }
 }
 
+namespace {
+
+// DiskRenderer::ComputeDensity (DiskRenderer.cpp:180-193): density at
+// arbitrary points, thread per point, the 27 cells in canonical order (9 rows
+// of 3 contiguous cells).  Bit-identical to the march's sums at the same point.
+__global__ void k_density_probe(const GridDev g, const KernelDev k, const float* __restrict__ xyz, uint64_t n,
+                                uint32_t stride, float* __restrict__ out) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float px = xyz[i * stride], py = xyz[i * stride + 1], pz = xyz[i * stride + 2];
+    float rho = 0.0f;
+    int c[3];
+    if (sample_cell(g, px, py, pz, c[0], c[1], c[2])) {
+        const int x0 = max(c[0] - 1, 0), x1 = min(c[0] + 1, g.dims[0] - 1);
+        for (int z = max(c[2] - 1, 0); z <= min(c[2] + 1, g.dims[2] - 1); ++z)
+            for (int y = max(c[1] - 1, 0); y <= min(c[1] + 1, g.dims[1] - 1); ++y) {
+                if (x0 > x1) continue;
+                const uint32_t row = ((uint32_t)z * (uint32_t)g.dims[1] + (uint32_t)y) * (uint32_t)g.dims[0];
+                const uint32_t b = __ldg(g.sub + 8u * (row + (uint32_t)x0));
+                const uint32_t e = __ldg(g.sub + 8u * (row + (uint32_t)x1) + 8u);
+                for (uint32_t j = b; j < e; ++j) {
+                    const float4 q = __ldg(g.pts + j);
+                    const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+                    const float d = dot3(rx, ry, rz, rx, ry, rz);
+                    if (d < k.h2) rho = rho + w_in(k, d);
+                }
+            }
+    }
+    out[i] = rho;
+}
+
+}  // namespace
+
+int launch_density(fm_ctx* ctx, const fm_scene* s, const float* d_xyz, uint64_t n, uint32_t stride, float* d_out,
+                   cudaStream_t st) {
+    if (n == 0) return FM_OK;
+    k_density_probe<<<(unsigned)((n + 127) / 128), 128, 0, st>>>(grid_dev(s), make_kernel(s->support), d_xyz, n,
+                                                                 stride, d_out);
+    FM_CUDA(ctx, cudaGetLastError());
+    return FM_OK;
+}
+
 int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
                  const MarchOutDev& o, cudaStream_t st) {
     MarchArgs a = march_view_args(s, cam, p, o, ctx->tile);

@@ -42,7 +42,7 @@ EXPORTS = [
     "fm_batch_autotune", "fm_batch_info_get", "fm_batch_destroy", "fm_march_batch",
     "fm_proposal_create", "fm_proposal_destroy", "fm_set_proposal", "fm_proposal_features", "fm_proposal_intervals",
     "fm_judge", "fm_trainer_create", "fm_trainer_destroy", "fm_trainer_step", "fm_trainer_predict",
-    "fm_trainer_params",
+    "fm_trainer_params", "fm_density",
 ]
 
 
@@ -136,6 +136,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_march_stats_get.argtypes = [vp, C.POINTER(CMarchStats)]
     L.fm_grid_build_noalloc.argtypes = [vp, C.c_uint64, C.c_uint32, C.c_float, vp, vp, vp, vp, C.c_uint64,
                                         C.POINTER(CGridInfo), vp]
+    L.fm_density.argtypes = [vp, vp, vp, C.c_uint64, C.c_uint32, vp, C.c_int, vp]
     L.fm_set_tile_config.argtypes = [vp, C.POINTER(CTileConfig)]
     L.fm_get_tile_config.argtypes = [vp, C.POINTER(CTileConfig)]
     L.fm_batch_create.argtypes = [vp, C.POINTER(CView), C.c_int32, C.POINTER(CTileConfig), C.POINTER(vp)]
@@ -324,6 +325,20 @@ class MarchParams:
         flags = (FM_MARCH_EXTERNAL_DEPTH if self.external_depth else 0) | (FM_MARCH_PROPOSAL if self.proposal else 0)
         return CMarchParams(float(self.iso), float(self.step), int(self.max_steps), int(self.bisect),
                             int(self.skip_mode), flags)
+
+
+def density(scene: Scene, xyz, out=None, stride: int = 3, stream=None):
+    """SPH density at points (DiskRenderer::ComputeDensity); numpy in -> numpy out unless ``out`` is given."""
+    ctx = scene.ctx
+    n = int(xyz.shape[0])
+    if out is None:
+        out = np.empty(n, np.float32)
+    p, mem = _ptr(xyz)
+    q, mem2 = _ptr(out)
+    if mem != mem2:
+        raise ValueError("points and output must both be host or both be device buffers")
+    ctx.check(ctx.L.fm_density(ctx.h, scene.h, p, n, int(stride), q, mem, stream))
+    return out
 
 
 def splat_depth(scene: Scene, cam, out=None, stream=None):

@@ -220,6 +220,14 @@ int fm_splat_depth(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, flo
 int fm_march(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, const fm_march_params* params,
              const fm_frame_out* out, int mem, void* stream);
 
+/* DiskRenderer::ComputeDensity (DiskRenderer.cpp:180-193): SPH density at n
+ * points (xyz at a stride of `stride` floats, >= 3) into out[n], summed over
+ * the 27 grid cells around each point in the march's order (bit-identical to
+ * the march's density at the same point).  Host buffers: synchronous; device
+ * buffers: asynchronous on `stream`. */
+int fm_density(fm_ctx* ctx, const fm_scene* scene, const float* xyz, uint64_t n, uint32_t stride, float* out, int mem,
+               void* stream);
+
 /* Counters of the last fm_march / fm_batch_run on this context (enable with
  * fm_set_stats(ctx, 1); counting costs time, keep it off when timing). */
 int fm_set_stats(fm_ctx* ctx, int enable);

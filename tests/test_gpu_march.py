@@ -275,3 +275,18 @@ def test_march_rejects_bad_params(fmlib, ctx):
     c2.width = 0
     with pytest.raises(fmlib.FmError):
         fmlib.march(s, c2, fmlib.MarchParams(sc.iso, sc.step, 10), position=out)
+
+
+def test_density_probe_bitwise(fmlib, ctx):
+    """fm_density (DiskRenderer::ComputeDensity) equals the oracle's FP32 density bit for bit."""
+    sc = scenes.small_scene(seed=12, n=20000, width=64, height=48)
+    s = fmlib.Scene(ctx, sc.xyz, sc.support)
+    rng = np.random.default_rng(0)
+    pts = np.concatenate([sc.xyz[rng.choice(sc.n, 3000, replace=False)] + rng.normal(0, sc.support / 3, (3000, 3)),
+                          rng.uniform(-0.5, 1.5, (1000, 3))]).astype(np.float32)
+    got = fmlib.density(s, pts)
+    fr = O.build_frame(sc.xyz, sc.support)
+    ref = O.density(fr, pts).astype(np.float32)
+    assert np.array_equal(bits(got), bits(ref))
+    assert (got > 0).sum() > 2500
+    s.close()
