@@ -75,10 +75,13 @@ int check_config(fm_ctx* ctx, const fm_tile_config* c, TileConfig* out) {
     if (c->defer_iters < 1 || c->defer_iters > 4096)
         return set_err(ctx, FM_ERR_INVALID, "defer_iters must be in [1, 4096]");
     if (c->long_queue < 0) return set_err(ctx, FM_ERR_INVALID, "long_queue must be >= 0");
+    if (c->defer_lanes < 0 || c->defer_lanes > 31) return set_err(ctx, FM_ERR_INVALID, "defer_lanes must be in [0, 31]");
+    if (c->reserved != 0) return set_err(ctx, FM_ERR_INVALID, "reserved must be 0");
     out->tw_log2 = lg;
     out->claim = c->tiles_per_claim;
     out->cap = c->defer_iters;
     out->qlimit = (uint32_t)c->long_queue;
+    out->lanes = c->defer_lanes;
     return FM_OK;
 }
 
@@ -88,6 +91,7 @@ fm_tile_config to_public(const TileConfig& c) {
     o.tiles_per_claim = c.claim;
     o.defer_iters = c.cap;
     o.long_queue = (int32_t)c.qlimit;
+    o.defer_lanes = c.lanes;
     return o;
 }
 
@@ -354,12 +358,13 @@ int fm_batch_autotune(fm_batch* b, const fm_tile_config* cands, int32_t n_cands,
         }
     } else {
         for (int lg : {2, 3, 4, 5})
-            for (int cap : {16, 32, 64}) {
+            for (int cap : {16, 20, 24, 32, 64}) {
                 TileConfig t;
                 t.tw_log2 = lg;
                 t.claim = 1;
                 t.cap = cap;
                 t.qlimit = b->cfg.qlimit;
+                t.lanes = b->cfg.lanes;
                 list.push_back(t);
             }
     }

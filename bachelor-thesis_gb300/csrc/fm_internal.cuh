@@ -161,7 +161,8 @@ struct DevBuf {
 struct TileConfig {
     int tw_log2 = 3;  // 8x4 pixels
     int claim = 1;
-    int cap = 32;
+    int cap = 20;
+    int lanes = 2;        // a warp defers its rays once at most this many are active
     uint32_t qlimit = 0;  // long-ray queue entries (0: long_queue_entries of the pixels)
 };
 
@@ -325,6 +326,7 @@ struct MarchArgs {
     float4* longq;         // 4 float4 per entry
     unsigned int q_cap;
     int cap;               // shared-stream iterations per tile before the rays left are deferred
+    int defer_lanes;       // ... or once at most this many rays of the warp are active
     unsigned long long* stats;
     unsigned int* status;
 };

@@ -728,7 +728,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, ui
         bool need = advance<STATS, LEARNED>(a, r, L, px, py, idx, acc, true);
         uint32_t act = __ballot_sync(kFull, need);
         if (!act) break;
-        if (!keep && (__popc(act) <= 2 || iters >= a.cap)) {
+        if (!keep && (__popc(act) <= a.defer_lanes || iters >= a.cap)) {
             // Few rays left, or rays that march long (grazing the surface): hand
             // them to the long-ray pass, where each gets a whole warp, instead of
             // keeping this warp busy while the rest of the grid idles.  Rays that
@@ -915,6 +915,7 @@ MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_marc
     a.tw_log2 = cfg.tw_log2;
     a.claim = cfg.claim;
     a.cap = cfg.cap;
+    a.defer_lanes = cfg.lanes;
     const int tw = 1 << cfg.tw_log2, th = 32 >> cfg.tw_log2;
     a.tiles_x = (cam->width + tw - 1) / tw;
     a.ntiles = a.tiles_x * ((cam->height + th - 1) / th);

@@ -246,9 +246,12 @@ typedef struct fm_tile_config {
                                 rays it still has go to the long-ray pass: 1..4096 */
     int32_t long_queue;      /* entries of the long-ray queue; 0 = pixels / 8 + 65536.
                                 Rays that find it full stay with their warp. */
+    int32_t defer_lanes;     /* a warp also defers its rays once at most this many are
+                                still active: 0..31 */
+    int32_t reserved;        /* 0 */
 } fm_tile_config;
 
-/* Work split of fm_march on this context (default 8, 1, 32, 0). */
+/* Work split of fm_march on this context (default 8, 1, 20, 0, 2). */
 int fm_set_tile_config(fm_ctx* ctx, const fm_tile_config* cfg);
 int fm_get_tile_config(const fm_ctx* ctx, fm_tile_config* out);
 
