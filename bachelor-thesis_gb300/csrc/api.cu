@@ -153,6 +153,10 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->d_stats);
     cudaFree(ctx->d_work);
     cudaFree(ctx->longq.p);
+    cudaFree(ctx->longq2.p);
+    cudaFree(ctx->rg_keys.p);
+    cudaFree(ctx->rg_tmp.p);
+    cudaFree(ctx->rg_order.p);
     cudaFree(ctx->hiz.p);
     cudaFree(ctx->splat_list.p);
     cudaFree(ctx->prop_ivl.p);
@@ -393,6 +397,7 @@ int fm_march_stats_get(fm_ctx* ctx, fm_march_stats* out) {
     out->deferred = h[8];
     out->proposed = h[9];
     out->fallbacks = h[10];
+    out->regrouped = h[11];
     return FM_OK;
 }
 

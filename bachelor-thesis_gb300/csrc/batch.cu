@@ -30,6 +30,7 @@ struct fm_batch {
     fm::TileConfig cfg;
     // device buffers
     fm::DevBuf margs, tile_pfx, sviews, pfx64, pfx_tiles, depth, hiz, list, counters, longq;
+    fm::DevBuf longq2, rg_keys, rg_tmp, rg_order;  // regrouped second pass
     uint32_t q_cap = 0;
     fm::MarchArgs launch{};  // launch-wide march arguments
     fm::SplatBatch sb{};
@@ -57,8 +58,8 @@ void free_batch(fm_batch* b) {
     // a graph of this batch may still run on any stream
     cudaDeviceSynchronize();
     drop_graph(b);
-    DevBuf* bufs[] = {&b->margs, &b->tile_pfx, &b->sviews, &b->pfx64, &b->pfx_tiles,
-                      &b->depth, &b->hiz,      &b->list,   &b->counters, &b->longq};
+    DevBuf* bufs[] = {&b->margs, &b->tile_pfx, &b->sviews,  &b->pfx64,  &b->pfx_tiles, &b->depth, &b->hiz,
+                      &b->list,  &b->counters, &b->longq,   &b->longq2, &b->rg_keys,   &b->rg_tmp, &b->rg_order};
     for (DevBuf* d : bufs) cudaFree(d->p);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     delete b;
@@ -76,12 +77,14 @@ int check_config(fm_ctx* ctx, const fm_tile_config* c, TileConfig* out) {
         return set_err(ctx, FM_ERR_INVALID, "defer_iters must be in [1, 4096]");
     if (c->long_queue < 0) return set_err(ctx, FM_ERR_INVALID, "long_queue must be >= 0");
     if (c->defer_lanes < 0 || c->defer_lanes > 31) return set_err(ctx, FM_ERR_INVALID, "defer_lanes must be in [0, 31]");
-    if (c->reserved != 0) return set_err(ctx, FM_ERR_INVALID, "reserved must be 0");
+    if (c->regroup_iters < 0 || c->regroup_iters > 4096)
+        return set_err(ctx, FM_ERR_INVALID, "regroup_iters must be in [0, 4096]");
     out->tw_log2 = lg;
     out->claim = c->tiles_per_claim;
     out->cap = c->defer_iters;
     out->qlimit = (uint32_t)c->long_queue;
     out->lanes = c->defer_lanes;
+    out->cap2 = c->regroup_iters;
     return FM_OK;
 }
 
@@ -92,6 +95,7 @@ fm_tile_config to_public(const TileConfig& c) {
     o.defer_iters = c.cap;
     o.long_queue = (int32_t)c.qlimit;
     o.defer_lanes = c.lanes;
+    o.regroup_iters = c.cap2;
     return o;
 }
 
@@ -143,6 +147,11 @@ int prepare(fm_batch* b) {
         !grow_buf(b->list, 4ull * std::max<uint64_t>(pn[n], 1)) || !grow_buf(b->counters, 128) ||
         !grow_buf(b->longq, 64ull * entries))
         return set_err(ctx, FM_ERR_OOM, "batch buffer allocation failed");
+    const bool regroup = b->cfg.cap2 > 0;
+    const uint64_t nkeys = (uint64_t)tp[n] + 1;
+    if (regroup && (!grow_buf(b->longq2, 64ull * entries) || !grow_buf(b->rg_order, 4ull * entries) ||
+                    !grow_buf(b->rg_keys, 4ull * nkeys) || !grow_buf(b->rg_tmp, 4ull * scan_words(nkeys))))
+        return set_err(ctx, FM_ERR_OOM, "batch buffer allocation failed");
     b->q_cap = (uint32_t)entries;
     unsigned int* cnt = (unsigned int*)b->counters.p;
     // march arguments: per view, with the launch-wide fields in every block
@@ -166,6 +175,15 @@ int prepare(fm_batch* b) {
         a.q_cap = b->q_cap;
         a.status = ctx->d_status;
         a.stats = nullptr;
+        a.grp_counter = cnt + 4;
+        a.q2_tail = cnt + 5;
+        a.q2_head = cnt + 6;
+        if (regroup) {
+            a.longq2 = (float4*)b->longq2.p;
+            a.order = (uint32_t*)b->rg_order.p;
+            a.keys = (uint32_t*)b->rg_keys.p;
+            a.scan_tmp = (uint32_t*)b->rg_tmp.p;
+        }
         ma[i] = a;
         SplatView s{};
         s.a = splat_args(v.scene, &v.camera);
@@ -207,7 +225,7 @@ int prepare(fm_batch* b) {
 // The frame's work on `st`: counter reset, depth pass, march.
 int enqueue(fm_batch* b, cudaStream_t st, bool stats) {
     fm_ctx* ctx = b->ctx;
-    FM_CUDA(ctx, cudaMemsetAsync(b->counters.p, 0, 4 * sizeof(unsigned int), st));
+    FM_CUDA(ctx, cudaMemsetAsync(b->counters.p, 0, 8 * sizeof(unsigned int), st));
     int rc = launch_splat_batch(ctx, b->sb, st);
     if (rc) return rc;
     MarchArgs a = b->launch;
@@ -365,6 +383,7 @@ int fm_batch_autotune(fm_batch* b, const fm_tile_config* cands, int32_t n_cands,
                 t.cap = cap;
                 t.qlimit = b->cfg.qlimit;
                 t.lanes = b->cfg.lanes;
+                t.cap2 = b->cfg.cap2;
                 list.push_back(t);
             }
     }

@@ -163,6 +163,7 @@ struct TileConfig {
     int claim = 1;
     int cap = 20;
     int lanes = 2;        // a warp defers its rays once at most this many are active
+    int cap2 = 0;         // iterations of the regrouped second pass (0: no second pass)
     uint32_t qlimit = 0;  // long-ray queue entries (0: long_queue_entries of the pixels)
 };
 
@@ -191,6 +192,8 @@ struct fm_ctx {
     // long-ray queue of the march (64 B per entry, long_queue_entries(pixels)
     // entries for the largest view so far)
     fm::DevBuf longq;
+    // regrouped second pass: second queue, sort counters, scan temporaries, order
+    fm::DevBuf longq2, rg_keys, rg_tmp, rg_order;
     // splat depth tile maxima (4 B per 8x8 tile) and the list of particles that
     // survive the tile test; renders of one context on different streams must
     // not overlap
@@ -327,6 +330,15 @@ struct MarchArgs {
     unsigned int q_cap;
     int cap;               // shared-stream iterations per tile before the rays left are deferred
     int defer_lanes;       // ... or once at most this many rays of the warp are active
+    // regrouped second pass (launch-wide; order == null: no second pass)
+    int cap2;              // its iterations before the rays left go to the warp-per-ray pass
+    uint32_t* keys;        // ntiles + 1 counters of the counting sort
+    uint32_t* scan_tmp;    // scan temporaries
+    uint32_t* order;       // queue entries sorted by first-pass tile
+    float4* longq2;        // second queue (q_cap entries)
+    unsigned int* q2_tail;
+    unsigned int* q2_head;
+    unsigned int* grp_counter;
     unsigned long long* stats;
     unsigned int* status;
 };
@@ -355,6 +367,9 @@ int launch_density(fm_ctx* ctx, const fm_scene* s, const float* d_xyz, uint64_t 
 int check_camera(fm_ctx* ctx, const fm_camera* c, bool need_splat);
 int check_params(fm_ctx* ctx, const fm_march_params* p);
 bool grow_buf(DevBuf& b, size_t bytes);
+// Exclusive prefix sum of n words (in may equal out); tmp: scan_words(n) words (grid_build.cu).
+uint64_t scan_words(uint64_t n);
+void scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* tmp, cudaStream_t st);
 // Free the batches a context still holds (batch.cu).
 void destroy_batches(fm_ctx* ctx);
 

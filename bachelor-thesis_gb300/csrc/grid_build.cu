@@ -400,6 +400,12 @@ GridDev grid_dev(const fm_scene* s) {
     return g;
 }
 
+uint64_t scan_words(uint64_t n) { return scan_tmp_words(n); }
+
+void scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* tmp, cudaStream_t st) {
+    exclusive_scan(in, out, n, tmp, st);
+}
+
 int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     cudaStream_t st = ctx->stream;
     const uint64_t n = s->n;

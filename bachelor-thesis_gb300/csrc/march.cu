@@ -53,7 +53,7 @@ namespace {
 
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kThreads = 256;  // 8 warps per block
-constexpr int kStats = 11;  // fm_march_stats field order
+constexpr int kStats = 12;  // fm_march_stats field order
 
 struct Acc {
     uint32_t evals = 0;
@@ -64,6 +64,7 @@ struct Acc {
     uint32_t skipped = 0;
     uint32_t proposed = 0;   // rays that started inside a proposed interval
     uint32_t fallbacks = 0;  // of those, rays restarted as full marches
+    uint32_t regrouped = 0;  // rays the first pass handed to the regrouped second pass
     bool bad = false;  // an index guard fired (reported through the status word, bit 2)
 };
 
@@ -139,10 +140,31 @@ __device__ __forceinline__ void for_ranges_warp(const GridDev& g, const Loc& L, 
     }
 }
 
-// Density at p, identical on every lane (canonical order).  cnt: this lane counts the work.
+// Add the 32 lanes' terms to acc in lane order, identically on every lane:
+// the terms go through this warp's 32 words of shared memory.  Lanes without a
+// term contribute +0, and acc + 0 = acc exactly (acc starts at +0 and never
+// becomes -0), so the sum equals adding only the real terms in order.
+__device__ __forceinline__ float ordered_sum32(float* s, int lane, float w, float acc) {
+    __syncwarp();
+    s[lane] = w;
+    __syncwarp();
+    const float4* s4 = reinterpret_cast<const float4*>(s);
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        const float4 v = s4[i];
+        acc = acc + v.x;
+        acc = acc + v.y;
+        acc = acc + v.z;
+        acc = acc + v.w;
+    }
+    return acc;
+}
+
+// Density at p, identical on every lane (canonical order).  cnt: this lane
+// counts the work; red: this warp's 32 words of shared memory.
 template <bool STATS>
 __device__ __forceinline__ float density_warp(const GridDev& g, const KernelDev& k, const Loc& L, float px, float py,
-                                              float pz, float T, int lane, Acc& acc, bool cnt) {
+                                              float pz, float T, int lane, Acc& acc, bool cnt, float* red) {
     if (STATS && cnt) acc.evals++;
     float rho = 0.0f;
     for_ranges_warp<STATS>(g, L, T, lane, acc, cnt, [&](uint32_t b, uint32_t e) {
@@ -155,12 +177,7 @@ __device__ __forceinline__ float density_warp(const GridDev& g, const KernelDev&
                 const float d2 = dot3(rx, ry, rz, rx, ry, rz);
                 if (d2 < k.h2) w = w_in(k, d2);
             }
-            uint32_t bm = __ballot_sync(kFull, w != 0.0f);
-            while (bm) {
-                const int src = __ffs(bm) - 1;
-                bm &= bm - 1u;
-                rho = rho + __shfl_sync(kFull, w, src);
-            }
+            rho = ordered_sum32(red, lane, w, rho);
         }
     });
     return rho;
@@ -594,9 +611,14 @@ __device__ __forceinline__ void ray_setup(const MarchArgs& a, int px, int py, fl
 
 // Long-ray queue entry: 4 float4 = {pixel, phase | mode << 8, i, b}, {p, ks}, {q, kf}, {e, view}
 // (e: the pending evaluation point).  The step is recomputed from the pixel.
-__device__ __forceinline__ void push_long(const MarchArgs& a, uint32_t slot, uint32_t idx, uint32_t view,
-                                          const Ray& r) {
-    float4* d = a.longq + 4ull * slot;
+struct Queue {
+    float4* buf;          // 4 float4 per entry
+    unsigned int* tail;   // entries reserved
+    unsigned int cap;
+};
+
+__device__ __forceinline__ void push_long(const Queue& q, uint32_t slot, uint32_t idx, uint32_t view, const Ray& r) {
+    float4* d = q.buf + 4ull * slot;
     d[0] = make_float4(__uint_as_float(idx), __int_as_float(r.phase | (r.mode << 8)), __int_as_float(r.i),
                        __int_as_float(r.b));
     d[1] = make_float4(r.p[0], r.p[1], r.p[2], __int_as_float(r.ks));
@@ -618,7 +640,7 @@ __device__ __forceinline__ int find_view(const uint32_t* __restrict__ pfx, int n
 // Sum of gradW at p (canonical order) with the whole warp, identical on every lane.
 template <bool STATS>
 __device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, float px, float py, float pz, float T,
-                                          int lane, Acc& acc, bool cnt, float& gx, float& gy, float& gz) {
+                                          int lane, Acc& acc, bool cnt, float* red, float& gx, float& gy, float& gz) {
     gx = gy = gz = 0.0f;
     Loc L;
     if (STATS && cnt) acc.evals++;
@@ -627,23 +649,27 @@ __device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, 
         for (uint32_t j0 = b; j0 < e; j0 += 32) {
             const uint32_t j = j0 + (uint32_t)lane;
             float tx = 0.0f, ty = 0.0f, tz = 0.0f;
-            bool in = false;
             if (j < e) {
                 const float4 q = __ldg(g.pts + j);
                 const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
                 const float q2 = dot3(rx, ry, rz, rx, ry, rz);
-                if (q2 < k.h2 && q2 > 0.0f) {
-                    in = true;
-                    gradw_term(k, rx, ry, rz, q2, tx, ty, tz);
-                }
+                if (q2 < k.h2 && q2 > 0.0f) gradw_term(k, rx, ry, rz, q2, tx, ty, tz);
             }
-            uint32_t bm = __ballot_sync(kFull, in);
-            while (bm) {
-                const int src = __ffs(bm) - 1;
-                bm &= bm - 1u;
-                gx = gx + __shfl_sync(kFull, tx, src);
-                gy = gy + __shfl_sync(kFull, ty, src);
-                gz = gz + __shfl_sync(kFull, tz, src);
+            // in lane order, as ordered_sum32 (components never become -0)
+            __syncwarp();
+            red[lane] = tx;
+            red[32 + lane] = ty;
+            red[64 + lane] = tz;
+            __syncwarp();
+#pragma unroll
+            for (int i = 0; i < 32; i += 4) {
+                const float4 vx = *reinterpret_cast<const float4*>(red + i);
+                const float4 vy = *reinterpret_cast<const float4*>(red + 32 + i);
+                const float4 vz = *reinterpret_cast<const float4*>(red + 64 + i);
+                gx = gx + vx.x; gy = gy + vy.x; gz = gz + vz.x;
+                gx = gx + vx.y; gy = gy + vy.y; gz = gz + vz.y;
+                gx = gx + vx.z; gy = gy + vy.z; gz = gz + vz.z;
+                gx = gx + vx.w; gy = gy + vy.w; gz = gz + vz.w;
             }
         }
     });
@@ -675,9 +701,87 @@ __device__ __forceinline__ bool advance(const MarchArgs& a, Ray& r, Loc& L, int 
     return need;
 }
 
+// The lanes-are-rays loop: every iteration each active lane advances its ray
+// to its next density sum, and the warp computes all sums through one shared
+// candidate stream.  `pending`: the lane starts with a prepared evaluation
+// point (a ray resumed from a queue).  After `cap` iterations, or once at most
+// a.defer_lanes rays are left, the remaining rays go to queue q (rays that find
+// it full stay).  Returns true when this lane's ray was queued.
 template <bool STATS, bool LEARNED>
-__device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, uint32_t view, int lane, Acc& acc,
-                                           uint64_t& rays, uint64_t& started_n, uint64_t& hits) {
+__device__ __forceinline__ bool run_lanes(const MarchArgs& a, const Queue& q, Ray& r, Loc& L, bool pending, int px,
+                                          int py, uint64_t idx, uint32_t view, int cap, bool to_regroup, int lane,
+                                          Acc& acc) {
+    int iters = 0;
+    bool deferred = false, keep = false;
+    for (;;) {
+        bool need;
+        if (pending) {
+            pending = false;
+            need = locate(a.g, r.e[0], r.e[1], r.e[2], L);
+            if (!need) {  // a prepared point is always inside the evaluation range; be safe anyway
+                apply<LEARNED>(a, r, 0.0f);
+                need = advance<STATS, LEARNED>(a, r, L, px, py, idx, acc, true);
+            }
+        } else {
+            need = advance<STATS, LEARNED>(a, r, L, px, py, idx, acc, true);
+        }
+        uint32_t act = __ballot_sync(kFull, need);
+        if (!act) break;
+        if (!keep && (__popc(act) <= a.defer_lanes || iters >= cap)) {
+            // Few rays left, or rays that march long (grazing the surface): hand
+            // them on instead of keeping this warp busy with a sparse, scattered
+            // set of rays.  Rays that find the queue full stay here, and the
+            // warp stops deferring.
+            const uint32_t base = (lane == 0) ? atomicAdd(q.tail, (unsigned)__popc(act)) : 0u;
+            const uint32_t slot = __shfl_sync(kFull, base, 0) + __popc(act & ((1u << lane) - 1u));
+            if (need && slot < q.cap) {
+                push_long(q, slot, (uint32_t)idx, view, r);
+                deferred = true;
+                need = false;
+                r.phase = kDone;
+                if (STATS) {
+                    if (to_regroup) acc.regrouped++;
+                    else acc.deferred++;
+                }
+            }
+            act = __ballot_sync(kFull, need);
+            if (!act) break;
+            keep = true;
+        }
+        const float rho = union_density<STATS>(a, need, L, r.e, acc);
+        if (need) apply<LEARNED>(a, r, rho);
+        ++iters;
+    }
+    return deferred;
+}
+
+// Normals of the lanes' hit rays (shared stream), then their pixels.
+template <bool STATS>
+__device__ __forceinline__ void finish_lanes(const MarchArgs& a, const Ray& r, bool live, uint64_t idx, int px, int py,
+                                             Acc& acc, uint64_t& hits) {
+    const bool hit = live && r.phase == kNormal;
+    Loc Lh;
+    Lh.c[0] = Lh.c[1] = Lh.c[2] = 0;
+    Lh.u[0] = Lh.u[1] = Lh.u[2] = 0.0f;
+    const bool gn = hit && locate(a.g, r.p[0], r.p[1], r.p[2], Lh);
+    if (STATS && hit && !gn) acc.evals++;
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    if (__any_sync(kFull, gn)) union_grad<STATS>(a, gn, Lh, r.p, acc, gx, gy, gz);
+    float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+    if (hit) {
+        const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+        n0 = gx * gi;
+        n1 = gy * gi;
+        n2 = gz * gi;
+        if (STATS) hits++;
+    }
+    if (live) write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
+}
+
+template <bool STATS, bool LEARNED>
+__device__ __forceinline__ void march_tile(const MarchArgs& a, const Queue& q, bool to_regroup, unsigned tile,
+                                           uint32_t view, int lane, Acc& acc, uint64_t& rays, uint64_t& started_n,
+                                           uint64_t& hits) {
     const int tw = 1 << a.tw_log2;
     const int tx = (int)(tile % (unsigned)a.tiles_x), ty = (int)(tile / (unsigned)a.tiles_x);
     const int px = tx * tw + (lane & (tw - 1));
@@ -722,53 +826,25 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, unsigned tile, ui
     Loc L;
     L.c[0] = L.c[1] = L.c[2] = 0;
     L.u[0] = L.u[1] = L.u[2] = 0.0f;
-    int iters = 0;
-    bool deferred = false, keep = false;
-    for (;;) {
-        bool need = advance<STATS, LEARNED>(a, r, L, px, py, idx, acc, true);
-        uint32_t act = __ballot_sync(kFull, need);
-        if (!act) break;
-        if (!keep && (__popc(act) <= a.defer_lanes || iters >= a.cap)) {
-            // Few rays left, or rays that march long (grazing the surface): hand
-            // them to the long-ray pass, where each gets a whole warp, instead of
-            // keeping this warp busy while the rest of the grid idles.  Rays that
-            // find the queue full stay here, and the warp stops deferring.
-            const uint32_t base = (lane == 0) ? atomicAdd(a.q_tail, (unsigned)__popc(act)) : 0u;
-            const uint32_t slot = __shfl_sync(kFull, base, 0) + __popc(act & ((1u << lane) - 1u));
-            if (need && slot < a.q_cap) {
-                push_long(a, slot, (uint32_t)idx, view, r);
-                deferred = true;
-                need = false;
-                r.phase = kDone;
-                if (STATS) acc.deferred++;
-            }
-            act = __ballot_sync(kFull, need);
-            if (!act) break;
-            keep = true;
-        }
-        const float rho = union_density<STATS>(a, need, L, r.e, acc);
-        if (need) apply<LEARNED>(a, r, rho);
-        ++iters;
-    }
-    // normals of the hit rays (all in phase kNormal), then outputs; deferred
-    // rays are finished (and written) by the long-ray pass
-    const bool hit = !deferred && r.phase == kNormal;
-    Loc Lh;
-    Lh.c[0] = Lh.c[1] = Lh.c[2] = 0;
-    Lh.u[0] = Lh.u[1] = Lh.u[2] = 0.0f;
-    const bool gn = hit && locate(a.g, r.p[0], r.p[1], r.p[2], Lh);
-    if (STATS && hit && !gn) acc.evals++;
-    float gx = 0.f, gy = 0.f, gz = 0.f;
-    if (__any_sync(kFull, gn)) union_grad<STATS>(a, gn, Lh, r.p, acc, gx, gy, gz);
-    float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-    if (hit) {
-        const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
-        n0 = gx * gi;
-        n1 = gy * gi;
-        n2 = gz * gi;
-        if (STATS) hits++;
-    }
-    if (valid && !deferred) write_pixel(a, idx, px, py, hit, r.p[0], r.p[1], r.p[2], n0, n1, n2);
+    const bool deferred = run_lanes<STATS, LEARNED>(a, q, r, L, false, px, py, idx, view, a.cap, to_regroup, lane, acc);
+    // deferred rays are finished (and written) by a later pass
+    finish_lanes<STATS>(a, r, valid && !deferred, idx, px, py, acc, hits);
+}
+
+// Ray state of a queue entry (the step comes from the pixel: ray_setup).
+__device__ __forceinline__ void load_entry(const float4* __restrict__ d, Ray& r, uint32_t& idx, uint32_t& view) {
+    const float4 w0 = d[0], w1 = d[1], w2 = d[2], w3 = d[3];
+    idx = __float_as_uint(w0.x);
+    r.phase = __float_as_int(w0.y) & 0xff;
+    r.mode = __float_as_int(w0.y) >> 8;
+    r.i = __float_as_int(w0.z);
+    r.b = __float_as_int(w0.w);
+    r.p[0] = w1.x; r.p[1] = w1.y; r.p[2] = w1.z;
+    r.q[0] = w2.x; r.q[1] = w2.y; r.q[2] = w2.z;
+    r.e[0] = w3.x; r.e[1] = w3.y; r.e[2] = w3.z;
+    r.ks = __float_as_int(w1.w);
+    r.kf = __float_as_int(w2.w);
+    view = __float_as_uint(w3.w);
 }
 
 __device__ __forceinline__ void flush_stats(const MarchArgs& a, int lane, const Acc& acc, uint64_t rays,
@@ -777,7 +853,7 @@ __device__ __forceinline__ void flush_stats(const MarchArgs& a, int lane, const 
                                     (unsigned long long)acc.cand, (unsigned long long)acc.skipped,
                                     (unsigned long long)acc.tested, (unsigned long long)acc.streamed,
                                     (unsigned long long)acc.deferred, (unsigned long long)acc.proposed,
-                                    (unsigned long long)acc.fallbacks};
+                                    (unsigned long long)acc.fallbacks, (unsigned long long)acc.regrouped};
 #pragma unroll
     for (int j = 0; j < kStats; ++j) {
         unsigned long long x = v[j];
@@ -799,6 +875,8 @@ __global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a, const 
     Acc acc;
     uint64_t rays = 0, started_n = 0, hits = 0;
     const unsigned total = (unsigned)a.ntiles, claim = (unsigned)a.claim;
+    const Queue q{a.longq, a.q_tail, a.q_cap};
+    const bool to_regroup = a.order != nullptr;
     for (;;) {
         unsigned t0 = 0;
         if (lane == 0) t0 = atomicAdd(a.tile_counter, claim);
@@ -808,10 +886,10 @@ __global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a, const 
         for (unsigned t = t0; t < t1; ++t) {
             if (BATCH) {
                 const int v = find_view(tile_pfx, nviews, t);
-                march_tile<STATS, LEARNED>(views[v], t - __ldg(tile_pfx + v), (uint32_t)v, lane, acc, rays,
-                                           started_n, hits);
+                march_tile<STATS, LEARNED>(views[v], q, to_regroup, t - __ldg(tile_pfx + v), (uint32_t)v, lane, acc,
+                                           rays, started_n, hits);
             } else {
-                march_tile<STATS, LEARNED>(a, t, 0u, lane, acc, rays, started_n, hits);
+                march_tile<STATS, LEARNED>(a, q, to_regroup, t, 0u, lane, acc, rays, started_n, hits);
             }
         }
     }
@@ -819,10 +897,107 @@ __global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a, const 
     if (STATS) flush_stats(a, lane, acc, rays, started_n, hits, true);
 }
 
+// ---- regrouped second pass --------------------------------------------------------
+//
+// The rays the first pass handed on are sorted by the first-pass tile of their
+// pixel (a counting sort: tiles are the keys, so rays of neighbouring tiles
+// end up next to each other), then marched again 32 to a warp with the same
+// shared-stream loop: full warps of rays from the same part of the image
+// instead of the few scattered rays each first-pass warp had left.  What this
+// pass hands on goes to the warp-per-ray pass.
+
+template <bool BATCH>
+__device__ __forceinline__ uint32_t queue_key(const MarchArgs& a, const MarchArgs* __restrict__ views,
+                                              const uint32_t* __restrict__ tile_pfx, const float4* __restrict__ d) {
+    const float4 w0 = d[0], w3 = d[3];
+    const uint32_t idx = __float_as_uint(w0.x);
+    uint32_t base = 0;
+    int W = a.W, tiles_x = a.tiles_x, lg = a.tw_log2;
+    if (BATCH) {
+        const uint32_t v = __float_as_uint(w3.w);
+        base = __ldg(tile_pfx + v);
+        W = views[v].W;
+        tiles_x = views[v].tiles_x;
+    }
+    const uint32_t px = idx % (uint32_t)W, py = idx / (uint32_t)W;
+    return base + (py / (uint32_t)(32 >> lg)) * (uint32_t)tiles_x + (px >> lg);
+}
+
+template <bool BATCH>
+__global__ void k_queue_hist(const MarchArgs a, const MarchArgs* __restrict__ views,
+                             const uint32_t* __restrict__ tile_pfx) {
+    const unsigned n = min(*(volatile unsigned int*)a.q_tail, a.q_cap);
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x)
+        atomicAdd(a.keys + queue_key<BATCH>(a, views, tile_pfx, a.longq + 4ull * k), 1u);
+}
+
+template <bool BATCH>
+__global__ void k_queue_scatter(const MarchArgs a, const MarchArgs* __restrict__ views,
+                                const uint32_t* __restrict__ tile_pfx) {
+    const unsigned n = min(*(volatile unsigned int*)a.q_tail, a.q_cap);
+    for (unsigned k = blockIdx.x * blockDim.x + threadIdx.x; k < n; k += gridDim.x * blockDim.x) {
+        const uint32_t pos = atomicAdd(a.keys + queue_key<BATCH>(a, views, tile_pfx, a.longq + 4ull * k), 1u);
+        a.order[pos] = k;
+    }
+}
+
+template <bool STATS, bool BATCH, bool LEARNED>
+__global__ void __launch_bounds__(kThreads, 4) k_regroup(const MarchArgs a, const MarchArgs* __restrict__ views) {
+    const int lane = threadIdx.x & 31;
+    Acc acc;
+    uint64_t hits = 0;
+    const unsigned n = min(*(volatile unsigned int*)a.q_tail, a.q_cap);
+    const unsigned groups = (n + 31) / 32;
+    const Queue q2{a.longq2, a.q2_tail, a.q_cap};
+    for (;;) {
+        unsigned g = 0;
+        if (lane == 0) g = atomicAdd(a.grp_counter, 1u);
+        g = __shfl_sync(kFull, g, 0);
+        if (g >= groups) break;
+        const unsigned j = g * 32 + (unsigned)lane;
+        bool have = j < n;
+        Ray r;
+        r.phase = kDone;
+        r.i = r.b = r.ks = 0;
+        r.kf = -1;
+        r.mode = kWhole;
+        r.p[0] = r.p[1] = r.p[2] = 0.0f;
+        r.q[0] = r.q[1] = r.q[2] = 0.0f;
+        r.e[0] = r.e[1] = r.e[2] = 0.0f;
+        r.s[0] = r.s[1] = r.s[2] = 0.0f;
+        uint32_t idx = 0, view = 0;
+        if (have) load_entry(a.longq + 4ull * a.order[j], r, idx, view);
+        // a warp marches rays of one view: lanes of another view (only where the
+        // sorted list crosses a view boundary) go straight to the next queue
+        const uint32_t v0 = __shfl_sync(kFull, view, 0);
+        if (BATCH && have && view != v0) {
+            const uint32_t slot = atomicAdd(a.q2_tail, 1u);
+            if (slot < a.q_cap) push_long(q2, slot, idx, view, r);
+            if (STATS) acc.deferred++;
+            have = false;
+            r.phase = kDone;  // the ray is the long-ray pass's now: it must not march here
+        }
+        const MarchArgs& av = BATCH ? views[v0] : a;
+        const int px = have ? (int)(idx % (uint32_t)av.W) : 0, py = have ? (int)(idx / (uint32_t)av.W) : 0;
+        if (have) {
+            float p0[3];
+            ray_setup(av, px, py, av.zbuf[idx], p0, r.s);
+        }
+        Loc L;
+        L.c[0] = L.c[1] = L.c[2] = 0;
+        L.u[0] = L.u[1] = L.u[2] = 0.0f;
+        const bool deferred =
+            run_lanes<STATS, LEARNED>(av, q2, r, L, have, px, py, idx, v0, a.cap2, false, lane, acc);
+        finish_lanes<STATS>(av, r, have && !deferred, idx, px, py, acc, hits);
+    }
+    if (acc.bad) atomicOr(a.status, 2u);
+    if (STATS) flush_stats(a, lane, acc, 0, 0, hits, true);
+}
+
 // Finish one queued ray with the whole warp and write its pixel.
 template <bool STATS, bool LEARNED>
 __device__ __forceinline__ void finish_long(const MarchArgs& a, uint32_t idx, Ray& r, int lane, Acc& acc,
-                                            uint64_t& hits) {
+                                            uint64_t& hits, float* red) {
     const int px = (int)(idx % (uint32_t)a.W), py = (int)(idx / (uint32_t)a.W);
     float p0[3];
     ray_setup(a, px, py, a.zbuf[idx], p0, r.s);
@@ -830,7 +1005,7 @@ __device__ __forceinline__ void finish_long(const MarchArgs& a, uint32_t idx, Ra
     Loc L;
     bool need = locate(a.g, r.e[0], r.e[1], r.e[2], L);  // the pending point was prepared
     while (need) {
-        const float rho = density_warp<STATS>(a.g, a.k, L, r.e[0], r.e[1], r.e[2], a.cull, lane, acc, cnt);
+        const float rho = density_warp<STATS>(a.g, a.k, L, r.e[0], r.e[1], r.e[2], a.cull, lane, acc, cnt, red);
         apply<LEARNED>(a, r, rho);
         need = advance<STATS, LEARNED>(a, r, L, px, py, idx, acc, cnt);
     }
@@ -838,7 +1013,7 @@ __device__ __forceinline__ void finish_long(const MarchArgs& a, uint32_t idx, Ra
     float n0 = 0.f, n1 = 0.f, n2 = 0.f;
     if (hit) {
         float gx, gy, gz;
-        grad_warp<STATS>(a.g, a.k, r.p[0], r.p[1], r.p[2], a.cull, lane, acc, cnt, gx, gy, gz);
+        grad_warp<STATS>(a.g, a.k, r.p[0], r.p[1], r.p[2], a.cull, lane, acc, cnt, red, gx, gy, gz);
         const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
         n0 = gx * gi;
         n1 = gy * gi;
@@ -853,37 +1028,33 @@ __device__ __forceinline__ void finish_long(const MarchArgs& a, uint32_t idx, Ra
 // Long-ray pass: persistent warps take deferred rays one at a time and finish
 // them with all 32 lanes (density_warp / grad_warp), then write the pixel.
 template <bool STATS, bool BATCH, bool LEARNED>
-__global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a, const MarchArgs* __restrict__ views) {
+__global__ void __launch_bounds__(kThreads) k_march_long(const MarchArgs a, const MarchArgs* __restrict__ views,
+                                                         const float4* __restrict__ buf,
+                                                         const unsigned int* __restrict__ tail,
+                                                         unsigned int* __restrict__ head) {
+    __shared__ __align__(16) float red_all[kThreads / 32][96];
+    float* red = red_all[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     Acc acc;
     uint64_t hits = 0;
-    const unsigned total = min(*(volatile unsigned int*)a.q_tail, a.q_cap);
+    const unsigned total = min(*(volatile const unsigned int*)tail, a.q_cap);
     for (;;) {
         unsigned k = 0;
-        if (lane == 0) k = atomicAdd(a.q_head, 1u);
+        if (lane == 0) k = atomicAdd(head, 1u);
         k = __shfl_sync(kFull, k, 0);
         if (k >= total) break;
-        const float4* d = a.longq + 4ull * k;
-        const float4 w0 = d[0], w1 = d[1], w2 = d[2], w3 = d[3];
-        const uint32_t idx = __float_as_uint(w0.x);
         Ray r;
-        r.phase = __float_as_int(w0.y) & 0xff;
-        r.mode = __float_as_int(w0.y) >> 8;
-        r.i = __float_as_int(w0.z);
-        r.b = __float_as_int(w0.w);
-        r.p[0] = w1.x; r.p[1] = w1.y; r.p[2] = w1.z;
-        r.q[0] = w2.x; r.q[1] = w2.y; r.q[2] = w2.z;
-        r.e[0] = w3.x; r.e[1] = w3.y; r.e[2] = w3.z;
-        r.ks = __float_as_int(w1.w);
-        r.kf = __float_as_int(w2.w);
-        if (BATCH) finish_long<STATS, LEARNED>(views[__float_as_uint(w3.w)], idx, r, lane, acc, hits);
-        else finish_long<STATS, LEARNED>(a, idx, r, lane, acc, hits);
+        uint32_t idx, view;
+        load_entry(buf + 4ull * k, r, idx, view);
+        if (BATCH) finish_long<STATS, LEARNED>(views[view], idx, r, lane, acc, hits, red);
+        else finish_long<STATS, LEARNED>(a, idx, r, lane, acc, hits, red);
     }
     if (acc.bad) atomicOr(a.status, 2u);
     if (STATS) {
         acc.streamed = 0;
         acc.deferred = 0;
         acc.proposed = 0;
+        acc.regrouped = 0;
         flush_stats(a, lane, acc, 0, 0, hits, false);
     }
 }
@@ -916,6 +1087,8 @@ MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_marc
     a.claim = cfg.claim;
     a.cap = cfg.cap;
     a.defer_lanes = cfg.lanes;
+    a.cap2 = cfg.cap2;
+    a.order = nullptr;
     const int tw = 1 << cfg.tw_log2, th = 32 >> cfg.tw_log2;
     a.tiles_x = (cam->width + tw - 1) / tw;
     a.ntiles = a.tiles_x * ((cam->height + th - 1) / th);
@@ -945,10 +1118,30 @@ int launch_variant(fm_ctx* ctx, const MarchArgs& a, const MarchArgs* d_views, co
     if (blocks < 1) blocks = 1;
     k_march<STATS, BATCH, LEARNED><<<blocks, kThreads, 0, st>>>(a, d_views, d_tile_pfx, nviews);
     FM_CUDA(ctx, cudaGetLastError());
+    const float4* lbuf = a.longq;
+    const unsigned int* ltail = a.q_tail;
+    unsigned int* lhead = a.q_head;
+    if (a.order) {
+        // regroup: counting sort of the queued rays by first-pass tile, second pass
+        const unsigned sblocks = (unsigned)ctx->sm_count * 4;
+        FM_CUDA(ctx, cudaMemsetAsync(a.keys, 0, ((size_t)a.ntiles + 1) * sizeof(uint32_t), st));
+        k_queue_hist<BATCH><<<sblocks, 256, 0, st>>>(a, d_views, d_tile_pfx);
+        scan_exclusive(a.keys, a.keys, (uint64_t)a.ntiles + 1, a.scan_tmp, st);
+        k_queue_scatter<BATCH><<<sblocks, 256, 0, st>>>(a, d_views, d_tile_pfx);
+        int rg_per_sm = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&rg_per_sm, k_regroup<STATS, BATCH, LEARNED>, kThreads, 0);
+        if (rg_per_sm < 1) rg_per_sm = 1;
+        k_regroup<STATS, BATCH, LEARNED><<<ctx->sm_count * rg_per_sm, kThreads, 0, st>>>(a, d_views);
+        FM_CUDA(ctx, cudaGetLastError());
+        lbuf = a.longq2;
+        ltail = a.q2_tail;
+        lhead = a.q2_head;
+    }
     int long_per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&long_per_sm, k_march_long<STATS, BATCH, LEARNED>, kThreads, 0);
     if (long_per_sm < 1) long_per_sm = 1;
-    k_march_long<STATS, BATCH, LEARNED><<<ctx->sm_count * long_per_sm, kThreads, 0, st>>>(a, d_views);
+    k_march_long<STATS, BATCH, LEARNED><<<ctx->sm_count * long_per_sm, kThreads, 0, st>>>(a, d_views, lbuf, ltail,
+                                                                                          lhead);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }
@@ -1019,19 +1212,37 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
     a.stats = ctx->stats_enabled ? ctx->d_stats : nullptr;
     a.status = ctx->d_status;
     // fresh counters per launch (a ring of slots, so launches on different
-    // streams do not share them): word 0 tiles, word 1 queue tail, word 2 queue head
+    // streams do not share them): tiles, queue tail, queue head, second-pass
+    // groups, second queue tail and head
     unsigned int* slot = ctx->d_work + (ctx->work_slot++ % kWorkSlots) * 32;
     a.tile_counter = slot;
     a.q_tail = slot + 1;
     a.q_head = slot + 2;
-    FM_CUDA(ctx, cudaMemsetAsync(slot, 0, 3 * sizeof(unsigned int), st));
+    a.grp_counter = slot + 3;
+    a.q2_tail = slot + 4;
+    a.q2_head = slot + 5;
+    FM_CUDA(ctx, cudaMemsetAsync(slot, 0, 6 * sizeof(unsigned int), st));
     const uint64_t entries = long_queue_entries((uint64_t)cam->width * (uint64_t)cam->height, ctx->tile.qlimit);
-    if (ctx->longq.bytes < entries * 64) {
-        FM_CUDA(ctx, cudaStreamSynchronize(st));  // the buffer may be in use by an earlier launch
-        if (!grow_buf(ctx->longq, entries * 64)) return set_err(ctx, FM_ERR_OOM, "long-ray queue allocation failed");
+    const bool regroup = ctx->tile.cap2 > 0;
+    const uint64_t nkeys = (uint64_t)a.ntiles + 1;
+    const bool small = ctx->longq.bytes < entries * 64 ||
+                       (regroup && (ctx->longq2.bytes < entries * 64 || ctx->rg_order.bytes < entries * 4 ||
+                                    ctx->rg_keys.bytes < nkeys * 4 || ctx->rg_tmp.bytes < scan_words(nkeys) * 4));
+    if (small) {
+        FM_CUDA(ctx, cudaStreamSynchronize(st));  // the buffers may be in use by an earlier launch
+        if (!grow_buf(ctx->longq, entries * 64) ||
+            (regroup && (!grow_buf(ctx->longq2, entries * 64) || !grow_buf(ctx->rg_order, entries * 4) ||
+                         !grow_buf(ctx->rg_keys, nkeys * 4) || !grow_buf(ctx->rg_tmp, scan_words(nkeys) * 4))))
+            return set_err(ctx, FM_ERR_OOM, "long-ray queue allocation failed");
     }
     a.longq = (float4*)ctx->longq.p;
     a.q_cap = (unsigned int)entries;
+    if (regroup) {
+        a.longq2 = (float4*)ctx->longq2.p;
+        a.order = (uint32_t*)ctx->rg_order.p;
+        a.keys = (uint32_t*)ctx->rg_keys.p;
+        a.scan_tmp = (uint32_t*)ctx->rg_tmp.p;
+    }
     return launch_march_kernels(ctx, a, nullptr, nullptr, 0, st);
 }
 

@@ -77,7 +77,7 @@ class CMarchStats(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("started", C.c_uint64), ("hits", C.c_uint64), ("evals", C.c_uint64),
                 ("candidates", C.c_uint64), ("skipped", C.c_uint64), ("tested", C.c_uint64),
                 ("streamed", C.c_uint64), ("deferred", C.c_uint64), ("proposed", C.c_uint64),
-                ("fallbacks", C.c_uint64)]
+                ("fallbacks", C.c_uint64), ("regrouped", C.c_uint64)]
 
 
 class CJudge(C.Structure):
@@ -87,7 +87,7 @@ class CJudge(C.Structure):
 
 class CTileConfig(C.Structure):
     _fields_ = [("tile_width", C.c_int32), ("tiles_per_claim", C.c_int32), ("defer_iters", C.c_int32),
-                ("long_queue", C.c_int32), ("defer_lanes", C.c_int32), ("reserved", C.c_int32)]
+                ("long_queue", C.c_int32), ("defer_lanes", C.c_int32), ("regroup_iters", C.c_int32)]
 
 
 class CView(C.Structure):
@@ -230,9 +230,10 @@ class Context:
         return {k: int(getattr(s, k)) for k, _ in CMarchStats._fields_}
 
     def set_tile_config(self, tile_width: int = 8, tiles_per_claim: int = 1, defer_iters: int = 32,
-                        long_queue: int = 0, defer_lanes: int = 2):
+                        long_queue: int = 0, defer_lanes: int = 2, regroup_iters: int = 0):
         """Work split of single-view marches (results do not depend on it)."""
-        c = CTileConfig(int(tile_width), int(tiles_per_claim), int(defer_iters), int(long_queue), int(defer_lanes), 0)
+        c = CTileConfig(int(tile_width), int(tiles_per_claim), int(defer_iters), int(long_queue), int(defer_lanes),
+                        int(regroup_iters))
         self.check(self.L.fm_set_tile_config(self.h, C.byref(c)))
 
     def tile_config(self) -> dict:
@@ -380,12 +381,13 @@ def render(scene: Scene, cam, params: MarchParams, want_start: bool = True) -> d
 
 def _tile_dict(c: CTileConfig) -> dict:
     return {"tile_width": int(c.tile_width), "tiles_per_claim": int(c.tiles_per_claim),
-            "defer_iters": int(c.defer_iters), "long_queue": int(c.long_queue), "defer_lanes": int(c.defer_lanes)}
+            "defer_iters": int(c.defer_iters), "long_queue": int(c.long_queue), "defer_lanes": int(c.defer_lanes),
+            "regroup_iters": int(c.regroup_iters)}
 
 
 def _tile_struct(d: dict) -> CTileConfig:
     return CTileConfig(int(d["tile_width"]), int(d.get("tiles_per_claim", 1)), int(d.get("defer_iters", 32)),
-                       int(d.get("long_queue", 0)), int(d.get("defer_lanes", 2)), 0)
+                       int(d.get("long_queue", 0)), int(d.get("defer_lanes", 2)), int(d.get("regroup_iters", 0)))
 
 
 @dataclass

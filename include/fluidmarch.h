@@ -129,6 +129,7 @@ typedef struct fm_march_stats {
     uint64_t deferred;      /* rays finished by the long-ray pass */
     uint64_t proposed;      /* rays that started inside a proposed interval (FM_MARCH_PROPOSAL) */
     uint64_t fallbacks;     /* of those, rays that went back for the samples before the interval */
+    uint64_t regrouped;     /* rays the first pass handed to the regrouped second pass */
 } fm_march_stats;
 
 /* ---- context ------------------------------------------------------------ */
@@ -248,10 +249,12 @@ typedef struct fm_tile_config {
                                 Rays that find it full stay with their warp. */
     int32_t defer_lanes;     /* a warp also defers its rays once at most this many are
                                 still active: 0..31 */
-    int32_t reserved;        /* 0 */
+    int32_t regroup_iters;   /* deferred rays are sorted by tile and marched again 32 to
+                                a warp for this many sums before the warp-per-ray pass
+                                takes the rest: 0 (no second pass)..4096 */
 } fm_tile_config;
 
-/* Work split of fm_march on this context (default 8, 1, 20, 0, 2). */
+/* Work split of fm_march on this context (default 8, 1, 20, 0, 2, 0). */
 int fm_set_tile_config(fm_ctx* ctx, const fm_tile_config* cfg);
 int fm_get_tile_config(const fm_ctx* ctx, fm_tile_config* out);
 

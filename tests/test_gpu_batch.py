@@ -120,6 +120,8 @@ def test_batch_view_matches_oracle(fmlib, ctx, small_batch, oracle_lib):
     dict(tile_width=1), dict(tile_width=2), dict(tile_width=4), dict(tile_width=16), dict(tile_width=32),
     dict(tile_width=8, tiles_per_claim=4), dict(tile_width=8, defer_iters=1), dict(tile_width=8, defer_iters=4096),
     dict(tile_width=8, long_queue=3), dict(tile_width=16, defer_iters=2, long_queue=1),
+    dict(tile_width=8, regroup_iters=0), dict(tile_width=8, defer_iters=4, regroup_iters=1),
+    dict(tile_width=4, defer_iters=8, regroup_iters=4096, defer_lanes=8),
 ])
 def test_tile_config_does_not_change_results(fmlib, ctx, cfg):
     sc = scenes.small_scene(seed=44, n=12000, width=130, height=70)
@@ -138,7 +140,7 @@ def test_tile_config_does_not_change_results(fmlib, ctx, cfg):
         ctx.set_tile_config(**old)
     assert_same(got, ref, str(cfg))
     if cfg.get("defer_iters") == 1 and "long_queue" not in cfg:
-        assert st["deferred"] > 0
+        assert st["deferred"] + st["regrouped"] > 0
 
 
 def test_batch_tile_configs_and_autotune(fmlib, ctx, small_batch):
