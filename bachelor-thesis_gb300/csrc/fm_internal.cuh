@@ -18,6 +18,7 @@
 namespace fm {
 
 constexpr int kWarp = 32;
+constexpr int kBoundBoxes = 64;         // exact-skip bound boxes per cell (4 x 4 x 4)
 constexpr int kProposalOcc = 64;        // occupancy grid resolution of the proposal
 constexpr int kProposalFeatures = FM_PROPOSAL_FEATURES;
 constexpr int kProposalParams = FM_PROPOSAL_PARAMS;
@@ -33,7 +34,7 @@ struct GridDev {
     uint32_t nsub;                        // 8 * n_cells + 1 (entries of sub)
     const float4* __restrict__ pts;       // sorted particles (w = 0): cell, 2x2x2 sub-cell, input index
     const uint32_t* __restrict__ sub;     // 8 * n_cells + 1 sub-cell starts; cell c = [sub[8c], sub[8c+8])
-    const float* __restrict__ bound;      // per sub-cell density upper bound (FM_SKIP_EXACT) or null
+    const float* __restrict__ bound;      // per bound box (64 per cell) density upper bound (FM_SKIP_EXACT) or null
     const uint8_t* __restrict__ flag;     // per-cell reference skip flag (FM_SKIP_REFERENCE) or null
 };
 
@@ -228,7 +229,7 @@ struct fm_scene {
     uint32_t* d_cell = nullptr;    // cell of each input particle
     uint32_t* d_perm = nullptr;    // input index of each sorted particle
     uint32_t* d_sub = nullptr;     // 8 * ncells + 1 sub-cell starts
-    float* d_bound = nullptr;      // per sub-cell density bound (lazy)
+    float* d_bound = nullptr;      // per bound box density bound, 64 per cell (lazy)
     uint8_t* d_flag = nullptr;     // per-cell reference flag (lazy)
     bool bound_valid = false;
     bool flag_valid = false;

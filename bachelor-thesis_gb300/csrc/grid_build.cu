@@ -280,30 +280,40 @@ __global__ void k_gather(const float* __restrict__ xyz, uint64_t n, uint32_t str
     out[k] = make_float4(p[0], p[1], p[2], 0.0f);
 }
 
-// Upper bound of the density any sample inside a sub-cell can reach: the sum
-// over the particles of the cell's 27-neighbourhood (the sample's candidate
-// set) of W at the particle's distance to the sub-cell box (shrunk by a slack
-// that covers the rounding of the sample's cell assignment), inflated by a
-// margin that covers the FP32 summation error of up to n terms.  One warp per
-// cell computes its 8 sub-cell bounds.
-__global__ void k_cell_bound(GridDev g, KernelDev k, float slack, float* __restrict__ bound) {
-    uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
-    uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
-    int l = threadIdx.x % kWarp;
-    if (c >= ncells) return;
-    int cc[3] = {(int)(c % (uint64_t)g.dims[0]), (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]),
-                 (int)(c / ((uint64_t)g.dims[0] * g.dims[1]))};
-    // slab edges: lo, mid, hi of the cell per axis
-    float e0[3], e1[3], e2[3];
+// Upper bound of the density any sample inside a bound box can reach.  Every
+// cell is divided into 4x4x4 bound boxes (a quarter cell per axis); a box's
+// bound is the sum over the particles of the cell's 27-neighbourhood (the
+// sample's candidate set) of W at the particle's distance to the box grown by
+// a slack that covers the rounding of the sample's cell assignment, inflated
+// by a margin that covers the FP32 summation error of up to n terms (the
+// bound's own and the sample's).  One warp per cell: the lanes stride over the
+// neighbourhood's particles and add W into the cell's 64 sums in shared memory
+// (the order of those additions does not matter: the margin covers it).
+// Per particle, the per-axis distances to the 4 slabs give every box's
+// distance; boxes beyond the support radius on one axis are not visited.
+constexpr int kBoundWarps = 8;
+
+__global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound(GridDev g, KernelDev k, float slack,
+                                                                    float* __restrict__ bound) {
+    __shared__ float sums[kBoundWarps][kBoundBoxes];
+    const uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
+    const uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
+    const int l = threadIdx.x % kWarp;
+    if (c >= ncells) return;  // warp-uniform
+    float* acc = sums[threadIdx.x / kWarp];
+    for (int i = l; i < kBoundBoxes; i += kWarp) acc[i] = 0.0f;
+    __syncwarp();
+    const int cc[3] = {(int)(c % (uint64_t)g.dims[0]), (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]),
+                       (int)(c / ((uint64_t)g.dims[0] * g.dims[1]))};
+    // box edges per axis, grown by the slack: [lo[i], hi[i]] for i = 0..3
+    float lo[3][4], hi[3][4];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        e0[a] = g.min[a] + (float)cc[a] * g.cell;
-        e1[a] = g.min[a] + ((float)cc[a] + 0.5f) * g.cell;
-        e2[a] = e0[a] + g.cell;
-    }
-    float acc[8];
+    for (int a = 0; a < 3; ++a)
 #pragma unroll
-    for (int s = 0; s < 8; ++s) acc[s] = 0.0f;
+        for (int i = 0; i < 4; ++i) {
+            lo[a][i] = g.min[a] + ((float)cc[a] + 0.25f * (float)i) * g.cell - slack;
+            hi[a][i] = g.min[a] + ((float)cc[a] + 0.25f * (float)(i + 1)) * g.cell + slack;
+        }
     uint32_t cnt = 0;
     const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, g.dims[0] - 1);
     for (int z = max(cc[2] - 1, 0); z <= min(cc[2] + 1, g.dims[2] - 1); ++z)
@@ -314,36 +324,36 @@ __global__ void k_cell_bound(GridDev g, KernelDev k, float slack, float* __restr
             for (uint32_t j = b + l; j < e; j += kWarp) {
                 const float4 q = g.pts[j];
                 const float qa[3] = {q.x, q.y, q.z};
-                float dlo[3], dhi[3];  // distance per axis to the lower / upper half slab
+                float d2[3][4];  // squared distance per axis to each grown slab
 #pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    dlo[a] = fmaxf(fmaxf(e0[a] - qa[a], qa[a] - e1[a]), 0.0f);
-                    dhi[a] = fmaxf(fmaxf(e1[a] - qa[a], qa[a] - e2[a]), 0.0f);
-                }
+                for (int a = 0; a < 3; ++a)
 #pragma unroll
-                for (int s = 0; s < 8; ++s) {
-                    float dx = (s & 1) ? dhi[0] : dlo[0];
-                    float dy = (s & 2) ? dhi[1] : dlo[1];
-                    float dz = (s & 4) ? dhi[2] : dlo[2];
-                    float d = fmaxf(sqrtf(dx * dx + dy * dy + dz * dz) - slack, 0.0f);
-                    float q2 = d * d;
-                    if (q2 < k.h2) acc[s] += w_in(k, q2);
+                    for (int i = 0; i < 4; ++i) {
+                        const float d = fmaxf(fmaxf(lo[a][i] - qa[a], qa[a] - hi[a][i]), 0.0f);
+                        d2[a][i] = d * d;
+                    }
+#pragma unroll
+                for (int iz = 0; iz < 4; ++iz) {
+                    if (d2[2][iz] >= k.h2) continue;
+#pragma unroll
+                    for (int iy = 0; iy < 4; ++iy) {
+                        const float syz = d2[2][iz] + d2[1][iy];
+                        if (syz >= k.h2) continue;
+#pragma unroll
+                        for (int ix = 0; ix < 4; ++ix) {
+                            const float r2 = syz + d2[0][ix];
+                            if (r2 < k.h2) atomicAdd(acc + (ix + 4 * iy + 16 * iz), w_in(k, r2));
+                        }
+                    }
                 }
             }
         }
-#pragma unroll
-    for (int s = 0; s < 8; ++s)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
-    if (l < 8) {
-        const float eps = 5.9604645e-8f;  // 2^-24
-        float n = (float)cnt;
-        float a = acc[0];
-#pragma unroll
-        for (int s = 1; s < 8; ++s)
-            if (l == s) a = acc[s];
-        float up = a * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
-        bound[8 * c + l] = (cnt == 0) ? 0.0f : up;
+    __syncwarp();
+    const float eps = 5.9604645e-8f;  // 2^-24
+    const float n = (float)cnt;
+    for (int i = l; i < kBoundBoxes; i += kWarp) {
+        const float up = acc[i] * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
+        bound[(uint64_t)kBoundBoxes * c + i] = (cnt == 0) ? 0.0f : up;
     }
 }
 
@@ -452,7 +462,7 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
         cudaFree(s->d_flag);
         s->d_sub = nullptr; s->d_bound = nullptr; s->d_flag = nullptr;
         if (cudaMalloc(&s->d_sub, (nkeys + 1) * sizeof(uint32_t)) != cudaSuccess ||
-            cudaMalloc(&s->d_bound, nkeys * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&s->d_bound, ncells * kBoundBoxes * sizeof(float)) != cudaSuccess ||
             cudaMalloc(&s->d_flag, ncells) != cudaSuccess) {
             s->cell_capacity = 0;
             return set_err(ctx, FM_ERR_OOM, "cell table allocation failed");
@@ -517,8 +527,8 @@ int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st) {
     float amax = 0.0f;
     for (int a = 0; a < 3; ++a) amax = std::max(amax, std::max(std::fabs(s->min[a]), std::fabs(s->max[a])));
     float slack = 1.0e-4f * s->support + 1.0e-6f * amax;
-    uint64_t threads = s->ncells * kWarp;
-    k_cell_bound<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, k, slack, s->d_bound);
+    const uint64_t blocks = (s->ncells + kBoundWarps - 1) / kBoundWarps;
+    k_cell_bound<<<(unsigned)blocks, kWarp * kBoundWarps, 0, st>>>(g, k, slack, s->d_bound);
     FM_CUDA(ctx, cudaGetLastError());
     s->bound_valid = true;
     return FM_OK;

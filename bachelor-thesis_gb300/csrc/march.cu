@@ -9,8 +9,9 @@
 //                  p; hit at the first sample with rho >= iso      (:276-343)
 //   skip           FM_SKIP_REFERENCE: the reference's flag/jump loop
 //                  (:281-306, intersectAABB :51-62);  FM_SKIP_EXACT: samples in
-//                  sub-cells whose density upper bound is below iso are stepped
-//                  over without evaluating, so results equal skip-off exactly
+//                  bound boxes (a quarter cell per axis) whose density upper
+//                  bound is below iso are stepped over without evaluating, so
+//                  results equal skip-off exactly
 //   refinement     bisection between the last outside and first inside sample
 //   normal         normalize(sum_j gradW(x_j - p_hit)) (:332-338, Kernel.cpp:34-52)
 //   shading        composition.frag:132-184 fused into the epilogue
@@ -334,7 +335,7 @@ __device__ __forceinline__ void apply(const MarchArgs& a, Ray& r, float rho) {
 }
 
 // Advance a ray to its next density evaluation: march samples are stepped
-// (and, for FM_SKIP_EXACT, skipped while their sub-cell bound is below iso),
+// (and, for FM_SKIP_EXACT, skipped while their bound box's bound is below iso),
 // samples out of reach of every particle get density 0 without a sum.
 // Returns true with r.e / L set when a sum is needed, false when the ray left
 // the march or bisection phases.
@@ -398,9 +399,10 @@ __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc&
                 L.c[1] < a.g.dims[1] && L.c[2] < a.g.dims[2]) {
                 const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)a.g.dims[0] +
                                    (uint32_t)L.c[2] * (uint32_t)a.g.dims[0] * (uint32_t)a.g.dims[1];
-                const uint32_t sc =
-                    (L.u[0] >= 0.5f ? 1u : 0u) | (L.u[1] >= 0.5f ? 2u : 0u) | (L.u[2] >= 0.5f ? 4u : 0u);
-                if (__ldg(a.g.bound + 8u * c + sc) < a.iso) {
+                // bound box: a quarter cell per axis (u < 1 inside the grid; clamped all the same)
+                const uint32_t bx = min((uint32_t)(4.0f * L.u[0]), 3u), by = min((uint32_t)(4.0f * L.u[1]), 3u),
+                               bz = min((uint32_t)(4.0f * L.u[2]), 3u);
+                if (__ldg(a.g.bound + (uint32_t)kBoundBoxes * c + (bx | (by << 2) | (bz << 4))) < a.iso) {
                     if (STATS && cnt) acc.skipped++;
                     r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
                     continue;

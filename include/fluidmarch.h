@@ -44,7 +44,8 @@ extern "C" {
 
 /* skip modes (march parameter) */
 #define FM_SKIP_OFF 0        /* evaluate the density at every sample (reference parity gate) */
-#define FM_SKIP_EXACT 1      /* skip samples whose cell's density upper bound is below iso;
+#define FM_SKIP_EXACT 1      /* skip samples whose bound box (a quarter cell per axis) has a
+                                density upper bound below iso;
                                 same samples, same results as FM_SKIP_OFF */
 #define FM_SKIP_REFERENCE 2  /* the reference's skip: flag = own-cell count * W0 > 1, jump to the
                                 cell's exit plus one step (RayMarcher.cpp:281-306) */
