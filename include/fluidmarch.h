@@ -255,7 +255,7 @@ typedef struct fm_tile_config {
                                 takes the rest: 0 (no second pass)..4096 */
 } fm_tile_config;
 
-/* Work split of fm_march on this context (default 8, 1, 20, 0, 2, 0). */
+/* Work split of fm_march on this context (default 8, 1, 15, 0, 2, 0). */
 int fm_set_tile_config(fm_ctx* ctx, const fm_tile_config* cfg);
 int fm_get_tile_config(const fm_ctx* ctx, fm_tile_config* out);
 
