@@ -73,8 +73,8 @@ int check_config(fm_ctx* ctx, const fm_tile_config* c, TileConfig* out) {
     if (lg < 0) return set_err(ctx, FM_ERR_INVALID, "tile_width must be 1, 2, 4, 8, 16 or 32");
     if (c->tiles_per_claim < 1 || c->tiles_per_claim > 16)
         return set_err(ctx, FM_ERR_INVALID, "tiles_per_claim must be in [1, 16]");
-    if (c->defer_iters < 1 || c->defer_iters > 4096)
-        return set_err(ctx, FM_ERR_INVALID, "defer_iters must be in [1, 4096]");
+    if (c->defer_iters < 0 || c->defer_iters > 4096)
+        return set_err(ctx, FM_ERR_INVALID, "defer_iters must be in [0, 4096]");
     if (c->long_queue < 0) return set_err(ctx, FM_ERR_INVALID, "long_queue must be >= 0");
     if (c->defer_lanes < 0 || c->defer_lanes > 31) return set_err(ctx, FM_ERR_INVALID, "defer_lanes must be in [0, 31]");
     if (c->regroup_iters < 0 || c->regroup_iters > 4096)
@@ -110,7 +110,7 @@ int prepare(fm_batch* b) {
     for (const fm_view& v : b->views) {
         fm_scene* s = const_cast<fm_scene*>(v.scene);
         int rc = FM_OK;
-        if (v.params.skip_mode == FM_SKIP_EXACT) rc = ensure_bound(ctx, s, ctx->stream);
+        if (v.params.skip_mode == FM_SKIP_EXACT) rc = ensure_bound(ctx, s, ctx->stream, true);
         if (v.params.skip_mode == FM_SKIP_REFERENCE) rc = ensure_flags(ctx, s, ctx->stream);
         if (rc) return rc;
     }

@@ -32,9 +32,10 @@ struct GridDev {
     float cell;  // cell width = support radius
     int dims[3];
     uint32_t nsub;                        // 8 * n_cells + 1 (entries of sub)
+    int bound_shift;                      // bound boxes per cell and axis: 1 << bound_shift (1 or 2)
     const float4* __restrict__ pts;       // sorted particles (w = 0): cell, 2x2x2 sub-cell, input index
     const uint32_t* __restrict__ sub;     // 8 * n_cells + 1 sub-cell starts; cell c = [sub[8c], sub[8c+8])
-    const float* __restrict__ bound;      // per bound box (64 per cell) density upper bound (FM_SKIP_EXACT) or null
+    const float* __restrict__ bound;      // per bound box density upper bound (FM_SKIP_EXACT) or null
     const uint8_t* __restrict__ flag;     // per-cell reference skip flag (FM_SKIP_REFERENCE) or null
 };
 
@@ -162,7 +163,7 @@ struct DevBuf {
 struct TileConfig {
     int tw_log2 = 3;  // 8x4 pixels
     int claim = 1;
-    int cap = 15;
+    int cap = 0;          // shared-stream sums before deferral; 0: 15 with the fine bound table, else 20
     int lanes = 2;        // a warp defers its rays once at most this many are active
     int cap2 = 0;         // iterations of the regrouped second pass (0: no second pass)
     uint32_t qlimit = 0;  // long-ray queue entries (0: long_queue_entries of the pixels)
@@ -229,9 +230,14 @@ struct fm_scene {
     uint32_t* d_cell = nullptr;    // cell of each input particle
     uint32_t* d_perm = nullptr;    // input index of each sorted particle
     uint32_t* d_sub = nullptr;     // 8 * ncells + 1 sub-cell starts
-    float* d_bound = nullptr;      // per bound box density bound, 64 per cell (lazy)
+    float* d_bound = nullptr;      // coarse bound table, 8 per cell (lazy)
+    float* d_bound4 = nullptr;     // fine bound table, 64 per cell (lazy; a separate buffer, so
+                                   // marches still reading the coarse one are not disturbed)
     uint8_t* d_flag = nullptr;     // per-cell reference flag (lazy)
-    bool bound_valid = false;
+    // exact-skip bound table: 0 none, 1 coarse (2x2x2 boxes per cell), 2 fine
+    // (4x4x4); the fine table is built once a scene is marched a second time
+    int bound_level = 0;
+    uint32_t marches = 0;          // marches since the last build
     bool flag_valid = false;
     uint64_t gen = 0;              // build generation: batches bound to an older one refuse to run
     uint16_t* d_occ = nullptr;     // 64^3 FP16 occupancy of the proposal (lazy)
@@ -244,7 +250,7 @@ namespace fm {
 int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride);
 // Lazily built skip tables, launched on `st` (valid for every later launch
 // on that stream; other streams must order after it).
-int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
+int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st, bool fine);
 int ensure_flags(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
 GridDev grid_dev(const fm_scene* s);
 
@@ -350,7 +356,7 @@ MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_marc
 // Long-ray queue entries for `pixels` rays (deferred rays are a few percent;
 // a full queue only keeps rays in the first pass).
 inline uint64_t long_queue_entries(uint64_t pixels, uint32_t limit = 0) {
-    uint64_t q = limit ? (uint64_t)limit : pixels / 8 + 65536;
+    uint64_t q = limit ? (uint64_t)limit : pixels / 4 + 65536;
     return q < pixels ? q : pixels;
 }
 // Both march passes.  nviews == 0: `launch` is the single view; otherwise

@@ -9,9 +9,10 @@
 //                  p; hit at the first sample with rho >= iso      (:276-343)
 //   skip           FM_SKIP_REFERENCE: the reference's flag/jump loop
 //                  (:281-306, intersectAABB :51-62);  FM_SKIP_EXACT: samples in
-//                  bound boxes (a quarter cell per axis) whose density upper
-//                  bound is below iso are stepped over without evaluating, so
-//                  results equal skip-off exactly
+//                  bound boxes (a half or, once a scene is marched again, a
+//                  quarter cell per axis) whose density upper bound is below
+//                  iso are stepped over without evaluating, so results equal
+//                  skip-off exactly
 //   refinement     bisection between the last outside and first inside sample
 //   normal         normalize(sum_j gradW(x_j - p_hit)) (:332-338, Kernel.cpp:34-52)
 //   shading        composition.frag:132-184 fused into the epilogue
@@ -399,10 +400,13 @@ __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc&
                 L.c[1] < a.g.dims[1] && L.c[2] < a.g.dims[2]) {
                 const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)a.g.dims[0] +
                                    (uint32_t)L.c[2] * (uint32_t)a.g.dims[0] * (uint32_t)a.g.dims[1];
-                // bound box: a quarter cell per axis (u < 1 inside the grid; clamped all the same)
-                const uint32_t bx = min((uint32_t)(4.0f * L.u[0]), 3u), by = min((uint32_t)(4.0f * L.u[1]), 3u),
-                               bz = min((uint32_t)(4.0f * L.u[2]), 3u);
-                if (__ldg(a.g.bound + (uint32_t)kBoundBoxes * c + (bx | (by << 2) | (bz << 4))) < a.iso) {
+                // bound box: 1/2 or 1/4 cell per axis (u < 1 inside the grid; clamped all the same)
+                const int sh = a.g.bound_shift;
+                const uint32_t nb = 1u << sh;
+                const float fb = (float)nb;
+                const uint32_t bx = min((uint32_t)(fb * L.u[0]), nb - 1u), by = min((uint32_t)(fb * L.u[1]), nb - 1u),
+                               bz = min((uint32_t)(fb * L.u[2]), nb - 1u);
+                if (__ldg(a.g.bound + (c << (3 * sh)) + (bx | (by << sh) | (bz << (2 * sh)))) < a.iso) {
                     if (STATS && cnt) acc.skipped++;
                     r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
                     continue;
@@ -1087,7 +1091,8 @@ MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_marc
     a.Hh = cam->height;
     a.tw_log2 = cfg.tw_log2;
     a.claim = cfg.claim;
-    a.cap = cfg.cap;
+    // measured optimum at 1080p: 15 sums with the fine bound table, 20 with the coarse one
+    a.cap = cfg.cap > 0 ? cfg.cap : (s->bound_level == 2 ? 15 : 20);
     a.defer_lanes = cfg.lanes;
     a.cap2 = cfg.cap2;
     a.order = nullptr;

@@ -229,7 +229,7 @@ class Context:
         self.check(self.L.fm_march_stats_get(self.h, C.byref(s)))
         return {k: int(getattr(s, k)) for k, _ in CMarchStats._fields_}
 
-    def set_tile_config(self, tile_width: int = 8, tiles_per_claim: int = 1, defer_iters: int = 32,
+    def set_tile_config(self, tile_width: int = 8, tiles_per_claim: int = 1, defer_iters: int = 0,
                         long_queue: int = 0, defer_lanes: int = 2, regroup_iters: int = 0):
         """Work split of single-view marches (results do not depend on it)."""
         c = CTileConfig(int(tile_width), int(tiles_per_claim), int(defer_iters), int(long_queue), int(defer_lanes),
@@ -386,7 +386,7 @@ def _tile_dict(c: CTileConfig) -> dict:
 
 
 def _tile_struct(d: dict) -> CTileConfig:
-    return CTileConfig(int(d["tile_width"]), int(d.get("tiles_per_claim", 1)), int(d.get("defer_iters", 32)),
+    return CTileConfig(int(d["tile_width"]), int(d.get("tiles_per_claim", 1)), int(d.get("defer_iters", 0)),
                        int(d.get("long_queue", 0)), int(d.get("defer_lanes", 2)), int(d.get("regroup_iters", 0)))
 
 

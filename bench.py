@@ -311,7 +311,7 @@ def run_batch(args, fm, torch, ctx, ext, dev):
             keep.append(o)
             views.append(fm.View(s, cam, p, **o))
     torch.cuda.synchronize()
-    b = fm.Batch(ctx, views)  # the context's work split (8x4 tiles, defer after 15 sums)
+    b = fm.Batch(ctx, views)  # the context's work split (8x4 tiles, deferral after 15 sums)
     tuned = None
     if args.autotune:
         best, ms = b.autotune(reps=1)

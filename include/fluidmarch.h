@@ -44,8 +44,9 @@ extern "C" {
 
 /* skip modes (march parameter) */
 #define FM_SKIP_OFF 0        /* evaluate the density at every sample (reference parity gate) */
-#define FM_SKIP_EXACT 1      /* skip samples whose bound box (a quarter cell per axis) has a
-                                density upper bound below iso;
+#define FM_SKIP_EXACT 1      /* skip samples whose bound box (half a cell per axis; a quarter
+                                once the scene is marched again) has a density upper bound
+                                below iso;
                                 same samples, same results as FM_SKIP_OFF */
 #define FM_SKIP_REFERENCE 2  /* the reference's skip: flag = own-cell count * W0 > 1, jump to the
                                 cell's exit plus one step (RayMarcher.cpp:281-306) */
@@ -245,8 +246,9 @@ typedef struct fm_tile_config {
                                 is tile_width x (32 / tile_width) pixels */
     int32_t tiles_per_claim; /* tiles a warp takes at a time: 1..16 */
     int32_t defer_iters;     /* density sums a warp runs for one tile before the
-                                rays it still has go to the long-ray pass: 1..4096 */
-    int32_t long_queue;      /* entries of the long-ray queue; 0 = pixels / 8 + 65536.
+                                rays it still has go to the long-ray pass: 1..4096;
+                                0 = 15 with the fine bound table, else 20 */
+    int32_t long_queue;      /* entries of the long-ray queue; 0 = pixels / 4 + 65536.
                                 Rays that find it full stay with their warp. */
     int32_t defer_lanes;     /* a warp also defers its rays once at most this many are
                                 still active: 0..31 */
@@ -255,7 +257,7 @@ typedef struct fm_tile_config {
                                 takes the rest: 0 (no second pass)..4096 */
 } fm_tile_config;
 
-/* Work split of fm_march on this context (default 8, 1, 15, 0, 2, 0). */
+/* Work split of fm_march on this context (default 8, 1, 0, 0, 2, 0). */
 int fm_set_tile_config(fm_ctx* ctx, const fm_tile_config* cfg);
 int fm_get_tile_config(const fm_ctx* ctx, fm_tile_config* out);
 

@@ -290,3 +290,26 @@ def test_density_probe_bitwise(fmlib, ctx):
     assert np.array_equal(bits(got), bits(ref))
     assert (got > 0).sum() > 2500
     s.close()
+
+
+def test_fine_bound_table_on_reuse(fmlib, ctx):
+    """A scene marched again gets the 4x4x4 bound table: more samples skipped, same bits."""
+    sc = scenes.small_scene(seed=23, n=20000, width=128, height=96)
+    cam = sc.cameras[0]
+    s = fmlib.Scene(ctx, sc.xyz, sc.support)
+    p = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_EXACT)
+    ctx.set_stats(True)
+    try:
+        first = fmlib.render(s, cam, p)
+        st1 = ctx.stats()
+        second = fmlib.render(s, cam, p)
+        st2 = ctx.stats()
+    finally:
+        ctx.set_stats(False)
+    fr = O.build_frame(sc.xyz, sc.support)
+    o = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 8, O.splat(sc.xyz, sc.support, cam))
+    for g in (first, second):
+        for k in ("position", "normal", "depth", "colour"):
+            assert np.array_equal(bits(g[k]), bits(o[k])), k
+    assert st2["skipped"] > st1["skipped"] and st2["evals"] < st1["evals"]
+    s.close()
