@@ -404,6 +404,14 @@ __global__ void __launch_bounds__(kRows) k_propose(const ProposeArgs a) {
 #pragma unroll
             for (int j = 0; j < kF; ++j) f[j] = 0.0f;
         }
+        // a tile without any ray needs no network
+        if (!__syncthreads_or(has)) {
+            if (pix < a.npx) {
+                a.ivl[pix] = make_int2(0, -1);
+                if (a.raw) a.raw[pix] = make_float2(0.0f, 0.0f);
+            }
+            continue;
+        }
 #pragma unroll
         for (int k = 0; k < kF; k += 8) store8(a1, tid, k, kF, f + k);
         // layer 1: D[:, 0:64) = A1 (128 x 32) * W1^T
