@@ -462,6 +462,257 @@ void march_pixel(const Scene& s, const OrcCamera& cam, const OrcParams& P, const
     if (o.rho) o.rho[idx] = double(hit_rho);
 }
 
+// ---- anisotropic march (RayMarcher.cpp:114-254, 346-423; Kernel.cpp:55-107) ----
+
+struct OrcAniso {
+    float radius_mult;  // ParticleRadiusExt / ParticleRadius (Dataset.cpp:175)
+    float k_n, k_r, k_s;
+    int32_t n_eps;
+    int32_t pad;
+};
+
+// Eigen-decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations
+// (Jacobi's method; Golub & Van Loan, Matrix Computations, 8.5), in double:
+// A = V diag(w) V^T, V's columns the eigenvectors.
+inline void eig3_jacobi(const double Ain[3][3], double w[3], double V[3][3]) {
+    double A[3][3];
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+            A[i][j] = Ain[i][j];
+            V[i][j] = (i == j) ? 1.0 : 0.0;
+        }
+    for (int sweep = 0; sweep < 32; ++sweep) {
+        const double off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+        const double diag = A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2];
+        if (off <= 1e-30 * diag || off == 0.0) break;
+        for (int p = 0; p < 2; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                if (A[p][q] == 0.0) continue;
+                const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+                const double t = (theta >= 0.0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+                const double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+                for (int k = 0; k < 3; ++k) {  // A <- J^T A J
+                    const double akp = A[k][p], akq = A[k][q];
+                    A[k][p] = c * akp - sn * akq;
+                    A[k][q] = sn * akp + c * akq;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    const double apk = A[p][k], aqk = A[q][k];
+                    A[p][k] = c * apk - sn * aqk;
+                    A[q][k] = sn * apk + c * aqk;
+                }
+                for (int k = 0; k < 3; ++k) {
+                    const double vkp = V[k][p], vkq = V[k][q];
+                    V[k][p] = c * vkp - sn * vkq;
+                    V[k][q] = sn * vkp + c * vkq;
+                }
+            }
+    }
+    for (int i = 0; i < 3; ++i) w[i] = A[i][i];
+}
+
+// WPCA at p over the extended neighbours x (RayMarcher.cpp:114-249): CubicKernel
+// weights 1 - (|r| / Hext)^3, weighted mean and covariance, eigen-decomposition,
+// the [YT13] eq. 15 clamp, G = (1/H) R Sigma^-1 R^T.  glm / Eigen FP32 order for
+// the sums; the eigen-decomposition in double.  G as glm's mat3: G[col][row].
+inline void wpca(V3<float> p, const std::vector<V3<float>>& x, float Hext, float Hinv, const OrcAniso& a,
+                 float G[3][3]) {
+    const size_t N = x.size();
+    std::vector<float> wts(N);
+    float wsum = 0.0f;
+    V3<float> mean{0.0f, 0.0f, 0.0f};
+    const float hinv_ext = 1.0f / Hext;
+    for (size_t j = 0; j < N; ++j) {
+        const V3<float> r = sub(x[j], p);
+        const float d = std::sqrt(dot(r, r));
+        float w = 0.0f;
+        if (d < Hext) {
+            const float k = d * hinv_ext;
+            w = 1.0f - k * k * k;
+        }
+        wts[j] = w;
+        wsum += w;
+        mean = add(mean, mul(w, x[j]));
+    }
+    const float inv = 1.0f / wsum;
+    mean = mul(mean, inv);
+    float C[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (size_t j = 0; j < N; ++j) {
+        const V3<float> d = sub(x[j], mean);
+        const float v[3] = {d.x, d.y, d.z};
+        for (int r = 0; r < 3; ++r)
+            for (int c = 0; c < 3; ++c) C[r][c] += (wts[j] * v[r]) * v[c];  // (w x) x^T
+    }
+    double Cd[3][3], sig[3], R[3][3];
+    for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 3; ++c) Cd[r][c] = double(C[r][c] * inv);
+    eig3_jacobi(Cd, sig, R);
+    float S[3];
+    if (int64_t(N) <= int64_t(a.n_eps)) {
+        S[0] = S[1] = S[2] = a.k_n;
+    } else {
+        const float mx = std::max(float(sig[0]), std::max(float(sig[1]), float(sig[2])));
+        const float mn = mx / a.k_r;
+        for (int k = 0; k < 3; ++k) S[k] = std::max(float(sig[k]), mn) * a.k_s;
+    }
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) {
+            double g = 0.0;
+            for (int k = 0; k < 3; ++k) g += R[r][k] * R[c][k] / double(S[k]);
+            G[c][r] = float(double(Hinv) * g);
+        }
+}
+
+// glm::determinant(mat3) cofactor expansion along the first column.
+inline float det3(const float m[3][3]) {
+    return m[0][0] * (m[1][1] * m[2][2] - m[2][1] * m[1][2]) - m[1][0] * (m[0][1] * m[2][2] - m[2][1] * m[0][2]) +
+           m[2][0] * (m[0][1] * m[1][2] - m[1][1] * m[0][2]);
+}
+
+// glm mat3 * vec3 (column-major): out_i = sum_j m[j][i] r_j, glm's add order.
+inline V3<float> mat_vec(const float m[3][3], V3<float> r) {
+    return {m[0][0] * r.x + m[1][0] * r.y + m[2][0] * r.z, m[0][1] * r.x + m[1][1] * r.y + m[2][1] * r.z,
+            m[0][2] * r.x + m[1][2] * r.y + m[2][2] * r.z};
+}
+
+// AnisotropicKernel::W / gradW (Kernel.cpp:55-107): h = H, sig = 8 / pi.
+inline float aniso_W(float H, const float G[3][3], float detG, V3<float> r0) {
+    const V3<float> r = mat_vec(G, r0);
+    float q = dot(r, r);
+    if (q >= H * H) return 0.0f;
+    q = std::sqrt(q) * (1.0f / H);
+    const float sig = 8.0f / 3.14159265358979323846f;
+    if (q >= 0.5f) {
+        const float q_ = 1.0f - q;
+        return sig * detG * (2.0f * q_ * q_ * q_);
+    }
+    return sig * detG * (6.0f * (q * q * q - q * q) + 1.0f);
+}
+
+inline V3<float> aniso_gradW(float H, const float G[3][3], float detG, V3<float> r0) {
+    const V3<float> r = mat_vec(G, r0);
+    const float rn = dot(r, r);
+    if (rn >= H * H || rn == 0.0f) return {0.0f, 0.0f, 0.0f};
+    const float rl = std::sqrt(rn);
+    const float q = rl * (1.0f / H);
+    const V3<float> gq = divs(normalize(r), rl * H);
+    const float sig = 8.0f / 3.14159265358979323846f;
+    if (q >= 0.5f) {
+        const float q_ = 1.0f - q;
+        return mul(mul(-sig * detG, gq), 6.0f * q_ * q_);
+    }
+    return mul(mul(sig * detG, gq), 6.0f * (3.0f * q * q - 2.0f * q));
+}
+
+// Neighbours of p within the extended radius (5x5x5 cells of width H in
+// increasing linear index, each cell in sorted order), and the ones within H.
+inline void aniso_neighbours(const Scene& s, V3<float> p, float Hext, std::vector<V3<float>>& ext,
+                             std::vector<V3<float>>& rel) {
+    ext.clear();
+    rel.clear();
+    int cx, cy, cz;
+    if (!sample_cell_f32(s.g, p.x, p.y, p.z, cx, cy, cz)) return;
+    const int W = s.g.dims[0], Hh = s.g.dims[1], D = s.g.dims[2];
+    const float he2 = Hext * Hext, h2 = s.H * s.H;
+    for (int z = std::max(cz - 2, 0); z <= std::min(cz + 2, D - 1); ++z)
+        for (int y = std::max(cy - 2, 0); y <= std::min(cy + 2, Hh - 1); ++y) {
+            const int x0 = std::max(cx - 2, 0), x1 = std::min(cx + 2, W - 1);
+            if (x0 > x1) continue;
+            const int64_t row = (int64_t(z) * Hh + y) * W;
+            for (uint32_t j = s.start[row + x0]; j < s.start[row + x1 + 1]; ++j) {
+                const float* q = s.sorted + 4 * size_t(j);
+                const V3<float> xj{q[0], q[1], q[2]};
+                const V3<float> r = sub(xj, p);
+                const float d2 = dot(r, r);
+                if (d2 < he2 && ext.size() < 8192) {
+                    ext.push_back(xj);
+                    if (d2 < h2) rel.push_back(r);
+                }
+            }
+        }
+}
+
+// Density and G at p; false when p has no extended neighbour.
+inline bool aniso_density(const Scene& s, V3<float> p, const OrcAniso& a, float& rho, float G[3][3], float& detG,
+                          std::vector<V3<float>>& ext, std::vector<V3<float>>& rel) {
+    const float Hext = a.radius_mult * s.H;
+    aniso_neighbours(s, p, Hext, ext, rel);
+    rho = 0.0f;
+    if (ext.empty()) return false;
+    wpca(p, ext, Hext, 1.0f / s.H, a, G);
+    detG = det3(G);
+    for (const auto& r : rel) rho += aniso_W(s.H, G, detG, r);
+    return true;
+}
+
+void march_pixel_aniso(const Scene& s, const OrcCamera& cam, const OrcParams& P, const OrcAniso& A,
+                       const float* depth_in, int64_t idx, const MarchOut& o) {
+    const int W = cam.width, Hh = cam.height;
+    const int px = int(idx % W), py = int(idx / W);
+    bool hit = false;
+    V3<float> hp{0, 0, 0}, nn{0, 0, 0};
+    const float z = depth_in[idx];
+    int64_t evals = 0;
+    if (z != 1.0f) {
+        const float twoWinv = 2.0f / float(W), twoHinv = 2.0f / float(Hh);
+        float clip[4] = {float(px) * twoWinv - 1.0f, float(py) * twoHinv - 1.0f, z, 1.0f};
+        float wh[4];
+        mat4_mul<float>(cam.inv_proj_view, clip, wh);
+        V3<float> p{wh[0] / wh[3], wh[1] / wh[3], wh[2] / wh[3]};
+        V3<float> cam_pos{cam.position[0], cam.position[1], cam.position[2]};
+        V3<float> step = mul(P.step, normalize(sub(p, cam_pos)));
+        std::vector<V3<float>> ext, rel;
+        float G[3][3], detG = 0.0f, rho = 0.0f;
+        V3<float> prev = p;
+        for (int i = 0; i < P.max_steps; ++i) {
+            p = add(p, step);
+            if (P.skip_mode == 2 && s.ref_flag) p = ref_skip(s, p, step);
+            if (outside_forever(s.g, p, step)) break;
+            ++evals;
+            aniso_density(s, p, A, rho, G, detG, ext, rel);
+            if (rho >= P.iso) {
+                hit = true;
+                break;
+            }
+            prev = p;
+        }
+        if (hit) {
+            V3<float> lo = prev, hi = p;
+            for (int b = 0; b < P.bisect_iters; ++b) {
+                V3<float> mid{(lo.x + hi.x) * 0.5f, (lo.y + hi.y) * 0.5f, (lo.z + hi.z) * 0.5f};
+                ++evals;
+                aniso_density(s, mid, A, rho, G, detG, ext, rel);
+                if (rho >= P.iso) hi = mid;
+                else lo = mid;
+            }
+            hp = hi;
+            // RayMarcher.cpp:411-416: gradient sum with G at the hit point
+            ++evals;
+            aniso_density(s, hp, A, rho, G, detG, ext, rel);
+            V3<float> g{0, 0, 0};
+            for (const auto& r : rel) g = add(g, aniso_gradW(s.H, G, detG, r));
+            nn = normalize(g);
+        }
+    }
+    if (o.pos) {
+        float* d = o.pos + 4 * idx;
+        d[0] = hit ? hp.x : 0.f; d[1] = hit ? hp.y : 0.f; d[2] = hit ? hp.z : 0.f; d[3] = hit ? 1.f : 0.f;
+    }
+    if (o.nrm) {
+        float* d = o.nrm + 4 * idx;
+        d[0] = hit ? nn.x : 0.f; d[1] = hit ? nn.y : 0.f; d[2] = hit ? nn.z : 0.f; d[3] = hit ? 1.f : 0.f;
+    }
+    if (o.depth) {
+        float dd = 0.0f;
+        if (hit) {
+            V3<float> r{hp.x - cam.position[0], hp.y - cam.position[1], hp.z - cam.position[2]};
+            dd = std::sqrt(dot(r, r));
+        }
+        o.depth[idx] = dd;
+    }
+    if (o.evals) o.evals[idx] = int32_t(evals);
+}
+
 // Pi/2 as the depth shader writes it (1.57079632679), rounded to float.
 constexpr float kHalfPi = 1.57079632679f;
 
@@ -685,6 +936,43 @@ int orc_march(const float* sorted, const uint32_t* start, const OrcGrid* g, floa
               int32_t* out_evals, int64_t* out_cand, double* out_rho) {
     return orc_march_ivl(sorted, start, g, H, ref_flag, cam, P, depth_in, pixels, npix, threads, precision, out_pos,
                          out_nrm, out_depth, out_col, out_evals, out_cand, out_rho, nullptr);
+}
+
+// Anisotropic march (RayMarcher.cpp:346-423) of the given pixels (or all),
+// bisect_iters refining the hit as in the isotropic march.
+int orc_march_aniso(const float* sorted, const uint32_t* start, const OrcGrid* g, float H, const uint8_t* ref_flag,
+                    const OrcCamera* cam, const OrcParams* P, const OrcAniso* A, const float* depth_in,
+                    const int64_t* pixels, int64_t npix, int32_t threads, float* out_pos, float* out_nrm,
+                    float* out_depth, int32_t* out_evals) {
+    Scene s{sorted, start, *g, H, ref_flag};
+    MarchOut o{out_pos, out_nrm, out_depth, nullptr, out_evals, nullptr, nullptr};
+    const int64_t total = pixels ? npix : int64_t(cam->width) * cam->height;
+    int nt = threads > 0 ? threads : std::max(1, int(std::thread::hardware_concurrency()) - 1);
+    std::atomic<int64_t> next{0};
+    auto worker = [&]() {
+        for (;;) {
+            int64_t k = next.fetch_add(1);
+            if (k >= total) break;
+            march_pixel_aniso(s, *cam, *P, *A, depth_in, pixels ? pixels[k] : k, o);
+        }
+    };
+    if (nt == 1) { worker(); return 0; }
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nt; ++t) pool.emplace_back(worker);
+    for (auto& t : pool) t.join();
+    return 0;
+}
+
+// Anisotropic density at arbitrary points.
+void orc_density_aniso(const float* sorted, const uint32_t* start, const OrcGrid* g, float H, const OrcAniso* A,
+                       const float* pts, int64_t n, float* out) {
+    Scene s{sorted, start, *g, H, nullptr};
+    std::vector<V3<float>> ext, rel;
+    float G[3][3], detG, rho;
+    for (int64_t i = 0; i < n; ++i) {
+        aniso_density(s, V3<float>{pts[3 * i], pts[3 * i + 1], pts[3 * i + 2]}, *A, rho, G, detG, ext, rel);
+        out[i] = rho;
+    }
 }
 
 // Density at arbitrary points (FP32 canonical order, or FP64).

@@ -38,6 +38,11 @@ class OrcParams(C.Structure):
                 ("skip_mode", C.c_int32), ("flags", C.c_int32)]
 
 
+class OrcAniso(C.Structure):
+    _fields_ = [("radius_mult", C.c_float), ("k_n", C.c_float), ("k_r", C.c_float), ("k_s", C.c_float),
+                ("n_eps", C.c_int32), ("pad", C.c_int32)]
+
+
 def build_oracle(ref: bool = True) -> None:
     """Compile liboracle.so (and oracle/_ref when the reference tree exists)."""
     target = "all" if ref else "oracle"
@@ -71,6 +76,11 @@ def lib():
                                 C.POINTER(OrcParams), _f32p, C.c_void_p, C.c_int64, C.c_int32, C.c_int32,
                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_march_ivl.argtypes = L.orc_march.argtypes + [C.c_void_p]
+        L.orc_density_aniso.argtypes = [_f32p, _u32p, C.POINTER(OrcGrid), C.c_float, C.POINTER(OrcAniso), _f32p,
+                                        C.c_int64, _f32p]
+        L.orc_march_aniso.argtypes = [_f32p, _u32p, C.POINTER(OrcGrid), C.c_float, C.c_void_p, C.POINTER(OrcCamera),
+                                      C.POINTER(OrcParams), C.POINTER(OrcAniso), _f32p, C.c_void_p, C.c_int64,
+                                      C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_density.argtypes = [_f32p, _u32p, C.POINTER(OrcGrid), C.c_float, _f32p, C.c_int64, C.c_int32,
                                   np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")]
         _lib = L
@@ -88,6 +98,9 @@ def ref():
         R.ref_march.restype = C.c_double
         R.ref_march.argtypes = [_f32p, C.c_int64, C.c_float, _f32p, _f32p, C.c_int32, C.c_int32, _f32p, C.c_int32,
                                 C.c_float, C.c_float, C.c_int32, _f32p, _f32p, C.c_void_p, C.c_void_p, C.c_void_p]
+        R.ref_march_any.restype = C.c_double
+        R.ref_march_any.argtypes = R.ref_march.argtypes + [C.c_int32, C.c_float, C.c_float, C.c_float, C.c_float,
+                                                           C.c_int32]
         R.ref_W.restype = C.c_float
         R.ref_W.argtypes = [C.c_float] * 4
         R.ref_gradW.argtypes = [C.c_float] * 4 + [_f32p]
@@ -199,6 +212,40 @@ def march(frame: Frame, cam, iso: float, step: float, max_steps: int, bisect: in
             "rho": rho}
 
 
+def march_aniso(frame: Frame, cam, iso: float, step: float, max_steps: int, bisect: int, depth: np.ndarray,
+                aniso=(2.0, 0.5, 2.0, 2000.0, 1), skip_mode: int = 0, pixels=None, threads: int = 0):
+    """The anisotropic march (fm_oracle.cpp march_pixel_aniso); aniso = (radius_mult, k_n, k_r, k_s, n_eps)."""
+    L = lib()
+    npx = cam.width * cam.height
+    P = OrcParams(float(iso), float(step), int(max_steps), int(bisect), int(skip_mode), 0)
+    A = OrcAniso(float(aniso[0]), float(aniso[1]), float(aniso[2]), float(aniso[3]), int(aniso[4]), 0)
+    cs = camera_struct(cam)
+    pos = np.zeros((npx, 4), np.float32)
+    nrm = np.zeros((npx, 4), np.float32)
+    dep = np.zeros(npx, np.float32)
+    evals = np.zeros(npx, np.int32)
+    flags = ref_flags(frame) if skip_mode == 2 else None
+    pix = None
+    npix = 0
+    if pixels is not None:
+        pix = np.ascontiguousarray(pixels, np.int64)
+        npix = pix.shape[0]
+    L.orc_march_aniso(np.ascontiguousarray(frame.sorted.reshape(-1)), frame.start, C.byref(frame.grid),
+                      frame.support, flags.ctypes.data if flags is not None else None, C.byref(cs), C.byref(P),
+                      C.byref(A), np.ascontiguousarray(depth, np.float32), pix.ctypes.data if pix is not None else None,
+                      npix, int(threads), pos.ctypes.data, nrm.ctypes.data, dep.ctypes.data, evals.ctypes.data)
+    return {"position": pos, "normal": nrm, "depth": dep, "evals": evals}
+
+
+def density_aniso(frame: Frame, pts: np.ndarray, aniso=(2.0, 0.5, 2.0, 2000.0, 1)) -> np.ndarray:
+    pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
+    out = np.empty(pts.shape[0], np.float32)
+    A = OrcAniso(float(aniso[0]), float(aniso[1]), float(aniso[2]), float(aniso[3]), int(aniso[4]), 0)
+    lib().orc_density_aniso(np.ascontiguousarray(frame.sorted.reshape(-1)), frame.start, C.byref(frame.grid),
+                            frame.support, C.byref(A), pts, pts.shape[0], out)
+    return out
+
+
 def density(frame: Frame, pts: np.ndarray, precision: int = 32) -> np.ndarray:
     pts = np.ascontiguousarray(pts, np.float32).reshape(-1, 3)
     out = np.empty(pts.shape[0], np.float64)
@@ -208,8 +255,11 @@ def density(frame: Frame, pts: np.ndarray, precision: int = 32) -> np.ndarray:
 
 
 def ref_march(xyz: np.ndarray, support: float, cam, depth: np.ndarray, max_steps: int, step: float, iso: float,
-              box_mode: int = 0):
-    """Run the reference's own RayMarcher (Oracle A) on the whole image."""
+              box_mode: int = 0, aniso=None):
+    """Run the reference's own RayMarcher (Oracle A) on the whole image.
+
+    aniso: None (isotropic) or (radius_mult, k_n, k_r, k_s, n_eps) for the
+    reference's anisotropic marcher."""
     R = ref()
     xyz = np.ascontiguousarray(xyz, np.float32)
     npx = cam.width * cam.height
@@ -218,10 +268,12 @@ def ref_march(xyz: np.ndarray, support: float, cam, depth: np.ndarray, max_steps
     srt = np.zeros((xyz.shape[0], 3), np.float32)
     grid = np.zeros(7, np.float32)
     build_s = C.c_double(0.0)
-    secs = R.ref_march(xyz, xyz.shape[0], support, np.ascontiguousarray(cam.inv_proj_view, np.float32),
-                       np.ascontiguousarray(cam.position, np.float32), cam.width, cam.height,
-                       np.ascontiguousarray(depth, np.float32), int(max_steps), float(step), float(iso),
-                       int(box_mode), pos, nrm, srt.ctypes.data, grid.ctypes.data, C.byref(build_s))
+    an = (0, 2.0, 0.5, 2.0, 2000.0, 1) if aniso is None else (1,) + tuple(aniso)
+    secs = R.ref_march_any(xyz, xyz.shape[0], support, np.ascontiguousarray(cam.inv_proj_view, np.float32),
+                           np.ascontiguousarray(cam.position, np.float32), cam.width, cam.height,
+                           np.ascontiguousarray(depth, np.float32), int(max_steps), float(step), float(iso),
+                           int(box_mode), pos, nrm, srt.ctypes.data, grid.ctypes.data, C.byref(build_s),
+                           int(an[0]), float(an[1]), float(an[2]), float(an[3]), float(an[4]), int(an[5]))
     if secs < 0:
         raise RuntimeError("reference march rejected its input")
     return {"position": pos, "normal": nrm, "sorted": srt, "grid": grid, "seconds": secs,

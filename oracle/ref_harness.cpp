@@ -52,13 +52,16 @@ extern "C" {
 // Build the reference Frame (search, AABB, density grid) for the particles.
 // Writes the sorted particle order (xyz, stride 3) when sorted_out is given
 // and the grid origin/dims when grid_out (min[3], cellwidth, dims[3] as float).
-// Then marches the whole W x H image with the reference's isotropic marcher.
+// Then marches the whole W x H image with the reference's isotropic marcher
+// (aniso == 0) or its anisotropic marcher (RayMarcher.cpp:346-423) with the
+// extended radius radius_mult * radius and the k_n / k_r / k_s / N_eps clamp.
 // box_mode: 0 = every skip flag true (skip off), 1 = own-cell counts.
 // Returns the wall time of Prepare -> Start -> Exit in seconds, or < 0 on error.
-double ref_march(const float* xyz, int64_t n, float radius, const float* inv_proj_view, const float* cam_pos,
-                 int32_t width, int32_t height, const float* depth_in, int32_t max_steps, float step_size,
-                 float iso, int32_t box_mode, float* out_pos, float* out_nrm, float* sorted_out, float* grid_out,
-                 double* build_seconds)
+double ref_march_any(const float* xyz, int64_t n, float radius, const float* inv_proj_view, const float* cam_pos,
+                     int32_t width, int32_t height, const float* depth_in, int32_t max_steps, float step_size,
+                     float iso, int32_t box_mode, float* out_pos, float* out_nrm, float* sorted_out, float* grid_out,
+                     double* build_seconds, int32_t aniso, float radius_mult, float k_n, float k_r, float k_s,
+                     int32_t n_eps)
 {
     if (n <= 0 || width <= 0 || height <= 0) return -1.0;
     fm_shim_box_mode = box_mode;
@@ -68,7 +71,7 @@ double ref_march(const float* xyz, int64_t n, float radius, const float* inv_pro
     auto t0 = std::chrono::steady_clock::now();
     Dataset* ds = new Dataset();
     ds->ParticleRadius = radius;
-    ds->ParticleRadiusExt = 2.0f * radius;
+    ds->ParticleRadiusExt = radius_mult * radius;  // Dataset.cpp:175
     ds->ParticleRadiusInv = 1.0f / radius;
     ds->ParticleRadiusExtInv = 1.0f / ds->ParticleRadiusExt;
     ds->m_IsotropicKernel = CubicSplineKernel(radius);
@@ -109,8 +112,8 @@ double ref_march(const float* xyz, int64_t n, float radius, const float* inv_pro
     s.MaxSteps = max_steps;
     s.StepSize = step_size;
     s.IsoDensity = iso;
-    s.EnableAnisotropy = false;
-    s.k_n = 0.5f; s.k_r = 2.0f; s.k_s = 2000.0f; s.N_eps = 1;
+    s.EnableAnisotropy = aniso != 0;
+    s.k_n = k_n; s.k_r = k_r; s.k_s = k_s; s.N_eps = n_eps;
 
     const size_t npx = size_t(width) * size_t(height);
     std::vector<glm::vec4> pos(npx, glm::vec4(0)), nrm(npx, glm::vec4(0));
@@ -129,6 +132,16 @@ double ref_march(const float* xyz, int64_t n, float radius, const float* inv_pro
     delete rm;
     delete ds;
     return std::chrono::duration<double>(t3 - t2).count();
+}
+
+double ref_march(const float* xyz, int64_t n, float radius, const float* inv_proj_view, const float* cam_pos,
+                 int32_t width, int32_t height, const float* depth_in, int32_t max_steps, float step_size,
+                 float iso, int32_t box_mode, float* out_pos, float* out_nrm, float* sorted_out, float* grid_out,
+                 double* build_seconds)
+{
+    return ref_march_any(xyz, n, radius, inv_proj_view, cam_pos, width, height, depth_in, max_steps, step_size, iso,
+                         box_mode, out_pos, out_nrm, sorted_out, grid_out, build_seconds, 0, 2.0f, 0.5f, 2.0f,
+                         2000.0f, 1);
 }
 
 // The reference kernel values (Kernel.cpp:16-52) for known-answer tests.
