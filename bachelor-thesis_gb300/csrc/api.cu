@@ -88,8 +88,14 @@ int check_params(fm_ctx* ctx, const fm_march_params* p) {
     if (p->bisect_iters < 0 || p->bisect_iters > 64) return set_err(ctx, FM_ERR_INVALID, "bisect_iters must be in [0, 64]");
     if (p->skip_mode < FM_SKIP_OFF || p->skip_mode > FM_SKIP_REFERENCE)
         return set_err(ctx, FM_ERR_INVALID, "unknown skip mode");
-    if (p->flags & ~(FM_MARCH_EXTERNAL_DEPTH | FM_MARCH_PROPOSAL))
+    if (p->flags & ~(FM_MARCH_EXTERNAL_DEPTH | FM_MARCH_PROPOSAL | FM_MARCH_ANISOTROPIC))
         return set_err(ctx, FM_ERR_INVALID, "unknown march flags");
+    if (p->flags & FM_MARCH_ANISOTROPIC) {
+        if (p->flags & FM_MARCH_PROPOSAL)
+            return set_err(ctx, FM_ERR_INVALID, "the anisotropic march takes no proposal");
+        if (p->skip_mode == FM_SKIP_EXACT)
+            return set_err(ctx, FM_ERR_INVALID, "the anisotropic march skips with the reference's flags or not at all");
+    }
     return FM_OK;
 }
 
@@ -375,6 +381,22 @@ int fm_density(fm_ctx* ctx, const fm_scene* s, const float* xyz, uint64_t n, uin
     return FM_OK;
 }
 
+int fm_set_anisotropy(fm_ctx* ctx, const fm_aniso_params* p) {
+    if (!ctx) return FM_ERR_INVALID;
+    if (!p) {
+        ctx->aniso = fm_aniso_params{2.0f, 0.5f, 2.0f, 2000.0f, 1, 0};
+        return FM_OK;
+    }
+    if (!(p->radius_mult >= 1.0f && p->radius_mult <= 2.0f))
+        return set_err(ctx, FM_ERR_INVALID, "radius_mult must be in [1, 2] (the march walks 5x5x5 cells)");
+    if (!(p->k_n > 0.0f) || !(p->k_r > 0.0f) || !(p->k_s > 0.0f) || !std::isfinite(p->k_n) || !std::isfinite(p->k_r) ||
+        !std::isfinite(p->k_s))
+        return set_err(ctx, FM_ERR_INVALID, "k_n, k_r and k_s must be positive and finite");
+    if (p->n_eps < 0 || p->reserved != 0) return set_err(ctx, FM_ERR_INVALID, "n_eps must be >= 0, reserved 0");
+    ctx->aniso = *p;
+    return FM_OK;
+}
+
 int fm_set_stats(fm_ctx* ctx, int enable) {
     if (!ctx) return FM_ERR_INVALID;
     ctx->stats_enabled = enable ? 1 : 0;
@@ -473,7 +495,8 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     o.depth = (float*)dev[2];
     o.col = (float4*)dev[3];
     if (ctx->stats_enabled) FM_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, fm::kStatSlots * sizeof(unsigned long long), st));
-    rc = launch_march(ctx, s, cam, p, o, st);
+    if (p->flags & FM_MARCH_ANISOTROPIC) rc = launch_march_aniso(ctx, s, cam, p, &ctx->aniso, o, st);
+    else rc = launch_march(ctx, s, cam, p, o, st);
     if (rc) return rc;
     if (host) {
         for (int i = 0; i < 4; ++i)

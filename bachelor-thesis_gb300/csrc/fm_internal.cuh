@@ -211,6 +211,8 @@ struct fm_ctx {
     std::vector<fm_batch*> batches;
     // work split of single-view marches (fm_set_tile_config)
     fm::TileConfig tile;
+    // anisotropic kernels (fm_set_anisotropy)
+    fm_aniso_params aniso{2.0f, 0.5f, 2.0f, 2000.0f, 1, 0};
     // source of scene generations (every successful build gets a new one)
     uint64_t gen_counter = 0;
     void* h_pinned_small = nullptr;  // 256 bytes of pinned memory for small readbacks
@@ -366,6 +368,9 @@ int launch_march_kernels(fm_ctx* ctx, const MarchArgs& launch, const MarchArgs* 
                          int nviews, cudaStream_t st);
 int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
                  const MarchOutDev& o, cudaStream_t st);
+// The anisotropic march (march.cu), warp per ray.
+int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
+                       const fm_aniso_params* ap, const MarchOutDev& o, cudaStream_t st);
 // Density at n points (xyz at a stride of `stride` floats), device pointers.
 int launch_density(fm_ctx* ctx, const fm_scene* s, const float* d_xyz, uint64_t n, uint32_t stride, float* d_out,
                    cudaStream_t st);

@@ -1204,6 +1204,355 @@ __global__ void k_density_probe(const GridDev g, const KernelDev k, const float*
 
 }  // namespace
 
+namespace {
+
+// ---- anisotropic march (RayMarcher.cpp:346-423, WPCA :114-249, Kernel.cpp:55-107) ----
+//
+// Warp per ray.  Every sample (march, bisection, normal) runs the reference's
+// WPCA over the particles within the extended radius (the 5x5x5 cells around
+// the sample): CubicKernel weights 1 - (|r| / Hext)^3, weighted mean,
+// weighted covariance, eigen-decomposition (cyclic Jacobi in double), the
+// [YT13] eq. 15 clamp (k_n, k_r, k_s, N_eps), G = (1/H) R Sigma^-1 R^T; then
+// the anisotropic density sum over the particles within H.  Sums are per lane
+// and reduced over the warp (a fixed butterfly), so the result agrees with the
+// CPU restatement to rounding, not bit for bit (the eigen solver's square
+// roots and the summation order differ).
+
+struct AnisoDev {
+    float hext, hext2, hext_inv;   // extended radius
+    float h, h2, hinv, sig;        // AnisotropicKernel(H): sig = 8 / pi
+    float k_n, k_r, k_s;
+    int n_eps;
+};
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+// Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations (double).
+__device__ __forceinline__ void eig3_jacobi(double A[3][3], double w[3], double V[3][3]) {
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
+    for (int sweep = 0; sweep < 32; ++sweep) {
+        const double off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+        const double diag = A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2];
+        if (off <= 1e-30 * diag || off == 0.0) break;
+#pragma unroll
+        for (int pq = 0; pq < 3; ++pq) {
+            const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
+            if (A[p][q] == 0.0) continue;
+            const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
+            const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
+            const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double akp = A[k][p], akq = A[k][q];
+                A[k][p] = c * akp - sn * akq;
+                A[k][q] = sn * akp + c * akq;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double apk = A[p][k], aqk = A[q][k];
+                A[p][k] = c * apk - sn * aqk;
+                A[q][k] = sn * apk + c * aqk;
+            }
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const double vkp = V[k][p], vkq = V[k][q];
+                V[k][p] = c * vkp - sn * vkq;
+                V[k][q] = sn * vkp + c * vkq;
+            }
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i) w[i] = A[i][i];
+}
+
+// Visit the particles of the rows of the (2 rr + 1)^3 cells around cell c
+// (rr = 1 or 2), 32 at a time; f(j, valid) per lane.
+template <typename F>
+__device__ __forceinline__ void for_block(const GridDev& g, const int c[3], int rr, int lane, F&& f) {
+    const int x0 = max(c[0] - rr, 0), x1 = min(c[0] + rr, g.dims[0] - 1);
+    if (x0 > x1) return;
+    for (int z = max(c[2] - rr, 0); z <= min(c[2] + rr, g.dims[2] - 1); ++z)
+        for (int y = max(c[1] - rr, 0); y <= min(c[1] + rr, g.dims[1] - 1); ++y) {
+            const uint32_t row = ((uint32_t)z * (uint32_t)g.dims[1] + (uint32_t)y) * (uint32_t)g.dims[0];
+            const uint32_t b = __ldg(g.sub + 8u * (row + (uint32_t)x0));
+            const uint32_t e = __ldg(g.sub + 8u * (row + (uint32_t)x1) + 8u);
+            for (uint32_t j0 = b; j0 < e; j0 += 32) {
+                const uint32_t j = j0 + (uint32_t)lane;
+                f(j, j < e);
+            }
+        }
+}
+
+// glm mat3 * vec3 (G[col][row]).
+__device__ __forceinline__ void mat_vec(const float G[3][3], float x, float y, float z, float& ox, float& oy,
+                                        float& oz) {
+    ox = G[0][0] * x + G[1][0] * y + G[2][0] * z;
+    oy = G[0][1] * x + G[1][1] * y + G[2][1] * z;
+    oz = G[0][2] * x + G[1][2] * y + G[2][2] * z;
+}
+
+// WPCA and the anisotropic density at p (identical on every lane).  False when
+// p has no particle within the extended radius (density 0).
+__device__ __forceinline__ bool aniso_eval(const GridDev& g, const AnisoDev& an, float px, float py, float pz, int lane,
+                                           float G[3][3], float& detG, float& rho) {
+    rho = 0.0f;
+    int c[3];
+    if (!sample_cell(g, px, py, pz, c[0], c[1], c[2])) return false;
+    // weights and weighted positions
+    float ws = 0.0f, mx = 0.0f, my = 0.0f, mz = 0.0f, cnt = 0.0f;
+    for_block(g, c, 2, lane, [&](uint32_t j, bool ok) {
+        if (!ok) return;
+        const float4 q = __ldg(g.pts + j);
+        const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+        const float d2 = dot3(rx, ry, rz, rx, ry, rz);
+        if (d2 < an.hext2) {
+            const float k = sqrtf(d2) * an.hext_inv;
+            const float w = 1.0f - k * k * k;
+            ws += w;
+            mx += w * q.x;
+            my += w * q.y;
+            mz += w * q.z;
+            cnt += 1.0f;
+        }
+    });
+    ws = warp_sum(ws);
+    cnt = warp_sum(cnt);
+    if (cnt == 0.0f) return false;
+    const float inv = 1.0f / ws;
+    const float mux = warp_sum(mx) * inv, muy = warp_sum(my) * inv, muz = warp_sum(mz) * inv;
+    // weighted covariance about the mean
+    float c00 = 0.f, c01 = 0.f, c02 = 0.f, c11 = 0.f, c12 = 0.f, c22 = 0.f;
+    for_block(g, c, 2, lane, [&](uint32_t j, bool ok) {
+        if (!ok) return;
+        const float4 q = __ldg(g.pts + j);
+        const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+        const float d2 = dot3(rx, ry, rz, rx, ry, rz);
+        if (d2 < an.hext2) {
+            const float k = sqrtf(d2) * an.hext_inv;
+            const float w = 1.0f - k * k * k;
+            const float dx = q.x - mux, dy = q.y - muy, dz = q.z - muz;
+            c00 += (w * dx) * dx;
+            c01 += (w * dx) * dy;
+            c02 += (w * dx) * dz;
+            c11 += (w * dy) * dy;
+            c12 += (w * dy) * dz;
+            c22 += (w * dz) * dz;
+        }
+    });
+    double A[3][3];
+    A[0][0] = (double)(warp_sum(c00) * inv);
+    A[0][1] = A[1][0] = (double)(warp_sum(c01) * inv);
+    A[0][2] = A[2][0] = (double)(warp_sum(c02) * inv);
+    A[1][1] = (double)(warp_sum(c11) * inv);
+    A[1][2] = A[2][1] = (double)(warp_sum(c12) * inv);
+    A[2][2] = (double)(warp_sum(c22) * inv);
+    double sg[3], R[3][3];
+    eig3_jacobi(A, sg, R);
+    float S[3];
+    if ((int)fminf(cnt, 8192.0f) <= an.n_eps) {
+        S[0] = S[1] = S[2] = an.k_n;
+    } else {
+        const float mxs = fmaxf((float)sg[0], fmaxf((float)sg[1], (float)sg[2]));
+        const float mn = mxs / an.k_r;
+#pragma unroll
+        for (int k = 0; k < 3; ++k) S[k] = fmaxf((float)sg[k], mn) * an.k_s;
+    }
+#pragma unroll
+    for (int cc = 0; cc < 3; ++cc)
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < 3; ++k) acc += R[r][k] * R[cc][k] / (double)S[k];
+            G[cc][r] = (float)((double)an.hinv * acc);
+        }
+    detG = G[0][0] * (G[1][1] * G[2][2] - G[2][1] * G[1][2]) - G[1][0] * (G[0][1] * G[2][2] - G[2][1] * G[0][2]) +
+           G[2][0] * (G[0][1] * G[1][2] - G[1][1] * G[0][2]);
+    // anisotropic density over the particles within H (AnisotropicKernel::W)
+    float sum = 0.0f;
+    for_block(g, c, 1, lane, [&](uint32_t j, bool ok) {
+        if (!ok) return;
+        const float4 q = __ldg(g.pts + j);
+        const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+        if (dot3(rx, ry, rz, rx, ry, rz) >= an.h2) return;
+        float gx, gy, gz;
+        mat_vec(G, rx, ry, rz, gx, gy, gz);
+        float qq = dot3(gx, gy, gz, gx, gy, gz);
+        if (qq >= an.h2) return;
+        qq = sqrtf(qq) * an.hinv;
+        if (qq >= 0.5f) {
+            const float q_ = 1.0f - qq;
+            sum += an.sig * detG * (2.0f * q_ * q_ * q_);
+        } else {
+            sum += an.sig * detG * (6.0f * (qq * qq * qq - qq * qq) + 1.0f);
+        }
+    });
+    rho = warp_sum(sum);
+    return true;
+}
+
+// Sum of AnisotropicKernel::gradW at p with the G of p (identical on every lane).
+__device__ __forceinline__ void aniso_grad(const GridDev& g, const AnisoDev& an, float px, float py, float pz, int lane,
+                                           const float G[3][3], float detG, float& ox, float& oy, float& oz) {
+    float sx = 0.f, sy = 0.f, sz = 0.f;
+    int c[3];
+    if (sample_cell(g, px, py, pz, c[0], c[1], c[2])) {
+        for_block(g, c, 1, lane, [&](uint32_t j, bool ok) {
+            if (!ok) return;
+            const float4 q = __ldg(g.pts + j);
+            const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+            if (dot3(rx, ry, rz, rx, ry, rz) >= an.h2) return;
+            float gx, gy, gz;
+            mat_vec(G, rx, ry, rz, gx, gy, gz);
+            const float rn = dot3(gx, gy, gz, gx, gy, gz);
+            if (rn >= an.h2 || rn == 0.0f) return;
+            const float rl = sqrtf(rn);
+            const float qq = rl * an.hinv;
+            const float inv = 1.0f / sqrtf(rn);
+            const float den = rl * an.h;
+            const float nx = (gx * inv) / den, ny = (gy * inv) / den, nz = (gz * inv) / den;
+            if (qq >= 0.5f) {
+                const float q_ = 1.0f - qq;
+                const float a0 = -an.sig * detG;
+                sx += (a0 * nx) * (6.0f * q_ * q_);
+                sy += (a0 * ny) * (6.0f * q_ * q_);
+                sz += (a0 * nz) * (6.0f * q_ * q_);
+            } else {
+                const float f = 6.0f * (3.0f * qq * qq - 2.0f * qq);
+                const float a0 = an.sig * detG;
+                sx += (a0 * nx) * f;
+                sy += (a0 * ny) * f;
+                sz += (a0 * nz) * f;
+            }
+        });
+    }
+    ox = warp_sum(sx);
+    oy = warp_sum(sy);
+    oz = warp_sum(sz);
+}
+
+// Persistent warps take 32 consecutive pixels at a time and march the started
+// rays among them one after the other with the whole warp.
+template <bool STATS>
+__global__ void __launch_bounds__(kThreads) k_march_aniso(const MarchArgs a, const AnisoDev an) {
+    const int lane = threadIdx.x & 31;
+    uint64_t evals = 0, hits = 0, rays = 0, started_n = 0;
+    const uint64_t npx = (uint64_t)a.W * (uint64_t)a.Hh;
+    for (;;) {
+        unsigned chunk = 0;
+        if (lane == 0) chunk = atomicAdd(a.tile_counter, 1u);
+        chunk = __shfl_sync(kFull, chunk, 0);
+        const uint64_t base = (uint64_t)chunk * 32u;
+        if (base >= npx) break;
+        const uint64_t my = base + (uint64_t)lane;
+        const bool valid = my < npx;
+        const float zl = valid ? a.zbuf[my] : 1.0f;
+        uint32_t todo = __ballot_sync(kFull, valid && zl != 1.0f);
+        if (STATS) { rays += valid; started_n += valid && zl != 1.0f; }
+        // misses without a ray start are written by their own lane
+        if (valid && zl == 1.0f)
+            write_pixel(a, my, (int)(my % (uint64_t)a.W), (int)(my / (uint64_t)a.W), false, 0.f, 0.f, 0.f, 0.f,
+                        0.f, 0.f);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1u;
+            const uint64_t idx = base + (uint64_t)src;
+            const int px = (int)(idx % (uint64_t)a.W), py = (int)(idx / (uint64_t)a.W);
+            float p[3], s[3];
+            ray_setup(a, px, py, a.zbuf[idx], p, s);
+            float q[3] = {p[0], p[1], p[2]};
+            float G[3][3], detG = 0.0f, rho = 0.0f;
+            bool hit = false;
+            for (int i = 0; i < a.max_steps; ++i) {
+                p[0] = p[0] + s[0];
+                p[1] = p[1] + s[1];
+                p[2] = p[2] + s[2];
+                if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p[0], p[1], p[2], s[0], s[1], s[2], a.status);
+                if (outside_forever(a.g, p[0], p[1], p[2], s[0], s[1], s[2])) break;
+                if (STATS) evals++;
+                aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
+                if (rho >= a.iso) {
+                    hit = true;
+                    break;
+                }
+                q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+            }
+            float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+            if (hit) {
+                for (int b = 0; b < a.bisect; ++b) {
+                    const float m[3] = {(q[0] + p[0]) * 0.5f, (q[1] + p[1]) * 0.5f, (q[2] + p[2]) * 0.5f};
+                    if (STATS) evals++;
+                    aniso_eval(a.g, an, m[0], m[1], m[2], lane, G, detG, rho);
+                    if (rho >= a.iso) { p[0] = m[0]; p[1] = m[1]; p[2] = m[2]; }
+                    else { q[0] = m[0]; q[1] = m[1]; q[2] = m[2]; }
+                }
+                // RayMarcher.cpp:411-416: the gradient sum with the G of the hit point
+                if (STATS) evals++;
+                aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
+                float gx, gy, gz;
+                aniso_grad(a.g, an, p[0], p[1], p[2], lane, G, detG, gx, gy, gz);
+                const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+                n0 = gx * gi;
+                n1 = gy * gi;
+                n2 = gz * gi;
+                if (STATS) hits++;
+            }
+            if (lane == src) write_pixel(a, idx, px, py, hit, p[0], p[1], p[2], n0, n1, n2);
+        }
+    }
+    if (STATS) {
+        // fm_march_stats order: rays, started, hits, evals
+        const unsigned long long v[4] = {rays, started_n, lane == 0 ? hits : 0ull, lane == 0 ? evals : 0ull};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+            unsigned long long x = v[j];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);
+            if (lane == 0 && x) atomicAdd(a.stats + j, x);
+        }
+    }
+}
+
+}  // namespace
+
+int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
+                       const fm_aniso_params* ap, const MarchOutDev& o, cudaStream_t st) {
+    MarchArgs a = march_view_args(s, cam, p, o, ctx->tile);
+    a.stats = ctx->stats_enabled ? ctx->d_stats : nullptr;
+    a.status = ctx->d_status;
+    unsigned int* slot = ctx->d_work + (ctx->work_slot++ % kWorkSlots) * 32;
+    a.tile_counter = slot;
+    FM_CUDA(ctx, cudaMemsetAsync(slot, 0, sizeof(unsigned int), st));
+    AnisoDev an;
+    an.hext = ap->radius_mult * s->support;  // Dataset.cpp:175
+    an.hext2 = an.hext * an.hext;
+    an.hext_inv = 1.0f / an.hext;
+    an.h = s->support;
+    an.h2 = s->support * s->support;
+    an.hinv = 1.0f / s->support;
+    an.sig = 8.0f / 3.14159265358979323846f;
+    an.k_n = ap->k_n;
+    an.k_r = ap->k_r;
+    an.k_s = ap->k_s;
+    an.n_eps = ap->n_eps;
+    int per_sm = 0;
+    if (a.stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_aniso<true>, kThreads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_aniso<false>, kThreads, 0);
+    if (per_sm < 1) per_sm = 1;
+    const unsigned blocks = (unsigned)(ctx->sm_count * per_sm);
+    if (a.stats) k_march_aniso<true><<<blocks, kThreads, 0, st>>>(a, an);
+    else k_march_aniso<false><<<blocks, kThreads, 0, st>>>(a, an);
+    FM_CUDA(ctx, cudaGetLastError());
+    return FM_OK;
+}
+
 int launch_density(fm_ctx* ctx, const fm_scene* s, const float* d_xyz, uint64_t n, uint32_t stride, float* d_out,
                    cudaStream_t st) {
     if (n == 0) return FM_OK;

@@ -31,6 +31,7 @@ FM_MEM_HOST, FM_MEM_DEVICE = 0, 1
 FM_SKIP_OFF, FM_SKIP_EXACT, FM_SKIP_REFERENCE = 0, 1, 2
 FM_MARCH_EXTERNAL_DEPTH = 1
 FM_MARCH_PROPOSAL = 2
+FM_MARCH_ANISOTROPIC = 4
 FM_PROPOSAL_FEATURES = 32
 FM_PROPOSAL_PARAMS = 6402
 
@@ -42,7 +43,7 @@ EXPORTS = [
     "fm_batch_autotune", "fm_batch_info_get", "fm_batch_destroy", "fm_march_batch",
     "fm_proposal_create", "fm_proposal_destroy", "fm_set_proposal", "fm_proposal_features", "fm_proposal_intervals",
     "fm_judge", "fm_trainer_create", "fm_trainer_destroy", "fm_trainer_step", "fm_trainer_predict",
-    "fm_trainer_params", "fm_density",
+    "fm_trainer_params", "fm_density", "fm_set_anisotropy",
 ]
 
 
@@ -83,6 +84,11 @@ class CMarchStats(C.Structure):
 class CJudge(C.Structure):
     _fields_ = [("pixels", C.c_uint64), ("hits_ref", C.c_uint64), ("hits_test", C.c_uint64),
                 ("mask_mismatch", C.c_uint64), ("within_tol", C.c_uint64), ("max_err", C.c_float), ("tol", C.c_float)]
+
+
+class CAniso(C.Structure):
+    _fields_ = [("radius_mult", C.c_float), ("k_n", C.c_float), ("k_r", C.c_float), ("k_s", C.c_float),
+                ("n_eps", C.c_int32), ("reserved", C.c_int32)]
 
 
 class CTileConfig(C.Structure):
@@ -137,6 +143,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_grid_build_noalloc.argtypes = [vp, C.c_uint64, C.c_uint32, C.c_float, vp, vp, vp, vp, C.c_uint64,
                                         C.POINTER(CGridInfo), vp]
     L.fm_density.argtypes = [vp, vp, vp, C.c_uint64, C.c_uint32, vp, C.c_int, vp]
+    L.fm_set_anisotropy.argtypes = [vp, C.POINTER(CAniso)]
     L.fm_set_tile_config.argtypes = [vp, C.POINTER(CTileConfig)]
     L.fm_get_tile_config.argtypes = [vp, C.POINTER(CTileConfig)]
     L.fm_batch_create.argtypes = [vp, C.POINTER(CView), C.c_int32, C.POINTER(CTileConfig), C.POINTER(vp)]
@@ -236,6 +243,12 @@ class Context:
                         int(regroup_iters))
         self.check(self.L.fm_set_tile_config(self.h, C.byref(c)))
 
+    def set_anisotropy(self, radius_mult: float = 2.0, k_n: float = 0.5, k_r: float = 2.0, k_s: float = 2000.0,
+                       n_eps: int = 1):
+        """Kernels of the anisotropic march (VisualizationSettings k_n, k_r, k_s, N_eps)."""
+        a = CAniso(float(radius_mult), float(k_n), float(k_r), float(k_s), int(n_eps), 0)
+        self.check(self.L.fm_set_anisotropy(self.h, C.byref(a)))
+
     def tile_config(self) -> dict:
         c = CTileConfig()
         self.check(self.L.fm_get_tile_config(self.h, C.byref(c)))
@@ -321,9 +334,11 @@ class MarchParams:
     skip_mode: int = FM_SKIP_OFF
     external_depth: bool = False
     proposal: bool = False
+    anisotropic: bool = False
 
     def cstruct(self) -> CMarchParams:
         flags = (FM_MARCH_EXTERNAL_DEPTH if self.external_depth else 0) | (FM_MARCH_PROPOSAL if self.proposal else 0)
+        flags |= FM_MARCH_ANISOTROPIC if self.anisotropic else 0
         return CMarchParams(float(self.iso), float(self.step), int(self.max_steps), int(self.bisect),
                             int(self.skip_mode), flags)
 

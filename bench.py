@@ -26,6 +26,10 @@ learned  the same frame with the learned hit-interval proposal
        same frame (hit masks, |depth difference| <= 1e-4 x scene extent).
 batch  64 scenes of the sloshing family (50k..2M particles, 1-4 views each
        at 640x480 / 1280x720 / 1920x1080) in one graph launch per frame.
+anisotropic  the same frame with the reference's default marcher
+       (PerPixel_Anisotropic: per-sample WPCA kernels, k_n 0.5, k_r 2, k_s 2000,
+       N_eps 1, extended radius 2 H, iso = half the median anisotropic density
+       inside the fluid), next to the CPU port of it on a pixel sample.
 """
 
 from __future__ import annotations
@@ -64,6 +68,7 @@ def parse():
     ap.add_argument("--profile", action="store_true", help="short plain run of --steps frames for ncu")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-proposal comparison")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-scene measurement")
+    ap.add_argument("--no-aniso", action="store_true", help="skip the anisotropic-march measurement")
     ap.add_argument("--autotune", action="store_true", help="autotune the batch's work split first")
     return ap.parse_args()
 
@@ -292,6 +297,53 @@ def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, pla
                          "heldout_scenes": meta.get("heldout_scenes"), "heldout": meta.get("heldout")}}
 
 
+def run_aniso(args, fm, torch, ctx, ext, scene, sc, cam, out):
+    """The reference's default (anisotropic) march of the same frame, GPU and the CPU port."""
+    import oracle as O
+
+    O.build_oracle(ref=False)
+    aniso = (2.0, 0.5, 2.0, 2000.0, 1)
+    fr = O.build_frame(sc.xyz, sc.support)
+    x = sc.xyz
+    inner = x[(x[:, 1] < 0.2) & (x[:, 0] > 0.3) & (x[:, 0] < 0.7) & (x[:, 2] > 0.3) & (x[:, 2] < 0.7)][:200]
+    iso = float(np.float32(0.5 * np.median(O.density_aniso(fr, inner, aniso))))
+    ctx.set_anisotropy(*aniso)
+    P = fm.MarchParams(iso, sc.step, sc.max_steps, sc.bisect, fm.FM_SKIP_OFF, external_depth=True, anisotropic=True)
+    npx = cam.width * cam.height
+
+    def frame():
+        fm.splat_depth(scene, cam, out["start_depth"])
+        fm.march(scene, cam, P, out["position"], out["normal"], out["depth"], out["colour"], out["start_depth"])
+
+    frame()
+    ctx.sync()
+    steps = 3
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(ext):
+        for e0, e1 in ev:
+            e0.record(ext)
+            frame()
+            e1.record(ext)
+        ext.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+    hits = int((out["depth"] > 0).sum().item())
+    # the CPU port on a sample of started pixels (bisection 0, as the reference)
+    depth = out["start_depth"].cpu().numpy()
+    started = np.nonzero(depth < 1)[0]
+    rng = np.random.default_rng(9)
+    pix = np.sort(rng.choice(started, min(600, started.size), replace=False)).astype(np.int64)
+    cores, _ = cpu_info()
+    t0 = time.perf_counter()
+    O.march_aniso(fr, cam, iso, sc.step, sc.max_steps, 0, depth, aniso, pixels=pix, threads=max(1, cores - 1))
+    cpu_s = time.perf_counter() - t0
+    frac = started.size / npx
+    return {"iso": iso, "params": {"radius_mult": 2.0, "k_n": 0.5, "k_r": 2.0, "k_s": 2000.0, "n_eps": 1},
+            "ms_per_frame": ms, "rays_per_s": npx / (ms / 1e3), "hits": hits, "bisect_iters": sc.bisect,
+            "cpu_port_rays_per_s": (pix.size / cpu_s) / frac if frac > 0 else None,
+            "cpu_sample": f"{pix.size} started pixels, bisection 0, {max(1, cores - 1)} threads, scaled by the "
+                          f"started fraction {frac:.3f} to all pixels"}
+
+
 def run_batch(args, fm, torch, ctx, ext, dev):
     """The batched configuration: 64 sloshing-family scenes, 1-4 views each, one graph launch per frame."""
     from fluidmarch import scenes
@@ -460,6 +512,9 @@ def run_ours(args):
     batch = None
     if rank == 0 and not args.no_batch:
         batch = run_batch(args, fm, torch, ctx, ext, dev)
+    aniso = None
+    if rank == 0 and not args.no_aniso:
+        aniso = run_aniso(args, fm, torch, ctx, ext, scene, sc, cam, out)
 
     if rank == 0:
         peak, peak_kind = measured_peaks()
@@ -490,6 +545,8 @@ def run_ours(args):
             line["learned"] = learned
         if batch:
             line["batch"] = batch
+        if aniso:
+            line["anisotropic"] = aniso
         if world == 1 and not args.no_cpu_baseline:
             import oracle as O
 

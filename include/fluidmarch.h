@@ -59,6 +59,11 @@ extern "C" {
                                      crossing, march the rest of the ray (skip mode off or
                                      exact only) */
 
+#define FM_MARCH_ANISOTROPIC 4    /* the reference's anisotropic march (RayMarcher.cpp:346-423):
+                                     per-sample WPCA kernels with the context's
+                                     fm_aniso_params (fm_set_anisotropy); skip mode off or
+                                     reference, no proposal */
+
 /* learned proposal: features per ray and MLP parameter count */
 #define FM_PROPOSAL_FEATURES 32
 #define FM_PROPOSAL_PARAMS 6402
@@ -222,6 +227,21 @@ int fm_splat_depth(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, flo
  * written. */
 int fm_march(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, const fm_march_params* params,
              const fm_frame_out* out, int mem, void* stream);
+
+/* Anisotropic kernels: VisualizationSettings k_n, k_r, k_s, N_eps
+ * (RayMarcher.h:12-26; defaults AdvancedRenderer.cpp:23-27) and the
+ * Dataset's particleRadiusMultiplier (extended radius = radius_mult x support
+ * radius, Dataset.cpp:175; main.cpp default 2). */
+typedef struct fm_aniso_params {
+    float radius_mult;
+    float k_n;
+    float k_r;
+    float k_s;
+    int32_t n_eps;
+    int32_t reserved; /* 0 */
+} fm_aniso_params;
+/* The parameters FM_MARCH_ANISOTROPIC uses on this context (NULL: 2, 0.5, 2, 2000, 1). */
+int fm_set_anisotropy(fm_ctx* ctx, const fm_aniso_params* params);
 
 /* DiskRenderer::ComputeDensity (DiskRenderer.cpp:180-193): SPH density at n
  * points (xyz at a stride of `stride` floats, >= 3) into out[n], summed over

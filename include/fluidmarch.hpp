@@ -31,15 +31,17 @@ inline void check(fm_ctx* ctx, int rc, const char* what) {
     if (rc != FM_OK) throw Error(rc, std::string(what) + ": " + fm_last_error(ctx));
 }
 
-// The isotropic fields of the reference's settings, plus bisection and skip mode.
+// The reference's settings (RayMarcher.h:12-26), plus bisection, skip mode and
+// the Dataset's extended-radius multiplier (Dataset.cpp:175).
 struct VisualizationSettings {
     int Frame = 0;
     int MaxSteps = 128;
     float StepSize = 0.009f;
     float IsoDensity = 1.0f;
-    bool EnableAnisotropy = false;  // the anisotropic path is not provided: must be false
+    bool EnableAnisotropy = false;  // RayMarcher::PerPixel_Anisotropic (RayMarcher.cpp:346-423)
     float k_n = 0.5f, k_r = 2.0f, k_s = 2000.0f;
     int N_eps = 1;
+    float ParticleRadiusMultiplier = 2.0f;
     int BisectIters = 0;               // 0: the reference's first-sample hit
     int SkipMode = FM_SKIP_REFERENCE;  // the reference's empty-space skip
 };
@@ -76,7 +78,6 @@ public:
     // (splat) depth buffer the reference consumes, 1.0 = no particle.
     void Prepare(const VisualizationSettings& settings, const fm_camera& camera, Frame& frame, float* positions,
                  float* normals, float* depth) {
-        if (settings.EnableAnisotropy) throw Error(FM_ERR_INVALID, "the anisotropic march is not available");
         settings_ = settings;
         camera_ = camera;
         frame_ = &frame;
@@ -96,6 +97,13 @@ public:
         p.bisect_iters = settings_.BisectIters;
         p.skip_mode = settings_.SkipMode;
         p.flags = FM_MARCH_EXTERNAL_DEPTH;
+        if (settings_.EnableAnisotropy) {
+            fm_aniso_params a{settings_.ParticleRadiusMultiplier, settings_.k_n, settings_.k_r, settings_.k_s,
+                              settings_.N_eps, 0};
+            check(ctx_, fm_set_anisotropy(ctx_, &a), "fm_set_anisotropy");
+            p.flags |= FM_MARCH_ANISOTROPIC;
+            if (p.skip_mode == FM_SKIP_EXACT) p.skip_mode = FM_SKIP_REFERENCE;  // the reference always skips here
+        }
         check(ctx_, fm_march(ctx_, frame_->handle(), &camera_, &p, &out_, FM_MEM_HOST, nullptr), "fm_march");
         done_ = true;
     }
