@@ -1211,7 +1211,7 @@ namespace {
 // Warp per ray.  Every sample (march, bisection, normal) runs the reference's
 // WPCA over the particles within the extended radius (the 5x5x5 cells around
 // the sample): CubicKernel weights 1 - (|r| / Hext)^3, weighted mean,
-// weighted covariance, eigen-decomposition (cyclic Jacobi in double), the
+// weighted covariance, eigen-decomposition (cyclic Jacobi in FP32), the
 // [YT13] eq. 15 clamp (k_n, k_r, k_s, N_eps), G = (1/H) R Sigma^-1 R^T; then
 // the anisotropic density sum over the particles within H.  Sums are per lane
 // and reduced over the warp (a fixed butterfly), so the result agrees with the
@@ -1219,6 +1219,7 @@ namespace {
 // roots and the summation order differ).
 
 struct AnisoDev {
+    float reach2_ext, reach2;      // squared sub-cell reach (cell units) of Hext and H, with a rounding margin
     float hext, hext2, hext_inv;   // extended radius
     float h, h2, hinv, sig;        // AnisotropicKernel(H): sig = 8 / pi
     float k_n, k_r, k_s;
@@ -1231,38 +1232,41 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
-// Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations (double).
-__device__ __forceinline__ void eig3_jacobi(double A[3][3], double w[3], double V[3][3]) {
+// Symmetric 3x3 eigen-decomposition by cyclic Jacobi rotations in FP32 (the
+// reference solves in FP32 too; FP64 runs at a small fraction of the FP32 rate
+// on this part).  Stops when the off-diagonal mass is below 1e-14 of the
+// diagonal's, after at most 16 sweeps.
+__device__ __forceinline__ void eig3_jacobi(float A[3][3], float w[3], float V[3][3]) {
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
-        for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? 1.0 : 0.0;
-    for (int sweep = 0; sweep < 32; ++sweep) {
-        const double off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
-        const double diag = A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2];
-        if (off <= 1e-30 * diag || off == 0.0) break;
+        for (int j = 0; j < 3; ++j) V[i][j] = (i == j) ? 1.0f : 0.0f;
+    for (int sweep = 0; sweep < 16; ++sweep) {
+        const float off = A[0][1] * A[0][1] + A[0][2] * A[0][2] + A[1][2] * A[1][2];
+        const float diag = A[0][0] * A[0][0] + A[1][1] * A[1][1] + A[2][2] * A[2][2];
+        if (off <= 1e-14f * diag || off == 0.0f) break;
 #pragma unroll
         for (int pq = 0; pq < 3; ++pq) {
             const int p = pq == 2 ? 1 : 0, q = pq == 0 ? 1 : 2;
-            if (A[p][q] == 0.0) continue;
-            const double theta = (A[q][q] - A[p][p]) / (2.0 * A[p][q]);
-            const double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(theta * theta + 1.0));
-            const double c = 1.0 / sqrt(t * t + 1.0), sn = t * c;
+            if (A[p][q] == 0.0f) continue;
+            const float theta = (A[q][q] - A[p][p]) / (2.0f * A[p][q]);
+            const float t = (theta >= 0.0f ? 1.0f : -1.0f) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+            const float c = 1.0f / sqrtf(t * t + 1.0f), sn = t * c;
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const double akp = A[k][p], akq = A[k][q];
+                const float akp = A[k][p], akq = A[k][q];
                 A[k][p] = c * akp - sn * akq;
                 A[k][q] = sn * akp + c * akq;
             }
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const double apk = A[p][k], aqk = A[q][k];
+                const float apk = A[p][k], aqk = A[q][k];
                 A[p][k] = c * apk - sn * aqk;
                 A[q][k] = sn * apk + c * aqk;
             }
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const double vkp = V[k][p], vkq = V[k][q];
+                const float vkp = V[k][p], vkq = V[k][q];
                 V[k][p] = c * vkp - sn * vkq;
                 V[k][q] = sn * vkp + c * vkq;
             }
@@ -1272,22 +1276,54 @@ __device__ __forceinline__ void eig3_jacobi(double A[3][3], double w[3], double 
     for (int i = 0; i < 3; ++i) w[i] = A[i][i];
 }
 
-// Visit the particles of the rows of the (2 rr + 1)^3 cells around cell c
-// (rr = 1 or 2), 32 at a time; f(j, valid) per lane.
+// Visit, 32 at a time, the particles of the sub-cells of the (2 rr + 1)^3 cells
+// around the sample (cell c, fraction u) whose box lies closer than
+// sqrt(reach2) cell widths; f(j, valid) per lane.  Row by row (z, y); a row's
+// up to 40 sub-cells are tested by the lanes (two ballots) and the runs of
+// reachable sub-cells are walked as contiguous sorted ranges.
 template <typename F>
-__device__ __forceinline__ void for_block(const GridDev& g, const int c[3], int rr, int lane, F&& f) {
+__device__ __forceinline__ void for_reach(const GridDev& g, const int c[3], const float u[3], int rr, float reach2,
+                                          int lane, F&& f) {
     const int x0 = max(c[0] - rr, 0), x1 = min(c[0] + rr, g.dims[0] - 1);
     if (x0 > x1) return;
-    for (int z = max(c[2] - rr, 0); z <= min(c[2] + rr, g.dims[2] - 1); ++z)
+    const int nsubs = 8 * (x1 - x0 + 1);  // <= 40
+    // squared x-distance of this lane's sub-cells k = lane and lane + 32 (cell x0 + k / 8, sub k % 8)
+    float dx2[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int k = lane + 32 * h;
+        const int cx = x0 + (k >> 3) - c[0];
+        dx2[h] = slab_d2(u[0], (float)cx + 0.5f * (float)(k & 1));
+    }
+    for (int z = max(c[2] - rr, 0); z <= min(c[2] + rr, g.dims[2] - 1); ++z) {
+        const float dz = (float)(z - c[2]);
+        const float z0 = slab_d2(u[2], dz), z1 = slab_d2(u[2], dz + 0.5f);
         for (int y = max(c[1] - rr, 0); y <= min(c[1] + rr, g.dims[1] - 1); ++y) {
+            const float dy = (float)(y - c[1]);
+            const float y0 = slab_d2(u[1], dy), y1 = slab_d2(u[1], dy + 0.5f);
             const uint32_t row = ((uint32_t)z * (uint32_t)g.dims[1] + (uint32_t)y) * (uint32_t)g.dims[0];
-            const uint32_t b = __ldg(g.sub + 8u * (row + (uint32_t)x0));
-            const uint32_t e = __ldg(g.sub + 8u * (row + (uint32_t)x1) + 8u);
-            for (uint32_t j0 = b; j0 < e; j0 += 32) {
-                const uint32_t j = j0 + (uint32_t)lane;
-                f(j, j < e);
+            const uint32_t base = 8u * (row + (uint32_t)x0);
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int k = lane + 32 * h;
+                const int sb = k & 7;
+                const float d2 = dx2[h] + ((sb & 2) ? y1 : y0) + ((sb & 4) ? z1 : z0);
+                uint32_t m = __ballot_sync(kFull, k < nsubs && d2 < reach2);
+                while (m) {
+                    const int s0 = __ffs(m) - 1;
+                    const uint32_t rest = ~(m >> s0);
+                    const int len = rest ? __ffs(rest) - 1 : 32 - s0;  // length of the run of set bits at s0
+                    m = (len + s0 >= 32) ? 0u : (m & ~(((1u << len) - 1u) << s0));
+                    const uint32_t b = __ldg(g.sub + base + (uint32_t)(32 * h + s0));
+                    const uint32_t e = __ldg(g.sub + base + (uint32_t)(32 * h + s0 + len));
+                    for (uint32_t j0 = b; j0 < e; j0 += 32) {
+                        const uint32_t j = j0 + (uint32_t)lane;
+                        f(j, j < e);
+                    }
+                }
             }
         }
+    }
 }
 
 // glm mat3 * vec3 (G[col][row]).
@@ -1299,15 +1335,18 @@ __device__ __forceinline__ void mat_vec(const float G[3][3], float x, float y, f
 }
 
 // WPCA and the anisotropic density at p (identical on every lane).  False when
-// p has no particle within the extended radius (density 0).
+// p has no particle within the extended radius (density 0).  The weighted
+// moments are taken about p in one pass: mean = p + m, C = S / W - m m^T with
+// m = sum w r / W and S = sum w r r^T, r = x - p (|r| < Hext, so no
+// cancellation to speak of).
 __device__ __forceinline__ bool aniso_eval(const GridDev& g, const AnisoDev& an, float px, float py, float pz, int lane,
                                            float G[3][3], float& detG, float& rho) {
     rho = 0.0f;
-    int c[3];
-    if (!sample_cell(g, px, py, pz, c[0], c[1], c[2])) return false;
-    // weights and weighted positions
+    Loc L;
+    if (!locate(g, px, py, pz, L)) return false;
     float ws = 0.0f, mx = 0.0f, my = 0.0f, mz = 0.0f, cnt = 0.0f;
-    for_block(g, c, 2, lane, [&](uint32_t j, bool ok) {
+    float c00 = 0.f, c01 = 0.f, c02 = 0.f, c11 = 0.f, c12 = 0.f, c22 = 0.f;
+    for_reach(g, L.c, L.u, 2, an.reach2_ext, lane, [&](uint32_t j, bool ok) {
         if (!ok) return;
         const float4 q = __ldg(g.pts + j);
         const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
@@ -1316,68 +1355,54 @@ __device__ __forceinline__ bool aniso_eval(const GridDev& g, const AnisoDev& an,
             const float k = sqrtf(d2) * an.hext_inv;
             const float w = 1.0f - k * k * k;
             ws += w;
-            mx += w * q.x;
-            my += w * q.y;
-            mz += w * q.z;
+            const float wx = w * rx, wy = w * ry, wz = w * rz;
+            mx += wx;
+            my += wy;
+            mz += wz;
+            c00 += wx * rx;
+            c01 += wx * ry;
+            c02 += wx * rz;
+            c11 += wy * ry;
+            c12 += wy * rz;
+            c22 += wz * rz;
             cnt += 1.0f;
         }
     });
     ws = warp_sum(ws);
     cnt = warp_sum(cnt);
     if (cnt == 0.0f) return false;
-    const float inv = 1.0f / ws;
-    const float mux = warp_sum(mx) * inv, muy = warp_sum(my) * inv, muz = warp_sum(mz) * inv;
-    // weighted covariance about the mean
-    float c00 = 0.f, c01 = 0.f, c02 = 0.f, c11 = 0.f, c12 = 0.f, c22 = 0.f;
-    for_block(g, c, 2, lane, [&](uint32_t j, bool ok) {
-        if (!ok) return;
-        const float4 q = __ldg(g.pts + j);
-        const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-        const float d2 = dot3(rx, ry, rz, rx, ry, rz);
-        if (d2 < an.hext2) {
-            const float k = sqrtf(d2) * an.hext_inv;
-            const float w = 1.0f - k * k * k;
-            const float dx = q.x - mux, dy = q.y - muy, dz = q.z - muz;
-            c00 += (w * dx) * dx;
-            c01 += (w * dx) * dy;
-            c02 += (w * dx) * dz;
-            c11 += (w * dy) * dy;
-            c12 += (w * dy) * dz;
-            c22 += (w * dz) * dz;
-        }
-    });
-    double A[3][3];
-    A[0][0] = (double)(warp_sum(c00) * inv);
-    A[0][1] = A[1][0] = (double)(warp_sum(c01) * inv);
-    A[0][2] = A[2][0] = (double)(warp_sum(c02) * inv);
-    A[1][1] = (double)(warp_sum(c11) * inv);
-    A[1][2] = A[2][1] = (double)(warp_sum(c12) * inv);
-    A[2][2] = (double)(warp_sum(c22) * inv);
-    double sg[3], R[3][3];
+    const float iw = 1.0f / ws;
+    const float m0 = warp_sum(mx) * iw, m1 = warp_sum(my) * iw, m2 = warp_sum(mz) * iw;
+    float A[3][3];
+    A[0][0] = warp_sum(c00) * iw - m0 * m0;
+    A[0][1] = A[1][0] = warp_sum(c01) * iw - m0 * m1;
+    A[0][2] = A[2][0] = warp_sum(c02) * iw - m0 * m2;
+    A[1][1] = warp_sum(c11) * iw - m1 * m1;
+    A[1][2] = A[2][1] = warp_sum(c12) * iw - m1 * m2;
+    A[2][2] = warp_sum(c22) * iw - m2 * m2;
+    float sg[3], R[3][3];
     eig3_jacobi(A, sg, R);
     float S[3];
     if ((int)fminf(cnt, 8192.0f) <= an.n_eps) {
         S[0] = S[1] = S[2] = an.k_n;
     } else {
-        const float mxs = fmaxf((float)sg[0], fmaxf((float)sg[1], (float)sg[2]));
+        const float mxs = fmaxf(sg[0], fmaxf(sg[1], sg[2]));
         const float mn = mxs / an.k_r;
 #pragma unroll
-        for (int k = 0; k < 3; ++k) S[k] = fmaxf((float)sg[k], mn) * an.k_s;
+        for (int k = 0; k < 3; ++k) S[k] = fmaxf(sg[k], mn) * an.k_s;
     }
+    const float is[3] = {1.0f / S[0], 1.0f / S[1], 1.0f / S[2]};
 #pragma unroll
     for (int cc = 0; cc < 3; ++cc)
 #pragma unroll
-        for (int r = 0; r < 3; ++r) {
-            double acc = 0.0;
-#pragma unroll
-            for (int k = 0; k < 3; ++k) acc += R[r][k] * R[cc][k] / (double)S[k];
-            G[cc][r] = (float)((double)an.hinv * acc);
-        }
+        for (int r = 0; r < 3; ++r)
+            G[cc][r] = an.hinv * ((R[r][0] * R[cc][0]) * is[0] + (R[r][1] * R[cc][1]) * is[1] +
+                                  (R[r][2] * R[cc][2]) * is[2]);
     detG = G[0][0] * (G[1][1] * G[2][2] - G[2][1] * G[1][2]) - G[1][0] * (G[0][1] * G[2][2] - G[2][1] * G[0][2]) +
            G[2][0] * (G[0][1] * G[1][2] - G[1][1] * G[0][2]);
     // anisotropic density over the particles within H (AnisotropicKernel::W)
     float sum = 0.0f;
-    for_block(g, c, 1, lane, [&](uint32_t j, bool ok) {
+    for_reach(g, L.c, L.u, 1, an.reach2, lane, [&](uint32_t j, bool ok) {
         if (!ok) return;
         const float4 q = __ldg(g.pts + j);
         const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
@@ -1402,9 +1427,9 @@ __device__ __forceinline__ bool aniso_eval(const GridDev& g, const AnisoDev& an,
 __device__ __forceinline__ void aniso_grad(const GridDev& g, const AnisoDev& an, float px, float py, float pz, int lane,
                                            const float G[3][3], float detG, float& ox, float& oy, float& oz) {
     float sx = 0.f, sy = 0.f, sz = 0.f;
-    int c[3];
-    if (sample_cell(g, px, py, pz, c[0], c[1], c[2])) {
-        for_block(g, c, 1, lane, [&](uint32_t j, bool ok) {
+    Loc L;
+    if (locate(g, px, py, pz, L)) {
+        for_reach(g, L.c, L.u, 1, an.reach2, lane, [&](uint32_t j, bool ok) {
             if (!ok) return;
             const float4 q = __ldg(g.pts + j);
             const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
@@ -1532,6 +1557,11 @@ int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, con
     FM_CUDA(ctx, cudaMemsetAsync(slot, 0, sizeof(unsigned int), st));
     AnisoDev an;
     an.hext = ap->radius_mult * s->support;  // Dataset.cpp:175
+    {
+        const float r = ap->radius_mult * (1.0f + 1.0e-3f), r1 = 1.0f + 1.0e-3f;
+        an.reach2_ext = r * r;
+        an.reach2 = r1 * r1;
+    }
     an.hext2 = an.hext * an.hext;
     an.hext_inv = 1.0f / an.hext;
     an.h = s->support;
