@@ -409,6 +409,7 @@ def run_ours(args):
     ge.build()
     import fluidmarch as fm
     from fluidmarch import scenes
+    from fluidmarch.replicas import throughput
 
     sc = scenes.sloshing(seed=1000 + rank, width=args.width, height=args.height)
     cam = sc.cameras[0]
@@ -473,12 +474,9 @@ def run_ours(args):
     total_ms = sum(e0.elapsed_time(e2) for e0, _, e2 in ev)
     march_ms = sum(e1.elapsed_time(e2) for _, e1, e2 in ev)
     splat_ms = sum(e0.elapsed_time(e1) for e0, e1, _ in ev)
-    t_max = total_ms
-    if dist:
-        t = torch.tensor([total_ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_max = float(t.item())
-    value = npx * args.steps * world / (t_max / 1000.0)
+    # replicas: every rank rendered its own frames; all rays over the slowest rank's time
+    value, _, t_max_s = throughput(npx * args.steps, total_ms / 1000.0, dist, dev)
+    t_max = 1000.0 * t_max_s
 
     # e2e through the C ABI with pinned host buffers
     xyz_h = torch.from_numpy(sc.xyz).pin_memory()
@@ -500,11 +498,7 @@ def run_ours(args):
     for _ in range(args.steps):
         e2e_frame()
     e2e_s = time.perf_counter() - t0
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e_value = npx * args.steps * world / e2e_s
+    e2e_value, _, _ = throughput(npx * args.steps, e2e_s, dist, dev)
 
     learned = None
     if rank == 0 and not args.no_learned:
