@@ -31,6 +31,12 @@ struct fm_batch {
     // device buffers
     fm::DevBuf margs, tile_pfx, sviews, pfx64, pfx_tiles, depth, hiz, list, counters, longq;
     fm::DevBuf longq2, rg_keys, rg_tmp, rg_order;  // regrouped second pass
+    // learned proposal of the views with FM_MARCH_PROPOSAL: the weights (a copy),
+    // per-view blocks, tile and low-resolution prefixes, low-resolution depths,
+    // intervals of every pixel
+    fm::DevBuf pw, pb, pviews, ptile_pfx, plow_pfx, plow, pivl;
+    float pmargins[3] = {0.0f, 0.0f, 0.0f};  // margin_lo, margin_hi, min_near of the copied proposal
+    fm::ProposeBatchDev pbatch{};
     uint32_t q_cap = 0;
     fm::MarchArgs launch{};  // launch-wide march arguments
     fm::SplatBatch sb{};
@@ -58,8 +64,10 @@ void free_batch(fm_batch* b) {
     // a graph of this batch may still run on any stream
     cudaDeviceSynchronize();
     drop_graph(b);
-    DevBuf* bufs[] = {&b->margs, &b->tile_pfx, &b->sviews,  &b->pfx64,  &b->pfx_tiles, &b->depth, &b->hiz,
-                      &b->list,  &b->counters, &b->longq,   &b->longq2, &b->rg_keys,   &b->rg_tmp, &b->rg_order};
+    DevBuf* bufs[] = {&b->margs,  &b->tile_pfx, &b->sviews,  &b->pfx64,   &b->pfx_tiles, &b->depth,
+                      &b->hiz,    &b->list,     &b->counters, &b->longq,  &b->longq2,    &b->rg_keys,
+                      &b->rg_tmp, &b->rg_order, &b->pw,       &b->pb,     &b->pviews,    &b->ptile_pfx,
+                      &b->plow_pfx, &b->plow,   &b->pivl};
     for (DevBuf* d : bufs) cudaFree(d->p);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     delete b;
@@ -111,7 +119,8 @@ int prepare(fm_batch* b) {
         fm_scene* s = const_cast<fm_scene*>(v.scene);
         int rc = FM_OK;
         if (v.params.skip_mode == FM_SKIP_EXACT) rc = ensure_bound(ctx, s, ctx->stream, true);
-        if (v.params.skip_mode == FM_SKIP_REFERENCE) rc = ensure_flags(ctx, s, ctx->stream);
+        if (!rc && v.params.skip_mode == FM_SKIP_REFERENCE) rc = ensure_flags(ctx, s, ctx->stream);
+        if (!rc && (v.params.flags & FM_MARCH_PROPOSAL)) rc = ensure_occupancy(ctx, s, ctx->stream);
         if (rc) return rc;
     }
     FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
@@ -154,6 +163,24 @@ int prepare(fm_batch* b) {
         return set_err(ctx, FM_ERR_OOM, "batch buffer allocation failed");
     b->q_cap = (uint32_t)entries;
     unsigned int* cnt = (unsigned int*)b->counters.p;
+    // learned proposal: blocks for the views that use it
+    std::vector<int> pv_idx;
+    for (int i = 0; i < n; ++i)
+        if (b->views[i].params.flags & FM_MARCH_PROPOSAL) pv_idx.push_back(i);
+    const int np = (int)pv_idx.size();
+    std::vector<uint64_t> ptp(np + 1, 0), plp(np + 1, 0);
+    for (int k = 0; k < np; ++k) {
+        const fm_view& v = b->views[pv_idx[k]];
+        const uint64_t npx = (uint64_t)v.camera.width * v.camera.height;
+        ptp[k + 1] = ptp[k] + (npx + 127) / 128;
+        plp[k + 1] = plp[k] + propose_low_pixels(&v.camera);
+    }
+    if (np > 0) {
+        if (!grow_buf(b->pviews, propose_view_bytes() * np) || !grow_buf(b->ptile_pfx, 8ull * (np + 1)) ||
+            !grow_buf(b->plow_pfx, 8ull * (np + 1)) || !grow_buf(b->plow, 4ull * std::max<uint64_t>(plp[np], 1)) ||
+            !grow_buf(b->pivl, 8ull * std::max<uint64_t>(px[n], 1)))
+            return set_err(ctx, FM_ERR_OOM, "batch buffer allocation failed");
+    }
     // march arguments: per view, with the launch-wide fields in every block
     std::vector<MarchArgs> ma(n);
     std::vector<SplatView> sv(n);
@@ -162,6 +189,7 @@ int prepare(fm_batch* b) {
         const fm_view& v = b->views[i];
         float* z = v.out.start_depth ? v.out.start_depth : depth + px[i];
         MarchOutDev o{};
+        o.ivl = (v.params.flags & FM_MARCH_PROPOSAL) ? (const int2*)b->pivl.p + px[i] : nullptr;
         o.pos = (float4*)v.out.position;
         o.nrm = (float4*)v.out.normal;
         o.depth = v.out.depth;
@@ -195,6 +223,22 @@ int prepare(fm_batch* b) {
     }
     b->launch = ma[0];
     b->launch.ntiles = (int)tp[n];
+    // the learned instantiation runs when any view has a proposal (views without one march fully)
+    b->launch.ivl = np > 0 ? (const int2*)b->pivl.p : nullptr;
+    if (np > 0) {
+        std::vector<uint8_t> blocks(propose_view_bytes() * np);
+        for (int k = 0; k < np; ++k) {
+            const int i = pv_idx[k];
+            const fm_view& v = b->views[i];
+            propose_view(v.scene, &v.camera, &v.params, b->pmargins, ma[i].zbuf, (float*)b->plow.p + plp[k],
+                         (int2*)b->pivl.p + px[i], blocks.data() + propose_view_bytes() * k);
+        }
+        FM_CUDA(ctx, cudaMemcpy(b->pviews.p, blocks.data(), blocks.size(), cudaMemcpyHostToDevice));
+        FM_CUDA(ctx, cudaMemcpy(b->ptile_pfx.p, ptp.data(), 8ull * (np + 1), cudaMemcpyHostToDevice));
+        FM_CUDA(ctx, cudaMemcpy(b->plow_pfx.p, plp.data(), 8ull * (np + 1), cudaMemcpyHostToDevice));
+    }
+    b->pbatch = ProposeBatchDev{b->pviews.p, (const uint64_t*)b->ptile_pfx.p, (const uint64_t*)b->plow_pfx.p, np,
+                                ptp[np], plp[np], b->pw.p, (const float*)b->pb.p};
     b->gens.resize(n);
     for (int i = 0; i < n; ++i) b->gens[i] = b->views[i].scene->gen;
     FM_CUDA(ctx, cudaMemcpy(b->margs.p, ma.data(), sizeof(MarchArgs) * n, cudaMemcpyHostToDevice));
@@ -228,6 +272,7 @@ int enqueue(fm_batch* b, cudaStream_t st, bool stats) {
     FM_CUDA(ctx, cudaMemsetAsync(b->counters.p, 0, 8 * sizeof(unsigned int), st));
     int rc = launch_splat_batch(ctx, b->sb, st);
     if (rc) return rc;
+    if (b->pbatch.nviews > 0 && (rc = launch_propose_batch(ctx, b->pbatch, st)) != FM_OK) return rc;
     MarchArgs a = b->launch;
     a.stats = stats ? ctx->d_stats : nullptr;
     return launch_march_kernels(ctx, a, (const MarchArgs*)b->margs.p, (const uint32_t*)b->tile_pfx.p,
@@ -299,7 +344,12 @@ int fm_batch_create(fm_ctx* ctx, const fm_view* views, int32_t n_views, const fm
             return set_err(ctx, FM_ERR_INVALID, "view scene is NULL or not a live scene of this context");
         int rc = check_params(ctx, &v.params);
         if (rc) return rc;
-        if (v.params.flags != 0) return set_err(ctx, FM_ERR_INVALID, "batched views are splatted: flags must be 0");
+        if (v.params.flags & ~FM_MARCH_PROPOSAL)
+            return set_err(ctx, FM_ERR_INVALID, "batched views are splatted and isotropic: flags may only hold FM_MARCH_PROPOSAL");
+        if ((v.params.flags & FM_MARCH_PROPOSAL) && !ctx->proposal)
+            return set_err(ctx, FM_ERR_INVALID, "FM_MARCH_PROPOSAL needs a proposal (fm_set_proposal)");
+        if ((v.params.flags & FM_MARCH_PROPOSAL) && v.params.skip_mode == FM_SKIP_REFERENCE)
+            return set_err(ctx, FM_ERR_INVALID, "FM_MARCH_PROPOSAL marches the plain sample lattice: skip mode must be off or exact");
         rc = check_camera(ctx, &v.camera, true);
         if (rc) return rc;
         if (v.scene->n == 0) return set_err(ctx, FM_ERR_INVALID, "view scene has no particles");
@@ -314,7 +364,17 @@ int fm_batch_create(fm_ctx* ctx, const fm_view* views, int32_t n_views, const fm
         free_batch(b);
         return set_err(ctx, FM_ERR_CUDA, "stream creation failed");
     }
-    int rc = prepare(b);
+    int rc = FM_OK;
+    // the batch keeps its own copy of the context's proposal: later fm_set_proposal or
+    // fm_proposal_destroy calls do not change it
+    bool learned = false;
+    for (const fm_view& v : b->views) learned |= (v.params.flags & FM_MARCH_PROPOSAL) != 0;
+    if (learned) {
+        rc = proposal_weights(ctx, ctx->proposal, b->pw, b->pb, b->pmargins, ctx->stream);
+        if (!rc && cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+            rc = set_err(ctx, FM_ERR_CUDA, "proposal copy failed");
+    }
+    if (!rc) rc = prepare(b);
     if (!rc) rc = capture(b);
     if (rc) {
         free_batch(b);

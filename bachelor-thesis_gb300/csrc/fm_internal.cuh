@@ -391,6 +391,24 @@ int launch_features(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const float*
                     cudaStream_t st);
 int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const fm_proposal* pr,
                    const float* zbuf, int2* ivl, float2* raw, cudaStream_t st);
+// Batched proposal: per-view blocks (propose_view) laid out by the caller.
+struct ProposeBatchDev {
+    const void* views;         // nviews blocks of propose_view_bytes()
+    const uint64_t* tile_pfx;  // nviews + 1: first 128-ray tile of every view
+    const uint64_t* low_pfx;   // nviews + 1: first low-resolution pixel of every view
+    int nviews;
+    uint64_t ntiles, nlow;
+    const void* weights;       // the proposal's BF16 weight image (a copy the batch owns)
+    const float* bias;
+};
+size_t propose_view_bytes();
+uint64_t propose_low_pixels(const fm_camera* cam);
+// margins = {margin_lo, margin_hi, min_near} of the proposal (proposal_weights reads them)
+void propose_view(const fm_scene* s, const fm_camera* cam, const fm_march_params* p, const float margins[3],
+                  const float* zbuf, float* zlow, int2* ivl, void* out);
+// copies the proposal's weights and bias into buffers the caller owns, and its margins
+int proposal_weights(fm_ctx* ctx, const fm_proposal* pr, DevBuf& w, DevBuf& b, float margins[3], cudaStream_t st);
+int launch_propose_batch(fm_ctx* ctx, const ProposeBatchDev& b, cudaStream_t st);
 
 int set_err(fm_ctx* ctx, int code, const std::string& msg);
 int cuda_err(fm_ctx* ctx, cudaError_t e, const char* what);

@@ -803,7 +803,7 @@ __device__ __forceinline__ void march_tile(const MarchArgs& a, const Queue& q, b
     r.mode = kWhole;
     if (valid && z != 1.0f) {
         ray_setup(a, px, py, z, r.p, r.s);
-        if (LEARNED) {
+        if (LEARNED && a.ivl) {  // a batch may mix views with and without a proposal
             // start at sample ks of the plain march (the same FP32 additions),
             // evaluate samples ks+1 .. kf
             const int2 iv = a.ivl[idx];

@@ -140,6 +140,7 @@ __global__ void k_lowres(const float* __restrict__ z, int W, int Hh, int lw, int
 
 // ---- features -------------------------------------------------------------------
 
+
 struct FeatArgs {
     float ipv[16];
     float cam[3];
@@ -334,14 +335,23 @@ __device__ __forceinline__ void store8(uint8_t* tile, int row, int k0, int K, co
     *(uint4*)(tile + canon_off(row, k0, K)) = q;
 }
 
-struct ProposeArgs {
+// One view of the proposal: its features, interval settings and outputs.
+struct ProposeView {
     FeatArgs f;
     IvlArgs v;
-    const uint8_t* __restrict__ weights;  // kWeightBytes: W1, W2, W3 in the shared-memory image
-    const float* __restrict__ bias;       // b1[64], b2[64], b3[2]
     int2* __restrict__ ivl;
     float2* __restrict__ raw;             // optional (near, far) outputs
     uint64_t npx;
+};
+
+struct ProposeArgs {
+    ProposeView one;                      // single view
+    const ProposeView* __restrict__ views;  // batch: per-view blocks (device)
+    const uint64_t* __restrict__ tile_pfx;  // batch: first tile of every view, nviews + 1
+    int nviews;
+    uint64_t ntiles;                      // tiles of 128 rays over all views
+    const uint8_t* __restrict__ weights;  // kWeightBytes: W1, W2, W3 in the shared-memory image
+    const float* __restrict__ bias;       // b1[64], b2[64], b3[2]
     unsigned int* status;
 };
 
@@ -359,6 +369,103 @@ __device__ __forceinline__ void hidden_epilogue(uint32_t tmem_row, uint32_t c0, 
     }
 }
 
+// Shared-memory and tensor-memory state of a k_propose CTA.
+struct ProposeCta {
+    uint8_t* sm;
+    uint32_t sbase, bar, tmem, tmem_row;
+};
+
+// Tile `lt` (128 rays) of view pv: features -> three MMA layers -> intervals.
+// Uniform over the CTA; false when an MMA did not complete in time.
+__device__ __forceinline__ bool propose_tile(const ProposeView& pv, uint64_t lt, const ProposeCta& c, uint32_t& phase) {
+    const int tid = threadIdx.x;
+    const float* bias = (const float*)(c.sm + kSmBias);
+    uint8_t* a1 = c.sm + kSmA1;
+    uint8_t* a2 = c.sm + kSmA2;
+    const uint32_t a1s = c.sbase + kSmA1, a2s = c.sbase + kSmA2;
+    const uint32_t w1s = c.sbase + kSmW1, w2s = c.sbase + kSmW2, w3s = c.sbase + kSmW3;
+    const uint64_t pix = lt * kRows + (uint64_t)tid;
+    float f[kF], t0 = 0.0f;
+    bool has = false;
+    if (pix < pv.npx) has = ray_features(pv.f, (int)(pix % pv.f.W), (int)(pix / pv.f.W), f, t0);
+    else {
+#pragma unroll
+        for (int j = 0; j < kF; ++j) f[j] = 0.0f;
+    }
+    // a tile without any ray needs no network
+    if (!__syncthreads_or(has)) {
+        if (pix < pv.npx) {
+            pv.ivl[pix] = make_int2(0, -1);
+            if (pv.raw) pv.raw[pix] = make_float2(0.0f, 0.0f);
+        }
+        return true;
+    }
+#pragma unroll
+    for (int k = 0; k < kF; k += 8) store8(a1, tid, k, kF, f + k);
+    // layer 1: D[:, 0:64) = A1 (128 x 32) * W1^T
+    fence_async_smem();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    if (tid == 0) {
+#pragma unroll
+        for (int kk = 0; kk < kF / 16; ++kk)
+            mma_bf16(c.tmem, mdesc(a1s + 256 * kk, 128, (kF / 8) * 128), mdesc(w1s + 256 * kk, 128, (kF / 8) * 128),
+                     idesc_bf16(kH), kk > 0 ? 1u : 0u);
+        mma_commit(c.bar);
+    }
+    bool ok = __syncthreads_and(mbar_wait(c.bar, phase));
+    phase ^= 1;
+    if (!ok) return false;
+    tc_after();
+    hidden_epilogue(c.tmem_row, 0, bias, a2, tid);
+    // layer 2: D[:, 64:128) = H1 (128 x 64) * W2^T
+    fence_async_smem();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    if (tid == 0) {
+#pragma unroll
+        for (int kk = 0; kk < kH / 16; ++kk)
+            mma_bf16(c.tmem + kH, mdesc(a2s + 256 * kk, 128, (kH / 8) * 128),
+                     mdesc(w2s + 256 * kk, 128, (kH / 8) * 128), idesc_bf16(kH), kk > 0 ? 1u : 0u);
+        mma_commit(c.bar);
+    }
+    ok = __syncthreads_and(mbar_wait(c.bar, phase));
+    phase ^= 1;
+    if (!ok) return false;
+    tc_after();
+    hidden_epilogue(c.tmem_row, kH, bias + kH, a2, tid);
+    // layer 3: D[:, 0:16) = H2 (128 x 64) * W3^T (rows 2..15 of W3 are zero)
+    fence_async_smem();
+    tc_before();
+    __syncthreads();
+    tc_after();
+    if (tid == 0) {
+#pragma unroll
+        for (int kk = 0; kk < kH / 16; ++kk)
+            mma_bf16(c.tmem, mdesc(a2s + 256 * kk, 128, (kH / 8) * 128), mdesc(w3s + 256 * kk, 128, (kH / 8) * 128),
+                     idesc_bf16(kN3), kk > 0 ? 1u : 0u);
+        mma_commit(c.bar);
+    }
+    ok = __syncthreads_and(mbar_wait(c.bar, phase));
+    phase ^= 1;
+    if (!ok) return false;
+    tc_after();
+    float o[16];
+    tmem_ld16(c.tmem_row, o);
+    if (pix < pv.npx) {
+        const float y0 = o[0] + bias[2 * kH], y1 = o[1] + bias[2 * kH + 1];
+        pv.ivl[pix] = has ? to_interval(pv.v, y0, y1) : make_int2(0, -1);
+        if (pv.raw) pv.raw[pix] = make_float2(y0, y1);
+    }
+    tc_before();
+    __syncthreads();
+    tc_after();
+    return true;
+}
+
+template <bool BATCH>
 __global__ void __launch_bounds__(kRows) k_propose(const ProposeArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
     const int tid = threadIdx.x, warp = tid >> 5;
@@ -369,14 +476,16 @@ __global__ void __launch_bounds__(kRows) k_propose(const ProposeArgs a) {
         float* b = (float*)(sm + kSmBias);
         for (int i = tid; i < 2 * kH + kO; i += kRows) b[i] = a.bias[i];
     }
-    const uint32_t sbase = smem_u32(sm);
-    const uint32_t bar = sbase + kSmBar;
+    ProposeCta c;
+    c.sm = sm;
+    c.sbase = smem_u32(sm);
+    c.bar = c.sbase + kSmBar;
     if (tid == 0) {
-        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(c.bar) : "memory");
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == 0) {
-        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(sbase + kSmTmem),
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(c.sbase + kSmTmem),
                      "r"(kTmemCols)
                      : "memory");
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
@@ -385,96 +494,24 @@ __global__ void __launch_bounds__(kRows) k_propose(const ProposeArgs a) {
     tc_before();
     __syncthreads();
     tc_after();
-    const uint32_t tmem = *(volatile uint32_t*)(sm + kSmTmem);
-    const uint32_t tmem_row = tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
-    const float* bias = (const float*)(sm + kSmBias);
-    uint8_t* a1 = sm + kSmA1;
-    uint8_t* a2 = sm + kSmA2;
-    const uint32_t a1s = sbase + kSmA1, a2s = sbase + kSmA2;
-    const uint32_t w1s = sbase + kSmW1, w2s = sbase + kSmW2, w3s = sbase + kSmW3;
+    c.tmem = *(volatile uint32_t*)(sm + kSmTmem);
+    c.tmem_row = c.tmem + ((uint32_t)(warp * 32) << 16);  // this warp's 32 lanes
     uint32_t phase = 0;
     bool ok = true;
-    const uint64_t ntiles = (a.npx + kRows - 1) / kRows;
-    for (uint64_t t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        const uint64_t pix = t * kRows + (uint64_t)tid;
-        float f[kF], t0 = 0.0f;
-        bool has = false;
-        if (pix < a.npx) has = ray_features(a.f, (int)(pix % a.f.W), (int)(pix / a.f.W), f, t0);
-        else {
-#pragma unroll
-            for (int j = 0; j < kF; ++j) f[j] = 0.0f;
-        }
-        // a tile without any ray needs no network
-        if (!__syncthreads_or(has)) {
-            if (pix < a.npx) {
-                a.ivl[pix] = make_int2(0, -1);
-                if (a.raw) a.raw[pix] = make_float2(0.0f, 0.0f);
+    for (uint64_t t = blockIdx.x; t < a.ntiles && ok; t += gridDim.x) {
+        if (BATCH) {
+            int lo = 0, hi = a.nviews - 1;  // the view of tile t: largest v with tile_pfx[v] <= t
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (a.tile_pfx[mid] <= t) lo = mid;
+                else hi = mid - 1;
             }
-            continue;
+            ok = propose_tile(a.views[lo], t - a.tile_pfx[lo], c, phase);
+        } else {
+            ok = propose_tile(a.one, t, c, phase);
         }
-#pragma unroll
-        for (int k = 0; k < kF; k += 8) store8(a1, tid, k, kF, f + k);
-        // layer 1: D[:, 0:64) = A1 (128 x 32) * W1^T
-        fence_async_smem();
-        tc_before();
-        __syncthreads();
-        tc_after();
-        if (tid == 0) {
-#pragma unroll
-            for (int kk = 0; kk < kF / 16; ++kk)
-                mma_bf16(tmem, mdesc(a1s + 256 * kk, 128, (kF / 8) * 128), mdesc(w1s + 256 * kk, 128, (kF / 8) * 128),
-                         idesc_bf16(kH), kk > 0 ? 1u : 0u);
-            mma_commit(bar);
-        }
-        ok = __syncthreads_and(mbar_wait(bar, phase));
-        phase ^= 1;
-        if (!ok) break;
-        tc_after();
-        hidden_epilogue(tmem_row, 0, bias, a2, tid);
-        // layer 2: D[:, 64:128) = H1 (128 x 64) * W2^T
-        fence_async_smem();
-        tc_before();
-        __syncthreads();
-        tc_after();
-        if (tid == 0) {
-#pragma unroll
-            for (int kk = 0; kk < kH / 16; ++kk)
-                mma_bf16(tmem + kH, mdesc(a2s + 256 * kk, 128, (kH / 8) * 128),
-                         mdesc(w2s + 256 * kk, 128, (kH / 8) * 128), idesc_bf16(kH), kk > 0 ? 1u : 0u);
-            mma_commit(bar);
-        }
-        ok = __syncthreads_and(mbar_wait(bar, phase));
-        phase ^= 1;
-        if (!ok) break;
-        tc_after();
-        hidden_epilogue(tmem_row, kH, bias + kH, a2, tid);
-        // layer 3: D[:, 0:16) = H2 (128 x 64) * W3^T (rows 2..15 of W3 are zero)
-        fence_async_smem();
-        tc_before();
-        __syncthreads();
-        tc_after();
-        if (tid == 0) {
-#pragma unroll
-            for (int kk = 0; kk < kH / 16; ++kk)
-                mma_bf16(tmem, mdesc(a2s + 256 * kk, 128, (kH / 8) * 128), mdesc(w3s + 256 * kk, 128, (kH / 8) * 128),
-                         idesc_bf16(kN3), kk > 0 ? 1u : 0u);
-            mma_commit(bar);
-        }
-        ok = __syncthreads_and(mbar_wait(bar, phase));
-        phase ^= 1;
-        if (!ok) break;
-        tc_after();
-        float o[16];
-        tmem_ld16(tmem_row, o);
-        if (pix < a.npx) {
-            const float y0 = o[0] + bias[2 * kH], y1 = o[1] + bias[2 * kH + 1];
-            a.ivl[pix] = has ? to_interval(a.v, y0, y1) : make_int2(0, -1);
-            if (a.raw) a.raw[pix] = make_float2(y0, y1);
-        }
-        tc_before();
-        __syncthreads();
-        tc_after();
     }
+    const uint32_t tmem = c.tmem, bar = c.bar;
     if (!ok) {
         // an MMA did not complete in time: report, give the last commit another
         // bounded wait, then release the tensor memory
@@ -695,23 +732,18 @@ int ensure_occupancy(fm_ctx* ctx, fm_scene* s, cudaStream_t st) {
 
 namespace {
 
-int feat_args(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const float* zbuf, cudaStream_t st,
-              FeatArgs& f) {
+FeatArgs make_feat(const fm_scene* s, const fm_camera* cam, const float* zbuf, const float* zlow) {
+    FeatArgs f;
     const int W = cam->width, Hh = cam->height;
-    const int lw = (W + kLow - 1) / kLow, lh = (Hh + kLow - 1) / kLow;
-    if (!grow_buf(ctx->prop_low, (size_t)lw * lh * sizeof(float)))
-        return set_err(ctx, FM_ERR_OOM, "low-resolution depth allocation failed");
-    k_lowres<<<(lw * lh + 255) / 256, 256, 0, st>>>(zbuf, W, Hh, lw, lh, (float*)ctx->prop_low.p);
-    FM_CUDA(ctx, cudaGetLastError());
     for (int i = 0; i < 16; ++i) f.ipv[i] = cam->inv_proj_view[i];
     for (int k = 0; k < 3; ++k) f.cam[k] = cam->position[k];
     f.twoWinv = 2.0f / (float)W;
     f.twoHinv = 2.0f / (float)Hh;
     f.W = W;
     f.Hh = Hh;
-    f.lw = lw;
+    f.lw = (W + kLow - 1) / kLow;
     f.zbuf = zbuf;
-    f.zlow = (const float*)ctx->prop_low.p;
+    f.zlow = zlow;
     f.occ = (const __half*)s->d_occ;
     for (int k = 0; k < 3; ++k) {
         const float ext = s->max[k] - s->min[k];
@@ -722,10 +754,106 @@ int feat_args(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const float*
     }
     f.H = s->support;
     f.invH = 1.0f / s->support;
+    return f;
+}
+
+IvlArgs make_ivl(const fm_scene* s, const fm_march_params* p, const fm_proposal* pr) {
+    IvlArgs v;
+    v.H = s->support;
+    v.step = p->step_size;
+    v.max_steps = p->max_steps;
+    v.margin_lo = pr->margin_lo;
+    v.margin_hi = pr->margin_hi;
+    v.min_near = pr->min_near;
+    return v;
+}
+
+int feat_args(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const float* zbuf, cudaStream_t st,
+              FeatArgs& f) {
+    const int W = cam->width, Hh = cam->height;
+    const int lw = (W + kLow - 1) / kLow, lh = (Hh + kLow - 1) / kLow;
+    if (!grow_buf(ctx->prop_low, (size_t)lw * lh * sizeof(float)))
+        return set_err(ctx, FM_ERR_OOM, "low-resolution depth allocation failed");
+    k_lowres<<<(lw * lh + 255) / 256, 256, 0, st>>>(zbuf, W, Hh, lw, lh, (float*)ctx->prop_low.p);
+    FM_CUDA(ctx, cudaGetLastError());
+    f = make_feat(s, cam, zbuf, (const float*)ctx->prop_low.p);
     return FM_OK;
 }
 
+// Batched low-resolution depth: thread per low-resolution pixel of all views.
+__global__ void k_lowres_b(const ProposeView* __restrict__ views, const uint64_t* __restrict__ low_pfx, int nviews,
+                           uint64_t nlow) {
+    const uint64_t t = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (t >= nlow) return;
+    int lo = 0, hi = nviews - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (low_pfx[mid] <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    const FeatArgs& f = views[lo].f;
+    const uint64_t l = t - low_pfx[lo];
+    const int bx = (int)(l % (uint64_t)f.lw), by = (int)(l / (uint64_t)f.lw);
+    float m = 1.0f;
+    for (int y = by * kLow; y < min(by * kLow + kLow, f.Hh); ++y)
+        for (int x = bx * kLow; x < min(bx * kLow + kLow, f.W); ++x) m = fminf(m, f.zbuf[(uint64_t)y * f.W + x]);
+    const_cast<float*>(f.zlow)[l] = m;
+}
+
 }  // namespace
+
+size_t propose_view_bytes() { return sizeof(ProposeView); }
+
+uint64_t propose_low_pixels(const fm_camera* cam) {
+    return (uint64_t)((cam->width + kLow - 1) / kLow) * (uint64_t)((cam->height + kLow - 1) / kLow);
+}
+
+void propose_view(const fm_scene* s, const fm_camera* cam, const fm_march_params* p, const float margins[3],
+                  const float* zbuf, float* zlow, int2* ivl, void* out) {
+    fm_proposal pr;
+    pr.margin_lo = margins[0];
+    pr.margin_hi = margins[1];
+    pr.min_near = margins[2];
+    ProposeView v;
+    v.f = make_feat(s, cam, zbuf, zlow);
+    v.v = make_ivl(s, p, &pr);
+    v.ivl = ivl;
+    v.raw = nullptr;
+    v.npx = (uint64_t)cam->width * cam->height;
+    std::memcpy(out, &v, sizeof(v));
+}
+
+int proposal_weights(fm_ctx* ctx, const fm_proposal* pr, DevBuf& w, DevBuf& b, float margins[3], cudaStream_t st) {
+    margins[0] = pr->margin_lo;
+    margins[1] = pr->margin_hi;
+    margins[2] = pr->min_near;
+    if (!grow_buf(w, kWeightBytes) || !grow_buf(b, (2 * kH + kO) * sizeof(float)))
+        return set_err(ctx, FM_ERR_OOM, "proposal copy allocation failed");
+    FM_CUDA(ctx, cudaMemcpyAsync(w.p, pr->d_weights, kWeightBytes, cudaMemcpyDeviceToDevice, st));
+    FM_CUDA(ctx, cudaMemcpyAsync(b.p, pr->d_bias, (2 * kH + kO) * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    return FM_OK;
+}
+
+int launch_propose_batch(fm_ctx* ctx, const ProposeBatchDev& b, cudaStream_t st) {
+    if (b.nlow)
+        k_lowres_b<<<(unsigned)((b.nlow + 255) / 256), 256, 0, st>>>((const ProposeView*)b.views, b.low_pfx,
+                                                                     b.nviews, b.nlow);
+    ProposeArgs a;
+    std::memset(&a, 0, sizeof(a));
+    a.views = (const ProposeView*)b.views;
+    a.tile_pfx = b.tile_pfx;
+    a.nviews = b.nviews;
+    a.ntiles = b.ntiles;
+    a.weights = (const uint8_t*)b.weights;
+    a.bias = b.bias;
+    a.status = ctx->d_status;
+    FM_CUDA(ctx, cudaFuncSetAttribute(k_propose<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmRequest));
+    uint64_t grid = (uint64_t)ctx->sm_count * 4;
+    if (grid > b.ntiles) grid = b.ntiles;
+    if (grid) k_propose<true><<<(unsigned)grid, kRows, kSmRequest, st>>>(a);
+    FM_CUDA(ctx, cudaGetLastError());
+    return FM_OK;
+}
 
 int launch_features(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const float* zbuf, float* feat, float* t0,
                     cudaStream_t st) {
@@ -744,24 +872,20 @@ int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_marc
     int rc = ensure_occupancy(ctx, s, st);
     if (rc) return rc;
     ProposeArgs a;
-    if ((rc = feat_args(ctx, s, cam, zbuf, st, a.f)) != FM_OK) return rc;
-    a.v.H = s->support;
-    a.v.step = p->step_size;
-    a.v.max_steps = p->max_steps;
-    a.v.margin_lo = pr->margin_lo;
-    a.v.margin_hi = pr->margin_hi;
-    a.v.min_near = pr->min_near;
+    std::memset(&a, 0, sizeof(a));
+    if ((rc = feat_args(ctx, s, cam, zbuf, st, a.one.f)) != FM_OK) return rc;
+    a.one.v = make_ivl(s, p, pr);
+    a.one.ivl = ivl;
+    a.one.raw = raw;
+    a.one.npx = (uint64_t)cam->width * cam->height;
+    a.ntiles = (a.one.npx + kRows - 1) / kRows;
     a.weights = (const uint8_t*)pr->d_weights;
     a.bias = pr->d_bias;
-    a.ivl = ivl;
-    a.raw = raw;
-    a.npx = (uint64_t)cam->width * cam->height;
     a.status = ctx->d_status;
-    FM_CUDA(ctx, cudaFuncSetAttribute(k_propose, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmRequest));
-    const uint64_t tiles = (a.npx + kRows - 1) / kRows;
+    FM_CUDA(ctx, cudaFuncSetAttribute(k_propose<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmRequest));
     uint64_t grid = (uint64_t)ctx->sm_count * 4;
-    if (grid > tiles) grid = tiles;
-    k_propose<<<(unsigned)grid, kRows, kSmRequest, st>>>(a);
+    if (grid > a.ntiles) grid = a.ntiles;
+    k_propose<false><<<(unsigned)grid, kRows, kSmRequest, st>>>(a);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }

@@ -217,3 +217,70 @@ def test_batch_rejects_bad_views(fmlib, ctx, small_batch):
         fmlib.Batch(ctx, [fmlib.View(s, cam, params, **o)], tile_config=dict(tile_width=3))
     with pytest.raises(ValueError):
         fmlib.View(s, cam, params, position=np.zeros((cam.width * cam.height, 4), np.float32)).cstruct()
+
+
+@pytest.mark.parametrize("which", ["constant", "trained"])
+def test_batch_with_learned_views(fmlib, ctx, small_batch, which):
+    """Views with FM_MARCH_PROPOSAL in a batch equal the same learned views marched alone.
+
+    Half the views use the proposal, the others march every sample; the batch
+    keeps its own copy of the proposal, so destroying the context's proposal
+    after fm_batch_create changes nothing.
+    """
+    from fluidmarch import proposal as prop_mod
+    if which == "constant":
+        P = np.zeros(fmlib.FM_PROPOSAL_PARAMS, np.float32)
+        P[-2:] = (0.6, 3.0)  # every ray: samples ks+1 .. kf with ks = floor(0.6 H / step)
+        pr = fmlib.Proposal(ctx, P)
+    else:
+        P, _ = prop_mod.load()
+        pr = fmlib.Proposal(ctx, P, margin_lo=0.5, margin_hi=0.5, min_near=2.0)
+    fmlib.set_proposal(ctx, pr)
+    items = []
+    for i, (sc, s, cam, params) in enumerate(small_batch):
+        learned = i % 2 == 0
+        skip = params.skip_mode if not learned or params.skip_mode != fmlib.FM_SKIP_REFERENCE else fmlib.FM_SKIP_EXACT
+        p = fmlib.MarchParams(params.iso, params.step, params.max_steps, params.bisect, skip, proposal=learned)
+        items.append((sc, s, cam, p))
+    try:
+        want = [single(fmlib, s, cam, p) for sc, s, cam, p in items]
+        views, outs = make_views(fmlib, items)
+        b = fmlib.Batch(ctx, views)
+        fmlib.set_proposal(ctx, None)
+        pr.close()
+        ctx.set_stats(True)
+        try:
+            b.run()
+            ctx.sync()
+            st = ctx.stats()
+        finally:
+            ctx.set_stats(False)
+        for i in range(len(items)):
+            assert_same(host(outs[i]), want[i], f"{which} view {i}")
+        assert st["proposed"] > 0
+        assert st["rays"] == b.info()["pixels"]
+        b.close()
+    finally:
+        fmlib.set_proposal(ctx, None)
+        pr.close()
+
+
+def test_batch_learned_view_needs_a_proposal(fmlib, ctx, small_batch):
+    sc, s, cam, params = small_batch[1]
+    fmlib.set_proposal(ctx, None)
+    o = device_outputs(cam)
+    p = fmlib.MarchParams(params.iso, params.step, params.max_steps, 8, fmlib.FM_SKIP_EXACT, proposal=True)
+    with pytest.raises(fmlib.FmError):
+        fmlib.Batch(ctx, [fmlib.View(s, cam, p, **o)])
+    pr = fmlib.Proposal(ctx, np.zeros(fmlib.FM_PROPOSAL_PARAMS, np.float32))
+    fmlib.set_proposal(ctx, pr)
+    try:
+        bad = fmlib.MarchParams(params.iso, params.step, params.max_steps, 8, fmlib.FM_SKIP_REFERENCE, proposal=True)
+        with pytest.raises(fmlib.FmError):
+            fmlib.Batch(ctx, [fmlib.View(s, cam, bad, **o)])
+        aniso = fmlib.MarchParams(params.iso, params.step, params.max_steps, 8, fmlib.FM_SKIP_OFF, anisotropic=True)
+        with pytest.raises(fmlib.FmError):
+            fmlib.Batch(ctx, [fmlib.View(s, cam, aniso, **o)])
+    finally:
+        fmlib.set_proposal(ctx, None)
+        pr.close()
