@@ -205,6 +205,7 @@ struct fm_ctx {
     // intervals, occupancy counts, low-resolution depth, judge counters
     fm_proposal* proposal = nullptr;
     fm::DevBuf prop_ivl, prop_scratch, prop_low, prop_judge;
+    fm::DevBuf file_rec, file_xyz;  // particle-file loader: point records, gathered positions
     // live scenes of this context; fm_destroy frees the ones still alive
     std::vector<fm_scene*> scenes;
     // live batches of this context; fm_destroy frees the ones still alive

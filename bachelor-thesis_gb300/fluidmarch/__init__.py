@@ -44,6 +44,9 @@ EXPORTS = [
     "fm_proposal_create", "fm_proposal_destroy", "fm_set_proposal", "fm_proposal_features", "fm_proposal_intervals",
     "fm_judge", "fm_trainer_create", "fm_trainer_destroy", "fm_trainer_step", "fm_trainer_predict",
     "fm_trainer_params", "fm_density", "fm_set_anisotropy",
+    "fm_bgeo_read", "fm_gunzip", "fm_scene_create_bgeo", "fm_dataset_open", "fm_dataset_frames", "fm_dataset_path",
+    "fm_dataset_frame_info", "fm_dataset_max_particles", "fm_dataset_read", "fm_dataset_scene",
+    "fm_dataset_last_error", "fm_dataset_close",
 ]
 
 
@@ -56,6 +59,12 @@ class FmError(RuntimeError):
 class CCamera(C.Structure):
     _fields_ = [("view", C.c_float * 16), ("proj", C.c_float * 16), ("inv_proj_view", C.c_float * 16),
                 ("position", C.c_float * 3), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class CBgeoInfo(C.Structure):
+    _fields_ = [("points", C.c_uint64), ("record_words", C.c_uint32), ("attributes", C.c_uint32),
+                ("file_bytes", C.c_uint64), ("data_bytes", C.c_uint64), ("compressed", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class CMarchParams(C.Structure):
@@ -168,6 +177,22 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_trainer_step.argtypes = [vp, vp, vp, C.c_uint32, C.c_float, C.c_float, C.c_float, C.POINTER(C.c_float)]
     L.fm_trainer_predict.argtypes = [vp, vp, C.c_uint32, vp]
     L.fm_trainer_params.argtypes = [vp, vp]
+    L.fm_bgeo_read.argtypes = [C.c_char_p, vp, C.c_uint64, C.POINTER(CBgeoInfo), C.c_char_p, C.c_uint64]
+    L.fm_gunzip.argtypes = [vp, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.fm_scene_create_bgeo.argtypes = [vp, C.c_char_p, C.c_float, C.POINTER(vp)]
+    L.fm_dataset_open.argtypes = [C.c_char_p, C.c_char_p, C.c_int32, C.c_int32, C.POINTER(vp), C.c_char_p, C.c_uint64]
+    L.fm_dataset_frames.argtypes = [vp]
+    L.fm_dataset_frames.restype = C.c_int32
+    L.fm_dataset_path.argtypes = [vp, C.c_int32]
+    L.fm_dataset_path.restype = C.c_char_p
+    L.fm_dataset_frame_info.argtypes = [vp, C.c_int32, C.POINTER(CBgeoInfo)]
+    L.fm_dataset_max_particles.argtypes = [vp, C.POINTER(C.c_uint64)]
+    L.fm_dataset_read.argtypes = [vp, C.c_int32, vp, C.c_uint64, C.POINTER(C.c_uint64)]
+    L.fm_dataset_scene.argtypes = [vp, vp, C.c_int32, C.c_float, C.POINTER(vp)]
+    L.fm_dataset_last_error.argtypes = [vp]
+    L.fm_dataset_last_error.restype = C.c_char_p
+    L.fm_dataset_close.argtypes = [vp]
+    L.fm_dataset_close.restype = None
     _lib = L
     return L
 
@@ -287,6 +312,16 @@ class Scene:
         self.h = h
         self.support = float(support)
         ctx._scenes.add(self)
+
+    @classmethod
+    def wrap(cls, ctx: Context, handle, support: float) -> "Scene":
+        """A Scene object for a handle the library created (particle files, datasets)."""
+        s = cls.__new__(cls)
+        s.ctx = ctx
+        s.h = handle if isinstance(handle, C.c_void_p) else C.c_void_p(handle)
+        s.support = float(support)
+        ctx._scenes.add(s)
+        return s
 
     def update(self, xyz, stride: int = 3):
         p, mem = _ptr(xyz)

@@ -390,6 +390,59 @@ int fm_trainer_step(fm_trainer* t, const float* features, const float* targets, 
 int fm_trainer_predict(fm_trainer* t, const float* features, uint32_t n, float* out);
 int fm_trainer_params(fm_trainer* t, float* host_params);
 
+/* ---- Particle files (Dataset.cpp:169-227, Dataset::ReadFile :292-306) ----
+ * Houdini classic BGEO, version 5, plain or gzip-compressed (detected by the
+ * gzip magic), the format the reference reads through Partio
+ * (vendor/partio/src/io/BGEO.cpp readBGEO): the position of every point (the
+ * first three words of its big-endian record).  Other point attributes are
+ * skipped, as Dataset::ReadFile ignores them. */
+typedef struct fm_bgeo_info {
+    uint64_t points;
+    uint32_t record_words;  /* 32-bit words per point record: 4 (x y z w) + attribute sizes */
+    uint32_t attributes;    /* point attributes besides position */
+    uint64_t file_bytes;
+    uint64_t data_bytes;    /* after decompression (0 when only the header was read) */
+    int32_t compressed;     /* 1: gzip */
+    int32_t reserved;
+} fm_bgeo_info;
+
+/* Host read, no GPU needed: the positions of the first min(capacity, points)
+ * points into xyz (3 floats each; xyz NULL: header only).  err (may be NULL):
+ * the message of a failure. */
+int fm_bgeo_read(const char* path, float* xyz, uint64_t capacity, fm_bgeo_info* info, char* err, uint64_t err_len);
+/* First member of a gzip stream (RFC 1952), CRC-32 and length checked.
+ * out_len = the decoded size; FM_ERR_INVALID when it exceeds out_cap (nothing
+ * copied) or the stream is corrupt.  No GPU needed. */
+int fm_gunzip(const void* in, uint64_t in_len, void* out, uint64_t out_cap, uint64_t* out_len);
+/* A scene from a BGEO file: decompressed on the host, the point records
+ * copied to the device, positions byte-swapped by a kernel, then the grid
+ * build of fm_scene_create (replaces Partio::read + Frame::Frame).  Synchronous. */
+int fm_scene_create_bgeo(fm_ctx* ctx, const char* path, float support_radius, fm_scene** out);
+
+/* A numbered series prefix + i + suffix, i = 1, 2, ... until a file is
+ * missing or i > count (count < 0: no limit), as the Dataset constructor
+ * collects it.  threads > 0 host threads decode the 2 * threads frames after
+ * the one last asked for (autoplay, AdvancedRenderer.cpp:281-297). */
+typedef struct fm_dataset fm_dataset;
+int fm_dataset_open(const char* prefix, const char* suffix, int32_t count, int32_t threads, fm_dataset** out,
+                    char* err, uint64_t err_len);
+int32_t fm_dataset_frames(const fm_dataset* ds);
+const char* fm_dataset_path(const fm_dataset* ds, int32_t i);
+/* Header of frame i (data_bytes 0). */
+int fm_dataset_frame_info(fm_dataset* ds, int32_t i, fm_bgeo_info* info);
+/* Largest particle count over the frames (Dataset::MaxParticles, Dataset.cpp:222-224). */
+int fm_dataset_max_particles(fm_dataset* ds, uint64_t* out);
+/* Positions of frame i on the host (n = its particle count). */
+int fm_dataset_read(fm_dataset* ds, int32_t i, float* xyz, uint64_t capacity, uint64_t* n);
+/* Frame i as a scene.  *scene NULL: created.  Otherwise rebuilt in place
+ * (fm_scene_update) when frame i has at most the particles it was created
+ * with and the same support radius, else replaced (the handle changes;
+ * batches holding the old one must be recreated).  Synchronous.  Errors go
+ * to fm_last_error(ctx). */
+int fm_dataset_scene(fm_dataset* ds, fm_ctx* ctx, int32_t i, float support_radius, fm_scene** scene);
+const char* fm_dataset_last_error(const fm_dataset* ds);
+void fm_dataset_close(fm_dataset* ds);
+
 /* Library version (major * 10000 + minor * 100 + patch). */
 int fm_version(void);
 

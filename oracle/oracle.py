@@ -106,6 +106,12 @@ def ref():
         R.ref_gradW.argtypes = [C.c_float] * 4 + [_f32p]
         R.ref_query_cells.argtypes = [_f32p, C.c_int64, C.c_float, _f32p, C.c_int64,
                                       np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")]
+        R.ref_bgeo_positions.restype = C.c_int64
+        R.ref_bgeo_positions.argtypes = [C.c_char_p, C.c_void_p, C.c_int64]
+        R.ref_bgeo_write.argtypes = [C.c_char_p, _f32p, C.c_int64, C.c_int32]
+        R.ref_dataset_load.restype = C.c_int32
+        R.ref_dataset_load.argtypes = [C.c_char_p, C.c_char_p, C.c_int32, C.c_float, C.c_void_p, C.c_int32,
+                                       C.POINTER(C.c_int64), C.c_void_p, C.c_int64]
         _ref = R
     return _ref
 
@@ -278,3 +284,34 @@ def ref_march(xyz: np.ndarray, support: float, cam, depth: np.ndarray, max_steps
         raise RuntimeError("reference march rejected its input")
     return {"position": pos, "normal": nrm, "sorted": srt, "grid": grid, "seconds": secs,
             "build_seconds": build_s.value}
+
+
+def ref_bgeo_positions(path: str) -> np.ndarray:
+    """Positions of a particle file as the reference reads it (Partio::read + Dataset::ReadFile)."""
+    R = ref()
+    n = R.ref_bgeo_positions(path.encode(), None, 0)
+    if n < 0:
+        raise IOError(f"Partio could not read {path}")
+    out = np.zeros((n, 3), np.float32)
+    R.ref_bgeo_positions(path.encode(), out.ctypes.data, n)
+    return out
+
+
+def ref_bgeo_write(path: str, xyz: np.ndarray, compressed: bool) -> None:
+    """A particle file written by the reference's Partio."""
+    x = np.ascontiguousarray(xyz, np.float32).reshape(-1)
+    ref().ref_bgeo_write(path.encode(), x, x.size // 3, int(compressed))
+
+
+def ref_dataset_load(prefix: str, suffix: str, count: int, radius: float, cap_points: int):
+    """(frames, counts, max_particles, xyz of all frames) of the reference's Dataset constructor, or None."""
+    R = ref()
+    counts = np.zeros(4096, np.int64)
+    mp = C.c_int64()
+    xyz = np.zeros((cap_points, 3), np.float32)
+    nf = R.ref_dataset_load(prefix.encode(), suffix.encode(), int(count), float(radius), counts.ctypes.data,
+                            counts.size, C.byref(mp), xyz.ctypes.data, xyz.size)
+    if nf < 0:
+        return None
+    return nf, counts[:nf].copy(), int(mp.value), xyz
+

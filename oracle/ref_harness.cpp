@@ -13,6 +13,11 @@
 // done while a worker may still be writing its last pixel; Exit waits for it).
 // Pixel W*H-1 is never marched by the reference (ThreadPool.cpp:50); the
 // output buffers are zeroed first so that pixel reads as a miss.
+//
+// The reference's vendored Partio (vendor/partio/src, compiled unmodified
+// against the system zlib) is linked in, so the Dataset constructor reads
+// particle files as the application does; ref_bgeo_* below pin the library's
+// own BGEO reader against it.
 
 #include <engine/hzpch.h>
 
@@ -31,10 +36,6 @@ float RandomFloat(float min, float max) { return min + (max - min) * 0.5f; }
 
 CameraController3D::CameraController3D(Camera3D& camera) : Camera(camera) {}
 
-namespace Partio
-{
-ParticlesDataMutable* read(const char*, bool, std::ostream&) { return nullptr; }
-}
 
 namespace
 {
@@ -182,6 +183,75 @@ int ref_query_cells(const float* xyz, int64_t n, float radius, const float* quer
     }
     delete ds;
     return 0;
+}
+
+// ---- particle files --------------------------------------------------------
+
+// Partio::read + the copy of Dataset::ReadFile (Dataset.cpp:292-306): the
+// "position" of every particle, in file order.  Returns the particle count
+// (positions written up to cap), -1 when Partio returns no file.
+int64_t ref_bgeo_positions(const char* path, float* xyz, int64_t cap)
+{
+    Partio::ParticlesDataMutable* file = Partio::read(path, false);
+    if (!file) return -1;
+    Partio::ParticleAttribute attr;
+    file->attributeInfo("position", attr);
+    const int64_t n = file->numParticles();
+    for (int64_t i = 0; i < n && i < cap; ++i)
+    {
+        const float* p = file->data<float>(attr, int(i));
+        xyz[3 * i] = p[0];
+        xyz[3 * i + 1] = p[1];
+        xyz[3 * i + 2] = p[2];
+    }
+    file->release();
+    return n;
+}
+
+// Partio's writer: n positions as a BGEO file (gzip-compressed when
+// compressed != 0, Partio::write's forceCompressed).  0 on success.
+int ref_bgeo_write(const char* path, const float* xyz, int64_t n, int32_t compressed)
+{
+    Partio::ParticlesDataMutable* p = Partio::create();
+    Partio::ParticleAttribute attr = p->addAttribute("position", Partio::VECTOR, 3);
+    p->addParticles(int(n));
+    for (int64_t i = 0; i < n; ++i)
+    {
+        float* d = p->dataWrite<float>(attr, int(i));
+        d[0] = xyz[3 * i];
+        d[1] = xyz[3 * i + 1];
+        d[2] = xyz[3 * i + 2];
+    }
+    Partio::write(path, *p, compressed != 0, false);
+    p->release();
+    return 0;
+}
+
+// The reference's Dataset constructor over prefix + i + suffix (count < 0: no
+// limit), radius multiplier 2.  Returns the frame count (-1 when !Loaded);
+// counts[i] = particles of frame i (up to max_frames), *max_particles =
+// Dataset::MaxParticles, and xyz (cap floats) the frames' particles one after
+// another in the order the Frame keeps them (the search's spatial order).
+int32_t ref_dataset_load(const char* prefix, const char* suffix, int32_t count, float radius, int64_t* counts,
+                         int32_t max_frames, int64_t* max_particles, float* xyz, int64_t cap)
+{
+    Dataset ds(prefix, suffix, radius, 2.0f, count);
+    if (!ds.Loaded) return -1;
+    int64_t at = 0;
+    for (size_t f = 0; f < ds.Frames.size(); ++f)
+    {
+        const auto& ps = ds.Frames[f].m_Particles;
+        if (int32_t(f) < max_frames) counts[f] = int64_t(ps.size());
+        for (const auto& q : ps)
+        {
+            if (at + 3 > cap) break;
+            xyz[at++] = q.x;
+            xyz[at++] = q.y;
+            xyz[at++] = q.z;
+        }
+    }
+    *max_particles = int64_t(ds.MaxParticles);
+    return int32_t(ds.Frames.size());
 }
 
 }  // extern "C"
