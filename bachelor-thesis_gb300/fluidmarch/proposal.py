@@ -131,11 +131,14 @@ def collect(ctx: fm.Context, seeds, per_scene: int = 4096, n: int = 1_000_000, w
 
 
 def train(ctx: fm.Context, X, T, epochs: int = 12, batch: int = 8192, lr: float = 2e-3, tau_lo: float = 0.05,
-          tau_hi: float = 0.97, seed: int = 0, log=None) -> np.ndarray:
-    """Adam on the pinball loss with a cosine learning-rate decay; returns the FP32 parameters."""
+          tau_hi: float = 0.97, seed: int = 0, log=None, init=None) -> np.ndarray:
+    """Adam on the pinball loss with a cosine learning-rate decay; returns the FP32 parameters.
+
+    init: parameters to start from (fine-tuning), else a seeded initialisation.
+    """
     torch = _torch()
     n = X.shape[0]
-    tr = fm.Trainer(ctx, seed=seed)
+    tr = fm.Trainer(ctx, seed=seed, init=init)
     g = torch.Generator(device="cuda")
     g.manual_seed(int(seed))
     steps_per_epoch = max(1, n // batch)
