@@ -36,6 +36,11 @@ struct fm_batch {
     // intervals of every pixel
     fm::DevBuf pw, pb, pviews, ptile_pfx, plow_pfx, plow, pivl;
     float pmargins[3] = {0.0f, 0.0f, 0.0f};  // margin_lo, margin_hi, min_near of the copied proposal
+    // anisotropic views: the context's kernel settings at creation, per-view
+    // blocks, 32-pixel chunk prefixes, the chunk total
+    fm_aniso_params aniso{};
+    fm::DevBuf aviews, apfx;
+    uint32_t achunks = 0;
     fm::ProposeBatchDev pbatch{};
     uint32_t q_cap = 0;
     fm::MarchArgs launch{};  // launch-wide march arguments
@@ -67,7 +72,7 @@ void free_batch(fm_batch* b) {
     DevBuf* bufs[] = {&b->margs,  &b->tile_pfx, &b->sviews,  &b->pfx64,   &b->pfx_tiles, &b->depth,
                       &b->hiz,    &b->list,     &b->counters, &b->longq,  &b->longq2,    &b->rg_keys,
                       &b->rg_tmp, &b->rg_order, &b->pw,       &b->pb,     &b->pviews,    &b->ptile_pfx,
-                      &b->plow_pfx, &b->plow,   &b->pivl};
+                      &b->plow_pfx, &b->plow,   &b->pivl,     &b->aviews,   &b->apfx};
     for (DevBuf* d : bufs) cudaFree(d->p);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     delete b;
@@ -126,7 +131,7 @@ int prepare(fm_batch* b) {
     FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     // prefix sums
     std::vector<uint64_t> px(n + 1, 0), smp(n + 1, 0), pn(n + 1, 0);
-    std::vector<uint32_t> ht(n + 1, 0), tp(n + 1, 0);
+    std::vector<uint32_t> ht(n + 1, 0), tp(n + 1, 0), ap(n + 1, 0);
     const int tw = 1 << b->cfg.tw_log2, th = 32 >> b->cfg.tw_log2;
     for (int i = 0; i < n; ++i) {
         const fm_view& v = b->views[i];
@@ -135,11 +140,16 @@ int prepare(fm_batch* b) {
         smp[i + 1] = smp[i] + (v.scene->n + kSplatSample - 1) / kSplatSample;
         pn[i + 1] = pn[i] + v.scene->n;
         const uint64_t hz = ((w + kSplatHizTile - 1) / kSplatHizTile) * ((h + kSplatHizTile - 1) / kSplatHizTile);
-        const uint64_t tl = ((w + tw - 1) / tw) * ((h + th - 1) / th);
-        if ((uint64_t)ht[i] + hz >= (1ull << 32) || (uint64_t)tp[i] + tl >= (1ull << 31))
+        // anisotropic views are marched by their own launch in 32-pixel chunks
+        const bool an = (v.params.flags & FM_MARCH_ANISOTROPIC) != 0;
+        const uint64_t tl = an ? 0 : ((w + tw - 1) / tw) * ((h + th - 1) / th);
+        const uint64_t ch = an ? (w * h + 31) / 32 : 0;
+        if ((uint64_t)ht[i] + hz >= (1ull << 32) || (uint64_t)tp[i] + tl >= (1ull << 31) ||
+            (uint64_t)ap[i] + ch >= (1ull << 31))
             return set_err(ctx, FM_ERR_INVALID, "batch has too many tiles");
         ht[i + 1] = ht[i] + (uint32_t)hz;
         tp[i + 1] = tp[i] + (uint32_t)tl;
+        ap[i + 1] = ap[i] + (uint32_t)ch;
     }
     if (pn[n] >= (1ull << 32)) return set_err(ctx, FM_ERR_INVALID, "batch has 2^32 or more particles");
     const uint64_t entries = long_queue_entries(px[n], b->cfg.qlimit);
@@ -154,7 +164,8 @@ int prepare(fm_batch* b) {
         !grow_buf(b->pfx_tiles, 4ull * (n + 1)) || !grow_buf(b->depth, 4ull * std::max<uint64_t>(px[n], 1)) ||
         !grow_buf(b->hiz, 4ull * std::max<uint32_t>(ht[n], 1)) ||
         !grow_buf(b->list, 4ull * std::max<uint64_t>(pn[n], 1)) || !grow_buf(b->counters, 128) ||
-        !grow_buf(b->longq, 64ull * entries))
+        !grow_buf(b->longq, 64ull * entries) || !grow_buf(b->aviews, aniso_view_bytes() * n) ||
+        !grow_buf(b->apfx, 4ull * (n + 1)))
         return set_err(ctx, FM_ERR_OOM, "batch buffer allocation failed");
     const bool regroup = b->cfg.cap2 > 0;
     const uint64_t nkeys = (uint64_t)tp[n] + 1;
@@ -239,6 +250,15 @@ int prepare(fm_batch* b) {
     }
     b->pbatch = ProposeBatchDev{b->pviews.p, (const uint64_t*)b->ptile_pfx.p, (const uint64_t*)b->plow_pfx.p, np,
                                 ptp[np], plp[np], b->pw.p, (const float*)b->pb.p};
+    {
+        std::vector<uint8_t> blocks(aniso_view_bytes() * n, 0);
+        for (int i = 0; i < n; ++i)
+            if (b->views[i].params.flags & FM_MARCH_ANISOTROPIC)
+                aniso_view(b->views[i].scene, &b->aniso, blocks.data() + aniso_view_bytes() * i);
+        FM_CUDA(ctx, cudaMemcpy(b->aviews.p, blocks.data(), blocks.size(), cudaMemcpyHostToDevice));
+        FM_CUDA(ctx, cudaMemcpy(b->apfx.p, ap.data(), 4ull * (n + 1), cudaMemcpyHostToDevice));
+        b->achunks = ap[n];
+    }
     b->gens.resize(n);
     for (int i = 0; i < n; ++i) b->gens[i] = b->views[i].scene->gen;
     FM_CUDA(ctx, cudaMemcpy(b->margs.p, ma.data(), sizeof(MarchArgs) * n, cudaMemcpyHostToDevice));
@@ -275,8 +295,14 @@ int enqueue(fm_batch* b, cudaStream_t st, bool stats) {
     if (b->pbatch.nviews > 0 && (rc = launch_propose_batch(ctx, b->pbatch, st)) != FM_OK) return rc;
     MarchArgs a = b->launch;
     a.stats = stats ? ctx->d_stats : nullptr;
-    return launch_march_kernels(ctx, a, (const MarchArgs*)b->margs.p, (const uint32_t*)b->tile_pfx.p,
-                                (int)b->views.size(), st);
+    const int n = (int)b->views.size();
+    if (a.ntiles > 0 &&
+        (rc = launch_march_kernels(ctx, a, (const MarchArgs*)b->margs.p, (const uint32_t*)b->tile_pfx.p, n, st)))
+        return rc;
+    if (b->achunks == 0) return FM_OK;
+    a.tile_counter = (unsigned int*)b->counters.p + 7;
+    return launch_march_aniso_batch(ctx, a, (const MarchArgs*)b->margs.p, b->aviews.p, (const uint32_t*)b->apfx.p, n,
+                                    b->achunks, st);
 }
 
 int capture(fm_batch* b) {
@@ -344,8 +370,8 @@ int fm_batch_create(fm_ctx* ctx, const fm_view* views, int32_t n_views, const fm
             return set_err(ctx, FM_ERR_INVALID, "view scene is NULL or not a live scene of this context");
         int rc = check_params(ctx, &v.params);
         if (rc) return rc;
-        if (v.params.flags & ~FM_MARCH_PROPOSAL)
-            return set_err(ctx, FM_ERR_INVALID, "batched views are splatted and isotropic: flags may only hold FM_MARCH_PROPOSAL");
+        if (v.params.flags & FM_MARCH_EXTERNAL_DEPTH)
+            return set_err(ctx, FM_ERR_INVALID, "batched views are splatted: FM_MARCH_EXTERNAL_DEPTH is not allowed");
         if ((v.params.flags & FM_MARCH_PROPOSAL) && !ctx->proposal)
             return set_err(ctx, FM_ERR_INVALID, "FM_MARCH_PROPOSAL needs a proposal (fm_set_proposal)");
         if ((v.params.flags & FM_MARCH_PROPOSAL) && v.params.skip_mode == FM_SKIP_REFERENCE)
@@ -360,6 +386,7 @@ int fm_batch_create(fm_ctx* ctx, const fm_view* views, int32_t n_views, const fm
     b->ctx = ctx;
     b->views.assign(views, views + n_views);
     b->cfg = t;
+    b->aniso = ctx->aniso;
     if (cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
         free_batch(b);
         return set_err(ctx, FM_ERR_CUDA, "stream creation failed");

@@ -372,6 +372,14 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
 // The anisotropic march (march.cu), warp per ray.
 int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
                        const fm_aniso_params* ap, const MarchOutDev& o, cudaStream_t st);
+// Batched anisotropic march: per-view device blocks of aniso_view_bytes()
+// (aniso_view fills one), chunks of 32 pixels with prefix pfx over the views
+// (0 chunks for views without anisotropic rays); a carries the launch-wide
+// counter (tile_counter, zeroed by the caller), stats and status.
+size_t aniso_view_bytes();
+void aniso_view(const fm_scene* s, const fm_aniso_params* ap, void* out);
+int launch_march_aniso_batch(fm_ctx* ctx, const MarchArgs& a, const MarchArgs* d_views, const void* d_aviews,
+                             const uint32_t* d_pfx, int nviews, uint32_t nchunks, cudaStream_t st);
 // Density at n points (xyz at a stride of `stride` floats), device pointers.
 int launch_density(fm_ctx* ctx, const fm_scene* s, const float* d_xyz, uint64_t n, uint32_t stride, float* d_out,
                    cudaStream_t st);

@@ -48,6 +48,8 @@
 
 #include <cuda_runtime.h>
 
+#include <cstring>
+
 #include "fm_internal.cuh"
 
 namespace fm {
@@ -1463,78 +1465,101 @@ __device__ __forceinline__ void aniso_grad(const GridDev& g, const AnisoDev& an,
     oz = warp_sum(sz);
 }
 
-// Persistent warps take 32 consecutive pixels at a time and march the started
-// rays among them one after the other with the whole warp.
+struct AnisoCount {
+    uint64_t evals = 0, hits = 0, rays = 0, started = 0;
+};
+
+// One chunk of 32 consecutive pixels of view `a` (from pixel `base`): the
+// started rays among them are marched one after the other with the whole warp.
 template <bool STATS>
-__global__ void __launch_bounds__(kThreads) k_march_aniso(const MarchArgs a, const AnisoDev an) {
+__device__ __forceinline__ void aniso_chunk(const MarchArgs& a, const AnisoDev& an, uint64_t base, int lane,
+                                            AnisoCount& c) {
+    const uint64_t npx = (uint64_t)a.W * (uint64_t)a.Hh;
+    const uint64_t my = base + (uint64_t)lane;
+    const bool valid = my < npx;
+    const float zl = valid ? a.zbuf[my] : 1.0f;
+    uint32_t todo = __ballot_sync(kFull, valid && zl != 1.0f);
+    if (STATS) { c.rays += valid; c.started += valid && zl != 1.0f; }
+    // misses without a ray start are written by their own lane
+    if (valid && zl == 1.0f)
+        write_pixel(a, my, (int)(my % (uint64_t)a.W), (int)(my / (uint64_t)a.W), false, 0.f, 0.f, 0.f, 0.f, 0.f,
+                    0.f);
+    while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1u;
+        const uint64_t idx = base + (uint64_t)src;
+        const int px = (int)(idx % (uint64_t)a.W), py = (int)(idx / (uint64_t)a.W);
+        float p[3], s[3];
+        ray_setup(a, px, py, a.zbuf[idx], p, s);
+        float q[3] = {p[0], p[1], p[2]};
+        float G[3][3], detG = 0.0f, rho = 0.0f;
+        bool hit = false;
+        for (int i = 0; i < a.max_steps; ++i) {
+            p[0] = p[0] + s[0];
+            p[1] = p[1] + s[1];
+            p[2] = p[2] + s[2];
+            if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p[0], p[1], p[2], s[0], s[1], s[2], a.status);
+            if (outside_forever(a.g, p[0], p[1], p[2], s[0], s[1], s[2])) break;
+            if (STATS) c.evals++;
+            aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
+            if (rho >= a.iso) {
+                hit = true;
+                break;
+            }
+            q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+        }
+        float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+        if (hit) {
+            for (int b = 0; b < a.bisect; ++b) {
+                const float m[3] = {(q[0] + p[0]) * 0.5f, (q[1] + p[1]) * 0.5f, (q[2] + p[2]) * 0.5f};
+                if (STATS) c.evals++;
+                aniso_eval(a.g, an, m[0], m[1], m[2], lane, G, detG, rho);
+                if (rho >= a.iso) { p[0] = m[0]; p[1] = m[1]; p[2] = m[2]; }
+                else { q[0] = m[0]; q[1] = m[1]; q[2] = m[2]; }
+            }
+            // RayMarcher.cpp:411-416: the gradient sum with the G of the hit point
+            if (STATS) c.evals++;
+            aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
+            float gx, gy, gz;
+            aniso_grad(a.g, an, p[0], p[1], p[2], lane, G, detG, gx, gy, gz);
+            const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+            n0 = gx * gi;
+            n1 = gy * gi;
+            n2 = gz * gi;
+            if (STATS) c.hits++;
+        }
+        if (lane == src) write_pixel(a, idx, px, py, hit, p[0], p[1], p[2], n0, n1, n2);
+    }
+}
+
+// Persistent warps take chunks of 32 consecutive pixels from a counter.
+// BATCH: chunk t belongs to view find_view(pfx, t) of `views` / `aviews`
+// (views without anisotropic rays own no chunks); otherwise to view `a`.
+template <bool STATS, bool BATCH>
+__global__ void __launch_bounds__(kThreads)
+    k_march_aniso(const __grid_constant__ MarchArgs a, const __grid_constant__ AnisoDev an,
+                  const MarchArgs* __restrict__ views, const AnisoDev* __restrict__ aviews,
+                  const uint32_t* __restrict__ pfx, int nviews, uint32_t nchunks) {
     const int lane = threadIdx.x & 31;
-    uint64_t evals = 0, hits = 0, rays = 0, started_n = 0;
+    AnisoCount c;
     const uint64_t npx = (uint64_t)a.W * (uint64_t)a.Hh;
     for (;;) {
         unsigned chunk = 0;
         if (lane == 0) chunk = atomicAdd(a.tile_counter, 1u);
         chunk = __shfl_sync(kFull, chunk, 0);
-        const uint64_t base = (uint64_t)chunk * 32u;
-        if (base >= npx) break;
-        const uint64_t my = base + (uint64_t)lane;
-        const bool valid = my < npx;
-        const float zl = valid ? a.zbuf[my] : 1.0f;
-        uint32_t todo = __ballot_sync(kFull, valid && zl != 1.0f);
-        if (STATS) { rays += valid; started_n += valid && zl != 1.0f; }
-        // misses without a ray start are written by their own lane
-        if (valid && zl == 1.0f)
-            write_pixel(a, my, (int)(my % (uint64_t)a.W), (int)(my / (uint64_t)a.W), false, 0.f, 0.f, 0.f, 0.f,
-                        0.f, 0.f);
-        while (todo) {
-            const int src = __ffs(todo) - 1;
-            todo &= todo - 1u;
-            const uint64_t idx = base + (uint64_t)src;
-            const int px = (int)(idx % (uint64_t)a.W), py = (int)(idx / (uint64_t)a.W);
-            float p[3], s[3];
-            ray_setup(a, px, py, a.zbuf[idx], p, s);
-            float q[3] = {p[0], p[1], p[2]};
-            float G[3][3], detG = 0.0f, rho = 0.0f;
-            bool hit = false;
-            for (int i = 0; i < a.max_steps; ++i) {
-                p[0] = p[0] + s[0];
-                p[1] = p[1] + s[1];
-                p[2] = p[2] + s[2];
-                if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p[0], p[1], p[2], s[0], s[1], s[2], a.status);
-                if (outside_forever(a.g, p[0], p[1], p[2], s[0], s[1], s[2])) break;
-                if (STATS) evals++;
-                aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
-                if (rho >= a.iso) {
-                    hit = true;
-                    break;
-                }
-                q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
-            }
-            float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-            if (hit) {
-                for (int b = 0; b < a.bisect; ++b) {
-                    const float m[3] = {(q[0] + p[0]) * 0.5f, (q[1] + p[1]) * 0.5f, (q[2] + p[2]) * 0.5f};
-                    if (STATS) evals++;
-                    aniso_eval(a.g, an, m[0], m[1], m[2], lane, G, detG, rho);
-                    if (rho >= a.iso) { p[0] = m[0]; p[1] = m[1]; p[2] = m[2]; }
-                    else { q[0] = m[0]; q[1] = m[1]; q[2] = m[2]; }
-                }
-                // RayMarcher.cpp:411-416: the gradient sum with the G of the hit point
-                if (STATS) evals++;
-                aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
-                float gx, gy, gz;
-                aniso_grad(a.g, an, p[0], p[1], p[2], lane, G, detG, gx, gy, gz);
-                const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
-                n0 = gx * gi;
-                n1 = gy * gi;
-                n2 = gz * gi;
-                if (STATS) hits++;
-            }
-            if (lane == src) write_pixel(a, idx, px, py, hit, p[0], p[1], p[2], n0, n1, n2);
+        if (BATCH) {
+            if (chunk >= nchunks) break;
+            const int v = find_view(pfx, nviews, chunk);
+            aniso_chunk<STATS>(views[v], aviews[v], (uint64_t)(chunk - __ldg(pfx + v)) * 32u, lane, c);
+        } else {
+            const uint64_t base = (uint64_t)chunk * 32u;
+            if (base >= npx) break;
+            aniso_chunk<STATS>(a, an, base, lane, c);
         }
     }
     if (STATS) {
         // fm_march_stats order: rays, started, hits, evals
-        const unsigned long long v[4] = {rays, started_n, lane == 0 ? hits : 0ull, lane == 0 ? evals : 0ull};
+        const unsigned long long v[4] = {c.rays, c.started, lane == 0 ? c.hits : 0ull, lane == 0 ? c.evals : 0ull};
 #pragma unroll
         for (int j = 0; j < 4; ++j) {
             unsigned long long x = v[j];
@@ -1545,16 +1570,7 @@ __global__ void __launch_bounds__(kThreads) k_march_aniso(const MarchArgs a, con
     }
 }
 
-}  // namespace
-
-int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
-                       const fm_aniso_params* ap, const MarchOutDev& o, cudaStream_t st) {
-    MarchArgs a = march_view_args(s, cam, p, o, ctx->tile);
-    a.stats = ctx->stats_enabled ? ctx->d_stats : nullptr;
-    a.status = ctx->d_status;
-    unsigned int* slot = ctx->d_work + (ctx->work_slot++ % kWorkSlots) * 32;
-    a.tile_counter = slot;
-    FM_CUDA(ctx, cudaMemsetAsync(slot, 0, sizeof(unsigned int), st));
+AnisoDev make_aniso(const fm_scene* s, const fm_aniso_params* ap) {
     AnisoDev an;
     an.hext = ap->radius_mult * s->support;  // Dataset.cpp:175
     {
@@ -1572,15 +1588,53 @@ int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, con
     an.k_r = ap->k_r;
     an.k_s = ap->k_s;
     an.n_eps = ap->n_eps;
+    return an;
+}
+
+template <bool STATS, bool BATCH>
+int launch_aniso_variant(fm_ctx* ctx, const MarchArgs& a, const AnisoDev& an, const MarchArgs* views,
+                         const AnisoDev* aviews, const uint32_t* pfx, int nviews, uint32_t nchunks, cudaStream_t st) {
     int per_sm = 0;
-    if (a.stats) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_aniso<true>, kThreads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_aniso<false>, kThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_aniso<STATS, BATCH>, kThreads, 0);
     if (per_sm < 1) per_sm = 1;
     const unsigned blocks = (unsigned)(ctx->sm_count * per_sm);
-    if (a.stats) k_march_aniso<true><<<blocks, kThreads, 0, st>>>(a, an);
-    else k_march_aniso<false><<<blocks, kThreads, 0, st>>>(a, an);
+    k_march_aniso<STATS, BATCH><<<blocks, kThreads, 0, st>>>(a, an, views, aviews, pfx, nviews, nchunks);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
+}
+
+}  // namespace
+
+size_t aniso_view_bytes() { return sizeof(AnisoDev); }
+
+void aniso_view(const fm_scene* s, const fm_aniso_params* ap, void* out) {
+    const AnisoDev an = make_aniso(s, ap);
+    std::memcpy(out, &an, sizeof(an));
+}
+
+int launch_march_aniso_batch(fm_ctx* ctx, const MarchArgs& a, const MarchArgs* d_views, const void* d_aviews,
+                             const uint32_t* d_pfx, int nviews, uint32_t nchunks, cudaStream_t st) {
+    if (nchunks == 0) return FM_OK;
+    AnisoDev none;
+    std::memset(&none, 0, sizeof(none));
+    if (a.stats)
+        return launch_aniso_variant<true, true>(ctx, a, none, d_views, (const AnisoDev*)d_aviews, d_pfx, nviews,
+                                                nchunks, st);
+    return launch_aniso_variant<false, true>(ctx, a, none, d_views, (const AnisoDev*)d_aviews, d_pfx, nviews, nchunks,
+                                             st);
+}
+
+int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
+                       const fm_aniso_params* ap, const MarchOutDev& o, cudaStream_t st) {
+    MarchArgs a = march_view_args(s, cam, p, o, ctx->tile);
+    a.stats = ctx->stats_enabled ? ctx->d_stats : nullptr;
+    a.status = ctx->d_status;
+    unsigned int* slot = ctx->d_work + (ctx->work_slot++ % kWorkSlots) * 32;
+    a.tile_counter = slot;
+    FM_CUDA(ctx, cudaMemsetAsync(slot, 0, sizeof(unsigned int), st));
+    const AnisoDev an = make_aniso(s, ap);
+    if (a.stats) return launch_aniso_variant<true, false>(ctx, a, an, nullptr, nullptr, nullptr, 0, 0, st);
+    return launch_aniso_variant<false, false>(ctx, a, an, nullptr, nullptr, nullptr, 0, 0, st);
 }
 
 int launch_density(fm_ctx* ctx, const fm_scene* s, const float* d_xyz, uint64_t n, uint32_t stride, float* d_out,

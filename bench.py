@@ -70,6 +70,7 @@ def parse():
     ap.add_argument("--no-batch", action="store_true", help="skip the batched 64-scene measurement")
     ap.add_argument("--no-aniso", action="store_true", help="skip the anisotropic-march measurement")
     ap.add_argument("--autotune", action="store_true", help="autotune the batch's work split first")
+    ap.add_argument("--no-files", action="store_true", help="skip the particle-file loading measurement")
     return ap.parse_args()
 
 
@@ -270,25 +271,32 @@ def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, pla
     extent = float((sc.xyz.max(0) - sc.xyz.min(0)).max())
     tol = 1e-4 * extent
     j = fm.judge(ctx, out["depth"], lo["depth"], tol)
-    # the plain march without empty-space skipping, for reference (a few frames)
-    P_off = fm.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, fm.FM_SKIP_OFF, external_depth=True)
-    off = []
-    for k in range(3):
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        with torch.cuda.stream(ext):
-            flush.zero_()
-            e0.record(ext)
-            fm.splat_depth(scene, cam, lo["start_depth"])
-            fm.march(scene, cam, P_off, lo["position"], lo["normal"], lo["depth"], lo["colour"], lo["start_depth"])
-            e1.record(ext)
-            ext.synchronize()
-        if k > 0:
-            off.append(e0.elapsed_time(e1))
+    # the plain march without empty-space skipping (the reference's loop) and with
+    # the reference's own skip flags, for comparison (a few frames each)
+    def timed_plain(mode):
+        P_m = fm.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, mode, external_depth=True)
+        ts = []
+        for k in range(3):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            with torch.cuda.stream(ext):
+                flush.zero_()
+                e0.record(ext)
+                fm.splat_depth(scene, cam, lo["start_depth"])
+                fm.march(scene, cam, P_m, lo["position"], lo["normal"], lo["depth"], lo["colour"], lo["start_depth"])
+                e1.record(ext)
+                ext.synchronize()
+            if k > 0:
+                ts.append(e0.elapsed_time(e1))
+        return float(np.mean(ts))
+
+    off = [timed_plain(fm.FM_SKIP_OFF)]
+    ref_skip = timed_plain(fm.FM_SKIP_REFERENCE)
     fm.set_proposal(ctx, None)
     prop.close()
     return {"rays_per_s": npx / (ms / 1e3), "frames_per_s": 1e3 / ms, "ms_per_frame": ms,
             "vs_plain": plain_ms / ms, "plain_ms_per_frame": plain_ms,
             "plain_skip_off_ms_per_frame": float(np.mean(off)), "vs_plain_skip_off": float(np.mean(off)) / ms,
+            "plain_reference_skip_ms_per_frame": ref_skip, "vs_plain_reference_skip": ref_skip / ms,
             "depth_tol": tol, "judge": j, "hits_within_tol": j["within_tol"] / max(1, j["hits_ref"]),
             "mask_identical": j["mask_mismatch"] == 0,
             "margins_support_radii": [margin_lo, margin_hi], "min_near_support_radii": min_near,
@@ -342,6 +350,68 @@ def run_aniso(args, fm, torch, ctx, ext, scene, sc, cam, out):
             "cpu_port_rays_per_s": (pix.size / cpu_s) / frac if frac > 0 else None,
             "cpu_sample": f"{pix.size} started pixels, bisection 0, {max(1, cores - 1)} threads, scaled by the "
                           f"started fraction {frac:.3f} to all pixels"}
+
+
+def run_files(args, fm, torch, ctx, sc):
+    """Particle files: the bench scene as gzip BGEO frames, loaded into scenes (host decode + GPU gather +
+    grid build), against building the scene from positions already in host memory."""
+    import shutil
+    import tempfile
+
+    from fluidmarch import bgeo
+
+    tmp = tempfile.mkdtemp(prefix="fm_bgeo_")
+    try:
+        rng = np.random.default_rng(7)
+        n = sc.n
+        attrs = {"v": ("vector", rng.normal(size=(n, 3)).astype(np.float32)), "id": ("int", np.arange(n))}
+        frames = 6
+        prefix = os.path.join(tmp, "ParticleData_Fluid_")
+        for i in range(1, frames + 1):
+            jitter = rng.normal(0, 1e-4, sc.xyz.shape).astype(np.float32)
+            bgeo.write(f"{prefix}{i}.bgeo", sc.xyz + jitter, attrs, compressed=True, level=1)
+        path = f"{prefix}1.bgeo"
+        size = os.path.getsize(path)
+        t = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            bgeo.read(path)
+            t.append(time.perf_counter() - t0)
+        host_ms = 1e3 * min(t)
+        t = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            s = bgeo.load_scene(ctx, path, sc.support)
+            t.append(time.perf_counter() - t0)
+            s.close()
+        scene_ms = 1e3 * min(t)
+        t = []
+        for _ in range(3):
+            t0 = time.perf_counter()
+            s = fm.Scene(ctx, sc.xyz, sc.support)
+            ctx.sync()
+            t.append(time.perf_counter() - t0)
+            s.close()
+        mem_ms = 1e3 * min(t)
+        series = {}
+        for threads in (0, 4):
+            ds = bgeo.Dataset(prefix, ".bgeo", -1, threads)
+            ds.load(ctx, 0, sc.support)
+            t0 = time.perf_counter()
+            for i in range(1, frames):
+                ds.load(ctx, i, sc.support)
+            series[f"threads_{threads}"] = 1e3 * (time.perf_counter() - t0) / (frames - 1)
+            ds.close()
+        info = bgeo.info(path)
+        return {"particles": n, "record_words": info["record_words"], "file_mb": size / 1e6,
+                "data_mb": 4 * info["record_words"] * n / 1e6,
+                "host_decode_ms": host_ms, "scene_from_file_ms": scene_ms, "scene_from_host_memory_ms": mem_ms,
+                "autoplay_ms_per_frame": series,
+                "note": "gzip level 1 BGEO with velocity and id attributes; scene_from_file = decode on one host "
+                        "core + record upload + byte-swap gather kernel + grid build; autoplay = the next frame "
+                        "of a 6-frame series with host threads decoding ahead"}
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
 
 
 def run_batch(args, fm, torch, ctx, ext, dev):
@@ -509,6 +579,9 @@ def run_ours(args):
     aniso = None
     if rank == 0 and not args.no_aniso:
         aniso = run_aniso(args, fm, torch, ctx, ext, scene, sc, cam, out)
+    files = None
+    if rank == 0 and not args.no_files:
+        files = run_files(args, fm, torch, ctx, sc)
 
     if rank == 0:
         peak, peak_kind = measured_peaks()
@@ -541,6 +614,8 @@ def run_ours(args):
             line["batch"] = batch
         if aniso:
             line["anisotropic"] = aniso
+        if files:
+            line["particle_files"] = files
         if world == 1 and not args.no_cpu_baseline:
             import oracle as O
 

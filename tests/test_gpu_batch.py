@@ -278,9 +278,46 @@ def test_batch_learned_view_needs_a_proposal(fmlib, ctx, small_batch):
         bad = fmlib.MarchParams(params.iso, params.step, params.max_steps, 8, fmlib.FM_SKIP_REFERENCE, proposal=True)
         with pytest.raises(fmlib.FmError):
             fmlib.Batch(ctx, [fmlib.View(s, cam, bad, **o)])
-        aniso = fmlib.MarchParams(params.iso, params.step, params.max_steps, 8, fmlib.FM_SKIP_OFF, anisotropic=True)
+        aniso = fmlib.MarchParams(params.iso, params.step, params.max_steps, 8, fmlib.FM_SKIP_EXACT, anisotropic=True)
         with pytest.raises(fmlib.FmError):
             fmlib.Batch(ctx, [fmlib.View(s, cam, aniso, **o)])
     finally:
         fmlib.set_proposal(ctx, None)
         pr.close()
+
+
+def test_batch_with_anisotropic_views(fmlib, ctx, small_batch):
+    """Anisotropic views (skip off and the reference's flags) next to isotropic ones in one batch
+    equal the same views marched alone; the batch keeps the kernel settings it was created with."""
+    ctx.set_anisotropy(2.0, 0.5, 2.0, 2000.0, 1)
+    items = []
+    for i, (sc, s, cam, params) in enumerate(small_batch[:6]):
+        aniso = i % 2 == 1
+        skip = (fmlib.FM_SKIP_OFF, fmlib.FM_SKIP_REFERENCE)[i % 4 == 1] if aniso else params.skip_mode
+        p = fmlib.MarchParams(params.iso, params.step, params.max_steps, params.bisect, skip, anisotropic=aniso)
+        items.append((sc, s, cam, p))
+    want = [single(fmlib, s, cam, p) for sc, s, cam, p in items]
+    views, outs = make_views(fmlib, items)
+    b = fmlib.Batch(ctx, views)
+    ctx.set_anisotropy(1.5, 0.4, 3.0, 1000.0, 2)  # not seen by the batch
+    try:
+        ctx.set_stats(True)
+        try:
+            b.run()
+            ctx.sync()
+            st = ctx.stats()
+        finally:
+            ctx.set_stats(False)
+        for i in range(len(items)):
+            assert_same(host(outs[i]), want[i], f"view {i}")
+        assert st["rays"] == b.info()["pixels"]
+        for o in outs:
+            for v in o.values():
+                v.zero_()
+        b.run()  # the captured graph
+        ctx.sync()
+        for i in range(len(items)):
+            assert_same(host(outs[i]), want[i], f"graph view {i}")
+    finally:
+        ctx.set_anisotropy(2.0, 0.5, 2.0, 2000.0, 1)
+        b.close()
