@@ -283,8 +283,11 @@ int fm_get_tile_config(const fm_ctx* ctx, fm_tile_config* out);
 
 /* One view of a batch: a scene seen from a camera with its own march
  * settings.  Output pointers are DEVICE memory (NULL skips an output);
- * start_depth may be NULL (the batch keeps the splat depths itself).
- * params.flags must be 0: every view is splatted. */
+ * start_depth may be NULL (the batch keeps the splat depths itself).  Every
+ * view is splatted: params.flags may hold FM_MARCH_PROPOSAL (the batch copies
+ * the context's proposal at creation) or FM_MARCH_ANISOTROPIC (the batch
+ * copies the context's fm_set_anisotropy settings), not
+ * FM_MARCH_EXTERNAL_DEPTH. */
 typedef struct fm_view {
     const fm_scene* scene;
     fm_camera camera;
@@ -304,8 +307,9 @@ typedef struct fm_batch_info {
 } fm_batch_info;
 
 /* Prepare a batch of views: all views are splatted and marched by one launch
- * per pass (fill, sampled splat, tile maxima, cull, survivor splat, march,
- * long rays), captured once into a CUDA graph.  The views' scenes and output
+ * per pass (fill, sampled splat, tile maxima, cull, survivor splat, proposal
+ * when a view has one, march, long rays, anisotropic march when a view is
+ * anisotropic), captured once into a CUDA graph.  The views' scenes and output
  * buffers are bound at creation: after fm_scene_update of one of its scenes,
  * call fm_batch_refresh.  cfg NULL: the context's work split.  Synchronous. */
 int fm_batch_create(fm_ctx* ctx, const fm_view* views, int32_t n_views, const fm_tile_config* cfg, fm_batch** out);
