@@ -222,16 +222,42 @@ int fm_query(fm_ctx* ctx) {
 int fm_host_alloc(fm_ctx* ctx, size_t bytes, void** out) {
     if (!ctx || !out) return FM_ERR_INVALID;
     cudaSetDevice(ctx->device);
-    if (cudaHostAlloc(out, bytes, cudaHostAllocDefault) != cudaSuccess) {
+    if (cudaHostAlloc(out, bytes, cudaHostAllocMapped) != cudaSuccess) {
         *out = nullptr;
         return set_err(ctx, FM_ERR_OOM, "cudaHostAlloc failed");
     }
+    void* d = nullptr;
+    if (cudaHostGetDevicePointer(&d, *out, 0) != cudaSuccess) {
+        cudaGetLastError();
+        d = nullptr;  // not mapped: outputs placed here are staged as usual
+    }
+    if (d && bytes) ctx->host_allocs[(uintptr_t)*out] = {bytes, d};
     return FM_OK;
 }
 
 void fm_host_free(fm_ctx* ctx, void* p) {
-    if (ctx) cudaSetDevice(ctx->device);
+    if (ctx) {
+        cudaSetDevice(ctx->device);
+        // a kernel may still be writing into the block
+        cudaStreamSynchronize(ctx->stream);
+        ctx->host_allocs.erase((uintptr_t)p);
+    }
     if (p) cudaFreeHost(p);
+}
+
+// Device address of [p, p + bytes) when the range lies inside one fm_host_alloc
+// block of this context (page-locked and mapped: kernels may write it over the
+// host link directly), else null.
+static void* host_mapped(fm_ctx* ctx, const void* p, size_t bytes) {
+    if (!p || ctx->host_allocs.empty()) return nullptr;
+    const uintptr_t a = (uintptr_t)p;
+    auto it = ctx->host_allocs.upper_bound(a);
+    if (it == ctx->host_allocs.begin()) return nullptr;
+    --it;
+    const uintptr_t base = it->first;
+    const size_t size = it->second.first;
+    if (a - base > size || bytes > size - (a - base)) return nullptr;
+    return (char*)it->second.second + (a - base);
 }
 
 static int scene_build(fm_scene* s, const float* xyz, uint64_t n, uint32_t stride, int mem) {
@@ -483,8 +509,15 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     float* user[4] = {out->position, out->normal, out->depth, out->colour};
     const size_t per[4] = {16, 16, 4, 16};
     void* dev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool direct[4] = {false, false, false, false};
     for (int i = 0; i < 4; ++i) {
         if (!user[i]) continue;
+        // outputs in fm_host_alloc memory: the march writes them over the host link
+        // itself (each pixel once, coalesced), no copy afterwards
+        if (host && (dev[i] = host_mapped(ctx, user[i], npx * per[i])) != nullptr) {
+            direct[i] = true;
+            continue;
+        }
         if (host) {
             if (!grow(ctx->stage[2 + i], npx * per[i])) return set_err(ctx, FM_ERR_OOM, "staging allocation failed");
             dev[i] = ctx->stage[2 + i].p;
@@ -502,7 +535,8 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     if (rc) return rc;
     if (host) {
         for (int i = 0; i < 4; ++i)
-            if (user[i]) FM_CUDA(ctx, cudaMemcpyAsync(user[i], dev[i], npx * per[i], cudaMemcpyDeviceToHost, st));
+            if (user[i] && !direct[i])
+                FM_CUDA(ctx, cudaMemcpyAsync(user[i], dev[i], npx * per[i], cudaMemcpyDeviceToHost, st));
         if (out->start_depth && !external)
             FM_CUDA(ctx, cudaMemcpyAsync(out->start_depth, z, npx * 4, cudaMemcpyDeviceToHost, st));
         unsigned int* hs = (unsigned int*)ctx->h_pinned_small;

@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -217,6 +218,9 @@ struct fm_ctx {
     // source of scene generations (every successful build gets a new one)
     uint64_t gen_counter = 0;
     void* h_pinned_small = nullptr;  // 256 bytes of pinned memory for small readbacks
+    // fm_host_alloc blocks: host address -> (bytes, device address of the mapping);
+    // march outputs that lie inside one are written by the kernels directly
+    std::map<uintptr_t, std::pair<size_t, void*>> host_allocs;
 };
 
 struct fm_scene {

@@ -288,8 +288,8 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
 }
 
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase) {
-    for (uint32_t i = 0; i < kWaitLimit; ++i) {
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase, uint32_t limit = kWaitLimit) {
+    for (uint32_t i = 0; i < limit; ++i) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -525,6 +525,21 @@ __global__ void __launch_bounds__(kRows) k_propose(const ProposeArgs a) {
         asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(kTmemCols) : "memory");
 }
 
+// Diagnostics: the bounded wait of k_propose on an mbarrier that never
+// completes (two arrivals expected, one made).  The wait gives up after
+// `limit` polls, the kernel reports status bit 8 as k_propose does and exits.
+__global__ void k_wait_selftest(unsigned int* status, uint32_t limit) {
+    __shared__ __align__(8) uint64_t bar_mem;
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&bar_mem);
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(2u) : "memory");
+        asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(bar) : "memory");
+    }
+    __syncthreads();
+    const bool ok = __syncthreads_and(mbar_wait(bar, 0, limit));
+    if (!ok && threadIdx.x == 0) atomicOr(status, 8u);
+}
+
 // ---- training (FP32 SIMT) --------------------------------------------------------------
 
 // Forward pass of a batch: z1, z2 (pre-activations), y; with targets also the
@@ -603,7 +618,9 @@ __global__ void __launch_bounds__(128) k_train_bwd(const float* __restrict__ P, 
 }
 
 // Parameter gradients: every thread owns parameters p = tid + 256 i and sums
-// their per-sample terms over this block's chunk of the batch.
+// their per-sample terms over this block's chunk of the batch into the block's
+// row of `partial`; k_grad_reduce adds the rows in block order, so a training
+// step gives the same bits on every run (checkpoints resume exactly).
 constexpr int kGradThreads = 256;
 constexpr int kGradStage = 8;  // samples staged in shared memory at a time
 constexpr int kRowFloats = kF + 4 * kH + kO;  // x, h1, h2, dz1, dz2, dy
@@ -614,7 +631,7 @@ __global__ void __launch_bounds__(kGradThreads) k_train_grad(const float* __rest
                                                              const float* __restrict__ dz1,
                                                              const float* __restrict__ dz2,
                                                              const float* __restrict__ dy, uint32_t chunk,
-                                                             float* __restrict__ grad) {
+                                                             float* __restrict__ partial) {
     __shared__ float rows[kGradStage][kRowFloats];
     constexpr int kPer = (kProposalParams + kGradThreads - 1) / kGradThreads;
     float acc[kPer];
@@ -658,9 +675,18 @@ __global__ void __launch_bounds__(kGradThreads) k_train_grad(const float* __rest
             }
         }
     }
+    float* row = partial + (uint64_t)blockIdx.x * kProposalParams;
 #pragma unroll
     for (int i = 0; i < kPer; ++i)
-        if (ia[i] != -2 && acc[i] != 0.0f) atomicAdd(grad + threadIdx.x + kGradThreads * i, acc[i]);
+        if (ia[i] != -2) row[threadIdx.x + kGradThreads * i] = acc[i];
+}
+
+__global__ void k_grad_reduce(const float* __restrict__ partial, uint32_t rows, float* __restrict__ grad) {
+    const int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= kProposalParams) return;
+    float s = 0.0f;
+    for (uint32_t r = 0; r < rows; ++r) s += partial[(uint64_t)r * kProposalParams + p];
+    grad[p] = s;
 }
 
 __global__ void k_adam(float* __restrict__ P, float* __restrict__ G, float* __restrict__ M, float* __restrict__ V,
@@ -1081,9 +1107,12 @@ int fm_trainer_step(fm_trainer* t, const float* features, const float* targets, 
     cudaSetDevice(ctx->device);
     cudaStream_t st = ctx->stream;
     const size_t per = 4 * kH + 2 * kO;  // z1, z2, dz1, dz2, y, dy
+    const uint32_t chunk = 64;
+    const uint32_t gblocks = (n + chunk - 1) / chunk;
     if (n > t->cap) {
         FM_CUDA(ctx, cudaStreamSynchronize(st));
-        if (!grow_buf(t->work, (size_t)n * per * sizeof(float) + 64)) return set_err(ctx, FM_ERR_OOM, "trainer buffers");
+        const size_t bytes = (size_t)n * per * sizeof(float) + 64 + (size_t)gblocks * kProposalParams * sizeof(float);
+        if (!grow_buf(t->work, bytes)) return set_err(ctx, FM_ERR_OOM, "trainer buffers");
         t->cap = n;
     }
     float* z1 = (float*)t->work.p;
@@ -1093,6 +1122,7 @@ int fm_trainer_step(fm_trainer* t, const float* features, const float* targets, 
     float* y = dz2 + (size_t)n * kH;
     float* dy = y + (size_t)n * kO;
     float* lsum = dy + (size_t)n * kO;
+    float* partial = lsum + 16;  // 64-byte aligned: the work buffer is, and n * per is a multiple of 4
     float* P = t->d_p;
     float* G = P + kProposalParams;
     float* M = G + kProposalParams;
@@ -1101,8 +1131,8 @@ int fm_trainer_step(fm_trainer* t, const float* features, const float* targets, 
     const unsigned blocks = (n + 127) / 128;
     k_train_fwd<<<blocks, 128, 0, st>>>(P, features, targets, n, tau_lo, tau_hi, z1, z2, y, dy, lsum);
     k_train_bwd<<<blocks, 128, 0, st>>>(P, n, z1, z2, dy, dz1, dz2);
-    const uint32_t chunk = 64;
-    k_train_grad<<<(n + chunk - 1) / chunk, kGradThreads, 0, st>>>(features, n, z1, z2, dz1, dz2, dy, chunk, G);
+    k_train_grad<<<gblocks, kGradThreads, 0, st>>>(features, n, z1, z2, dz1, dz2, dy, chunk, partial);
+    k_grad_reduce<<<(kProposalParams + 255) / 256, 256, 0, st>>>(partial, gblocks, G);
     t->steps++;
     const float b1 = 0.9f, b2 = 0.999f;
     const float c1 = 1.0f - (float)std::pow((double)b1, t->steps), c2 = 1.0f - (float)std::pow((double)b2, t->steps);
@@ -1126,6 +1156,54 @@ int fm_trainer_predict(fm_trainer* t, const float* features, uint32_t n, float* 
     k_train_fwd<<<(n + 127) / 128, 128, 0, ctx->stream>>>(t->d_p, features, nullptr, n, 0.5f, 0.5f, nullptr, nullptr,
                                                           out, nullptr, nullptr);
     FM_CUDA(ctx, cudaGetLastError());
+    return FM_OK;
+}
+
+int fm_selftest_wait_timeout(fm_ctx* ctx, uint32_t polls) {
+    if (!ctx) return FM_ERR_INVALID;
+    if (polls == 0 || polls > kWaitLimit) return set_err(ctx, FM_ERR_INVALID, "polls must be in [1, 2^22]");
+    cudaSetDevice(ctx->device);
+    k_wait_selftest<<<1, 128, 0, ctx->stream>>>(ctx->d_status, polls);
+    FM_CUDA(ctx, cudaGetLastError());
+    unsigned int* hs = (unsigned int*)ctx->h_pinned_small;
+    FM_CUDA(ctx, cudaMemcpyAsync(hs, ctx->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost, ctx->stream));
+    FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    const unsigned int code = hs[0];
+    if (code != 0) {
+        FM_CUDA(ctx, cudaMemset(ctx->d_status, 0, sizeof(unsigned int)));
+        return set_err(ctx, FM_ERR_DEVICE, "wait timed out: kernel status word " + std::to_string(code));
+    }
+    return FM_OK;
+}
+
+int fm_trainer_get_state(fm_trainer* t, float* host_state, int64_t* step) {
+    if (!t) return FM_ERR_INVALID;
+    if (!host_state || !step) return set_err(t->ctx, FM_ERR_INVALID, "NULL argument");
+    cudaSetDevice(t->ctx->device);
+    FM_CUDA(t->ctx, cudaStreamSynchronize(t->ctx->stream));
+    const float* P = t->d_p;
+    FM_CUDA(t->ctx, cudaMemcpy(host_state, P, kProposalParams * sizeof(float), cudaMemcpyDeviceToHost));
+    FM_CUDA(t->ctx, cudaMemcpy(host_state + kProposalParams, P + 2 * kProposalParams,
+                               2 * kProposalParams * sizeof(float), cudaMemcpyDeviceToHost));
+    *step = t->steps;
+    return FM_OK;
+}
+
+int fm_trainer_set_state(fm_trainer* t, const float* host_state, int64_t step) {
+    if (!t) return FM_ERR_INVALID;
+    if (!host_state) return set_err(t->ctx, FM_ERR_INVALID, "NULL argument");
+    if (step < 0 || step > (int64_t)1 << 30) return set_err(t->ctx, FM_ERR_INVALID, "step out of range");
+    for (int i = 0; i < 3 * kProposalParams; ++i)
+        if (!std::isfinite(host_state[i]) || (i >= 2 * kProposalParams && host_state[i] < 0.0f))
+            return set_err(t->ctx, FM_ERR_INVALID, "state is not finite (or a second moment is negative)");
+    cudaSetDevice(t->ctx->device);
+    FM_CUDA(t->ctx, cudaStreamSynchronize(t->ctx->stream));
+    float* P = t->d_p;
+    FM_CUDA(t->ctx, cudaMemcpy(P, host_state, kProposalParams * sizeof(float), cudaMemcpyHostToDevice));
+    FM_CUDA(t->ctx, cudaMemset(P + kProposalParams, 0, kProposalParams * sizeof(float)));
+    FM_CUDA(t->ctx, cudaMemcpy(P + 2 * kProposalParams, host_state + kProposalParams,
+                               2 * kProposalParams * sizeof(float), cudaMemcpyHostToDevice));
+    t->steps = (int)step;
     return FM_OK;
 }
 

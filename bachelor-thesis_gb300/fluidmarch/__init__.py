@@ -44,7 +44,7 @@ EXPORTS = [
     "fm_proposal_create", "fm_proposal_destroy", "fm_set_proposal", "fm_proposal_features", "fm_proposal_intervals",
     "fm_judge", "fm_trainer_create", "fm_trainer_destroy", "fm_trainer_step", "fm_trainer_predict",
     "fm_trainer_params", "fm_density", "fm_set_anisotropy",
-    "fm_bgeo_read", "fm_gunzip", "fm_scene_create_bgeo", "fm_dataset_open", "fm_dataset_frames", "fm_dataset_path",
+    "fm_trainer_get_state", "fm_trainer_set_state", "fm_selftest_wait_timeout", "fm_bgeo_read", "fm_gunzip", "fm_scene_create_bgeo", "fm_dataset_open", "fm_dataset_frames", "fm_dataset_path",
     "fm_dataset_frame_info", "fm_dataset_max_particles", "fm_dataset_read", "fm_dataset_scene",
     "fm_dataset_last_error", "fm_dataset_close",
 ]
@@ -59,6 +59,20 @@ class FmError(RuntimeError):
 class CCamera(C.Structure):
     _fields_ = [("view", C.c_float * 16), ("proj", C.c_float * 16), ("inv_proj_view", C.c_float * 16),
                 ("position", C.c_float * 3), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class _HostBlock:
+    """Frees an fm_host_alloc block when the array over it goes away."""
+
+    def __init__(self, ctx, p: int):
+        self.ctx, self.p = ctx, p
+
+    def __del__(self):
+        try:
+            if self.p:
+                self.ctx.L.fm_host_free(getattr(self.ctx, "h", None), C.c_void_p(self.p))
+        except Exception:
+            pass
 
 
 class CBgeoInfo(C.Structure):
@@ -177,6 +191,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_trainer_step.argtypes = [vp, vp, vp, C.c_uint32, C.c_float, C.c_float, C.c_float, C.POINTER(C.c_float)]
     L.fm_trainer_predict.argtypes = [vp, vp, C.c_uint32, vp]
     L.fm_trainer_params.argtypes = [vp, vp]
+    L.fm_trainer_get_state.argtypes = [vp, vp, C.POINTER(C.c_int64)]
+    L.fm_selftest_wait_timeout.argtypes = [vp, C.c_uint32]
+    L.fm_trainer_set_state.argtypes = [vp, vp, C.c_int64]
     L.fm_bgeo_read.argtypes = [C.c_char_p, vp, C.c_uint64, C.POINTER(CBgeoInfo), C.c_char_p, C.c_uint64]
     L.fm_gunzip.argtypes = [vp, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64)]
     L.fm_scene_create_bgeo.argtypes = [vp, C.c_char_p, C.c_float, C.POINTER(vp)]
@@ -267,6 +284,19 @@ class Context:
         c = CTileConfig(int(tile_width), int(tiles_per_claim), int(defer_iters), int(long_queue), int(defer_lanes),
                         int(regroup_iters))
         self.check(self.L.fm_set_tile_config(self.h, C.byref(c)))
+
+    def host_array(self, shape, dtype=np.float32) -> np.ndarray:
+        """A numpy array in page-locked host memory of this context (fm_host_alloc).
+
+        March outputs placed in such arrays are written by the kernels directly,
+        without a copy after the march; the block is freed with the array."""
+        dt = np.dtype(dtype)
+        nbytes = max(1, int(np.prod(shape)) * dt.itemsize)
+        p = C.c_void_p()
+        self.check(self.L.fm_host_alloc(self.h, nbytes, C.byref(p)))
+        buf = (C.c_char * nbytes).from_address(p.value)
+        buf._fm_block = _HostBlock(self, p.value)
+        return np.frombuffer(buf, dt, count=int(np.prod(shape))).reshape(shape)
 
     def set_anisotropy(self, radius_mult: float = 2.0, k_n: float = 0.5, k_r: float = 2.0, k_s: float = 2000.0,
                        n_eps: int = 1):
@@ -601,6 +631,19 @@ class Trainer:
         p = np.empty(FM_PROPOSAL_PARAMS, np.float32)
         self.ctx.check(self.ctx.L.fm_trainer_params(self.h, p.ctypes.data))
         return p
+
+    def state(self) -> tuple:
+        """(3 x FM_PROPOSAL_PARAMS state: parameters, Adam first and second moments; Adam step)."""
+        s = np.empty(3 * FM_PROPOSAL_PARAMS, np.float32)
+        step = C.c_int64()
+        self.ctx.check(self.ctx.L.fm_trainer_get_state(self.h, s.ctypes.data, C.byref(step)))
+        return s, int(step.value)
+
+    def set_state(self, state, step: int):
+        s = np.ascontiguousarray(state, np.float32).reshape(-1)
+        if s.size != 3 * FM_PROPOSAL_PARAMS:
+            raise ValueError(f"expected {3 * FM_PROPOSAL_PARAMS} floats, got {s.size}")
+        self.ctx.check(self.ctx.L.fm_trainer_set_state(self.h, s.ctypes.data, int(step)))
 
     def close(self):
         if getattr(self, "h", None):

@@ -186,6 +186,48 @@ def evaluate(ctx: fm.Context, P: np.ndarray, X, T, H: float = None, step: float 
     return r
 
 
+CKPT_MAGIC = b"FMTRAIN\0"
+CKPT_VERSION = 1
+
+
+def save_checkpoint(path: str, trainer: fm.Trainer, meta: dict | None = None) -> None:
+    """Trainer checkpoint: magic, version (uint32), JSON header length (uint32), the JSON header
+    (layout, Adam step, caller metadata), then the state as little-endian float32 (parameters,
+    Adam first moments, second moments: 3 x FM_PROPOSAL_PARAMS).  Written to a temporary file
+    and renamed, so a crash never leaves a torn checkpoint."""
+    state, step = trainer.state()
+    head = json.dumps({"version": CKPT_VERSION, "params": fm.FM_PROPOSAL_PARAMS, "step": step,
+                       "layout": ["parameters", "adam_m", "adam_v"], "dtype": "<f4",
+                       "meta": meta or {}}).encode()
+    tmp = path + ".tmp"
+    with open(tmp, "wb") as f:
+        f.write(CKPT_MAGIC)
+        f.write(np.array([CKPT_VERSION, len(head)], "<u4").tobytes())
+        f.write(head)
+        f.write(state.astype("<f4").tobytes())
+    os.replace(tmp, path)
+
+
+def load_checkpoint(path: str, ctx: fm.Context) -> tuple:
+    """(trainer restored from the checkpoint, its JSON header)."""
+    with open(path, "rb") as f:
+        data = f.read()
+    if data[:8] != CKPT_MAGIC:
+        raise ValueError(f"{path}: not a trainer checkpoint")
+    version, hlen = np.frombuffer(data[8:16], "<u4")
+    if version != CKPT_VERSION:
+        raise ValueError(f"{path}: checkpoint version {version}, expected {CKPT_VERSION}")
+    head = json.loads(data[16:16 + hlen].decode())
+    if head["params"] != fm.FM_PROPOSAL_PARAMS:
+        raise ValueError(f"{path}: {head['params']} parameters, expected {fm.FM_PROPOSAL_PARAMS}")
+    state = np.frombuffer(data[16 + hlen:], "<f4")
+    if state.size != 3 * fm.FM_PROPOSAL_PARAMS:
+        raise ValueError(f"{path}: truncated state")
+    tr = fm.Trainer(ctx, init=state[: fm.FM_PROPOSAL_PARAMS])
+    tr.set_state(state, head["step"])
+    return tr, head
+
+
 def load(path: str = WEIGHTS):
     d = np.load(path, allow_pickle=False)
     meta = json.loads(str(d["meta"])) if "meta" in d else {}

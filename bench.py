@@ -548,13 +548,13 @@ def run_ours(args):
     value, _, t_max_s = throughput(npx * args.steps, total_ms / 1000.0, dist, dev)
     t_max = 1000.0 * t_max_s
 
-    # e2e through the C ABI with pinned host buffers
-    xyz_h = torch.from_numpy(sc.xyz).pin_memory()
-    host = {"position": torch.empty((npx, 4)).pin_memory(), "normal": torch.empty((npx, 4)).pin_memory(),
-            "depth": torch.empty(npx).pin_memory(), "colour": torch.empty((npx, 4)).pin_memory()}
+    # e2e through the C ABI with host buffers in the library's pinned memory
+    # (fm_host_alloc: the march writes the outputs there directly)
+    xyz_np = ctx.host_array(sc.xyz.shape)
+    xyz_np[...] = sc.xyz
+    hp = {"position": ctx.host_array((npx, 4)), "normal": ctx.host_array((npx, 4)), "depth": ctx.host_array((npx,)),
+          "colour": ctx.host_array((npx, 4))}
     P_full = fm.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, skip)
-    hp = {k: v.numpy() for k, v in host.items()}  # numpy views of the pinned buffers
-    xyz_np = xyz_h.numpy()
 
     def e2e_frame():
         scene.update(xyz_np)

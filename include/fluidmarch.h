@@ -393,6 +393,12 @@ int fm_trainer_step(fm_trainer* t, const float* features, const float* targets, 
 /* FP32 outputs (near, far) of the current parameters: out = n*2 floats (device). */
 int fm_trainer_predict(fm_trainer* t, const float* features, uint32_t n, float* out);
 int fm_trainer_params(fm_trainer* t, float* host_params);
+/* Checkpoint: state = 3 * FM_PROPOSAL_PARAMS floats (parameters | Adam first
+ * moments | second moments) and the Adam step count.  Gradients are reduced in
+ * a fixed order, so a trainer restored with fm_trainer_set_state continues
+ * bit for bit as the one that wrote the state. */
+int fm_trainer_get_state(fm_trainer* t, float* host_state, int64_t* step);
+int fm_trainer_set_state(fm_trainer* t, const float* host_state, int64_t step);
 
 /* ---- Particle files (Dataset.cpp:169-227, Dataset::ReadFile :292-306) ----
  * Houdini classic BGEO, version 5, plain or gzip-compressed (detected by the
@@ -446,6 +452,13 @@ int fm_dataset_read(fm_dataset* ds, int32_t i, float* xyz, uint64_t capacity, ui
 int fm_dataset_scene(fm_dataset* ds, fm_ctx* ctx, int32_t i, float support_radius, fm_scene** scene);
 const char* fm_dataset_last_error(const fm_dataset* ds);
 void fm_dataset_close(fm_dataset* ds);
+
+/* Diagnostics for failure detection: runs the bounded mbarrier wait of the
+ * tensor-core kernels on a barrier that never completes.  The wait gives up
+ * after `polls` polls (1 .. 2^22), the kernel sets status bit 8 as the
+ * proposal kernel does on a timeout, and the call returns FM_ERR_DEVICE with
+ * the status word in fm_last_error; the context stays usable. */
+int fm_selftest_wait_timeout(fm_ctx* ctx, uint32_t polls);
 
 /* Library version (major * 10000 + minor * 100 + patch). */
 int fm_version(void);

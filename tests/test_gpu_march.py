@@ -313,3 +313,24 @@ def test_fine_bound_table_on_reuse(fmlib, ctx):
             assert np.array_equal(bits(g[k]), bits(o[k])), k
     assert st2["skipped"] > st1["skipped"] and st2["evals"] < st1["evals"]
     s.close()
+
+
+def test_outputs_in_library_pinned_memory(fmlib, ctx):
+    """Outputs in fm_host_alloc memory are written by the kernels directly (no copy after the
+    march); they equal the staged outputs of pageable buffers, also for a view inside a larger
+    block and with only some outputs pinned."""
+    sc = scenes.small_scene(seed=13, n=15000, width=150, height=90)
+    cam = sc.cameras[0]
+    npx = cam.width * cam.height
+    s = fmlib.Scene(ctx, sc.xyz, sc.support)
+    p = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_EXACT)
+    want = fmlib.render(s, cam, p)
+    big = ctx.host_array((npx + 100, 4))  # the outputs start 64 pixels into the block
+    pin = {"position": big[64:64 + npx], "normal": ctx.host_array((npx, 4)), "depth": ctx.host_array((npx,)),
+           "colour": np.zeros((npx, 4), np.float32)}
+    for v in pin.values():
+        v[...] = -1.0
+    fmlib.march(s, cam, p, pin["position"], pin["normal"], pin["depth"], pin["colour"])
+    for k in pin:
+        assert np.array_equal(bits(pin[k]), bits(want[k])), k
+    s.close()

@@ -258,6 +258,49 @@ def test_trainer_matches_torch(fmlib, ctx):
     tr.close()
 
 
+def test_trainer_checkpoint_resumes_exactly(fmlib, ctx, tmp_path):
+    """Steps 1-6 in one go equal steps 1-3, a checkpoint, a fresh trainer from it, steps 4-6 (bits)."""
+    from fluidmarch import proposal as PR
+
+    rng = np.random.default_rng(9)
+    n = 3000
+    X = torch.from_numpy(rng.normal(0, 1, (6, n, NF)).astype(np.float32)).cuda()
+    T = torch.from_numpy(rng.uniform(0, 10, (6, n)).astype(np.float32)).cuda()
+    P0 = random_params(4)
+    a = fmlib.Trainer(ctx, init=P0)
+    for k in range(6):
+        a.step(X[k], T[k], n, 3e-3, 0.05, 0.97)
+    want, want_step = a.state()
+    b = fmlib.Trainer(ctx, init=P0)
+    for k in range(3):
+        b.step(X[k], T[k], n, 3e-3, 0.05, 0.97)
+    path = str(tmp_path / "trainer.ckpt")
+    PR.save_checkpoint(path, b, {"epoch": 0, "batch": 3})
+    b.close()
+    c, head = PR.load_checkpoint(path, ctx)
+    assert head["step"] == 3 and head["meta"]["batch"] == 3
+    for k in range(3, 6):
+        c.step(X[k], T[k], n, 3e-3, 0.05, 0.97)
+    got, got_step = c.state()
+    assert got_step == want_step == 6
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    # the same six steps again give the same bits (the gradient reduction has a fixed order)
+    d = fmlib.Trainer(ctx, init=P0)
+    for k in range(6):
+        d.step(X[k], T[k], n, 3e-3, 0.05, 0.97)
+    assert np.array_equal(d.state()[0].view(np.uint32), want.view(np.uint32))
+    bad = want.copy()
+    bad[2 * fmlib.FM_PROPOSAL_PARAMS] = -1.0  # a negative second moment
+    with pytest.raises(fmlib.FmError):
+        c.set_state(bad, 6)
+    with open(path, "r+b") as f:
+        f.write(b"XXXX")
+    with pytest.raises(ValueError):
+        PR.load_checkpoint(path, ctx)
+    for t in (a, c, d):
+        t.close()
+
+
 def test_trainer_learns(fmlib, ctx):
     rng = np.random.default_rng(8)
     n = 16384
