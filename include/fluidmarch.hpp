@@ -9,14 +9,20 @@
 //     Exit()           RayMarcher.cpp:71-74   -> fm_sync
 //   struct VisualizationSettings  RayMarcher.h:12-26
 //   class Frame        src/app/Dataset.h:37-65 -> fm_scene_create / fm_scene_destroy
+//   class Dataset      src/app/Dataset.h:67-105, Dataset.cpp:169-227 -> fm_dataset_* (every frame a
+//                      scene resident on the device, as the reference keeps every Frame in memory)
 //
 // Header only, on top of the C ABI in fluidmarch.h (no CUDA headers needed).
 // Errors throw fluidmarch::Error with the library's message.
 #pragma once
 
 #include <cstddef>
+#include <cstdint>
+#include <memory>
+#include <random>
 #include <stdexcept>
 #include <string>
+#include <vector>
 
 #include "fluidmarch.h"
 
@@ -53,6 +59,8 @@ public:
         : ctx_(ctx), radius_(particle_radius) {
         check(ctx_, fm_scene_create(ctx_, xyz, n, stride, particle_radius, FM_MEM_HOST, &scene_), "fm_scene_create");
     }
+    // adopts a scene the library created (particle files)
+    Frame(fm_ctx* ctx, fm_scene* scene, float particle_radius) : ctx_(ctx), scene_(scene), radius_(particle_radius) {}
     ~Frame() { fm_scene_destroy(scene_); }
     Frame(const Frame&) = delete;
     Frame& operator=(const Frame&) = delete;
@@ -63,6 +71,85 @@ private:
     fm_ctx* ctx_;
     fm_scene* scene_ = nullptr;
     float radius_;
+};
+
+// The reference's Dataset: the particle files pathPrefix + i + pathSuffix,
+// i = 1, 2, ... until one is missing or i > count, each read into a Frame at
+// construction.  As in the reference, a file that fails to load stops the
+// loading and leaves Loaded false (LastError() has the message).
+class Dataset {
+public:
+    Dataset() = default;
+    Dataset(fm_ctx* ctx, const std::string& pathPrefix, const std::string& pathSuffix, float particleRadius,
+            float particleRadiusMultiplier, int count = -1, int threads = 2)
+        : ParticleRadius(particleRadius),
+          ParticleRadiusExt(particleRadiusMultiplier * particleRadius),
+          ParticleRadiusInv(1.0f / particleRadius),
+          ParticleRadiusExtInv(1.0f / (particleRadiusMultiplier * particleRadius)) {
+        char err[512] = {0};
+        fm_dataset* ds = nullptr;
+        if (fm_dataset_open(pathPrefix.c_str(), pathSuffix.c_str(), count, threads, &ds, err, sizeof err) != FM_OK) {
+            error_ = err;
+            return;
+        }
+        const int32_t n = fm_dataset_frames(ds);
+        Frames.reserve((std::size_t)n);
+        for (int32_t i = 0; i < n; ++i) {
+            fm_scene* s = nullptr;
+            if (fm_dataset_scene(ds, ctx, i, ParticleRadius, &s) != FM_OK) {
+                error_ = fm_last_error(ctx);
+                fm_dataset_close(ds);
+                return;
+            }
+            fm_grid_info g{};
+            fm_scene_grid(s, &g);
+            MaxParticles = g.n_particles > MaxParticles ? (std::size_t)g.n_particles : MaxParticles;
+            Frames.push_back(std::unique_ptr<Frame>(new Frame(ctx, s, ParticleRadius)));
+        }
+        fm_dataset_close(ds);
+        Loaded = true;
+    }
+
+    // Dataset::makeCube (Dataset.cpp:228-262): a frame of numParticles uniform
+    // in [-extent, extent]^3 plus one particle at (0, 2 extent, 0), appended to
+    // Frames.  The positions come from a seeded std::mt19937_64, not from the
+    // reference's RandomFloat.
+    static void makeCube(fm_ctx* ctx, Dataset& r, float extent, std::size_t numParticles, float particleRadius,
+                         float particleRadiusMultiplier, uint64_t seed = 0) {
+        r.ParticleRadius = particleRadius;
+        r.ParticleRadiusExt = particleRadiusMultiplier * particleRadius;
+        r.ParticleRadiusInv = 1.0f / particleRadius;
+        r.ParticleRadiusExtInv = 1.0f / r.ParticleRadiusExt;
+        std::mt19937_64 rng(seed);
+        std::uniform_real_distribution<float> u(-extent, extent);
+        std::vector<float> xyz;
+        xyz.reserve(3 * (numParticles + 1));
+        for (std::size_t i = 0; i < numParticles; ++i) {
+            const float x = u(rng), y = u(rng), z = u(rng);
+            xyz.push_back(x);
+            xyz.push_back(y);
+            xyz.push_back(z);
+        }
+        xyz.push_back(0.0f);
+        xyz.push_back(2.0f * extent);
+        xyz.push_back(0.0f);
+        r.Frames.push_back(std::unique_ptr<Frame>(new Frame(ctx, xyz.data(), numParticles + 1, particleRadius)));
+        r.MaxParticles = r.MaxParticles > numParticles + 1 ? r.MaxParticles : numParticles + 1;
+        r.Loaded = true;
+    }
+
+    const std::string& LastError() const { return error_; }
+
+    float ParticleRadius = 0.0f;
+    float ParticleRadiusExt = 0.0f;
+    float ParticleRadiusInv = 0.0f;
+    float ParticleRadiusExtInv = 0.0f;
+    std::vector<std::unique_ptr<Frame>> Frames;
+    std::size_t MaxParticles = 0;
+    bool Loaded = false;
+
+private:
+    std::string error_;
 };
 
 class RayMarcher {

@@ -41,3 +41,46 @@ def test_cpp_raymarcher_adapter(fmlib, tmp_path):
     assert np.array_equal(res[0].view(np.uint32), o["position"].view(np.uint32))
     assert np.array_equal(res[1].view(np.uint32), o["normal"].view(np.uint32))
     assert (res[0][:, 3] == 1).sum() > 100
+
+
+def test_cpp_dataset_autoplay(fmlib, ctx, tmp_path):
+    """fluidmarch::Dataset loads a BGEO series at construction (Frames, MaxParticles, Loaded) and a
+    RayMarcher plays it frame by frame; every frame equals the oracle's march of its particles."""
+    from fluidmarch import bgeo
+
+    exe = tmp_path / "dataset"
+    libdir = os.path.dirname(fmlib.LIB_PATH)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "dataset_adapter.cpp"), "-L", libdir, "-lfluidmarch",
+                    "-Wl,-rpath," + libdir, "-o", str(exe)], check=True)
+    base = scenes.small_scene(seed=51, n=5000, width=64, height=48, max_steps=200)
+    cam = base.cameras[0]
+    prefix = str(tmp_path / "ParticleData_Fluid_")
+    frames = []
+    for i, n in enumerate((5000, 3500, 6500), start=1):
+        sc = scenes.small_scene(seed=60 + i, n=n, width=64, height=48, max_steps=200)
+        frames.append(sc.xyz)
+        bgeo.write(f"{prefix}{i}.bgeo", sc.xyz, compressed=i != 2)
+    depth = O.splat(frames[0], base.support, cam)
+    inp = tmp_path / "cam.bin"
+    with open(inp, "wb") as f:
+        np.array([cam.width, cam.height, base.max_steps], np.int32).tofile(f)
+        np.array([base.support, base.step, base.iso], np.float32).tofile(f)
+        for m in (cam.view, cam.proj, cam.inv_proj_view, cam.position):
+            np.asarray(m, np.float32).tofile(f)
+        depth.astype(np.float32).tofile(f)
+    out = tmp_path / "out.bin"
+    r = subprocess.run([str(exe), prefix, str(inp), str(out), "cube"], check=True, capture_output=True, text=True)
+    assert r.stdout.split() == ["cube", "1001", "1001", "1"]
+    data = open(out, "rb").read()
+    nf = int(np.frombuffer(data[:4], np.int32)[0])
+    maxp = int(np.frombuffer(data[4:12], np.int64)[0])
+    assert nf == 3 and maxp == 6500
+    pos = np.frombuffer(data[12:], np.float32).reshape(nf, cam.n_pixels, 4)
+    hits = 0
+    for i in range(nf):
+        fr = O.build_frame(frames[i], base.support)
+        o = O.march(fr, cam, base.iso, base.step, base.max_steps, 0, depth, threads=0)
+        assert np.array_equal(pos[i].view(np.uint32), o["position"].view(np.uint32)), i
+        hits += int((pos[i][:, 3] == 1).sum())
+    assert hits > 100
