@@ -91,16 +91,23 @@ __device__ __forceinline__ bool disc_box(const SplatArgs& a, const float4& q, fl
     return true;
 }
 
-// One pixel centre of a disc (depth.frag:19-34 restated).
-__device__ __forceinline__ void splat_pixel(const SplatArgs& a, float cx, float cy, float cz, int x, int y,
-                                            uint32_t* __restrict__ depth) {
-    const float R = a.R;
-    float ny = ((float)y + 0.5f) * a.twoHinv - 1.0f;
-    float vy = (ny * cz) / a.P11;
-    float vv = (vy - cy) * a.invR;
+// The disc's quad coordinates of pixel column x (uu) and row y (vv): the
+// view-plane point of the pixel centre relative to the particle, in radii.
+__device__ __forceinline__ float disc_u(const SplatArgs& a, float cx, float cz, int x) {
     float nx = ((float)x + 0.5f) * a.twoWinv - 1.0f;
     float vx = (nx * cz) / a.P00;
-    float uu = (vx - cx) * a.invR;
+    return (vx - cx) * a.invR;
+}
+__device__ __forceinline__ float disc_v(const SplatArgs& a, float cy, float cz, int y) {
+    float ny = ((float)y + 0.5f) * a.twoHinv - 1.0f;
+    float vy = (ny * cz) / a.P11;
+    return (vy - cy) * a.invR;
+}
+
+// One pixel centre of a disc (depth.frag:19-34 restated), from its quad coordinates.
+__device__ __forceinline__ void splat_uv(const SplatArgs& a, float cz, float uu, float vv, int x, int y,
+                                         uint32_t* __restrict__ depth) {
+    const float R = a.R;
     float l2 = uu * uu + vv * vv;
     if (l2 > 1.0f) return;
     float off = cos_poly(1.57079632679f * sqrtf(l2));
@@ -116,14 +123,34 @@ __device__ __forceinline__ void splat_pixel(const SplatArgs& a, float cx, float 
 }
 
 // The whole warp splats one disc: lane l starts at box pixel l and advances
-// 32 pixels per step.
+// 32 pixels per step.  The quad coordinates depend on the column or on the row
+// only: for boxes up to kBox pixels a side the warp computes them once per
+// column and row into shared memory (the same operations, so the same bits)
+// and every pixel reads two of them.
+constexpr int kBox = 128;
+
 __device__ __forceinline__ void splat_disc_warp(const SplatArgs& a, float cx, float cy, float cz, int x0, int x1,
                                                 int y0, int y1, int lane, uint32_t* __restrict__ depth) {
-    const int bw = x1 - x0 + 1;
+    __shared__ float s_u[kThreads / 32][kBox], s_v[kThreads / 32][kBox];
+    const int bw = x1 - x0 + 1, bh = y1 - y0 + 1;
     int x = x0 + lane, y = y0;
     while (x > x1) { x -= bw; ++y; }
+    if (bw <= kBox && bh <= kBox) {
+        float* su = s_u[threadIdx.x >> 5];
+        float* sv = s_v[threadIdx.x >> 5];
+        __syncwarp();  // the previous disc's reads are done
+        for (int i = lane; i < bw; i += 32) su[i] = disc_u(a, cx, cz, x0 + i);
+        for (int i = lane; i < bh; i += 32) sv[i] = disc_v(a, cy, cz, y0 + i);
+        __syncwarp();
+        while (y <= y1) {
+            splat_uv(a, cz, su[x - x0], sv[y - y0], x, y, depth);
+            x += 32;
+            while (x > x1) { x -= bw; ++y; }
+        }
+        return;
+    }
     while (y <= y1) {
-        splat_pixel(a, cx, cy, cz, x, y, depth);
+        splat_uv(a, cz, disc_u(a, cx, cz, x), disc_v(a, cy, cz, y), x, y, depth);
         x += 32;
         while (x > x1) { x -= bw; ++y; }
     }
