@@ -22,10 +22,12 @@
 //   2. a max-depth tile level (8x8 pixels) is built from the buffer, and every
 //      other particle is tested against it: it is kept only if some tile
 //      under its disc holds a depth above the nearest depth the disc can have
-//      (the depth at view z - R, lowered by 8 ulps for rounding); the buffer
+//      (disc_min_bits: the depth at view z - R, lowered for rounding); the buffer
 //      after pass 1 is >= the final one, so no fragment that would win a
 //      pixel is dropped;
 //   3. the kept particles are splatted.
+// Within a disc, a pixel whose buffer already holds a depth at or below the
+// disc's minimum is skipped before its fragment is computed.
 // Memory: 16 B per particle, 4 B read (+ atomic) per covered pixel of a
 // splatted particle, 4 B per tile.
 
@@ -104,22 +106,45 @@ __device__ __forceinline__ float disc_v(const SplatArgs& a, float cy, float cz, 
     return (vy - cy) * a.invR;
 }
 
-// One pixel centre of a disc (depth.frag:19-34 restated), from its quad coordinates.
+// Bits of a depth no fragment of a disc at view z = cz can go below, or 0
+// when there is no such bound.  Every fragment's view z, cz - R * cos(...)
+// with the cosine <= 1, rounds to >= cz - R; the projected depth
+// (P22 z + P32) / (P23 z + P33) grows with z when P22 P33 - P23 P32 > 0 and
+// the denominator is positive and non-decreasing.  The bound is the depth at
+// cz - R lowered by 64 ulps, taken only where the projection's two sums cancel
+// little (|terms| <= 4 |sum|): then the rounding of a depth is a few ulps and
+// two depths in order cannot come out more than ~40 ulps out of order.
+__device__ __forceinline__ uint32_t disc_min_bits(const SplatArgs& a, float cz) {
+    const float zv = cz - a.R;
+    const float num = a.P22 * zv, den = a.P23 * zv;
+    const float A = num + a.P32, B = den + a.P33;
+    if (!(a.P22 * a.P33 - a.P23 * a.P32 > 0.0f) || !(a.P23 >= 0.0f) || !(A > 0.0f) || !(B > 0.0f) ||
+        !(fabsf(num) + fabsf(a.P32) <= 4.0f * A) || !(fabsf(den) + fabsf(a.P33) <= 4.0f * B))
+        return 0u;
+    const uint32_t db = __float_as_uint(A / B);
+    return db > 64u ? db - 64u : 0u;
+}
+
+// One pixel centre of a disc (depth.frag:19-34 restated), from its quad
+// coordinates.  A pixel whose buffer already holds a depth at or below the
+// disc's minimum (dmin) cannot be lowered and is left alone.
 __device__ __forceinline__ void splat_uv(const SplatArgs& a, float cz, float uu, float vv, int x, int y,
-                                         uint32_t* __restrict__ depth) {
+                                         uint32_t dmin, uint32_t* __restrict__ depth) {
     const float R = a.R;
     float l2 = uu * uu + vv * vv;
     if (l2 > 1.0f) return;
+    uint32_t* dst = depth + (uint64_t)y * a.W + x;
+    // plain (possibly stale) read: the buffer only decreases, so a stale value
+    // is >= the current one and skipping on it is safe
+    const uint32_t cur = *dst;
+    if (dmin >= cur) return;
     float off = cos_poly(1.57079632679f * sqrtf(l2));
     float zv = cz - R * off;
     float d = (a.P22 * zv + a.P32) / (a.P23 * zv + a.P33);
     if (!(d >= 0.0f && d < 1.0f)) return;
     d = d + 0.0f;
-    uint32_t* dst = depth + (uint64_t)y * a.W + x;
-    uint32_t bits = __float_as_uint(d);
-    // plain (possibly stale) read first: the buffer only decreases, so a
-    // stale value is >= the current one and skipping on it is safe
-    if (bits < *dst) atomicMin(dst, bits);
+    const uint32_t bits = __float_as_uint(d);
+    if (bits < cur) atomicMin(dst, bits);
 }
 
 // The whole warp splats one disc: lane l starts at box pixel l and advances
@@ -133,6 +158,7 @@ __device__ __forceinline__ void splat_disc_warp(const SplatArgs& a, float cx, fl
                                                 int y0, int y1, int lane, uint32_t* __restrict__ depth) {
     __shared__ float s_u[kThreads / 32][kBox], s_v[kThreads / 32][kBox];
     const int bw = x1 - x0 + 1, bh = y1 - y0 + 1;
+    const uint32_t dmin = disc_min_bits(a, cz);
     int x = x0 + lane, y = y0;
     while (x > x1) { x -= bw; ++y; }
     if (bw <= kBox && bh <= kBox) {
@@ -143,14 +169,14 @@ __device__ __forceinline__ void splat_disc_warp(const SplatArgs& a, float cx, fl
         for (int i = lane; i < bh; i += 32) sv[i] = disc_v(a, cy, cz, y0 + i);
         __syncwarp();
         while (y <= y1) {
-            splat_uv(a, cz, su[x - x0], sv[y - y0], x, y, depth);
+            splat_uv(a, cz, su[x - x0], sv[y - y0], x, y, dmin, depth);
             x += 32;
             while (x > x1) { x -= bw; ++y; }
         }
         return;
     }
     while (y <= y1) {
-        splat_uv(a, cz, disc_u(a, cx, cz, x), disc_v(a, cy, cz, y), x, y, depth);
+        splat_uv(a, cz, disc_u(a, cx, cz, x), disc_v(a, cy, cz, y), x, y, dmin, depth);
         x += 32;
         while (x > x1) { x -= bw; ++y; }
     }
@@ -188,13 +214,7 @@ __device__ __forceinline__ bool cull_keep(const SplatArgs& a, const float4& q) {
     int x0, x1, y0, y1;
     if (!disc_box(a, q, cx, cy, cz, x0, x1, y0, y1)) return false;
     if (!a.cull) return true;
-    // nearest depth the disc can produce (every fragment has view z >= z - R),
-    // lowered by 8 ulps so that rounding in the fragment formula cannot go below it
-    const float zv = cz - a.R;
-    const float d0 = (a.P22 * zv + a.P32) / (a.P23 * zv + a.P33);
-    uint32_t db = __float_as_uint(fmaxf(d0, 0.0f));  // NaN -> 0
-    db = db > 8u ? db - 8u : 0u;
-    const float dmin = __uint_as_float(db);
+    const float dmin = __uint_as_float(disc_min_bits(a, cz));
     for (int ty = y0 / kHizTile; ty <= y1 / kHizTile; ++ty)
         for (int tx = x0 / kHizTile; tx <= x1 / kHizTile; ++tx)
             if (a.hiz[ty * a.hiz_w + tx] > dmin) return true;
