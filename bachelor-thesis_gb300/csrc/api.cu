@@ -93,8 +93,6 @@ int check_params(fm_ctx* ctx, const fm_march_params* p) {
     if (p->flags & FM_MARCH_ANISOTROPIC) {
         if (p->flags & FM_MARCH_PROPOSAL)
             return set_err(ctx, FM_ERR_INVALID, "the anisotropic march takes no proposal");
-        if (p->skip_mode == FM_SKIP_EXACT)
-            return set_err(ctx, FM_ERR_INVALID, "the anisotropic march skips with the reference's flags or not at all");
     }
     return FM_OK;
 }

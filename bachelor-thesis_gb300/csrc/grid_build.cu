@@ -285,8 +285,10 @@ __global__ void k_gather(const float* __restrict__ xyz, uint64_t n, uint32_t str
 // over the particles of the cell's 27-neighbourhood (the sample's candidate
 // set) of W at the particle's distance to the sub-cell box (shrunk by a slack
 // that covers the rounding of the sample's cell assignment), inflated by a
-// margin that covers the FP32 summation error of up to n terms.  One warp per
-// cell computes its 8 sub-cell bounds.
+// margin that covers the FP32 summation error of up to n terms.  The bound is
+// exactly 0 when no particle lies within the support radius of the box: then
+// every term of a sample's sum is 0 (the anisotropic march skips on that
+// too).  One warp per cell computes its 8 sub-cell bounds.
 __global__ void k_cell_bound2(GridDev g, KernelDev k, float slack, float* __restrict__ bound) {
     uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
     uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
@@ -344,7 +346,9 @@ __global__ void k_cell_bound2(GridDev g, KernelDev k, float slack, float* __rest
         for (int s = 1; s < 8; ++s)
             if (l == s) a = acc[s];
         float up = a * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
-        bound[8 * c + l] = (cnt == 0) ? 0.0f : up;
+        // no particle within the support radius of the (grown) box: every
+        // density term of a sample in it is 0, the sum exactly 0
+        bound[8 * c + l] = (cnt == 0 || a == 0.0f) ? 0.0f : up;
     }
 }
 
@@ -422,7 +426,7 @@ __global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, 
     const float n = (float)cnt;
     for (int i = l; i < kBoundBoxes; i += kWarp) {
         const float up = acc[i] * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
-        bound[(uint64_t)kBoundBoxes * c + i] = (cnt == 0) ? 0.0f : up;
+        bound[(uint64_t)kBoundBoxes * c + i] = (cnt == 0 || acc[i] == 0.0f) ? 0.0f : up;
     }
 }
 

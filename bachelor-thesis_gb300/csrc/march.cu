@@ -91,6 +91,23 @@ __device__ __forceinline__ bool locate(const GridDev& g, float px, float py, flo
     return true;
 }
 
+// Exact-skip bound of the bound box that holds a located sample (1/2 or 1/4
+// cell per axis; u < 1 inside the grid, clamped all the same): no sample in
+// the box reaches a density above it, and 0 means no particle lies within the
+// support radius of the box.  +inf for a cell outside the grid.
+__device__ __forceinline__ float box_bound(const GridDev& g, const Loc& L) {
+    if (L.c[0] < 0 || L.c[1] < 0 || L.c[2] < 0 || L.c[0] >= g.dims[0] || L.c[1] >= g.dims[1] || L.c[2] >= g.dims[2])
+        return __int_as_float(0x7f800000);
+    const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)g.dims[0] +
+                       (uint32_t)L.c[2] * (uint32_t)g.dims[0] * (uint32_t)g.dims[1];
+    const int sh = g.bound_shift;
+    const uint32_t nb = 1u << sh;
+    const float fb = (float)nb;
+    const uint32_t bx = min((uint32_t)(fb * L.u[0]), nb - 1u), by = min((uint32_t)(fb * L.u[1]), nb - 1u),
+                   bz = min((uint32_t)(fb * L.u[2]), nb - 1u);
+    return __ldg(g.bound + (c << (3 * sh)) + (bx | (by << sh) | (bz << (2 * sh))));
+}
+
 // Squared distance (cell units) from fraction u to the half-cell slab [lo, lo + 0.5].
 __device__ __forceinline__ float slab_d2(float u, float lo) {
     float d = fmaxf(fmaxf(lo - u, u - (lo + 0.5f)), 0.0f);
@@ -398,21 +415,10 @@ __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc&
                 apply<LEARNED>(a, r, 0.0f);
                 continue;
             }
-            if (a.skip_mode == FM_SKIP_EXACT && L.c[0] >= 0 && L.c[1] >= 0 && L.c[2] >= 0 && L.c[0] < a.g.dims[0] &&
-                L.c[1] < a.g.dims[1] && L.c[2] < a.g.dims[2]) {
-                const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)a.g.dims[0] +
-                                   (uint32_t)L.c[2] * (uint32_t)a.g.dims[0] * (uint32_t)a.g.dims[1];
-                // bound box: 1/2 or 1/4 cell per axis (u < 1 inside the grid; clamped all the same)
-                const int sh = a.g.bound_shift;
-                const uint32_t nb = 1u << sh;
-                const float fb = (float)nb;
-                const uint32_t bx = min((uint32_t)(fb * L.u[0]), nb - 1u), by = min((uint32_t)(fb * L.u[1]), nb - 1u),
-                               bz = min((uint32_t)(fb * L.u[2]), nb - 1u);
-                if (__ldg(a.g.bound + (c << (3 * sh)) + (bx | (by << sh) | (bz << (2 * sh)))) < a.iso) {
-                    if (STATS && cnt) acc.skipped++;
-                    r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
-                    continue;
-                }
+            if (a.skip_mode == FM_SKIP_EXACT && box_bound(a.g, L) < a.iso) {
+                if (STATS && cnt) acc.skipped++;
+                r.q[0] = r.p[0]; r.q[1] = r.p[1]; r.q[2] = r.p[2];
+                continue;
             }
             r.e[0] = r.p[0]; r.e[1] = r.p[1]; r.e[2] = r.p[2];
             return true;
@@ -1466,7 +1472,7 @@ __device__ __forceinline__ void aniso_grad(const GridDev& g, const AnisoDev& an,
 }
 
 struct AnisoCount {
-    uint64_t evals = 0, hits = 0, rays = 0, started = 0;
+    uint64_t evals = 0, hits = 0, rays = 0, started = 0, skipped = 0;
 };
 
 // One chunk of 32 consecutive pixels of view `a` (from pixel `base`): the
@@ -1500,6 +1506,16 @@ __device__ __forceinline__ void aniso_chunk(const MarchArgs& a, const AnisoDev& 
             p[2] = p[2] + s[2];
             if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p[0], p[1], p[2], s[0], s[1], s[2], a.status);
             if (outside_forever(a.g, p[0], p[1], p[2], s[0], s[1], s[2])) break;
+            if (a.skip_mode == FM_SKIP_EXACT && a.iso > 0.0f) {
+                // no particle within the support radius of the sample's bound box:
+                // the anisotropic density (its terms need |r| < H) is exactly 0
+                Loc L;
+                if (locate(a.g, p[0], p[1], p[2], L) && box_bound(a.g, L) == 0.0f) {
+                    if (STATS) c.skipped++;
+                    q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+                    continue;
+                }
+            }
             if (STATS) c.evals++;
             aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
             if (rho >= a.iso) {
@@ -1558,10 +1574,11 @@ __global__ void __launch_bounds__(kThreads)
         }
     }
     if (STATS) {
-        // fm_march_stats order: rays, started, hits, evals
-        const unsigned long long v[4] = {c.rays, c.started, lane == 0 ? c.hits : 0ull, lane == 0 ? c.evals : 0ull};
+        // fm_march_stats order: rays, started, hits, evals, candidates, skipped
+        const unsigned long long v[6] = {c.rays, c.started, lane == 0 ? c.hits : 0ull, lane == 0 ? c.evals : 0ull,
+                                         0ull, lane == 0 ? c.skipped : 0ull};
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < 6; ++j) {
             unsigned long long x = v[j];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(kFull, x, o);

@@ -335,6 +335,39 @@ def run_aniso(args, fm, torch, ctx, ext, scene, sc, cam, out):
         ext.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in ev) / steps
     hits = int((out["depth"] > 0).sum().item())
+    # with the reference's own skip flags (the renderer's mode; results differ from skip off
+    # where a flagged cell is jumped over)
+    P_ref = fm.MarchParams(iso, sc.step, sc.max_steps, sc.bisect, fm.FM_SKIP_REFERENCE, external_depth=True,
+                           anisotropic=True)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with torch.cuda.stream(ext):
+        e0.record(ext)
+        fm.splat_depth(scene, cam, out["start_depth"])
+        fm.march(scene, cam, P_ref, out["position"], out["normal"], out["depth"], out["colour"], out["start_depth"])
+        e1.record(ext)
+        ext.synchronize()
+    ms_ref = e0.elapsed_time(e1)
+    # exact skip (samples whose bound box has no particle within the support radius have
+    # density 0): the same outputs as skip off
+    P_ex = fm.MarchParams(iso, sc.step, sc.max_steps, sc.bisect, fm.FM_SKIP_EXACT, external_depth=True,
+                          anisotropic=True)
+    for _ in range(2):  # builds the coarse, then the fine bound table of the scene
+        fm.splat_depth(scene, cam, out["start_depth"])
+        fm.march(scene, cam, P_ex, out["position"], out["normal"], out["depth"], out["colour"], out["start_depth"])
+    ctx.sync()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(ext):
+        for e0, e1 in ev:
+            e0.record(ext)
+            fm.splat_depth(scene, cam, out["start_depth"])
+            fm.march(scene, cam, P_ex, out["position"], out["normal"], out["depth"], out["colour"],
+                     out["start_depth"])
+            e1.record(ext)
+        ext.synchronize()
+    ms_ex = sum(a.elapsed_time(b) for a, b in ev) / steps
+    hits_ex = int((out["depth"] > 0).sum().item())
+    frame()  # the skip-off outputs again, for the CPU sample below
+    ctx.sync()
     # the CPU port on a sample of started pixels (bisection 0, as the reference)
     depth = out["start_depth"].cpu().numpy()
     started = np.nonzero(depth < 1)[0]
@@ -347,6 +380,9 @@ def run_aniso(args, fm, torch, ctx, ext, scene, sc, cam, out):
     frac = started.size / npx
     return {"iso": iso, "params": {"radius_mult": 2.0, "k_n": 0.5, "k_r": 2.0, "k_s": 2000.0, "n_eps": 1},
             "ms_per_frame": ms, "rays_per_s": npx / (ms / 1e3), "hits": hits, "bisect_iters": sc.bisect,
+            "ms_per_frame_reference_skip": ms_ref, "rays_per_s_reference_skip": npx / (ms_ref / 1e3),
+            "ms_per_frame_exact_skip": ms_ex, "rays_per_s_exact_skip": npx / (ms_ex / 1e3),
+            "exact_skip_hits_equal": hits_ex == hits,
             "cpu_port_rays_per_s": (pix.size / cpu_s) / frac if frac > 0 else None,
             "cpu_sample": f"{pix.size} started pixels, bisection 0, {max(1, cores - 1)} threads, scaled by the "
                           f"started fraction {frac:.3f} to all pixels"}

@@ -61,8 +61,10 @@ extern "C" {
 
 #define FM_MARCH_ANISOTROPIC 4    /* the reference's anisotropic march (RayMarcher.cpp:346-423):
                                      per-sample WPCA kernels with the context's
-                                     fm_aniso_params (fm_set_anisotropy); skip mode off or
-                                     reference, no proposal */
+                                     fm_aniso_params (fm_set_anisotropy); no proposal.
+                                     FM_SKIP_EXACT skips the samples whose bound box has
+                                     no particle within the support radius (density
+                                     exactly 0; iso > 0): same results as FM_SKIP_OFF */
 
 /* learned proposal: features per ray and MLP parameter count */
 #define FM_PROPOSAL_FEATURES 32

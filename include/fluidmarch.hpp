@@ -189,7 +189,6 @@ public:
                               settings_.N_eps, 0};
             check(ctx_, fm_set_anisotropy(ctx_, &a), "fm_set_anisotropy");
             p.flags |= FM_MARCH_ANISOTROPIC;
-            if (p.skip_mode == FM_SKIP_EXACT) p.skip_mode = FM_SKIP_REFERENCE;  // the reference always skips here
         }
         check(ctx_, fm_march(ctx_, frame_->handle(), &camera_, &p, &out_, FM_MEM_HOST, nullptr), "fm_march");
         done_ = true;

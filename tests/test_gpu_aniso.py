@@ -62,11 +62,42 @@ def test_aniso_march_vs_oracle(fmlib, ctx, n, w, h, bisect, skip):
     s.close()
 
 
+@pytest.mark.parametrize("bisect", [0, 8])
+def test_aniso_exact_skip_equals_no_skip(fmlib, ctx, bisect):
+    """FM_SKIP_EXACT steps over samples whose bound box has no particle within the support radius
+    (anisotropic density exactly 0): every output equals the march without skipping, bit for bit,
+    with the coarse and with the fine bound table."""
+    sc = scenes.small_scene(seed=8, n=12000, width=72, height=54, max_steps=160)
+    cam = sc.cameras[0]
+    fr = O.build_frame(sc.xyz, sc.support)
+    iso = aniso_iso(fr, sc.xyz)
+    ctx.set_anisotropy(*ANISO)
+    s = fmlib.Scene(ctx, sc.xyz, sc.support)
+    off = fmlib.render(s, cam, fmlib.MarchParams(iso, sc.step, sc.max_steps, bisect, fmlib.FM_SKIP_OFF,
+                                                 anisotropic=True))
+    p = fmlib.MarchParams(iso, sc.step, sc.max_steps, bisect, fmlib.FM_SKIP_EXACT, anisotropic=True)
+    ctx.set_stats(True)
+    try:
+        coarse = fmlib.render(s, cam, p)  # the scene's first exact march: coarse table
+        st_c = ctx.stats()
+        fine = fmlib.render(s, cam, p)    # then the fine table
+        st_f = ctx.stats()
+    finally:
+        ctx.set_stats(False)
+    for got in (coarse, fine):
+        for k in ("position", "normal", "depth", "colour"):
+            assert np.array_equal(got[k].view(np.uint32), off[k].view(np.uint32)), k
+    assert (off["depth"] > 0).sum() > 200
+    assert st_c["skipped"] > 0 and st_f["skipped"] >= st_c["skipped"]
+    s.close()
+
+
 def test_aniso_rejects_bad_combinations(fmlib, ctx):
     sc = scenes.small_scene(seed=6, n=2000, width=16, height=12)
     s = fmlib.Scene(ctx, sc.xyz, sc.support)
     with pytest.raises(fmlib.FmError):
-        fmlib.render(s, sc.cameras[0], fmlib.MarchParams(1.0, sc.step, 10, 0, fmlib.FM_SKIP_EXACT, anisotropic=True))
+        fmlib.render(s, sc.cameras[0], fmlib.MarchParams(1.0, sc.step, 10, 0, fmlib.FM_SKIP_EXACT, anisotropic=True,
+                                                         proposal=True))
     with pytest.raises(fmlib.FmError):
         ctx.set_anisotropy(3.0)
     with pytest.raises(fmlib.FmError):

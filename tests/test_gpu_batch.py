@@ -278,7 +278,8 @@ def test_batch_learned_view_needs_a_proposal(fmlib, ctx, small_batch):
         bad = fmlib.MarchParams(params.iso, params.step, params.max_steps, 8, fmlib.FM_SKIP_REFERENCE, proposal=True)
         with pytest.raises(fmlib.FmError):
             fmlib.Batch(ctx, [fmlib.View(s, cam, bad, **o)])
-        aniso = fmlib.MarchParams(params.iso, params.step, params.max_steps, 8, fmlib.FM_SKIP_EXACT, anisotropic=True)
+        aniso = fmlib.MarchParams(params.iso, params.step, params.max_steps, 8, fmlib.FM_SKIP_EXACT, anisotropic=True,
+                                  proposal=True)
         with pytest.raises(fmlib.FmError):
             fmlib.Batch(ctx, [fmlib.View(s, cam, aniso, **o)])
     finally:
@@ -293,7 +294,7 @@ def test_batch_with_anisotropic_views(fmlib, ctx, small_batch):
     items = []
     for i, (sc, s, cam, params) in enumerate(small_batch[:6]):
         aniso = i % 2 == 1
-        skip = (fmlib.FM_SKIP_OFF, fmlib.FM_SKIP_REFERENCE)[i % 4 == 1] if aniso else params.skip_mode
+        skip = (fmlib.FM_SKIP_OFF, fmlib.FM_SKIP_REFERENCE, fmlib.FM_SKIP_EXACT)[i % 3] if aniso else params.skip_mode
         p = fmlib.MarchParams(params.iso, params.step, params.max_steps, params.bisect, skip, anisotropic=aniso)
         items.append((sc, s, cam, p))
     want = [single(fmlib, s, cam, p) for sc, s, cam, p in items]
