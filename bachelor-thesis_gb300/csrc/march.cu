@@ -1346,7 +1346,9 @@ __device__ __forceinline__ void mat_vec(const float G[3][3], float x, float y, f
 // p has no particle within the extended radius (density 0).  The weighted
 // moments are taken about p in one pass: mean = p + m, C = S / W - m m^T with
 // m = sum w r / W and S = sum w r r^T, r = x - p (|r| < Hext, so no
-// cancellation to speak of).
+// cancellation to speak of).  This march matches the reference to rounding,
+// not bit for bit, so its sums use fused multiply-adds (__fmaf_rn; the file
+// is compiled without contraction for the isotropic march's exact sums).
 __device__ __forceinline__ bool aniso_eval(const GridDev& g, const AnisoDev& an, float px, float py, float pz, int lane,
                                            float G[3][3], float& detG, float& rho) {
     rho = 0.0f;
@@ -1358,21 +1360,21 @@ __device__ __forceinline__ bool aniso_eval(const GridDev& g, const AnisoDev& an,
         if (!ok) return;
         const float4 q = __ldg(g.pts + j);
         const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-        const float d2 = dot3(rx, ry, rz, rx, ry, rz);
+        const float d2 = __fmaf_rn(rz, rz, __fmaf_rn(ry, ry, rx * rx));
         if (d2 < an.hext2) {
             const float k = sqrtf(d2) * an.hext_inv;
-            const float w = 1.0f - k * k * k;
+            const float w = __fmaf_rn(-(k * k), k, 1.0f);
             ws += w;
             const float wx = w * rx, wy = w * ry, wz = w * rz;
             mx += wx;
             my += wy;
             mz += wz;
-            c00 += wx * rx;
-            c01 += wx * ry;
-            c02 += wx * rz;
-            c11 += wy * ry;
-            c12 += wy * rz;
-            c22 += wz * rz;
+            c00 = __fmaf_rn(wx, rx, c00);
+            c01 = __fmaf_rn(wx, ry, c01);
+            c02 = __fmaf_rn(wx, rz, c02);
+            c11 = __fmaf_rn(wy, ry, c11);
+            c12 = __fmaf_rn(wy, rz, c12);
+            c22 = __fmaf_rn(wz, rz, c22);
             cnt += 1.0f;
         }
     });
@@ -1409,22 +1411,24 @@ __device__ __forceinline__ bool aniso_eval(const GridDev& g, const AnisoDev& an,
     detG = G[0][0] * (G[1][1] * G[2][2] - G[2][1] * G[1][2]) - G[1][0] * (G[0][1] * G[2][2] - G[2][1] * G[0][2]) +
            G[2][0] * (G[0][1] * G[1][2] - G[1][1] * G[0][2]);
     // anisotropic density over the particles within H (AnisotropicKernel::W)
+    const float sd = an.sig * detG;
     float sum = 0.0f;
     for_reach(g, L.c, L.u, 1, an.reach2, lane, [&](uint32_t j, bool ok) {
         if (!ok) return;
         const float4 q = __ldg(g.pts + j);
         const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-        if (dot3(rx, ry, rz, rx, ry, rz) >= an.h2) return;
-        float gx, gy, gz;
-        mat_vec(G, rx, ry, rz, gx, gy, gz);
-        float qq = dot3(gx, gy, gz, gx, gy, gz);
+        if (__fmaf_rn(rz, rz, __fmaf_rn(ry, ry, rx * rx)) >= an.h2) return;
+        const float gx = __fmaf_rn(G[2][0], rz, __fmaf_rn(G[1][0], ry, G[0][0] * rx));
+        const float gy = __fmaf_rn(G[2][1], rz, __fmaf_rn(G[1][1], ry, G[0][1] * rx));
+        const float gz = __fmaf_rn(G[2][2], rz, __fmaf_rn(G[1][2], ry, G[0][2] * rx));
+        float qq = __fmaf_rn(gz, gz, __fmaf_rn(gy, gy, gx * gx));
         if (qq >= an.h2) return;
         qq = sqrtf(qq) * an.hinv;
         if (qq >= 0.5f) {
             const float q_ = 1.0f - qq;
-            sum += an.sig * detG * (2.0f * q_ * q_ * q_);
+            sum = __fmaf_rn(sd, 2.0f * q_ * q_ * q_, sum);
         } else {
-            sum += an.sig * detG * (6.0f * (qq * qq * qq - qq * qq) + 1.0f);
+            sum = __fmaf_rn(sd, __fmaf_rn(6.0f, qq * qq * qq - qq * qq, 1.0f), sum);
         }
     });
     rho = warp_sum(sum);
