@@ -161,17 +161,21 @@ __device__ __forceinline__ void for_ranges_warp(const GridDev& g, const Loc& L, 
     }
 }
 
-// Add the 32 lanes' terms to acc in lane order, identically on every lane:
-// the terms go through this warp's 32 words of shared memory.  Lanes without a
-// term contribute +0, and acc + 0 = acc exactly (acc starts at +0 and never
-// becomes -0), so the sum equals adding only the real terms in order.
+// Add the 32 lanes' terms to acc in lane order, identically on every lane.
+// Terms are >= 0 and acc starts at +0, so acc is never -0 and acc + 0 = acc
+// exactly: only the nonzero terms need adding.  They are packed in lane order
+// into this warp's 32 words of shared memory (padded with +0 to a multiple of
+// 4) and added four per 16-byte read, which shortens the dependent chain of
+// additions to the number of terms inside the support.
 __device__ __forceinline__ float ordered_sum32(float* s, int lane, float w, float acc) {
+    const uint32_t m = __ballot_sync(kFull, w != 0.0f);
+    const int n = __popc(m);
     __syncwarp();
-    s[lane] = w;
+    if (w != 0.0f) s[__popc(m & ((1u << lane) - 1u))] = w;
+    if (lane >= n && lane < ((n + 3) & ~3)) s[lane] = 0.0f;
     __syncwarp();
     const float4* s4 = reinterpret_cast<const float4*>(s);
-#pragma unroll
-    for (int i = 0; i < 8; ++i) {
+    for (int i = 0; i < (n + 3) >> 2; ++i) {
         const float4 v = s4[i];
         acc = acc + v.x;
         acc = acc + v.y;
