@@ -19,7 +19,8 @@ OUT_DIR = os.path.join(HERE, "fluidmarch")
 LIB = os.path.join(OUT_DIR, "libfluidmarch.so")
 OBJ_DIR = os.path.join(HERE, "_build")
 
-SOURCES = ["api.cu", "grid_build.cu", "splat.cu", "march.cu", "batch.cu", "proposal.cu", "bgeo.cu", "inflate.cpp"]
+SOURCES = ["api.cu", "grid_build.cu", "splat.cu", "march.cu", "batch.cu", "proposal.cu", "bgeo.cu", "inflate.cpp",
+           "blur.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
               "-I" + os.path.join(HERE, "..", "include")]

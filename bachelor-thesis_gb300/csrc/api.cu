@@ -166,6 +166,8 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->splat_list.p);
     cudaFree(ctx->prop_ivl.p);
     cudaFree(ctx->file_rec.p);
+    cudaFree(ctx->blur_in.p);
+    cudaFree(ctx->blur_out.p);
     cudaFree(ctx->file_xyz.p);
     cudaFree(ctx->prop_scratch.p);
     cudaFree(ctx->prop_low.p);

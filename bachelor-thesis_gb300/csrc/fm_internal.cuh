@@ -207,6 +207,7 @@ struct fm_ctx {
     fm_proposal* proposal = nullptr;
     fm::DevBuf prop_ivl, prop_scratch, prop_low, prop_judge;
     fm::DevBuf file_rec, file_xyz;  // particle-file loader: point records, gathered positions
+    fm::DevBuf blur_in, blur_out;   // depth blur staging for host buffers
     // live scenes of this context; fm_destroy frees the ones still alive
     std::vector<fm_scene*> scenes;
     // live batches of this context; fm_destroy frees the ones still alive

@@ -44,7 +44,7 @@ EXPORTS = [
     "fm_proposal_create", "fm_proposal_destroy", "fm_set_proposal", "fm_proposal_features", "fm_proposal_intervals",
     "fm_judge", "fm_trainer_create", "fm_trainer_destroy", "fm_trainer_step", "fm_trainer_predict",
     "fm_trainer_params", "fm_density", "fm_set_anisotropy",
-    "fm_trainer_get_state", "fm_trainer_set_state", "fm_selftest_wait_timeout", "fm_bgeo_read", "fm_gunzip", "fm_scene_create_bgeo", "fm_dataset_open", "fm_dataset_frames", "fm_dataset_path",
+    "fm_trainer_get_state", "fm_trainer_set_state", "fm_selftest_wait_timeout", "fm_depth_blur", "fm_bgeo_read", "fm_gunzip", "fm_scene_create_bgeo", "fm_dataset_open", "fm_dataset_frames", "fm_dataset_path",
     "fm_dataset_frame_info", "fm_dataset_max_particles", "fm_dataset_read", "fm_dataset_scene",
     "fm_dataset_last_error", "fm_dataset_close",
 ]
@@ -193,6 +193,7 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_trainer_params.argtypes = [vp, vp]
     L.fm_trainer_get_state.argtypes = [vp, vp, C.POINTER(C.c_int64)]
     L.fm_selftest_wait_timeout.argtypes = [vp, C.c_uint32]
+    L.fm_depth_blur.argtypes = [vp, vp, vp, C.c_int32, C.c_int32, C.c_int32, C.c_float, C.c_int, vp]
     L.fm_trainer_set_state.argtypes = [vp, vp, C.c_int64]
     L.fm_bgeo_read.argtypes = [C.c_char_p, vp, C.c_uint64, C.POINTER(CBgeoInfo), C.c_char_p, C.c_uint64]
     L.fm_gunzip.argtypes = [vp, C.c_uint64, vp, C.c_uint64, C.POINTER(C.c_uint64)]
@@ -446,6 +447,19 @@ def march(scene: Scene, cam, params: MarchParams, position=None, normal=None, de
     cs = camera_struct(cam)
     ps = params.cstruct()
     ctx.check(ctx.L.fm_march(ctx.h, scene.h, C.byref(cs), C.byref(ps), C.byref(o), mem, stream))
+
+
+def depth_blur(ctx: Context, depth, width: int, height: int, n: int = 8, spread: float = 1.0, out=None,
+               stream=None):
+    """The depth Gaussian blur pass (GaussRenderPass / gauss.frag); numpy in -> numpy out unless out is given."""
+    if out is None:
+        out = np.empty(width * height, np.float32)
+    p, mem = _ptr(depth)
+    q, mem2 = _ptr(out)
+    if mem != mem2:
+        raise ValueError("depth and output must both be host or both be device buffers")
+    ctx.check(ctx.L.fm_depth_blur(ctx.h, p, q, int(width), int(height), int(n), float(spread), mem, stream))
+    return out
 
 
 def render(scene: Scene, cam, params: MarchParams, want_start: bool = True) -> dict:

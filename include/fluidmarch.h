@@ -455,6 +455,17 @@ int fm_dataset_scene(fm_dataset* ds, fm_ctx* ctx, int32_t i, float support_radiu
 const char* fm_dataset_last_error(const fm_dataset* ds);
 void fm_dataset_close(fm_dataset* ds);
 
+/* The depth Gaussian blur pass (GaussRenderPass.cpp:13-57,347-355, gauss.frag):
+ * out = sum over i, j = -n..n of ComputeGaussKernel's weight(|i|, |j|) times the
+ * depth image sampled at the pixel centre's UV + (i, j) * (spread / width,
+ * spread / height), linear filtering with clamp-to-edge (8 sub-texel bits).
+ * n in [0, 31] (the reference's GaussN, default 8), spread > 0 (the "Blur
+ * spread" slider, default 1: every tap reads one texel).  Host buffers are
+ * staged and the call returns when out is written; device buffers run on
+ * `stream`. */
+int fm_depth_blur(fm_ctx* ctx, const float* depth, float* out, int32_t width, int32_t height, int32_t n,
+                  float spread, int mem, void* stream);
+
 /* Diagnostics for failure detection: runs the bounded mbarrier wait of the
  * tensor-core kernels on a barrier that never completes.  The wait gives up
  * after `polls` polls (1 .. 2^22), the kernel sets status bit 8 as the

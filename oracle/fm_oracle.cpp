@@ -991,4 +991,63 @@ void orc_density(const float* sorted, const uint32_t* start, const OrcGrid* g, f
     }
 }
 
+// ---- depth Gaussian blur (GaussRenderPass.cpp:13-57,347-355, gauss.frag) ----
+
+// ComputeGaussKernel (GaussRenderPass.cpp:24-57): weights for i, j = 0..N at
+// out[j + i (N + 1)], normalised over the whole (2N+1)^2 grid.
+void orc_gauss_weights(int32_t N, float* out) {
+    const float e = 2.71828182845904523536f;
+    float sum = 0.0f;
+    for (int i = 0; i <= N; ++i)
+        for (int j = 0; j <= N; ++j) {
+            const float r = std::sqrt((float)i * (float)i + (float)j * (float)j);
+            const float y = std::pow(e, -0.5f * r * r);
+            out[j + i * (N + 1)] = y;
+            if (i == 0 && j == 0) sum += y;
+            else if (i != 0 && j != 0) sum += 4.0f * y;
+            else sum += 2.0f * y;
+        }
+    for (int k = 0; k < (N + 1) * (N + 1); ++k) out[k] /= sum;
+}
+
+// gauss.frag: sum over i (outer) and j (inner) of weight(|i|, |j|) times the
+// depth texture at UV + (i, j) * (spread / W, spread / H), UV the pixel centre;
+// linear filtering (texel coordinate u W - 1/2, floor, fraction kept to 8
+// sub-texel bits), clamp-to-edge.  FP32, every operation rounded separately.
+void orc_depth_blur(const float* in, float* out, int32_t W, int32_t H, int32_t N, float spread) {
+    std::vector<float> w((size_t)(N + 1) * (N + 1));
+    orc_gauss_weights(N, w.data());
+    const float tw = spread / (float)W, th = spread / (float)H;
+    auto texel = [&](int x, int y) {
+        x = std::min(std::max(x, 0), W - 1);
+        y = std::min(std::max(y, 0), H - 1);
+        return in[(size_t)y * W + x];
+    };
+    auto sample = [&](float s, float t) {
+        const float u = s * (float)W - 0.5f, v = t * (float)H - 0.5f;
+        const float fu = std::floor(u), fv = std::floor(v);
+        float al = u - fu, be = v - fv;
+        al = std::nearbyint(al * 256.0f) * 0.00390625f;
+        be = std::nearbyint(be * 256.0f) * 0.00390625f;
+        const int i0 = (int)std::fmax(std::fmin(fu, (float)W), -1.0f);
+        const int j0 = (int)std::fmax(std::fmin(fv, (float)H), -1.0f);
+        const float t00 = texel(i0, j0), t10 = texel(i0 + 1, j0), t01 = texel(i0, j0 + 1), t11 = texel(i0 + 1, j0 + 1);
+        const float ia = 1.0f - al, ib = 1.0f - be;
+        return (ia * ib) * t00 + (al * ib) * t10 + (ia * be) * t01 + (al * be) * t11;
+    };
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            const float u0 = ((float)x + 0.5f) / (float)W, v0 = ((float)y + 0.5f) / (float)H;
+            float sum = 0.0f;
+            for (int i = -N; i <= N; ++i) {
+                const float s = u0 + (float)i * tw;
+                for (int j = -N; j <= N; ++j) {
+                    const float t = v0 + (float)j * th;
+                    sum = sum + w[(size_t)std::abs(i) * (N + 1) + std::abs(j)] * sample(s, t);
+                }
+            }
+            out[(size_t)y * W + x] = sum;
+        }
+}
+
 }  // extern "C"

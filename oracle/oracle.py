@@ -83,6 +83,8 @@ def lib():
                                       C.c_int32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         L.orc_density.argtypes = [_f32p, _u32p, C.POINTER(OrcGrid), C.c_float, _f32p, C.c_int64, C.c_int32,
                                   np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")]
+        L.orc_gauss_weights.argtypes = [C.c_int32, _f32p]
+        L.orc_depth_blur.argtypes = [_f32p, _f32p, C.c_int32, C.c_int32, C.c_int32, C.c_float]
         _lib = L
     return _lib
 
@@ -314,4 +316,19 @@ def ref_dataset_load(prefix: str, suffix: str, count: int, radius: float, cap_po
     if nf < 0:
         return None
     return nf, counts[:nf].copy(), int(mp.value), xyz
+
+
+def gauss_weights(n: int) -> np.ndarray:
+    """ComputeGaussKernel's (n + 1) x (n + 1) weights (GaussRenderPass.cpp:24-57)."""
+    out = np.zeros((n + 1) * (n + 1), np.float32)
+    lib().orc_gauss_weights(int(n), out)
+    return out.reshape(n + 1, n + 1)
+
+
+def depth_blur(depth: np.ndarray, width: int, height: int, n: int = 8, spread: float = 1.0) -> np.ndarray:
+    """The depth Gaussian blur of gauss.frag restated in FP32 (fm_oracle.cpp orc_depth_blur)."""
+    src = np.ascontiguousarray(depth, np.float32).reshape(-1)
+    out = np.zeros(width * height, np.float32)
+    lib().orc_depth_blur(src, out, int(width), int(height), int(n), float(spread))
+    return out
 
