@@ -64,11 +64,12 @@ __device__ __forceinline__ float dot3(float ax, float ay, float az, float bx, fl
 // CubicSplineKernel::W for q2 = dot(r, r) < h2 (Kernel.cpp:16-32).
 __device__ __forceinline__ float w_in(const KernelDev& k, float q2) {
     float q = sqrtf(q2) * k.hinv;
-    if (q >= 0.5f) {
-        float q_ = 1.0f - q;
-        return k.sig * (((2.0f * q_) * q_) * q_);
-    }
-    return k.sig * (6.0f * (((q * q) * q) - (q * q)) + 1.0f);
+    // both branches of the reference's kernel, then a select: lanes of a warp
+    // fall on either side of q = 0.5, and a select costs less than two paths
+    float q_ = 1.0f - q;
+    float a = k.sig * (((2.0f * q_) * q_) * q_);
+    float b = k.sig * (6.0f * (((q * q) * q) - (q * q)) + 1.0f);
+    return q >= 0.5f ? a : b;
 }
 
 // CubicSplineKernel::gradW for 0 < rn < h2 (Kernel.cpp:34-52): the term itself.
@@ -302,7 +303,7 @@ struct SplatBatch {
 };
 SplatArgs splat_args(const fm_scene* s, const fm_camera* cam);
 constexpr int kSplatHizTile = 8;
-constexpr uint64_t kSplatSample = 8;
+constexpr uint64_t kSplatSample = 16;
 int launch_splat_batch(fm_ctx* ctx, const SplatBatch& b, cudaStream_t st);
 
 // March (march.cu): all pointers device pointers.

@@ -17,8 +17,9 @@
 // at a time.  Three passes keep the work near the visible surface without
 // changing the result (the buffer is a minimum, so leaving out a particle that
 // cannot lower any pixel is exact):
-//   1. every 8th particle is splatted: the discs, about five particle spacings
-//      wide, already form an opaque cover of the front surface;
+//   1. every 16th particle (in cell order) is splatted: the discs, about five
+//      particle spacings wide, already form a nearly opaque cover of the front
+//      surface;
 //   2. a max-depth tile level (8x8 pixels) is built from the buffer, and every
 //      other particle is tested against it: it is kept only if some tile
 //      under its disc holds a depth above the nearest depth the disc can have
