@@ -887,7 +887,7 @@ __device__ __forceinline__ void flush_stats(const MarchArgs& a, int lane, const 
 // the launch's counter.  BATCH: `a` holds the launch-wide fields and the total
 // tile count; tile t belongs to view find_view(tile_pfx, t) of `views`.
 template <bool STATS, bool BATCH, bool LEARNED>
-__global__ void __launch_bounds__(kThreads, 4) k_march(const MarchArgs a, const MarchArgs* __restrict__ views,
+__global__ void __launch_bounds__(kThreads, 3) k_march(const MarchArgs a, const MarchArgs* __restrict__ views,
                                                       const uint32_t* __restrict__ tile_pfx, int nviews) {
     const int lane = threadIdx.x & 31;
     Acc acc;
