@@ -359,34 +359,35 @@ __global__ void k_cell_bound2(GridDev g, KernelDev k, float slack, float* __rest
 // sample's candidate set) of W at the particle's distance to the box grown by
 // a slack that covers the rounding of the sample's cell assignment, inflated
 // by a margin that covers the FP32 summation error of up to n terms (the
-// bound's own and the sample's).  One warp per cell: the lanes stride over the
-// neighbourhood's particles and add W into the cell's 64 sums in shared memory
-// (the order of those additions does not matter: the margin covers it).
-// Per particle, the per-axis distances to the 4 slabs give every box's
-// distance; boxes beyond the support radius on one axis are not visited.
+// bound's own and the sample's), and exactly 0 when no particle lies within
+// the support radius of the box.  One warp per cell, lane l owns boxes l and
+// l + 32: the warp loads 32 neighbourhood particles at a time (one coalesced
+// 512-byte read) and passes them to every lane by shuffles, so each lane adds
+// W for its two boxes in registers (the order of the additions does not
+// matter: the margin covers it).
 constexpr int kBoundWarps = 8;
 
 __global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, KernelDev k, float slack,
                                                                      float* __restrict__ bound) {
-    __shared__ float sums[kBoundWarps][kBoundBoxes];
     const uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
     const uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
     const int l = threadIdx.x % kWarp;
     if (c >= ncells) return;  // warp-uniform
-    float* acc = sums[threadIdx.x / kWarp];
-    for (int i = l; i < kBoundBoxes; i += kWarp) acc[i] = 0.0f;
-    __syncwarp();
     const int cc[3] = {(int)(c % (uint64_t)g.dims[0]), (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]),
                        (int)(c / ((uint64_t)g.dims[0] * g.dims[1]))};
-    // box edges per axis, grown by the slack: [lo[i], hi[i]] for i = 0..3
-    float lo[3][4], hi[3][4];
+    // this lane's boxes b = l and l + 32 (b = ix + 4 iy + 16 iz), edges grown by the slack
+    float lo[2][3], hi[2][3];
 #pragma unroll
-    for (int a = 0; a < 3; ++a)
+    for (int h = 0; h < 2; ++h) {
+        const int b = l + 32 * h;
+        const int ib[3] = {b & 3, (b >> 2) & 3, b >> 4};
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
-            lo[a][i] = g.min[a] + ((float)cc[a] + 0.25f * (float)i) * g.cell - slack;
-            hi[a][i] = g.min[a] + ((float)cc[a] + 0.25f * (float)(i + 1)) * g.cell + slack;
+        for (int a = 0; a < 3; ++a) {
+            lo[h][a] = g.min[a] + ((float)cc[a] + 0.25f * (float)ib[a]) * g.cell - slack;
+            hi[h][a] = g.min[a] + ((float)cc[a] + 0.25f * (float)(ib[a] + 1)) * g.cell + slack;
         }
+    }
+    float acc0 = 0.0f, acc1 = 0.0f;
     uint32_t cnt = 0;
     const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, g.dims[0] - 1);
     for (int z = max(cc[2] - 1, 0); z <= min(cc[2] + 1, g.dims[2] - 1); ++z)
@@ -394,39 +395,37 @@ __global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, 
             const uint64_t row = ((uint64_t)z * g.dims[1] + y) * g.dims[0];
             const uint32_t b = g.sub[8 * (row + x0)], e = g.sub[8 * (row + x1) + 8];
             cnt += e - b;
-            for (uint32_t j = b + l; j < e; j += kWarp) {
-                const float4 q = g.pts[j];
-                const float qa[3] = {q.x, q.y, q.z};
-                float d2[3][4];  // squared distance per axis to each grown slab
+            for (uint32_t j0 = b; j0 < e; j0 += kWarp) {
+                const uint32_t j = j0 + (uint32_t)l;
+                const float4 mine = j < e ? g.pts[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const int m = (int)min(e - j0, (uint32_t)kWarp);
+                for (int t = 0; t < m; ++t) {
+                    const float qx = __shfl_sync(0xffffffffu, mine.x, t);
+                    const float qy = __shfl_sync(0xffffffffu, mine.y, t);
+                    const float qz = __shfl_sync(0xffffffffu, mine.z, t);
+                    const float q[3] = {qx, qy, qz};
+                    float d2[2];
 #pragma unroll
-                for (int a = 0; a < 3; ++a)
+                    for (int h = 0; h < 2; ++h) {
+                        d2[h] = 0.0f;
 #pragma unroll
-                    for (int i = 0; i < 4; ++i) {
-                        const float d = fmaxf(fmaxf(lo[a][i] - qa[a], qa[a] - hi[a][i]), 0.0f);
-                        d2[a][i] = d * d;
-                    }
-#pragma unroll
-                for (int iz = 0; iz < 4; ++iz) {
-                    if (d2[2][iz] >= k.h2) continue;
-#pragma unroll
-                    for (int iy = 0; iy < 4; ++iy) {
-                        const float syz = d2[2][iz] + d2[1][iy];
-                        if (syz >= k.h2) continue;
-#pragma unroll
-                        for (int ix = 0; ix < 4; ++ix) {
-                            const float r2 = syz + d2[0][ix];
-                            if (r2 < k.h2) atomicAdd(acc + (ix + 4 * iy + 16 * iz), w_in(k, r2));
+                        for (int a = 0; a < 3; ++a) {
+                            const float d = fmaxf(fmaxf(lo[h][a] - q[a], q[a] - hi[h][a]), 0.0f);
+                            d2[h] += d * d;
                         }
                     }
+                    if (d2[0] < k.h2) acc0 += w_in(k, d2[0]);
+                    if (d2[1] < k.h2) acc1 += w_in(k, d2[1]);
                 }
             }
         }
-    __syncwarp();
     const float eps = 5.9604645e-8f;  // 2^-24
     const float n = (float)cnt;
-    for (int i = l; i < kBoundBoxes; i += kWarp) {
-        const float up = acc[i] * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
-        bound[(uint64_t)kBoundBoxes * c + i] = (cnt == 0 || acc[i] == 0.0f) ? 0.0f : up;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float a = h ? acc1 : acc0;
+        const float up = a * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
+        bound[(uint64_t)kBoundBoxes * c + l + 32 * h] = (cnt == 0 || a == 0.0f) ? 0.0f : up;
     }
 }
 
