@@ -238,8 +238,8 @@ int fm_host_alloc(fm_ctx* ctx, size_t bytes, void** out) {
 void fm_host_free(fm_ctx* ctx, void* p) {
     if (ctx) {
         cudaSetDevice(ctx->device);
-        // a kernel may still be writing into the block
-        cudaStreamSynchronize(ctx->stream);
+        // a kernel on any stream may still be writing into the block
+        cudaDeviceSynchronize();
         ctx->host_allocs.erase((uintptr_t)p);
     }
     if (p) cudaFreeHost(p);

@@ -161,7 +161,9 @@ int fm_sync(fm_ctx* ctx, int timeout_ms);
  * stream is idle, 0 when work is pending, < 0 on error.  Unlike the reference,
  * "done" means every output has been written. */
 int fm_query(fm_ctx* ctx);
-/* Pinned host memory for staged, asynchronous copies. */
+/* Pinned (page-locked, mapped) host memory.  March outputs that lie inside
+ * such a block are written by the kernels directly, with no copy after the
+ * march.  fm_host_free waits for the device before it frees the block. */
 int fm_host_alloc(fm_ctx* ctx, size_t bytes, void** out);
 void fm_host_free(fm_ctx* ctx, void* p);
 
