@@ -539,6 +539,12 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
                 FM_CUDA(ctx, cudaMemcpyAsync(user[i], dev[i], npx * per[i], cudaMemcpyDeviceToHost, st));
         if (out->start_depth && !external)
             FM_CUDA(ctx, cudaMemcpyAsync(out->start_depth, z, npx * 4, cudaMemcpyDeviceToHost, st));
+        // every host buffer in fm_host_alloc memory: nothing has to wait here, the
+        // call is asynchronous as with device buffers (fm_query / fm_sync)
+        bool all_pinned = true;
+        for (int i = 0; i < 4; ++i) all_pinned = all_pinned && (!user[i] || direct[i]);
+        if (out->start_depth) all_pinned = all_pinned && host_mapped(ctx, out->start_depth, npx * 4) != nullptr;
+        if (all_pinned) return FM_OK;
         unsigned int* hs = (unsigned int*)ctx->h_pinned_small;
         FM_CUDA(ctx, cudaMemcpyAsync(hs, ctx->d_status, sizeof(unsigned int), cudaMemcpyDeviceToHost, st));
         FM_CUDA(ctx, cudaStreamSynchronize(st));

@@ -436,7 +436,11 @@ def splat_depth(scene: Scene, cam, out=None, stream=None):
 
 def march(scene: Scene, cam, params: MarchParams, position=None, normal=None, depth=None, colour=None,
           start_depth=None, stream=None):
-    """Render one view.  Outputs are the given buffers (all host or all device)."""
+    """Render one view.  Outputs are the given buffers (all host or all device).
+
+    Asynchronous for device buffers and for host buffers that all come from
+    ``Context.host_array`` (call ``ctx.sync()`` before reading them); other host
+    buffers are written when the call returns."""
     ctx = scene.ctx
     bufs = [position, normal, depth, colour, start_depth]
     mems = {m for m in (_ptr(b)[1] for b in bufs) if m is not None}

@@ -185,6 +185,7 @@ class Dataset:
             else:
                 fm.march(scene, camera, params, out["position"], out["normal"], out["depth"], out.get("colour"),
                          out.get("start_depth"))
+                ctx.sync()  # outputs in the library's pinned memory are written asynchronously
                 yield i, out
 
     def close(self):

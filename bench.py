@@ -598,11 +598,13 @@ def run_ours(args):
 
     for _ in range(max(1, args.warmup // 2)):
         e2e_frame()
+    ctx.sync()
     if dist:
         dist.barrier()
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_frame()
+    ctx.sync()  # the march into pinned buffers returns at once; the last frame must be written
     e2e_s = time.perf_counter() - t0
     e2e_value, _, _ = throughput(npx * args.steps, e2e_s, dist, dev)
 

@@ -163,7 +163,10 @@ int fm_sync(fm_ctx* ctx, int timeout_ms);
 int fm_query(fm_ctx* ctx);
 /* Pinned (page-locked, mapped) host memory.  March outputs that lie inside
  * such a block are written by the kernels directly, with no copy after the
- * march.  fm_host_free waits for the device before it frees the block. */
+ * march; when every host buffer of an fm_march call (outputs and start depth)
+ * lies in such blocks the call is asynchronous, as with device buffers: poll
+ * fm_query, finish with fm_sync (which also reports kernel status).
+ * fm_host_free waits for the device before it frees the block. */
 int fm_host_alloc(fm_ctx* ctx, size_t bytes, void** out);
 void fm_host_free(fm_ctx* ctx, void* p);
 
@@ -227,8 +230,8 @@ int fm_splat_depth(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, flo
 /* RayMarcher::Start + PerPixel_Isotropic (RayMarcher.cpp:102-112,256-344)
  * plus the composition shading: splat (unless FM_MARCH_EXTERNAL_DEPTH),
  * march every pixel, bisect, take the gradient normal, shade.  Asynchronous
- * for device outputs; for host outputs the call returns once they are
- * written. */
+ * for device outputs and for host buffers that all lie in fm_host_alloc
+ * blocks; for other host buffers the call returns once they are written. */
 int fm_march(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, const fm_march_params* params,
              const fm_frame_out* out, int mem, void* stream);
 

@@ -4,8 +4,9 @@
 //   class RayMarcher   src/app/AdvancedRenderer/RayMarcher.h:28-77
 //     RayMarcher()     RayMarcher.cpp:66-69   -> fm_create
 //     Prepare(...)     RayMarcher.cpp:76-100  -> stores the arguments
-//     Start()          RayMarcher.cpp:102-112 -> fm_march (returns when the outputs are written)
-//     IsDone()         RayMarcher.h:44        -> true once Start() returned (no race on the last pixel)
+//     Start()          RayMarcher.cpp:102-112 -> fm_march into library-pinned blocks (asynchronous)
+//     IsDone()         RayMarcher.h:44        -> fm_query; on completion the outputs are copied to the
+//                                                caller's buffers (no race on the last pixel)
 //     Exit()           RayMarcher.cpp:71-74   -> fm_sync
 //   struct VisualizationSettings  RayMarcher.h:12-26
 //   class Frame        src/app/Dataset.h:37-65 -> fm_scene_create / fm_scene_destroy
@@ -18,6 +19,7 @@
 
 #include <cstddef>
 #include <cstdint>
+#include <cstring>
 #include <memory>
 #include <random>
 #include <stdexcept>
@@ -155,7 +157,11 @@ private:
 class RayMarcher {
 public:
     explicit RayMarcher(int device = 0) { check(nullptr, fm_create(&ctx_, device), "fm_create"); }
-    ~RayMarcher() { fm_destroy(ctx_); }
+    ~RayMarcher() {
+        if (started_) fm_sync(ctx_, -1);
+        release();
+        fm_destroy(ctx_);
+    }
     RayMarcher(const RayMarcher&) = delete;
     RayMarcher& operator=(const RayMarcher&) = delete;
 
@@ -165,18 +171,24 @@ public:
     // (splat) depth buffer the reference consumes, 1.0 = no particle.
     void Prepare(const VisualizationSettings& settings, const fm_camera& camera, Frame& frame, float* positions,
                  float* normals, float* depth) {
+        if (started_) Exit();
         settings_ = settings;
         camera_ = camera;
         frame_ = &frame;
-        out_ = fm_frame_out{};
-        out_.position = positions;
-        out_.normal = normals;
-        out_.start_depth = depth;
+        positions_ = positions;
+        normals_ = normals;
+        depth_ = depth;
         done_ = false;
     }
 
+    // Asynchronous, like the reference's thread pool: the march runs into
+    // pinned blocks of the library (written by the kernels directly) and
+    // returns at once; IsDone() polls the context's stream.
     void Start() {
         if (!frame_) throw Error(FM_ERR_INVALID, "Prepare() first");
+        if (started_) Exit();
+        const std::size_t npx = (std::size_t)camera_.width * (std::size_t)camera_.height;
+        reserve(npx);
         fm_march_params p{};
         p.iso_density = settings_.IsoDensity;
         p.step_size = settings_.StepSize;
@@ -190,21 +202,70 @@ public:
             check(ctx_, fm_set_anisotropy(ctx_, &a), "fm_set_anisotropy");
             p.flags |= FM_MARCH_ANISOTROPIC;
         }
-        check(ctx_, fm_march(ctx_, frame_->handle(), &camera_, &p, &out_, FM_MEM_HOST, nullptr), "fm_march");
-        done_ = true;
+        std::memcpy(pin_depth_, depth_, npx * sizeof(float));
+        fm_frame_out out{};
+        out.position = positions_ ? pin_pos_ : nullptr;
+        out.normal = normals_ ? pin_nrm_ : nullptr;
+        out.start_depth = pin_depth_;
+        check(ctx_, fm_march(ctx_, frame_->handle(), &camera_, &p, &out, FM_MEM_HOST, nullptr), "fm_march");
+        started_ = true;
+        done_ = false;
     }
 
-    bool IsDone() const { return done_; }
+    // True once every pixel is written (the reference's IsDone could report done
+    // while a worker still wrote its last pixel; this one cannot).
+    bool IsDone() {
+        if (!started_) return done_;
+        const int q = fm_query(ctx_);
+        if (q < 0) throw Error(-q, std::string("fm_query: ") + fm_last_error(ctx_));
+        if (q == 0) return false;
+        finish();
+        return true;
+    }
 
-    void Exit() { check(ctx_, fm_sync(ctx_, -1), "fm_sync"); }
+    // Waits for the march and delivers its outputs (RayMarcher::Exit joins the workers).
+    void Exit() {
+        if (started_) finish();
+        check(ctx_, fm_sync(ctx_, -1), "fm_sync");
+    }
 
 private:
+    void finish() {
+        check(ctx_, fm_sync(ctx_, -1), "fm_sync");  // also reports kernel status
+        const std::size_t npx = (std::size_t)camera_.width * (std::size_t)camera_.height;
+        if (positions_) std::memcpy(positions_, pin_pos_, npx * 16);
+        if (normals_) std::memcpy(normals_, pin_nrm_, npx * 16);
+        started_ = false;
+        done_ = true;
+    }
+    void reserve(std::size_t npx) {
+        if (npx <= cap_) return;
+        release();
+        void* p = nullptr;
+        check(ctx_, fm_host_alloc(ctx_, npx * 16, &p), "fm_host_alloc");
+        pin_pos_ = (float*)p;
+        check(ctx_, fm_host_alloc(ctx_, npx * 16, &p), "fm_host_alloc");
+        pin_nrm_ = (float*)p;
+        check(ctx_, fm_host_alloc(ctx_, npx * 4, &p), "fm_host_alloc");
+        pin_depth_ = (float*)p;
+        cap_ = npx;
+    }
+    void release() {
+        fm_host_free(ctx_, pin_pos_);
+        fm_host_free(ctx_, pin_nrm_);
+        fm_host_free(ctx_, pin_depth_);
+        pin_pos_ = pin_nrm_ = pin_depth_ = nullptr;
+        cap_ = 0;
+    }
+
     fm_ctx* ctx_ = nullptr;
     VisualizationSettings settings_{};
     fm_camera camera_{};
     Frame* frame_ = nullptr;
-    fm_frame_out out_{};
-    bool done_ = false;
+    float *positions_ = nullptr, *normals_ = nullptr, *depth_ = nullptr;
+    float *pin_pos_ = nullptr, *pin_nrm_ = nullptr, *pin_depth_ = nullptr;
+    std::size_t cap_ = 0;
+    bool started_ = false, done_ = false;
 };
 
 }  // namespace fluidmarch

@@ -333,4 +333,13 @@ def test_outputs_in_library_pinned_memory(fmlib, ctx):
     fmlib.march(s, cam, p, pin["position"], pin["normal"], pin["depth"], pin["colour"])
     for k in pin:
         assert np.array_equal(bits(pin[k]), bits(want[k])), k
+    # every host buffer in the library's memory: the call returns at once and
+    # fm_sync completes it
+    allp = {k: ctx.host_array(v.shape) for k, v in want.items()}
+    for v in allp.values():
+        v[...] = -1.0
+    fmlib.march(s, cam, p, allp["position"], allp["normal"], allp["depth"], allp["colour"], allp["start_depth"])
+    ctx.sync()
+    for k in allp:
+        assert np.array_equal(bits(allp[k]), bits(want[k])), k
     s.close()
