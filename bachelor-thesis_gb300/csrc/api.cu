@@ -182,6 +182,8 @@ const char* fm_last_error(const fm_ctx* ctx) {
     return ctx->err.c_str();
 }
 
+const char* fm_last_error_string(const fm_ctx* ctx) { return fm_last_error(ctx); }
+
 void* fm_stream(fm_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
 
 int fm_sync(fm_ctx* ctx, int timeout_ms) {
@@ -320,6 +322,12 @@ int fm_scene_update(fm_scene* s, const float* xyz, uint64_t n, uint32_t stride, 
     if (mem != FM_MEM_HOST && mem != FM_MEM_DEVICE) return set_err(ctx, FM_ERR_INVALID, "unknown memory kind");
     cudaSetDevice(ctx->device);
     return scene_build(s, xyz, n, stride, mem);
+}
+
+int fm_scene_upload(fm_ctx* ctx, const float* xyz, uint64_t n, int32_t stride_floats, float support_radius,
+                    fm_scene** out) {
+    if (stride_floats < 0) return ctx ? set_err(ctx, FM_ERR_INVALID, "negative stride") : FM_ERR_INVALID;
+    return fm_scene_create(ctx, xyz, n, (uint32_t)stride_floats, support_radius, FM_MEM_HOST, out);
 }
 
 void fm_scene_destroy(fm_scene* s) {

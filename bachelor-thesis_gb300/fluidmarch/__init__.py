@@ -36,7 +36,7 @@ FM_PROPOSAL_FEATURES = 32
 FM_PROPOSAL_PARAMS = 6402
 
 EXPORTS = [
-    "fm_version", "fm_create", "fm_destroy", "fm_last_error", "fm_stream", "fm_sync", "fm_query", "fm_host_alloc",
+    "fm_version", "fm_create", "fm_destroy", "fm_last_error", "fm_last_error_string", "fm_scene_upload", "fm_stream", "fm_sync", "fm_query", "fm_host_alloc",
     "fm_host_free", "fm_scene_create", "fm_scene_update", "fm_scene_destroy", "fm_scene_grid", "fm_scene_download",
     "fm_splat_depth", "fm_march", "fm_set_stats", "fm_march_stats_get", "fm_grid_build_noalloc",
     "fm_set_tile_config", "fm_get_tile_config", "fm_batch_create", "fm_batch_run", "fm_batch_refresh",
@@ -146,6 +146,9 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_destroy.restype = None
     L.fm_last_error.argtypes = [vp]
     L.fm_last_error.restype = C.c_char_p
+    L.fm_last_error_string.argtypes = [vp]
+    L.fm_last_error_string.restype = C.c_char_p
+    L.fm_scene_upload.argtypes = [vp, vp, C.c_uint64, C.c_int32, C.c_float, C.POINTER(vp)]
     L.fm_stream.argtypes = [vp]
     L.fm_stream.restype = vp
     L.fm_sync.argtypes = [vp, C.c_int]

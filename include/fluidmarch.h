@@ -152,6 +152,8 @@ int fm_create(fm_ctx** out, int device);
 void fm_destroy(fm_ctx* ctx);
 /* Message of the last failing call on this context (never NULL). */
 const char* fm_last_error(const fm_ctx* ctx);
+/* The same message under the name a binding of the reference's renderer may expect. */
+const char* fm_last_error_string(const fm_ctx* ctx);
 /* The context's stream as a cudaStream_t. */
 void* fm_stream(fm_ctx* ctx);
 /* Wait for all work on the context's stream; FM_ERR_TIMEOUT after timeout_ms
@@ -183,6 +185,10 @@ int fm_scene_create(fm_ctx* ctx, const float* xyz, uint64_t n, uint32_t stride, 
  * radius): a new frame of the same dataset (Dataset::ReadFile adds one,
  * Dataset.cpp:292-306). */
 int fm_scene_update(fm_scene* scene, const float* xyz, uint64_t n, uint32_t stride, int mem);
+/* fm_scene_create from host memory (the reference builds a Frame from a host
+ * std::vector of positions, Dataset.cpp:9-24). */
+int fm_scene_upload(fm_ctx* ctx, const float* xyz, uint64_t n, int32_t stride_floats, float support_radius,
+                    fm_scene** out);
 void fm_scene_destroy(fm_scene* scene);
 int fm_scene_grid(const fm_scene* scene, fm_grid_info* out);
 /* Download the grid build (host pointers; any may be NULL):

@@ -55,6 +55,8 @@ def test_invalid_arguments_without_device(fmlib):
     assert L.fm_scene_create(None, None, 0, 3, 0.1, 0, None) == fmlib.FM_ERR_INVALID
     assert L.fm_march(None, None, None, None, None, 0, None) == fmlib.FM_ERR_INVALID
     assert L.fm_last_error(None) == b"no context"
+    assert L.fm_last_error_string(None) == b"no context"
+    assert L.fm_scene_upload(None, None, 0, 3, 0.1, None) == fmlib.FM_ERR_INVALID
     assert L.fm_selftest_wait_timeout(None, 1) == fmlib.FM_ERR_INVALID
     assert L.fm_trainer_set_state(None, None, 0) == fmlib.FM_ERR_INVALID
 

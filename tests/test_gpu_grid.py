@@ -83,6 +83,22 @@ def test_scene_from_device_memory(fmlib, ctx):
     assert np.array_equal(s.download()["perm"], fr.perm)
 
 
+def test_scene_upload_entry(fmlib, ctx):
+    """fm_scene_upload (host positions) builds the same grid as fm_scene_create."""
+    import ctypes as C
+
+    sc = scenes.small_scene(seed=7, n=5000)
+    h = C.c_void_p()
+    xyz = np.ascontiguousarray(sc.xyz)
+    assert ctx.L.fm_scene_upload(ctx.h, xyz.ctypes.data, xyz.shape[0], 3, sc.support, C.byref(h)) == fmlib.FM_OK
+    s = fmlib.Scene.wrap(ctx, h, sc.support)
+    fr = O.build_frame(sc.xyz, sc.support)
+    d = s.download()
+    assert np.array_equal(d["perm"], fr.perm) and np.array_equal(d["start"], fr.start)
+    assert ctx.L.fm_scene_upload(ctx.h, xyz.ctypes.data, xyz.shape[0], -3, sc.support, C.byref(h)) != fmlib.FM_OK
+    s.close()
+
+
 def test_rejects_bad_input(fmlib, ctx):
     xyz = np.zeros((10, 3), np.float32)
     xyz[3, 1] = np.nan
