@@ -225,8 +225,12 @@ def run_reference(args):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000 * total / len(times),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded)",
-            "config": dict(workload_config(sc, cam, "off"), bisect_iters=0,
-                           sample=f"{per_step} random pixels of the 1920x1080 frame per step"),
+            # the GPU arm's workload; the reference's loop has no bisection and here
+            # evaluates every sample (its skip flags are a CompactNSearch call that is
+            # not part of the reference tree), on a pixel sample of that frame
+            "config": workload_config(sc, cam, args.skip),
+            "reference_loop": {"bisect_iters": 0, "skip": "off",
+                               "sample": f"{per_step} random pixels of the 1920x1080 frame per step"},
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": f"{per_step} seeded random pixels per step, {len(times)} steps; "
                                        f"CPU {model}, {cores} host cores"},
