@@ -34,7 +34,7 @@ struct fm_batch {
     // learned proposal of the views with FM_MARCH_PROPOSAL: the weights (a copy),
     // per-view blocks, tile and low-resolution prefixes, low-resolution depths,
     // intervals of every pixel
-    fm::DevBuf pw, pb, pviews, ptile_pfx, plow_pfx, plow, pivl;
+    fm::DevBuf pw, pb, pviews, ptile_pfx, plow_pfx, plow, pivl, pblk_pfx;
     float pmargins[3] = {0.0f, 0.0f, 0.0f};  // margin_lo, margin_hi, min_near of the copied proposal
     // anisotropic views: the context's kernel settings at creation, per-view
     // blocks, 32-pixel chunk prefixes, the chunk total
@@ -72,7 +72,7 @@ void free_batch(fm_batch* b) {
     DevBuf* bufs[] = {&b->margs,  &b->tile_pfx, &b->sviews,  &b->pfx64,   &b->pfx_tiles, &b->depth,
                       &b->hiz,    &b->list,     &b->counters, &b->longq,  &b->longq2,    &b->rg_keys,
                       &b->rg_tmp, &b->rg_order, &b->pw,       &b->pb,     &b->pviews,    &b->ptile_pfx,
-                      &b->plow_pfx, &b->plow,   &b->pivl,     &b->aviews,   &b->apfx};
+                      &b->plow_pfx, &b->plow,   &b->pivl,     &b->aviews,   &b->apfx,      &b->pblk_pfx};
     for (DevBuf* d : bufs) cudaFree(d->p);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     delete b;
@@ -179,16 +179,18 @@ int prepare(fm_batch* b) {
     for (int i = 0; i < n; ++i)
         if (b->views[i].params.flags & FM_MARCH_PROPOSAL) pv_idx.push_back(i);
     const int np = (int)pv_idx.size();
-    std::vector<uint64_t> ptp(np + 1, 0), plp(np + 1, 0);
+    std::vector<uint64_t> ptp(np + 1, 0), plp(np + 1, 0), pbp(np + 1, 0);
     for (int k = 0; k < np; ++k) {
         const fm_view& v = b->views[pv_idx[k]];
         const uint64_t npx = (uint64_t)v.camera.width * v.camera.height;
         ptp[k + 1] = ptp[k] + (npx + 127) / 128;
         plp[k + 1] = plp[k] + propose_low_pixels(&v.camera);
+        pbp[k + 1] = pbp[k] + propose_view_blocks(&v.camera);
     }
     if (np > 0) {
         if (!grow_buf(b->pviews, propose_view_bytes() * np) || !grow_buf(b->ptile_pfx, 8ull * (np + 1)) ||
-            !grow_buf(b->plow_pfx, 8ull * (np + 1)) || !grow_buf(b->plow, 4ull * std::max<uint64_t>(plp[np], 1)) ||
+            !grow_buf(b->plow_pfx, 8ull * (np + 1)) || !grow_buf(b->pblk_pfx, 8ull * (np + 1)) ||
+            !grow_buf(b->plow, 4ull * std::max<uint64_t>(plp[np], 1)) ||
             !grow_buf(b->pivl, 8ull * std::max<uint64_t>(px[n], 1)))
             return set_err(ctx, FM_ERR_OOM, "batch buffer allocation failed");
     }
@@ -247,9 +249,11 @@ int prepare(fm_batch* b) {
         FM_CUDA(ctx, cudaMemcpy(b->pviews.p, blocks.data(), blocks.size(), cudaMemcpyHostToDevice));
         FM_CUDA(ctx, cudaMemcpy(b->ptile_pfx.p, ptp.data(), 8ull * (np + 1), cudaMemcpyHostToDevice));
         FM_CUDA(ctx, cudaMemcpy(b->plow_pfx.p, plp.data(), 8ull * (np + 1), cudaMemcpyHostToDevice));
+        FM_CUDA(ctx, cudaMemcpy(b->pblk_pfx.p, pbp.data(), 8ull * (np + 1), cudaMemcpyHostToDevice));
     }
     b->pbatch = ProposeBatchDev{b->pviews.p, (const uint64_t*)b->ptile_pfx.p, (const uint64_t*)b->plow_pfx.p, np,
-                                ptp[np], plp[np], b->pw.p, (const float*)b->pb.p};
+                                ptp[np], plp[np], (const uint64_t*)b->pblk_pfx.p, pbp[np], b->pw.p,
+                                (const float*)b->pb.p};
     {
         std::vector<uint8_t> blocks(aniso_view_bytes() * n, 0);
         for (int i = 0; i < n; ++i)

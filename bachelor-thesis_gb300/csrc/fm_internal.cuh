@@ -413,10 +413,13 @@ struct ProposeBatchDev {
     const uint64_t* low_pfx;   // nviews + 1: first low-resolution pixel of every view
     int nviews;
     uint64_t ntiles, nlow;
+    const uint64_t* blk_pfx;   // first 8x4 interval block of every view, nviews + 1
+    uint64_t nblk;
     const void* weights;       // the proposal's BF16 weight image (a copy the batch owns)
     const float* bias;
 };
 size_t propose_view_bytes();
+uint64_t propose_view_blocks(const fm_camera* cam);  // 8x4 interval blocks of a view
 uint64_t propose_low_pixels(const fm_camera* cam);
 // margins = {margin_lo, margin_hi, min_near} of the proposal (proposal_weights reads them)
 void propose_view(const fm_scene* s, const fm_camera* cam, const fm_march_params* p, const float margins[3],

@@ -465,6 +465,49 @@ __device__ __forceinline__ bool propose_tile(const ProposeView& pv, uint64_t lt,
     return true;
 }
 
+// The rays of an 8x4 pixel block start their intervals together: every usable
+// interval of the block begins at the block's earliest start.  Evaluating more
+// samples ahead of a proposed interval never loses a crossing (it can only
+// find an earlier one), and the lanes of a march tile (8x4 pixels by default)
+// then step through the same sample indices.  Warp per block.
+constexpr int kIvlBlockW = 8, kIvlBlockH = 4;
+
+__device__ __forceinline__ void ivl_block(int2* ivl, int W, int Hh, uint64_t blk, int lane) {
+    const uint64_t bw = (uint64_t)((W + kIvlBlockW - 1) / kIvlBlockW);
+    const int x = (int)(blk % bw) * kIvlBlockW + (lane % kIvlBlockW);
+    const int y = (int)(blk / bw) * kIvlBlockH + (lane / kIvlBlockW);
+    const bool in = x < W && y < Hh;
+    int2 iv = make_int2(0, -1);
+    if (in) iv = ivl[(uint64_t)y * (uint64_t)W + (uint64_t)x];
+    const bool ok = in && iv.x >= 1 && iv.x < iv.y;
+    const int m = __reduce_min_sync(0xffffffffu, ok ? iv.x : 0x7fffffff);
+    if (ok && m < iv.x) ivl[(uint64_t)y * (uint64_t)W + (uint64_t)x] = make_int2(m, iv.y);
+}
+
+__global__ void k_ivl_blocks(int2* ivl, int W, int Hh, uint64_t nblk) {
+    const uint64_t blk = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    if (blk >= nblk) return;  // warp-uniform
+    ivl_block(ivl, W, Hh, blk, threadIdx.x & 31);
+}
+
+__global__ void k_ivl_blocks_b(const ProposeView* __restrict__ views, const uint64_t* __restrict__ pfx, int nviews,
+                               uint64_t nblk) {
+    const uint64_t blk = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    if (blk >= nblk) return;  // warp-uniform
+    int lo = 0, hi = nviews - 1;  // the view of block blk: largest v with pfx[v] <= blk
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (pfx[mid] <= blk) lo = mid;
+        else hi = mid - 1;
+    }
+    const ProposeView& v = views[lo];
+    ivl_block(v.ivl, v.f.W, v.f.Hh, blk - pfx[lo], threadIdx.x & 31);
+}
+
+uint64_t ivl_blocks(int W, int Hh) {
+    return (uint64_t)((W + kIvlBlockW - 1) / kIvlBlockW) * (uint64_t)((Hh + kIvlBlockH - 1) / kIvlBlockH);
+}
+
 template <bool BATCH>
 __global__ void __launch_bounds__(kRows) k_propose(const ProposeArgs a) {
     extern __shared__ __align__(1024) uint8_t sm[];
@@ -877,9 +920,14 @@ int launch_propose_batch(fm_ctx* ctx, const ProposeBatchDev& b, cudaStream_t st)
     uint64_t grid = (uint64_t)ctx->sm_count * 4;
     if (grid > b.ntiles) grid = b.ntiles;
     if (grid) k_propose<true><<<(unsigned)grid, kRows, kSmRequest, st>>>(a);
+    if (b.nblk)
+        k_ivl_blocks_b<<<(unsigned)((b.nblk * 32 + 255) / 256), 256, 0, st>>>((const ProposeView*)b.views, b.blk_pfx,
+                                                                             b.nviews, b.nblk);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }
+
+uint64_t propose_view_blocks(const fm_camera* cam) { return ivl_blocks(cam->width, cam->height); }
 
 int launch_features(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const float* zbuf, float* feat, float* t0,
                     cudaStream_t st) {
@@ -912,6 +960,8 @@ int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_marc
     uint64_t grid = (uint64_t)ctx->sm_count * 4;
     if (grid > a.ntiles) grid = a.ntiles;
     k_propose<false><<<(unsigned)grid, kRows, kSmRequest, st>>>(a);
+    const uint64_t nblk = ivl_blocks(cam->width, cam->height);
+    k_ivl_blocks<<<(unsigned)((nblk * 32 + 255) / 256), 256, 0, st>>>(ivl, cam->width, cam->height, nblk);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }

@@ -374,7 +374,9 @@ int fm_proposal_features(fm_ctx* ctx, const fm_scene* scene, const fm_camera* ca
                          float* features, float* t0, void* stream);
 /* Intervals the march would use, device buffers: intervals = W*H pairs
  * (first sample - 1, last sample) of the march's sample index, (0, -1) for a
- * full march; near_far = W*H raw (near, far) outputs (may be NULL). */
+ * full march; near_far = W*H raw (near, far) outputs (may be NULL).  The
+ * usable intervals of every 8x4 pixel block start at the block's earliest
+ * start, so that the rays of a march tile step together. */
 int fm_proposal_intervals(fm_ctx* ctx, const fm_scene* scene, const fm_camera* cam, const fm_march_params* params,
                           const float* start_depth, int32_t* intervals, float* near_far, void* stream);
 
