@@ -467,7 +467,7 @@ int fm_batch_autotune(fm_batch* b, const fm_tile_config* cands, int32_t n_cands,
         }
     } else {
         for (int lg : {2, 3, 4, 5})
-            for (int cap : {12, 15, 20, 24, 32}) {
+            for (int cap : {12, 15, 20, 24, 32, 48, 64}) {
                 TileConfig t;
                 t.tw_log2 = lg;
                 t.claim = 1;
