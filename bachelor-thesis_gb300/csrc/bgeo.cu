@@ -282,30 +282,40 @@ struct fm_dataset {
         }
     }
 
-    // decoded frame i (waits for a worker that has it, or decodes it here);
-    // then queues the next `window` frames and drops the others
+    // decoded frame i (waits for a thread that is decoding it, or decodes it
+    // here); then queues the next `window` frames and drops the others.  A slot
+    // being decoded is never dropped; a finished one may be dropped by another
+    // reader before a waiter wakes, and is then decoded again.
     std::shared_ptr<fm::io::BgeoFile> get(int i, std::string& e) {
         std::unique_lock<std::mutex> lk(mu);
-        auto it = cache.find(i);
-        if (it == cache.end() || it->second.state == 0) {
-            Slot& sl = cache[i];
-            sl.state = 1;
+        std::shared_ptr<fm::io::BgeoFile> f;
+        for (;;) {
+            auto it = cache.find(i);
+            if (it != cache.end() && it->second.state >= 2) {
+                f = it->second.file;
+                e = it->second.err;
+                break;
+            }
+            if (it != cache.end() && it->second.state == 1) {
+                cv.wait(lk);
+                continue;
+            }
+            cache[i].state = 1;  // absent or only queued: decode it here
             lk.unlock();
-            auto f = std::make_shared<fm::io::BgeoFile>();
+            auto nf = std::make_shared<fm::io::BgeoFile>();
             std::string le;
-            const int rc = fm::io::bgeo_load(files[i].c_str(), false, *f, le);
+            const int rc = fm::io::bgeo_load(files[i].c_str(), false, *nf, le);
             lk.lock();
-            sl.err = le;
+            Slot& sl = cache[i];
             sl.state = rc ? 3 : 2;
-            sl.file = rc ? nullptr : f;
-            if (!rc) points[i] = (int64_t)f->layout.points;
+            sl.file = rc ? nullptr : nf;
+            sl.err = le;
+            if (!rc) points[i] = (int64_t)nf->layout.points;
             cv.notify_all();
-        } else {
-            cv.wait(lk, [&] { return cache[i].state >= 2; });
+            f = sl.file;
+            e = le;
+            break;
         }
-        Slot& sl = cache[i];
-        auto f = sl.file;
-        e = sl.err;
         // keep [i, i + window]; queue what is missing of it
         for (auto jt = cache.begin(); jt != cache.end();) {
             const bool keep = jt->first >= i && jt->first <= i + window && jt->second.state != 3;

@@ -237,3 +237,32 @@ def test_dataset_matches_reference(fm, oracle_lib, tmp_path):
             assert np.array_equal(ref_rows, mine), i
             at += counts[i]
         ds.close()
+
+
+def test_dataset_concurrent_readers(fm, tmp_path):
+    """Several host threads reading frames of one series in random orders while the decode-ahead
+    threads work: every read returns its frame's positions."""
+    import threading
+
+    counts = [900, 1300, 700, 1100, 500, 1000, 800]
+    prefix, frames = write_series(tmp_path, counts)
+    ds = bgeo.Dataset(prefix, ".bgeo", -1, 3)
+    errors = []
+
+    def reader(seed):
+        rng = np.random.default_rng(seed)
+        try:
+            for i in rng.integers(0, len(counts), 40):
+                got = ds.read(int(i))
+                if not np.array_equal(bits(got), bits(frames[i])):
+                    errors.append(int(i))
+        except Exception as e:  # noqa: BLE001 - reported below
+            errors.append(repr(e))
+
+    ts = [threading.Thread(target=reader, args=(s,)) for s in range(4)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    ds.close()
+    assert not errors, errors[:5]
