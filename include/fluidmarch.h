@@ -17,6 +17,11 @@
  * pointers are staged through device buffers the context owns.
  * No entry point falls back to a CPU path: without a usable CUDA device every
  * call that needs one returns FM_ERR_CUDA.
+ *
+ * Threads: a context, its scenes, batches, proposals and trainers are used by
+ * one host thread at a time (the reference drives its marcher from the render
+ * thread); separate contexts are independent.  A particle-file series
+ * (fm_dataset_*) may be read from several threads at once.
  */
 #ifndef FLUIDMARCH_H
 #define FLUIDMARCH_H
