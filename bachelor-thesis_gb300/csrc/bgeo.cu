@@ -65,6 +65,31 @@ int read_file(const char* path, size_t limit, std::vector<uint8_t>& out, uint64_
     return rc;
 }
 
+// The last 4 bytes of a file (a gzip member's size field), little-endian.
+bool read_tail32(const char* path, uint32_t& v) {
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return false;
+    uint8_t b[4];
+    const bool ok = std::fseek(f, -4, SEEK_END) == 0 && std::fread(b, 1, 4, f) == 4;
+    std::fclose(f);
+    v = (uint32_t)b[0] | (uint32_t)b[1] << 8 | (uint32_t)b[2] << 16 | (uint32_t)b[3] << 24;
+    return ok;
+}
+
+// A header whose point block cannot fit the file: plain files by their size,
+// gzip files by the member's size field (when the data is below 4 GB).
+int check_point_block(const char* path, const BgeoFile& f, std::string& err) {
+    const uint64_t need = (uint64_t)f.layout.data_offset + f.layout.points * 4ull * f.layout.words;
+    if (!f.compressed) {
+        if (need > f.file_bytes) return fail(err, "BGEO point data is truncated");
+        return 0;
+    }
+    uint32_t isize = 0;
+    if (need < (1ull << 32) && read_tail32(path, isize) && need > isize)
+        return fail(err, "BGEO point data is truncated");
+    return 0;
+}
+
 }  // namespace
 
 int bgeo_layout(const uint8_t* d, size_t n, bool need_points, BgeoLayout& L, std::string& err) {
@@ -164,7 +189,8 @@ int bgeo_load(const char* path, bool header_only, BgeoFile& f, std::string& err)
             r = bgeo_layout(f.data, f.size, false, f.layout, err);
             if (r == 1 && whole) return fail(err, "BGEO header is truncated");
         }
-        if (r <= 0) return r;
+        if (r == 0) return check_point_block(path, f, err);
+        if (r < 0) return r;
     }
 }
 

@@ -170,6 +170,23 @@ def test_reader_errors(fm, tmp_path):
         bgeo.read(str(tmp_path / "missing.bgeo"))
 
 
+def test_header_read_rejects_short_point_block(fm, tmp_path):
+    """A header that claims more points than the file holds fails at the header read already, plain
+    or gzip (by the gzip member's size field), so a loader sizes no buffer from it."""
+    x = sample_xyz(100, 7)
+    good = bgeo.encode(x)
+    for name, data in {"plain": good[:-8], "gzip": gzip.compress(good[:-8])}.items():
+        p = str(tmp_path / f"short_{name}.bgeo")
+        with open(p, "wb") as f:
+            f.write(data)
+        with pytest.raises(fm.FmError, match="truncated"):
+            bgeo.info(p)
+    p = str(tmp_path / "whole.bgeo")
+    with open(p, "wb") as f:
+        f.write(gzip.compress(good))
+    assert bgeo.info(p)["points"] == 100
+
+
 @needs_ref
 @pytest.mark.parametrize("compressed", [True, False])
 def test_reader_matches_partio(fm, oracle_lib, tmp_path, compressed):
@@ -266,3 +283,34 @@ def test_dataset_concurrent_readers(fm, tmp_path):
         t.join()
     ds.close()
     assert not errors, errors[:5]
+
+
+def test_decoders_survive_corrupt_input(fm, tmp_path):
+    """Random byte flips and truncations of a gzip stream and of a BGEO file end in an error or
+    some output, never in a crash or a hang."""
+    rng = np.random.default_rng(11)
+    data = payloads()["text"][:20000]
+    good = gz(data)
+    for _ in range(300):
+        bad = bytearray(good)
+        for _ in range(int(rng.integers(1, 6))):
+            bad[int(rng.integers(10, len(bad)))] = int(rng.integers(0, 256))
+        if rng.random() < 0.3:
+            bad = bad[: int(rng.integers(10, len(bad)))]
+        try:
+            bgeo.gunzip(bytes(bad))
+        except fm.FmError:
+            pass
+    x = sample_xyz(300, 12)
+    raw = bgeo.encode(x, attrs(300, 13))
+    p = str(tmp_path / "fuzz.bgeo")
+    for k in range(200):
+        bad = bytearray(raw)
+        for _ in range(int(rng.integers(1, 4))):
+            bad[int(rng.integers(0, min(len(bad), 400)))] = int(rng.integers(0, 256))
+        with open(p, "wb") as f:
+            f.write(gzip.compress(bytes(bad)) if k % 2 else bytes(bad))
+        try:
+            bgeo.read(p)
+        except (fm.FmError, ValueError, MemoryError):
+            pass
