@@ -138,7 +138,6 @@ static void scene_free(fm_scene* s) {
     cudaFree(s->d_perm);
     cudaFree(s->d_sub);
     cudaFree(s->d_bound);
-    cudaFree(s->d_bound4);
     cudaFree(s->d_flag);
     cudaFree(s->d_occ);
     delete s;
@@ -478,8 +477,7 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     fm_scene* sm = const_cast<fm_scene*>(s);
     // the grid itself was built synchronously; skip tables are built once, on this stream
     // the fine bound table pays off once a scene is marched more than once
-    if (p->skip_mode == FM_SKIP_EXACT && (rc = ensure_bound(ctx, sm, st, sm->marches > 0)) != FM_OK) return rc;
-    sm->marches++;
+    if (p->skip_mode == FM_SKIP_EXACT && (rc = ensure_bound(ctx, sm, st, p->iso_density)) != FM_OK) return rc;
     if (p->skip_mode == FM_SKIP_REFERENCE && (rc = ensure_flags(ctx, sm, st)) != FM_OK) return rc;
     MarchOutDev o{};
     const bool host = mem == FM_MEM_HOST;

@@ -123,7 +123,7 @@ int prepare(fm_batch* b) {
     for (const fm_view& v : b->views) {
         fm_scene* s = const_cast<fm_scene*>(v.scene);
         int rc = FM_OK;
-        if (v.params.skip_mode == FM_SKIP_EXACT) rc = ensure_bound(ctx, s, ctx->stream, true);
+        if (v.params.skip_mode == FM_SKIP_EXACT) rc = ensure_bound(ctx, s, ctx->stream, v.params.iso_density);
         if (!rc && v.params.skip_mode == FM_SKIP_REFERENCE) rc = ensure_flags(ctx, s, ctx->stream);
         if (!rc && (v.params.flags & FM_MARCH_PROPOSAL)) rc = ensure_occupancy(ctx, s, ctx->stream);
         if (rc) return rc;

@@ -33,7 +33,6 @@ struct GridDev {
     float cell;  // cell width = support radius
     int dims[3];
     uint32_t nsub;                        // 8 * n_cells + 1 (entries of sub)
-    int bound_shift;                      // bound boxes per cell and axis: 1 << bound_shift (1 or 2)
     const float4* __restrict__ pts;       // sorted particles (w = 0): cell, 2x2x2 sub-cell, input index
     const uint32_t* __restrict__ sub;     // 8 * n_cells + 1 sub-cell starts; cell c = [sub[8c], sub[8c+8])
     const float* __restrict__ bound;      // per bound box density upper bound (FM_SKIP_EXACT) or null
@@ -239,14 +238,10 @@ struct fm_scene {
     uint32_t* d_cell = nullptr;    // cell of each input particle
     uint32_t* d_perm = nullptr;    // input index of each sorted particle
     uint32_t* d_sub = nullptr;     // 8 * ncells + 1 sub-cell starts
-    float* d_bound = nullptr;      // coarse bound table, 8 per cell (lazy)
-    float* d_bound4 = nullptr;     // fine bound table, 64 per cell (lazy; a separate buffer, so
-                                   // marches still reading the coarse one are not disturbed)
+    float* d_bound = nullptr;      // exact-skip bound table, 4x4x4 boxes per cell (lazy)
     uint8_t* d_flag = nullptr;     // per-cell reference flag (lazy)
-    // exact-skip bound table: 0 none, 1 coarse (2x2x2 boxes per cell), 2 fine
-    // (4x4x4); the fine table is built once a scene is marched a second time
-    int bound_level = 0;
-    uint32_t marches = 0;          // marches since the last build
+    bool bound_valid = false;      // built by the first exact-skip march after a build
+    float bound_iso = 0.0f;        // the bound table holds +inf for boxes whose sum reached it
     bool flag_valid = false;
     uint64_t gen = 0;              // build generation: batches bound to an older one refuse to run
     uint16_t* d_occ = nullptr;     // 64^3 FP16 occupancy of the proposal (lazy)
@@ -259,7 +254,7 @@ namespace fm {
 int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride);
 // Lazily built skip tables, launched on `st` (valid for every later launch
 // on that stream; other streams must order after it).
-int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st, bool fine);
+int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st, float iso);
 int ensure_flags(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
 GridDev grid_dev(const fm_scene* s);
 

@@ -280,79 +280,7 @@ __global__ void k_gather(const float* __restrict__ xyz, uint64_t n, uint32_t str
     out[k] = make_float4(p[0], p[1], p[2], 0.0f);
 }
 
-// Coarse bound: 2x2x2 boxes (the sub-cells) per cell.
-// Upper bound of the density any sample inside a sub-cell can reach: the sum
-// over the particles of the cell's 27-neighbourhood (the sample's candidate
-// set) of W at the particle's distance to the sub-cell box (shrunk by a slack
-// that covers the rounding of the sample's cell assignment), inflated by a
-// margin that covers the FP32 summation error of up to n terms.  The bound is
-// exactly 0 when no particle lies within the support radius of the box: then
-// every term of a sample's sum is 0 (the anisotropic march skips on that
-// too).  One warp per cell computes its 8 sub-cell bounds.
-__global__ void k_cell_bound2(GridDev g, KernelDev k, float slack, float* __restrict__ bound) {
-    uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
-    uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
-    int l = threadIdx.x % kWarp;
-    if (c >= ncells) return;
-    int cc[3] = {(int)(c % (uint64_t)g.dims[0]), (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]),
-                 (int)(c / ((uint64_t)g.dims[0] * g.dims[1]))};
-    // slab edges: lo, mid, hi of the cell per axis
-    float e0[3], e1[3], e2[3];
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-        e0[a] = g.min[a] + (float)cc[a] * g.cell;
-        e1[a] = g.min[a] + ((float)cc[a] + 0.5f) * g.cell;
-        e2[a] = e0[a] + g.cell;
-    }
-    float acc[8];
-#pragma unroll
-    for (int s = 0; s < 8; ++s) acc[s] = 0.0f;
-    uint32_t cnt = 0;
-    const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, g.dims[0] - 1);
-    for (int z = max(cc[2] - 1, 0); z <= min(cc[2] + 1, g.dims[2] - 1); ++z)
-        for (int y = max(cc[1] - 1, 0); y <= min(cc[1] + 1, g.dims[1] - 1); ++y) {
-            const uint64_t row = ((uint64_t)z * g.dims[1] + y) * g.dims[0];
-            const uint32_t b = g.sub[8 * (row + x0)], e = g.sub[8 * (row + x1) + 8];
-            cnt += e - b;
-            for (uint32_t j = b + l; j < e; j += kWarp) {
-                const float4 q = g.pts[j];
-                const float qa[3] = {q.x, q.y, q.z};
-                float dlo[3], dhi[3];  // distance per axis to the lower / upper half slab
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    dlo[a] = fmaxf(fmaxf(e0[a] - qa[a], qa[a] - e1[a]), 0.0f);
-                    dhi[a] = fmaxf(fmaxf(e1[a] - qa[a], qa[a] - e2[a]), 0.0f);
-                }
-#pragma unroll
-                for (int s = 0; s < 8; ++s) {
-                    float dx = (s & 1) ? dhi[0] : dlo[0];
-                    float dy = (s & 2) ? dhi[1] : dlo[1];
-                    float dz = (s & 4) ? dhi[2] : dlo[2];
-                    float d = fmaxf(sqrtf(dx * dx + dy * dy + dz * dz) - slack, 0.0f);
-                    float q2 = d * d;
-                    if (q2 < k.h2) acc[s] += w_in(k, q2);
-                }
-            }
-        }
-#pragma unroll
-    for (int s = 0; s < 8; ++s)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) acc[s] += __shfl_xor_sync(0xffffffffu, acc[s], o);
-    if (l < 8) {
-        const float eps = 5.9604645e-8f;  // 2^-24
-        float n = (float)cnt;
-        float a = acc[0];
-#pragma unroll
-        for (int s = 1; s < 8; ++s)
-            if (l == s) a = acc[s];
-        float up = a * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
-        // no particle within the support radius of the (grown) box: every
-        // density term of a sample in it is 0, the sum exactly 0
-        bound[8 * c + l] = (cnt == 0 || a == 0.0f) ? 0.0f : up;
-    }
-}
-
-// Fine bound: 4x4x4 boxes per cell.
+// Exact-skip bound table: 4x4x4 boxes per cell.
 // Upper bound of the density any sample inside a bound box can reach.  Every
 // cell is divided into 4x4x4 bound boxes (a quarter cell per axis); a box's
 // bound is the sum over the particles of the cell's 27-neighbourhood (the
@@ -365,9 +293,17 @@ __global__ void k_cell_bound2(GridDev g, KernelDev k, float slack, float* __rest
 // 512-byte read) and passes them to every lane by shuffles, so each lane adds
 // W for its two boxes in registers (the order of the additions does not
 // matter: the margin covers it).
+//
+// Once the partial sums of all 64 boxes reach `thr` (the iso density of the
+// march that asked for the table), the cell stores +inf for every box and
+// stops: a box whose bound is at least the iso density is never skipped, so
+// +inf gives the same march at that iso and at any lower one.  The rows are
+// taken centre row first, then the four sharing a face with it, then the
+// diagonal ones: inside the fluid the sums reach the iso density within the
+// first rows.
 constexpr int kBoundWarps = 8;
 
-__global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, KernelDev k, float slack,
+__global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, KernelDev k, float slack, float thr,
                                                                      float* __restrict__ bound) {
     const uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
     const uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
@@ -389,43 +325,54 @@ __global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, 
     }
     float acc0 = 0.0f, acc1 = 0.0f;
     uint32_t cnt = 0;
+    bool reached = false;  // every box's sum reached thr (warp-uniform)
     const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, g.dims[0] - 1);
-    for (int z = max(cc[2] - 1, 0); z <= min(cc[2] + 1, g.dims[2] - 1); ++z)
-        for (int y = max(cc[1] - 1, 0); y <= min(cc[1] + 1, g.dims[1] - 1); ++y) {
-            const uint64_t row = ((uint64_t)z * g.dims[1] + y) * g.dims[0];
-            const uint32_t b = g.sub[8 * (row + x0)], e = g.sub[8 * (row + x1) + 8];
-            cnt += e - b;
-            for (uint32_t j0 = b; j0 < e; j0 += kWarp) {
-                const uint32_t j = j0 + (uint32_t)l;
-                const float4 mine = j < e ? g.pts[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-                const int m = (int)min(e - j0, (uint32_t)kWarp);
-                for (int t = 0; t < m; ++t) {
-                    const float qx = __shfl_sync(0xffffffffu, mine.x, t);
-                    const float qy = __shfl_sync(0xffffffffu, mine.y, t);
-                    const float qz = __shfl_sync(0xffffffffu, mine.z, t);
-                    const float q[3] = {qx, qy, qz};
-                    float d2[2];
+    // row r: 4-bit code (dy + 1) | (dz + 1) << 2 at bit 4 r; (dy, dz) = (0, 0), (-1, 0), (1, 0),
+    // (0, -1), (0, 1), (-1, -1), (1, -1), (-1, 1), (1, 1)
+    constexpr uint64_t kRowOrder = 0xa82091645ull;
+    for (int r = 0; r < 9 && !reached; ++r) {
+        const int code = (int)((kRowOrder >> (4 * r)) & 15u);
+        const int y = cc[1] + (code & 3) - 1, z = cc[2] + (code >> 2) - 1;
+        if (y < 0 || y >= g.dims[1] || z < 0 || z >= g.dims[2]) continue;
+        const uint64_t row = ((uint64_t)z * g.dims[1] + y) * g.dims[0];
+        const uint32_t b = g.sub[8 * (row + x0)], e = g.sub[8 * (row + x1) + 8];
+        cnt += e - b;
+        for (uint32_t j0 = b; j0 < e; j0 += kWarp) {
+            const uint32_t j = j0 + (uint32_t)l;
+            const float4 mine = j < e ? g.pts[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+            const int m = (int)min(e - j0, (uint32_t)kWarp);
+            for (int t = 0; t < m; ++t) {
+                const float qx = __shfl_sync(0xffffffffu, mine.x, t);
+                const float qy = __shfl_sync(0xffffffffu, mine.y, t);
+                const float qz = __shfl_sync(0xffffffffu, mine.z, t);
+                const float q[3] = {qx, qy, qz};
+                float d2[2];
 #pragma unroll
-                    for (int h = 0; h < 2; ++h) {
-                        d2[h] = 0.0f;
+                for (int h = 0; h < 2; ++h) {
+                    d2[h] = 0.0f;
 #pragma unroll
-                        for (int a = 0; a < 3; ++a) {
-                            const float d = fmaxf(fmaxf(lo[h][a] - q[a], q[a] - hi[h][a]), 0.0f);
-                            d2[h] += d * d;
-                        }
+                    for (int a = 0; a < 3; ++a) {
+                        const float d = fmaxf(fmaxf(lo[h][a] - q[a], q[a] - hi[h][a]), 0.0f);
+                        d2[h] += d * d;
                     }
-                    if (d2[0] < k.h2) acc0 += w_in(k, d2[0]);
-                    if (d2[1] < k.h2) acc1 += w_in(k, d2[1]);
                 }
+                if (d2[0] < k.h2) acc0 += w_in(k, d2[0]);
+                if (d2[1] < k.h2) acc1 += w_in(k, d2[1]);
+            }
+            if (__all_sync(0xffffffffu, acc0 >= thr && acc1 >= thr)) {
+                reached = true;
+                break;
             }
         }
+    }
     const float eps = 5.9604645e-8f;  // 2^-24
     const float n = (float)cnt;
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
         const float a = h ? acc1 : acc0;
         const float up = a * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
-        bound[(uint64_t)kBoundBoxes * c + l + 32 * h] = (cnt == 0 || a == 0.0f) ? 0.0f : up;
+        bound[(uint64_t)kBoundBoxes * c + l + 32 * h] =
+            reached ? __int_as_float(0x7f800000) : ((cnt == 0 || a == 0.0f) ? 0.0f : up);
     }
 }
 
@@ -477,8 +424,7 @@ GridDev grid_dev(const fm_scene* s) {
     g.pts = s->d_pts;
     g.sub = s->d_sub;
     g.nsub = (uint32_t)(8 * s->ncells + 1);
-    g.bound = s->bound_level == 2 ? s->d_bound4 : (s->bound_level == 1 ? s->d_bound : nullptr);
-    g.bound_shift = s->bound_level;
+    g.bound = s->bound_valid ? s->d_bound : nullptr;
     g.flag = s->flag_valid ? s->d_flag : nullptr;
     return g;
 }
@@ -525,20 +471,17 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     if (ncells > (1ull << 28))
         return set_err(ctx, FM_ERR_INVALID, "grid would exceed 2^28 cells: support radius too small for the extent");
     s->ncells = ncells;
-    s->bound_level = 0;
-    s->marches = 0;
+    s->bound_valid = false;
     s->flag_valid = false;
     s->occ_valid = false;
     const uint64_t nkeys = 8 * ncells;
     if (ncells > s->cell_capacity) {
         cudaFree(s->d_sub);
         cudaFree(s->d_bound);
-        cudaFree(s->d_bound4);
         cudaFree(s->d_flag);
-        s->d_sub = nullptr; s->d_bound = nullptr; s->d_bound4 = nullptr; s->d_flag = nullptr;
+        s->d_sub = nullptr; s->d_bound = nullptr; s->d_flag = nullptr;
         if (cudaMalloc(&s->d_sub, (nkeys + 1) * sizeof(uint32_t)) != cudaSuccess ||
-            cudaMalloc(&s->d_bound, nkeys * sizeof(float)) != cudaSuccess ||
-            cudaMalloc(&s->d_bound4, ncells * kBoundBoxes * sizeof(float)) != cudaSuccess ||
+            cudaMalloc(&s->d_bound, ncells * kBoundBoxes * sizeof(float)) != cudaSuccess ||
             cudaMalloc(&s->d_flag, ncells) != cudaSuccess) {
             s->cell_capacity = 0;
             return set_err(ctx, FM_ERR_OOM, "cell table allocation failed");
@@ -596,23 +539,23 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     return FM_OK;
 }
 
-int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st, bool fine) {
-    const int want = fine ? 2 : 1;
-    if (s->bound_level >= want) return FM_OK;
+// The bound table stores +inf for the boxes of a cell once all their sums
+// reached the march's iso density, so it serves marches at that iso or a
+// lower one; a march at a higher iso builds it again (in place: a march still
+// reading it sees one valid bound or the other in every box).
+int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st, float iso) {
+    const float thr = (iso > 0.0f && std::isfinite(iso)) ? iso : INFINITY;
+    if (s->bound_valid && thr <= s->bound_iso) return FM_OK;
     GridDev g = grid_dev(s);
     KernelDev k = make_kernel(s->support);
     float amax = 0.0f;
     for (int a = 0; a < 3; ++a) amax = std::max(amax, std::max(std::fabs(s->min[a]), std::fabs(s->max[a])));
     float slack = 1.0e-4f * s->support + 1.0e-6f * amax;
-    if (fine) {
-        const uint64_t blocks = (s->ncells + kBoundWarps - 1) / kBoundWarps;
-        k_cell_bound4<<<(unsigned)blocks, kWarp * kBoundWarps, 0, st>>>(g, k, slack, s->d_bound4);
-    } else {
-        const uint64_t threads = s->ncells * kWarp;
-        k_cell_bound2<<<(unsigned)((threads + 255) / 256), 256, 0, st>>>(g, k, slack, s->d_bound);
-    }
+    const uint64_t blocks = (s->ncells + kBoundWarps - 1) / kBoundWarps;
+    k_cell_bound4<<<(unsigned)blocks, kWarp * kBoundWarps, 0, st>>>(g, k, slack, thr, s->d_bound);
     FM_CUDA(ctx, cudaGetLastError());
-    s->bound_level = want;
+    s->bound_valid = true;
+    s->bound_iso = thr;
     return FM_OK;
 }
 

@@ -91,8 +91,8 @@ __device__ __forceinline__ bool locate(const GridDev& g, float px, float py, flo
     return true;
 }
 
-// Exact-skip bound of the bound box that holds a located sample (1/2 or 1/4
-// cell per axis; u < 1 inside the grid, clamped all the same): no sample in
+// Exact-skip bound of the bound box that holds a located sample (1/4 cell per
+// axis; u < 1 inside the grid, clamped all the same): no sample in
 // the box reaches a density above it, and 0 means no particle lies within the
 // support radius of the box.  +inf for a cell outside the grid.
 __device__ __forceinline__ float box_bound(const GridDev& g, const Loc& L) {
@@ -100,12 +100,9 @@ __device__ __forceinline__ float box_bound(const GridDev& g, const Loc& L) {
         return __int_as_float(0x7f800000);
     const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)g.dims[0] +
                        (uint32_t)L.c[2] * (uint32_t)g.dims[0] * (uint32_t)g.dims[1];
-    const int sh = g.bound_shift;
-    const uint32_t nb = 1u << sh;
-    const float fb = (float)nb;
-    const uint32_t bx = min((uint32_t)(fb * L.u[0]), nb - 1u), by = min((uint32_t)(fb * L.u[1]), nb - 1u),
-                   bz = min((uint32_t)(fb * L.u[2]), nb - 1u);
-    return __ldg(g.bound + (c << (3 * sh)) + (bx | (by << sh) | (bz << (2 * sh))));
+    const uint32_t bx = min((uint32_t)(4.0f * L.u[0]), 3u), by = min((uint32_t)(4.0f * L.u[1]), 3u),
+                   bz = min((uint32_t)(4.0f * L.u[2]), 3u);
+    return __ldg(g.bound + (uint64_t)kBoundBoxes * c + (bx | (by << 2) | (bz << 4)));
 }
 
 // Squared distance (cell units) from fraction u to the half-cell slab [lo, lo + 0.5].
@@ -1105,8 +1102,8 @@ MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_marc
     a.Hh = cam->height;
     a.tw_log2 = cfg.tw_log2;
     a.claim = cfg.claim;
-    // measured optimum at 1080p: 15 sums with the fine bound table, 20 with the coarse one
-    a.cap = cfg.cap > 0 ? cfg.cap : (s->bound_level == 2 ? 15 : 20);
+    // measured optimum at 1080p with the exact-skip bound table: 15 sums
+    a.cap = cfg.cap > 0 ? cfg.cap : 15;
     a.defer_lanes = cfg.lanes;
     a.cap2 = cfg.cap2;
     a.order = nullptr;

@@ -30,6 +30,10 @@ anisotropic  the same frame with the reference's default marcher
        (PerPixel_Anisotropic: per-sample WPCA kernels, k_n 0.5, k_r 2, k_s 2000,
        N_eps 1, extended radius 2 H, iso = half the median anisotropic density
        inside the fluid), next to the CPU port of it on a pixel sample.
+particle_files  the bench frame as gzip BGEO files: host decode, scene from
+       a file, autoplay of a file series.
+grid_build  the uniform-grid build of the 1M frame and of a 4M frame from
+       device positions, against 64 B per particle + 16 B per cell.
 """
 
 from __future__ import annotations
@@ -72,6 +76,7 @@ def parse():
     ap.add_argument("--no-autotune", action="store_true",
                     help="time the batch with the context's work split instead of the autotuned one")
     ap.add_argument("--no-files", action="store_true", help="skip the particle-file loading measurement")
+    ap.add_argument("--no-grid", action="store_true", help="skip the grid-build measurement")
     return ap.parse_args()
 
 
@@ -356,7 +361,7 @@ def run_aniso(args, fm, torch, ctx, ext, scene, sc, cam, out):
     # density 0): the same outputs as skip off
     P_ex = fm.MarchParams(iso, sc.step, sc.max_steps, sc.bisect, fm.FM_SKIP_EXACT, external_depth=True,
                           anisotropic=True)
-    for _ in range(2):  # builds the coarse, then the fine bound table of the scene
+    for _ in range(2):  # the first builds the bound table of the scene at this iso
         fm.splat_depth(scene, cam, out["start_depth"])
         fm.march(scene, cam, P_ex, out["position"], out["normal"], out["depth"], out["colour"], out["start_depth"])
     ctx.sync()
@@ -453,6 +458,44 @@ def run_files(args, fm, torch, ctx, sc):
                         "of a 6-frame series with host threads decoding ahead"}
     finally:
         shutil.rmtree(tmp, ignore_errors=True)
+
+
+def run_grid(args, fm, torch, ctx, ext, sc, flush, peak):
+    """The uniform-grid build (AABB, cell keys, radix sort, start tables, sorted gather) of the bench frame
+    and of a 4M-particle frame of the same layout, from positions in device memory, L2 flushed before each
+    build; algorithmic bytes 64 B per particle + 16 B per cell."""
+    from fluidmarch import scenes
+
+    res = {}
+    cases = [("1m", sc.xyz, sc.support),
+             ("4m", scenes._sloshing_xyz(np.random.default_rng(4000), 4_000_000), float(np.float32(2 * 0.0126)))]
+    for name, xyz, support in cases:
+        xyz_d = torch.from_numpy(xyz).cuda()
+        torch.cuda.synchronize()
+        s = fm.Scene(ctx, xyz_d, support)
+        for _ in range(3):
+            s.update(xyz_d)
+        ctx.sync()
+        ts = []
+        with torch.cuda.stream(ext):
+            for _ in range(max(5, args.steps // 2)):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record(ext)
+                s.update(xyz_d)
+                e1.record(ext)
+                ext.synchronize()
+                ts.append(e0.elapsed_time(e1))
+        g = s.grid()
+        s.close()
+        ms = float(np.median(ts))
+        alg = 64 * g["n_particles"] + 16 * g["n_cells"]
+        res[name] = {"particles": g["n_particles"], "cells": g["n_cells"], "ms": ms, "algorithmic_bytes": alg,
+                     "achieved_gbs": alg / ms / 1e6, "frac_of_hbm_peak": alg / ms / 1e6 / peak}
+        del xyz_d
+    res["note"] = ("fm_scene_update from device positions: k_aabb, read-back of the bounds for the grid size, "
+                   "cell keys, 8-bit radix passes, sorted gather; median of the builds, each after an L2 flush")
+    return res
 
 
 def run_batch(args, fm, torch, ctx, ext, dev):
@@ -628,6 +671,9 @@ def run_ours(args):
     files = None
     if rank == 0 and not args.no_files:
         files = run_files(args, fm, torch, ctx, sc)
+    grid = None
+    if rank == 0 and not args.no_grid:
+        grid = run_grid(args, fm, torch, ctx, ext, sc, flush, measured_peaks()[0])
 
     if rank == 0:
         peak, peak_kind = measured_peaks()
@@ -662,6 +708,8 @@ def run_ours(args):
             line["anisotropic"] = aniso
         if files:
             line["particle_files"] = files
+        if grid:
+            line["grid_build"] = grid
         if world == 1 and not args.no_cpu_baseline:
             import oracle as O
 

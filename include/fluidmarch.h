@@ -49,10 +49,11 @@ extern "C" {
 
 /* skip modes (march parameter) */
 #define FM_SKIP_OFF 0        /* evaluate the density at every sample (reference parity gate) */
-#define FM_SKIP_EXACT 1      /* skip samples whose bound box (half a cell per axis; a quarter
-                                once the scene is marched again) has a density upper bound
-                                below iso;
-                                same samples, same results as FM_SKIP_OFF */
+#define FM_SKIP_EXACT 1      /* skip samples whose bound box (a quarter cell per axis) has a
+                                density upper bound below iso; same samples, same results
+                                as FM_SKIP_OFF.  The scene's bound table is built by its
+                                first such march and serves marches at that iso or a lower
+                                one; a march at a higher iso builds it again. */
 #define FM_SKIP_REFERENCE 2  /* the reference's skip: flag = own-cell count * W0 > 1, jump to the
                                 cell's exit plus one step (RayMarcher.cpp:281-306) */
 
@@ -285,7 +286,7 @@ typedef struct fm_tile_config {
     int32_t tiles_per_claim; /* tiles a warp takes at a time: 1..16 */
     int32_t defer_iters;     /* density sums a warp runs for one tile before the
                                 rays it still has go to the long-ray pass: 1..4096;
-                                0 = 15 with the fine bound table, else 20 */
+                                0 = 15 */
     int32_t long_queue;      /* entries of the long-ray queue; 0 = pixels / 4 + 65536.
                                 Rays that find it full stay with their warp. */
     int32_t defer_lanes;     /* a warp also defers its rays once at most this many are

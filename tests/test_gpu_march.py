@@ -292,8 +292,9 @@ def test_density_probe_bitwise(fmlib, ctx):
     s.close()
 
 
-def test_fine_bound_table_on_reuse(fmlib, ctx):
-    """A scene marched again gets the 4x4x4 bound table: more samples skipped, same bits."""
+def test_bound_table_on_reuse(fmlib, ctx):
+    """The scene's first exact-skip march builds the bound table, the next reuses it: the same samples
+    skipped, the oracle's bits both times."""
     sc = scenes.small_scene(seed=23, n=20000, width=128, height=96)
     cam = sc.cameras[0]
     s = fmlib.Scene(ctx, sc.xyz, sc.support)
@@ -311,7 +312,34 @@ def test_fine_bound_table_on_reuse(fmlib, ctx):
     for g in (first, second):
         for k in ("position", "normal", "depth", "colour"):
             assert np.array_equal(bits(g[k]), bits(o[k])), k
-    assert st2["skipped"] > st1["skipped"] and st2["evals"] < st1["evals"]
+    assert st1["skipped"] > 0 and (st2["skipped"], st2["evals"]) == (st1["skipped"], st1["evals"])
+    s.close()
+
+
+def test_bound_table_follows_iso(fmlib, ctx):
+    """The bound table stops summing a cell once every box reached the iso density of the march that
+    built it (+inf there): marches at that iso or a lower one reuse it, a march at a higher iso builds
+    it again.  Every march equals the march without skipping bit for bit, and a march skips the same
+    samples whether the table was built at its own iso or at a higher one."""
+    sc = scenes.small_scene(seed=29, n=20000, width=128, height=96)
+    cam = sc.cameras[0]
+    s = fmlib.Scene(ctx, sc.xyz, sc.support)
+    ctx.set_stats(True)
+    seen = {}
+    try:
+        # tables: built at iso, reused (iso, iso / 2), built at 2 iso, reused (iso), built at 3 iso,
+        # reused (iso / 2, 2 iso)
+        for iso in (sc.iso, sc.iso, 0.5 * sc.iso, 2.0 * sc.iso, sc.iso, 3.0 * sc.iso, 0.5 * sc.iso, 2.0 * sc.iso):
+            ref = fmlib.render(s, cam, fmlib.MarchParams(iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_OFF))
+            got = fmlib.render(s, cam, fmlib.MarchParams(iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_EXACT))
+            st = ctx.stats()
+            for k in ("position", "normal", "depth", "colour"):
+                assert np.array_equal(bits(got[k]), bits(ref[k])), (iso, k)
+            key = (st["skipped"], st["evals"])
+            assert seen.setdefault(iso, key) == key, iso
+        assert seen[sc.iso][0] > 0
+    finally:
+        ctx.set_stats(False)
     s.close()
 
 
