@@ -116,7 +116,14 @@ int fm_create(fm_ctx** out, int device) {
     ctx->device = device;
     if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
         cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        if (ctx->stream) cudaStreamDestroy(ctx->stream);
         delete ctx;
+        return FM_ERR_CUDA;
+    }
+    if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        fm_destroy(ctx);
         return FM_ERR_CUDA;
     }
     if (cudaMalloc(&ctx->d_status, 64) != cudaSuccess || cudaMalloc(&ctx->d_stats, fm::kStatSlots * sizeof(unsigned long long)) != cudaSuccess ||
@@ -172,6 +179,9 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->prop_low.p);
     cudaFree(ctx->prop_judge.p);
     if (ctx->h_pinned_small) cudaFreeHost(ctx->h_pinned_small);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -475,9 +485,12 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     cudaStream_t st = pick(ctx, stream);
     const size_t npx = (size_t)cam->width * cam->height;
     fm_scene* sm = const_cast<fm_scene*>(s);
-    // the grid itself was built synchronously; skip tables are built once, on this stream
-    // the fine bound table pays off once a scene is marched more than once
-    if (p->skip_mode == FM_SKIP_EXACT && (rc = ensure_bound(ctx, sm, st, p->iso_density)) != FM_OK) return rc;
+    // the grid itself was built synchronously; skip tables are built once per
+    // scene (the bound table again for a higher iso).  A bound table this
+    // march needs is built on the side stream while the splat runs here.
+    const bool overlap = p->skip_mode == FM_SKIP_EXACT && !external && bound_stale(sm, p->iso_density);
+    if (p->skip_mode == FM_SKIP_EXACT && !overlap && (rc = ensure_bound(ctx, sm, st, p->iso_density)) != FM_OK)
+        return rc;
     if (p->skip_mode == FM_SKIP_REFERENCE && (rc = ensure_flags(ctx, sm, st)) != FM_OK) return rc;
     MarchOutDev o{};
     const bool host = mem == FM_MEM_HOST;
@@ -498,7 +511,15 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
             if (!grow(ctx->stage[1], npx * 4)) return set_err(ctx, FM_ERR_OOM, "staging allocation failed");
             z = (float*)ctx->stage[1].p;
         }
+        if (overlap) {
+            FM_CUDA(ctx, cudaEventRecord(ctx->ev_fork, st));
+            FM_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_fork, 0));
+            if ((rc = ensure_bound(ctx, sm, ctx->side, p->iso_density)) != FM_OK) return rc;
+            FM_CUDA(ctx, cudaEventRecord(ctx->ev_join, ctx->side));
+        }
         rc = launch_splat(ctx, s, cam, z, st);
+        // whatever the splat returned, work queued on st after this point sees the table
+        if (overlap) FM_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_join, 0));
         if (rc) return rc;
     }
     o.start_depth = z;

@@ -177,6 +177,10 @@ struct fm_batch;
 struct fm_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
+    // a march that builds the scene's bound table does so on `side`, next to
+    // its splat; the march waits for it through ev_join
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string err;
     int sm_count = 0;
     // staging buffers for host in/outputs (grown on demand)
@@ -255,6 +259,7 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride);
 // Lazily built skip tables, launched on `st` (valid for every later launch
 // on that stream; other streams must order after it).
 int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st, float iso);
+bool bound_stale(const fm_scene* s, float iso);
 int ensure_flags(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
 GridDev grid_dev(const fm_scene* s);
 

@@ -543,9 +543,13 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
 // reached the march's iso density, so it serves marches at that iso or a
 // lower one; a march at a higher iso builds it again (in place: a march still
 // reading it sees one valid bound or the other in every box).
+static float bound_thr(float iso) { return (iso > 0.0f && std::isfinite(iso)) ? iso : INFINITY; }
+
+bool bound_stale(const fm_scene* s, float iso) { return !(s->bound_valid && bound_thr(iso) <= s->bound_iso); }
+
 int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st, float iso) {
-    const float thr = (iso > 0.0f && std::isfinite(iso)) ? iso : INFINITY;
-    if (s->bound_valid && thr <= s->bound_iso) return FM_OK;
+    const float thr = bound_thr(iso);
+    if (!bound_stale(s, iso)) return FM_OK;
     GridDev g = grid_dev(s);
     KernelDev k = make_kernel(s->support);
     float amax = 0.0f;
