@@ -290,9 +290,10 @@ __global__ void k_gather(const float* __restrict__ xyz, uint64_t n, uint32_t str
 // bound's own and the sample's), and exactly 0 when no particle lies within
 // the support radius of the box.  One warp per cell, lane l owns boxes l and
 // l + 32: the warp loads 32 neighbourhood particles at a time (one coalesced
-// 512-byte read) and passes them to every lane by shuffles, so each lane adds
-// W for its two boxes in registers (the order of the additions does not
-// matter: the margin covers it).
+// 512-byte read) into its 512 bytes of shared memory, from where every lane
+// reads each particle as a broadcast, and each lane adds W for its two boxes
+// in registers (the order of the additions does not matter: the margin
+// covers it).
 //
 // Once the partial sums of all 64 boxes reach `thr` (the iso density of the
 // march that asked for the table), the cell stores +inf for every box and
@@ -305,23 +306,23 @@ constexpr int kBoundWarps = 8;
 
 __global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, KernelDev k, float slack, float thr,
                                                                      float* __restrict__ bound) {
+    __shared__ float4 s_pts[kBoundWarps][kWarp];
     const uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
     const uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
     const int l = threadIdx.x % kWarp;
     if (c >= ncells) return;  // warp-uniform
+    float4* sp = s_pts[threadIdx.x / kWarp];
     const int cc[3] = {(int)(c % (uint64_t)g.dims[0]), (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]),
                        (int)(c / ((uint64_t)g.dims[0] * g.dims[1]))};
-    // this lane's boxes b = l and l + 32 (b = ix + 4 iy + 16 iz), edges grown by the slack
-    float lo[2][3], hi[2][3];
+    // this lane's boxes b = l and l + 32 (b = ix + 4 iy + 16 iz): the same ix and
+    // iy, iz and iz + 2; slab edges grown by the slack
+    const int ib[4] = {l & 3, (l >> 2) & 3, l >> 4, (l >> 4) + 2};  // ix, iy, iz of box l, iz of box l + 32
+    float lo[4], hi[4];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int b = l + 32 * h;
-        const int ib[3] = {b & 3, (b >> 2) & 3, b >> 4};
-#pragma unroll
-        for (int a = 0; a < 3; ++a) {
-            lo[h][a] = g.min[a] + ((float)cc[a] + 0.25f * (float)ib[a]) * g.cell - slack;
-            hi[h][a] = g.min[a] + ((float)cc[a] + 0.25f * (float)(ib[a] + 1)) * g.cell + slack;
-        }
+    for (int i = 0; i < 4; ++i) {
+        const int a = i < 3 ? i : 2;
+        lo[i] = g.min[a] + ((float)cc[a] + 0.25f * (float)ib[i]) * g.cell - slack;
+        hi[i] = g.min[a] + ((float)cc[a] + 0.25f * (float)(ib[i] + 1)) * g.cell + slack;
     }
     float acc0 = 0.0f, acc1 = 0.0f;
     uint32_t cnt = 0;
@@ -341,21 +342,20 @@ __global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, 
             const uint32_t j = j0 + (uint32_t)l;
             const float4 mine = j < e ? g.pts[j] : make_float4(0.f, 0.f, 0.f, 0.f);
             const int m = (int)min(e - j0, (uint32_t)kWarp);
+            __syncwarp();
+            sp[l] = mine;
+            __syncwarp();
             for (int t = 0; t < m; ++t) {
-                const float qx = __shfl_sync(0xffffffffu, mine.x, t);
-                const float qy = __shfl_sync(0xffffffffu, mine.y, t);
-                const float qz = __shfl_sync(0xffffffffu, mine.z, t);
-                const float q[3] = {qx, qy, qz};
-                float d2[2];
+                const float4 qv = sp[t];
+                const float q[4] = {qv.x, qv.y, qv.z, qv.z};
+                float dd[4];  // squared distance to the slab, per axis (z twice)
 #pragma unroll
-                for (int h = 0; h < 2; ++h) {
-                    d2[h] = 0.0f;
-#pragma unroll
-                    for (int a = 0; a < 3; ++a) {
-                        const float d = fmaxf(fmaxf(lo[h][a] - q[a], q[a] - hi[h][a]), 0.0f);
-                        d2[h] += d * d;
-                    }
+                for (int i = 0; i < 4; ++i) {
+                    const float d = fmaxf(fmaxf(lo[i] - q[i], q[i] - hi[i]), 0.0f);
+                    dd[i] = d * d;
                 }
+                const float dxy = dd[0] + dd[1];
+                const float d2[2] = {dxy + dd[2], dxy + dd[3]};
                 if (d2[0] < k.h2) acc0 += w_in(k, d2[0]);
                 if (d2[1] < k.h2) acc1 += w_in(k, d2[1]);
             }
