@@ -9,10 +9,9 @@
 //                  p; hit at the first sample with rho >= iso      (:276-343)
 //   skip           FM_SKIP_REFERENCE: the reference's flag/jump loop
 //                  (:281-306, intersectAABB :51-62);  FM_SKIP_EXACT: samples in
-//                  bound boxes (a half or, once a scene is marched again, a
-//                  quarter cell per axis) whose density upper bound is below
-//                  iso are stepped over without evaluating, so results equal
-//                  skip-off exactly
+//                  bound boxes (a quarter cell per axis) whose density upper
+//                  bound is below iso are stepped over without evaluating, so
+//                  results equal skip-off exactly
 //   refinement     bisection between the last outside and first inside sample
 //   normal         normalize(sum_j gradW(x_j - p_hit)) (:332-338, Kernel.cpp:34-52)
 //   shading        composition.frag:132-184 fused into the epilogue
