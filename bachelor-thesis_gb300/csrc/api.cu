@@ -344,6 +344,7 @@ void fm_scene_destroy(fm_scene* s) {
     fm_ctx* ctx = s->ctx;
     cudaSetDevice(ctx->device);
     cudaStreamSynchronize(ctx->stream);
+    if (ctx->side) cudaStreamSynchronize(ctx->side);  // a bound table build of the scene
     for (size_t i = 0; i < ctx->scenes.size(); ++i)
         if (ctx->scenes[i] == s) {
             ctx->scenes.erase(ctx->scenes.begin() + i);

@@ -476,6 +476,8 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     s->occ_valid = false;
     const uint64_t nkeys = 8 * ncells;
     if (ncells > s->cell_capacity) {
+        // a bound table build of an earlier march may still be running on the side stream
+        if (ctx->side) cudaStreamSynchronize(ctx->side);
         cudaFree(s->d_sub);
         cudaFree(s->d_bound);
         cudaFree(s->d_flag);
