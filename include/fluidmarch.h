@@ -22,6 +22,14 @@
  * one host thread at a time (the reference drives its marcher from the render
  * thread); separate contexts are independent.  A particle-file series
  * (fm_dataset_*) may be read from several threads at once.
+ *
+ * Streams: a call's device work goes to the stream it is given (NULL: the
+ * context's own).  A march that has to build its scene's exact-skip bound
+ * table builds it on a second stream of the context while it splats, and the
+ * march's stream waits for it before the march kernels; fm_scene_destroy and
+ * a grid rebuild that grows the scene's tables wait for both streams of the
+ * context.  A scene is not updated or destroyed while a march on another
+ * stream still reads it.
  */
 #ifndef FLUIDMARCH_H
 #define FLUIDMARCH_H
