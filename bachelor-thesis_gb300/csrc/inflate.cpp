@@ -211,35 +211,70 @@ int fail(std::string& err, const char* msg) {
     return -1;
 }
 
-int codes_block(BitIn& b, const Huff& lit, const Huff& dist, Out& o, size_t base, std::string& err) {
+int codes_block(BitIn& bin, const Huff& lit, const Huff& dist, Out& o, size_t base, std::string& err) {
+    // The loop works on local copies of the bit reader and the output cursor:
+    // a byte store into the output may alias any object in memory, so state
+    // kept only in those structs would be reloaded after every literal.
+    BitIn b = bin;
+    uint8_t* out = o.v.data();
+    size_t pos = o.pos, cap = o.v.size();
+    int rc = 0;
     for (;;) {
-        if (b.past > 8) return fail(err, "deflate stream is truncated");
+        if (b.past > 8) {
+            rc = fail(err, "deflate stream is truncated");
+            break;
+        }
         if (b.cnt < 48) b.fill();
         const int s = lit.decode(b);
-        if (s < 0) return fail(err, "invalid literal/length code");
+        if (s < 0) {
+            rc = fail(err, "invalid literal/length code");
+            break;
+        }
         if (s < 256) {
-            o.reserve(1);
-            o.v[o.pos++] = (uint8_t)s;
+            if (pos == cap) {
+                o.pos = pos;
+                o.reserve(1);
+                out = o.v.data();
+                cap = o.v.size();
+            }
+            out[pos++] = (uint8_t)s;
             continue;
         }
-        if (s == 256) return 0;
+        if (s == 256) break;
         const int li = s - 257;
-        if (li >= 29) return fail(err, "invalid length symbol");
+        if (li >= 29) {
+            rc = fail(err, "invalid length symbol");
+            break;
+        }
         const size_t len = kLenBase[li] + b.bits(kLenExtra[li]);
         const int di = dist.decode(b);
-        if (di < 0 || di >= 30) return fail(err, "invalid distance code");
+        if (di < 0 || di >= 30) {
+            rc = fail(err, "invalid distance code");
+            break;
+        }
         const size_t d = kDistBase[di] + b.bits(kDistExtra[di]);
-        if (d > o.pos - base) return fail(err, "distance reaches before the start of the output");
-        o.reserve(len);
-        uint8_t* dst = o.v.data() + o.pos;
+        if (d > pos - base) {
+            rc = fail(err, "distance reaches before the start of the output");
+            break;
+        }
+        if (pos + len > cap) {
+            o.pos = pos;
+            o.reserve(len);
+            out = o.v.data();
+            cap = o.v.size();
+        }
+        uint8_t* dst = out + pos;
         const uint8_t* src = dst - d;
         if (d >= len) {
             std::memcpy(dst, src, len);
         } else {
             for (size_t k = 0; k < len; ++k) dst[k] = src[k];  // overlapping: a repeated pattern
         }
-        o.pos += len;
+        pos += len;
     }
+    o.pos = pos;
+    bin = b;
+    return rc;
 }
 
 int dynamic_codes(BitIn& b, Huff& lit, Huff& dist, std::string& err) {

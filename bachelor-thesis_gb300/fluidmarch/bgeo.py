@@ -105,12 +105,15 @@ def gunzip(data: bytes) -> bytes:
     L = fm.load()
     n = C.c_uint64()
     src = C.create_string_buffer(data, len(data))
-    rc = L.fm_gunzip(src, len(data), None, 0, C.byref(n))
-    if n.value == 0 and rc != fm.FM_OK and len(data) > 0:
-        # a corrupt stream, or an empty member (n = 0 fits a zero capacity)
-        raise fm.FmError(rc, "gzip decoding failed")
-    out = C.create_string_buffer(max(1, n.value))
-    rc = L.fm_gunzip(src, len(data), out, n.value, C.byref(n))
+    # the member's size field (last 4 bytes) sizes the buffer; DEFLATE expands
+    # at most ~1032:1, which bounds a corrupt field
+    cap = min(int.from_bytes(data[-4:], "little"), 1032 * len(data) + 65536) if len(data) >= 4 else 0
+    out = C.create_string_buffer(max(1, cap))
+    rc = L.fm_gunzip(src, len(data), out, cap, C.byref(n))
+    if rc != fm.FM_OK and n.value > cap:  # decoded, but larger than the size field said
+        cap = n.value
+        out = C.create_string_buffer(cap)
+        rc = L.fm_gunzip(src, len(data), out, cap, C.byref(n))
     if rc != fm.FM_OK:
         raise fm.FmError(rc, "gzip decoding failed")
     return out.raw[:n.value]
