@@ -77,7 +77,10 @@ bool read_tail32(const char* path, uint32_t& v) {
 }
 
 // A header whose point block cannot fit the file: plain files by their size,
-// gzip files by the member's size field (when the data is below 4 GB).
+// gzip files by the member's size field.  That field is the inflated size
+// modulo 2^32, so it proves a short block only for a member that cannot
+// inflate past 4 GB (DEFLATE expands at most ~1032:1: below ~4 MB
+// compressed); larger gzip files are checked when they are decoded.
 int check_point_block(const char* path, const BgeoFile& f, std::string& err) {
     const uint64_t need = (uint64_t)f.layout.data_offset + f.layout.points * 4ull * f.layout.words;
     if (!f.compressed) {
@@ -85,8 +88,8 @@ int check_point_block(const char* path, const BgeoFile& f, std::string& err) {
         return 0;
     }
     uint32_t isize = 0;
-    if (need < (1ull << 32) && read_tail32(path, isize) && need > isize)
-        return fail(err, "BGEO point data is truncated");
+    const bool exact = 1032ull * f.file_bytes + 65536 < (1ull << 32);
+    if (exact && read_tail32(path, isize) && need > isize) return fail(err, "BGEO point data is truncated");
     return 0;
 }
 

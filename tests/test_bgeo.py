@@ -172,7 +172,8 @@ def test_reader_errors(fm, tmp_path):
 
 def test_header_read_rejects_short_point_block(fm, tmp_path):
     """A header that claims more points than the file holds fails at the header read already, plain
-    or gzip (by the gzip member's size field), so a loader sizes no buffer from it."""
+    or gzip (by the gzip member's size field, exact for a small file), so a loader sizes no buffer
+    from it."""
     x = sample_xyz(100, 7)
     good = bgeo.encode(x)
     for name, data in {"plain": good[:-8], "gzip": gzip.compress(good[:-8])}.items():
