@@ -447,7 +447,9 @@ typedef struct fm_bgeo_info {
 
 /* Host read, no GPU needed: the positions of the first min(capacity, points)
  * points into xyz (3 floats each; xyz NULL: header only).  err (may be NULL):
- * the message of a failure. */
+ * the message of a failure.  A header read rejects a point count the file
+ * cannot hold for plain files and for gzip files below ~4 MB (whose size
+ * field is exact); a larger gzip file's count is checked when it is decoded. */
 int fm_bgeo_read(const char* path, float* xyz, uint64_t capacity, fm_bgeo_info* info, char* err, uint64_t err_len);
 /* First member of a gzip stream (RFC 1952), CRC-32 and length checked.
  * out_len = the decoded size; FM_ERR_INVALID when it exceeds out_cap (nothing
