@@ -15,8 +15,9 @@ value  rays/s over all N GPUs (each rank renders its own frame: replicas,
        events on the launching stream, L2 flushed (512 MiB write) between
        frames outside the events.
 e2e    the same frame through the C ABI with pinned HOST buffers: particle
-       upload + grid build + splat + march + shade + copy back of position,
-       normal, depth and colour, wall clock per frame.
+       upload + grid build + bound table (next to the splat) + splat + march +
+       shade, the march writing position, normal, depth and colour into the
+       library's pinned host memory; wall clock per frame.
 --impl reference times the CPU marcher (the oracle port of the reference's
        loop, bisection 0, skipping off, all host threads but one as
        RayMarcher.cpp:67 does) on a bounded random pixel sample per step.
