@@ -583,10 +583,10 @@ int ensure_flags(fm_ctx* ctx, fm_scene* s, cudaStream_t st) {
 //
 // For callers that must not allocate device memory: code that runs where
 // cudaMalloc is not allowed or not wanted (a renderer that reserves all of its
-// memory up front, a plugin living inside a host application's memory budget,
-// work recorded into a CUDA graph).  Same kernels and same results as the
-// grid build of fm_scene_create; the caller passes every output buffer, and
-// the scratch the build needs lives in one file-scope device array:
+// memory up front, a plugin living inside a host application's memory
+// budget).  Same kernels and same results as the grid build of
+// fm_scene_create; the caller passes every output buffer, and the scratch the
+// build needs lives in one file-scope device array:
 //   * the AABB words, the radix-sort histograms and the scan temporaries in
 //     g_noalloc_scratch (kNoAllocWords words, about 1.1 MB, which every device
 //     that loads this library keeps until the process exits);
@@ -597,8 +597,19 @@ int ensure_flags(fm_ctx* ctx, fm_scene* s, cudaStream_t st) {
 // threads) race; serialise them.  The array keeps the last call's contents;
 // the AABB words are cleared at the start of each call and everything else is
 // fully rewritten before it is read.
+//
+// The array's device address differs per CUDA context (the library's module
+// is loaded into each context that uses it), and a host application may run
+// this call under a driver-API context of its own rather than the device's
+// primary context.  So the address is looked up once per context, with that
+// context current, and cached under the context's unique id (cuCtxGetId,
+// reached through the runtime's driver entry points, so the library does not
+// link libcuda itself).
+
+#include <cuda.h>
 
 #include <mutex>
+#include <unordered_map>
 
 namespace fm {
 namespace {
@@ -612,21 +623,66 @@ constexpr uint64_t kNoAllocWords = kNoAllocAabbWords + kNoAllocHistWords + kNoAl
 
 __device__ __align__(256) uint32_t g_noalloc_scratch[kNoAllocWords];
 
-// Device address of g_noalloc_scratch, looked up once per device with that
-// device current (a host-side reference to the symbol is not a device address).
-std::mutex g_noalloc_mu;
-uint32_t* g_noalloc_addr[256] = {};
+typedef CUresult (*PfnCtxGetCurrent)(CUcontext*);
+typedef CUresult (*PfnCtxGetId)(CUcontext, unsigned long long*);
 
-int noalloc_scratch(int dev, uint32_t** out) {
-    if (dev < 0 || dev >= 256) return FM_ERR_CUDA;
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return FM_ERR_CUDA;
-        g_noalloc_addr[dev] = (uint32_t*)p;
+std::mutex g_noalloc_mu;
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
+constexpr size_t kNoAllocCacheMax = 4096;  // contexts remembered; beyond it the address is looked up per call
+std::unordered_map<unsigned long long, uint32_t*> g_noalloc_addr;
+
+// Unique id of the calling thread's current CUDA context (0 when none is current).
+int current_context_id(unsigned long long* id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        void* f1 = nullptr;
+        void* f2 = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+            cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+            q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f1 || !f2)
+            return FM_ERR_CUDA;
+        g_ctx_get_current = (PfnCtxGetCurrent)f1;
+        g_ctx_get_id = (PfnCtxGetId)f2;
     }
-    *out = g_noalloc_addr[dev];
+    CUcontext c = nullptr;
+    if (g_ctx_get_current(&c) != CUDA_SUCCESS) return FM_ERR_CUDA;
+    *id = 0;
+    if (c && g_ctx_get_id(c, id) != CUDA_SUCCESS) return FM_ERR_CUDA;
     return FM_OK;
+}
+
+// Device address of g_noalloc_scratch in the current context (a host-side
+// reference to the symbol is not a device address).
+int noalloc_scratch(uint32_t** out) {
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    unsigned long long id = 0;
+    if (current_context_id(&id) != FM_OK) return FM_ERR_CUDA;
+    if (id != 0) {
+        auto it = g_noalloc_addr.find(id);
+        if (it != g_noalloc_addr.end()) {
+            *out = it->second;
+            return FM_OK;
+        }
+    }
+    // with no context current yet, this lookup makes the device's primary context current
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) return FM_ERR_CUDA;
+    if (id == 0 && current_context_id(&id) != FM_OK) return FM_ERR_CUDA;
+    if (id != 0 && g_noalloc_addr.size() < kNoAllocCacheMax) g_noalloc_addr[id] = (uint32_t*)p;
+    *out = (uint32_t*)p;
+    return FM_OK;
+}
+
+// True for memory of `dev` itself or managed memory: the kernels of this call
+// read and write through these pointers.
+bool on_device(const void* ptr, int dev) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, ptr) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeManaged || (a.type == cudaMemoryTypeDevice && a.device == dev);
 }
 
 }  // namespace
@@ -643,7 +699,10 @@ extern "C" int fm_grid_build_noalloc(const float* xyz, uint64_t n, uint32_t stri
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return FM_ERR_CUDA;
     uint32_t* scratch = nullptr;
-    if (noalloc_scratch(dev, &scratch) != FM_OK) return FM_ERR_CUDA;
+    if (noalloc_scratch(&scratch) != FM_OK) return FM_ERR_CUDA;
+    for (const void* p : {(const void*)xyz, (const void*)sorted_xyzw, (const void*)cell, (const void*)sorted_index,
+                          (const void*)sub_start})
+        if (!on_device(p, dev)) return FM_ERR_INVALID;
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return FM_ERR_CUDA;
     cudaStream_t st = (cudaStream_t)stream;

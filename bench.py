@@ -167,14 +167,47 @@ def measured_peaks():
 
 
 def profiled_march():
-    """The march kernel's ncu figures from the committed summary, if present: DRAM bytes per launch,
-    issue-active fraction, FP32 instructions per cycle over the FP32 peak."""
+    """The march kernels' ncu figures from the committed summary (profiles/march_sloshing_1080p.json):
+    DRAM bytes, issue-active and lane fractions, L1/L2 throughput of k_march and k_march_long, with the
+    commit and date of the capture.  These are not measured by this run."""
     p = os.path.join(ROOT, "profiles", "march_sloshing_1080p.json")
     try:
         with open(p) as f:
             return json.load(f)
     except (OSError, ValueError):
         return {}
+
+
+def march_roofline(st, g, npx, march_ms, peak, peak_kind):
+    """Roofline of the march stage (k_march + k_march_long, CUDA events around fm_march).
+
+    HBM: the bytes the march has to move between HBM and the SMs once per frame -- the cell-sorted
+    particles (16 B each), the sub-cell start table (4 B x (8 n_cells + 1)), the exact-skip bound table
+    (4 B x 64 n_cells), the start depths (4 B per pixel) and the four output planes (position, normal,
+    colour 16 B, hit distance 4 B per pixel) -- over the stage's time.  The candidate stream the
+    reference's loop implies (16 B for every particle in the 27 cells of every density evaluation,
+    RayMarcher.cpp:308-325) is served from L1/L2 and reported beside it, not as an HBM figure."""
+    hbm_bytes = 16 * g["n_particles"] + 4 * (8 * g["n_cells"] + 1) + 4 * 64 * g["n_cells"] + (4 + 52) * npx
+    t = march_ms / 1000.0
+    achieved = hbm_bytes / t / 1e9
+    prof = profiled_march()
+    cand = 16 * st["candidates"]
+    traffic = None
+    if prof.get("kernels"):
+        traffic = sum(k.get("dram_bytes", 0) for k in prof["kernels"].values())
+    return {
+        "bound": "hbm", "kernel": "march stage (k_march + k_march_long)", "achieved": achieved, "peak": peak,
+        "unit": "GB/s", "frac": achieved / peak, "peak_kind": peak_kind, "traffic": traffic,
+        "algorithmic_bytes_per_launch": hbm_bytes,
+        "note": "HBM bytes the march must move once per frame over the stage time; the stage is far below "
+                "the HBM roof and is bound by instruction issue (profiled.issue_active); traffic is the "
+                "profiled DRAM bytes of both kernels",
+        "candidate_stream": {"bytes_per_frame": cand, "evals": st["evals"], "candidates": st["candidates"],
+                             "achieved_gbs": cand / t / 1e9,
+                             "note": "16 B x particles in the 27 cells of every density evaluation, served "
+                                     "from L1/L2 (each streamed particle serves the lanes that need it)"},
+        "profiled": prof or None,
+    }
 
 
 def cpu_baseline_sample(sc, cam, depth, fr, target_s, threads):
@@ -198,6 +231,51 @@ def cpu_baseline_sample(sc, cam, depth, fr, target_s, threads):
             break
         n = int(min(npx, max(n * 2, n * (target_s - spent) / max(dt, 1e-3))))
     return total_px / spent, total_px, spent
+
+
+def frame_parity(O, fr, sc, cam, gpu, threads):
+    """The bench frame's GPU outputs against the oracle, every pixel: the FP32 restatement of the
+    reference loop plus bisection (RayMarcher.cpp:256-344; bit-exact expected) and its FP64 twin (the
+    the benchmark spec's tolerances: hit masks identical except where |rho - iso| <= 1e-3 iso, depth within
+    1e-4 of the scene extent, normals within 0.5 degrees)."""
+    t0 = time.perf_counter()
+    z = gpu["start_depth"]
+    args = (fr, cam, sc.iso, sc.step, sc.max_steps)
+    o32 = O.march(*args, sc.bisect, z, threads=threads)
+    differ = np.zeros(z.size, bool)
+    for k in ("position", "normal", "depth", "colour"):
+        a = np.ascontiguousarray(gpu[k]).view(np.uint32).reshape(z.size, -1)
+        b = np.ascontiguousarray(o32[k]).view(np.uint32).reshape(z.size, -1)
+        differ |= np.any(a != b, axis=1)
+    hg = gpu["position"][:, 3] == 1
+    # masks: decided at the first sample with rho >= iso, so compared on the marches without bisection
+    o32_0 = O.march(*args, 0, z, threads=threads, want_colour=False)
+    o64_0 = O.march(*args, 0, z, threads=threads, precision=64, want_colour=False)
+    h64 = o64_0["position"][:, 3] == 1
+    mism = hg != h64
+    rho = np.where(hg & ~h64, o32_0["rho"], o64_0["rho"])
+    outside = int(np.sum(mism & (np.abs(rho - sc.iso) > 1e-3 * sc.iso)))
+    o64 = O.march(*args, sc.bisect, z, threads=threads, precision=64, want_colour=False)
+    both = hg & (o64["position"][:, 3] == 1)
+    ext = float(np.max(sc.xyz.max(0) - sc.xyz.min(0)))
+    derr = np.abs(gpu["depth"][both].astype(np.float64) - o64["depth"][both]) / ext
+    n1 = gpu["normal"][both, :3].astype(np.float64)
+    n2 = o64["normal"][both, :3].astype(np.float64)
+    c = np.sum(n1 * n2, 1) / np.linalg.norm(n1, axis=1) / np.linalg.norm(n2, axis=1)
+    ang = np.degrees(np.arccos(np.clip(c, -1.0, 1.0)))
+    return {
+        "pixels": int(z.size), "started": int(np.sum(z < 1)), "hits": int(hg.sum()),
+        "oracle_fp32": {"pixels_differing": int(differ.sum()),
+                        "hit_mask_mismatch": int(np.sum(hg != (o32["position"][:, 3] == 1))),
+                        "compared": "position, normal, hit distance, colour bits"},
+        "oracle_fp64": {"hit_mask_mismatch": int(mism.sum()), "mismatch_outside_1e-3_iso": outside,
+                        "hits_compared": int(both.sum()),
+                        "depth_within_1e-4_extent": float(np.mean(derr <= 1e-4)) if derr.size else None,
+                        "max_depth_err_extent": float(derr.max()) if derr.size else None,
+                        "normal_within_0.5_deg": float(np.mean(ang <= 0.5)) if ang.size else None,
+                        "max_normal_deg": float(ang.max()) if ang.size else None},
+        "seconds": time.perf_counter() - t0, "threads": threads,
+    }
 
 
 def run_reference(args):
@@ -678,10 +756,6 @@ def run_ours(args):
 
     if rank == 0:
         peak, peak_kind = measured_peaks()
-        alg_bytes = 16 * st["candidates"] + 36 * npx
-        prof = profiled_march()
-        march_s = march_ms / args.steps / 1000.0
-        achieved = alg_bytes / march_s / 1e9
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
@@ -690,14 +764,7 @@ def run_ours(args):
             "frames_per_s": 1000.0 * args.steps * world / t_max,
             "stage_ms": {"splat": splat_ms / args.steps, "march": march_ms / args.steps},
             "march_counters": st,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": prof.get("dram_bytes_per_launch"),
-                         "kernel": "k_march", "peak_kind": peak_kind,
-                         "algorithmic_bytes_per_launch": alg_bytes,
-                         "note": "16 B x particles in the 27 cells of every density evaluation + 36 B/ray outputs; "
-                                 "served from L1/L2, so frac > 1 means on-chip reuse",
-                         # what bounds the kernel (ncu, same workload): instruction issue, not FP32 math
-                         "issue_active": prof.get("issue_active"), "fp32_issue_frac": prof.get("fp32_issue_frac")},
+            "roofline": march_roofline(st, scene.grid(), npx, march_ms / args.steps, peak, peak_kind),
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 12 * sc.n,
                     "d2h_bytes_per_step": npx * (16 + 16 + 4 + 16)},
             # per frame: fill, sampled splat, tile maxima, cull, survivor splat, march, long rays
@@ -715,11 +782,16 @@ def run_ours(args):
         if grid:
             line["grid_build"] = grid
         if world == 1 and not args.no_cpu_baseline:
+            # CPU legs, after all GPU timing: the oracle port of the reference loop timed on a
+            # pixel sample (cpu_baseline), then the oracle as the checker of the bench frame (parity)
             import oracle as O
 
             O.build_oracle(ref=False)
             fr = O.build_frame(sc.xyz, sc.support)
-            depth = out["start_depth"].cpu().numpy()
+            frame()  # the plain frame again (the anisotropic leg wrote these planes)
+            ctx.sync()
+            gpu = {k: v.cpu().numpy() for k, v in out.items()}
+            depth = gpu["start_depth"]
             cores, model = cpu_info()
             threads = max(1, cores - 1)
             v, npix, secs = cpu_baseline_sample(sc, cam, depth, fr, args.cpu_seconds, threads)
@@ -727,6 +799,7 @@ def run_ours(args):
                                     "sample": f"{npix} seeded random pixels of the same 1920x1080 frame "
                                               f"({secs:.1f} s), bisection 0, skipping off; CPU {model}, "
                                               f"{cores} host cores"}
+            line["parity"] = frame_parity(O, fr, sc, cam, gpu, threads)
         print(json.dumps(line))
     if dist:
         dist.destroy_process_group()

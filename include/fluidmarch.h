@@ -216,8 +216,8 @@ int fm_scene_download(const fm_scene* scene, uint32_t* cell, uint32_t* sorted_in
 /* Grid build that allocates nothing.  No counterpart in the reference: it is
  * for callers that cannot or must not allocate device memory (a renderer that
  * reserves all its memory up front, a plugin inside a host application's
- * memory budget, work recorded into a CUDA graph).  Same results as the grid
- * build of fm_scene_create, on the current CUDA device, on `stream`:
+ * memory budget).  Same results as the grid build of fm_scene_create, on the
+ * current CUDA device and context, on `stream`:
  *   xyz            device, n particles at a stride of `stride` floats (>= 3)
  *   sorted_xyzw    device, 4n floats, 16-byte aligned: sorted positions (w = 0);
  *                  also holds the sort's temporaries until the last step
@@ -227,14 +227,18 @@ int fm_scene_download(const fm_scene* scene, uint32_t* cell, uint32_t* sorted_in
  *                  sub-cell starts (cell c = [sub_start[8c], sub_start[8c+8]))
  *   info           host: grid origin, dims, n_cells (also filled when the
  *                  capacity is too small, so a caller can size sub_start)
+ * The five device buffers must be memory of the current device or managed
+ * memory (FM_ERR_INVALID otherwise); their sizes are the caller's promise.
  * Limits: n <= 2^21 particles, n_cells <= 2^21; FM_ERR_INVALID beyond them.
  * Scratch lives in one device array of about 1.1 MB inside the library (held
  * by every device that loads it until the process exits), shared by all
  * calls: calls that overlap on the GPU race and must be serialised.  The
- * first call on a device looks up that array's device address; make it
- * before any stream capture.  Each call synchronises `stream` once (to read
- * the bounding box); the rest is enqueued asynchronously.  Returns FM_OK,
- * FM_ERR_INVALID or FM_ERR_CUDA; there is no context and no message. */
+ * first call in a CUDA context looks up that array's address in the context
+ * (a driver-API context of the host application works as well as the
+ * device's primary context); make that first call before any stream
+ * capture.  Each call synchronises `stream` once (to read the bounding box);
+ * the rest is enqueued asynchronously.  Returns FM_OK, FM_ERR_INVALID or
+ * FM_ERR_CUDA; there is no context and no message. */
 int fm_grid_build_noalloc(const float* xyz, uint64_t n, uint32_t stride, float support_radius, float* sorted_xyzw,
                           uint32_t* cell, uint32_t* sorted_index, uint32_t* sub_start, uint64_t sub_start_capacity,
                           fm_grid_info* info, void* stream);

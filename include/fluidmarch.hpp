@@ -46,7 +46,9 @@ struct VisualizationSettings {
     int MaxSteps = 128;
     float StepSize = 0.009f;
     float IsoDensity = 1.0f;
-    bool EnableAnisotropy = false;  // RayMarcher::PerPixel_Anisotropic (RayMarcher.cpp:346-423)
+    // RayMarcher::PerPixel_Anisotropic (RayMarcher.cpp:346-423), on by default as
+    // g_VisualizationSettings has it (AdvancedRenderer.cpp:23)
+    bool EnableAnisotropy = true;
     float k_n = 0.5f, k_r = 2.0f, k_s = 2000.0f;
     int N_eps = 1;
     float ParticleRadiusMultiplier = 2.0f;

@@ -125,8 +125,14 @@ double ref_march_any(const float* xyz, int64_t n, float radius, const float* inv
     rm->Prepare(s, ctl, ds, pos.data(), nrm.data(), depth.data());
     rm->Start();
     while (!rm->IsDone()) std::this_thread::sleep_for(std::chrono::microseconds(200));
-    rm->Exit();
     auto t3 = std::chrono::steady_clock::now();
+    // The reference's pool can deadlock in Exit() when the work is short: a worker
+    // released from the start barrier late reads m_Exit only after Exit() set it
+    // and returns without arriving at the barrier Exit() waits on
+    // (ThreadPool.cpp:17-18,43-46).  Giving every worker time to pass that check
+    // before Exit() avoids it; the wall time is taken before the pause.
+    std::this_thread::sleep_for(std::chrono::milliseconds(50));
+    rm->Exit();
 
     std::memcpy(out_pos, pos.data(), npx * sizeof(glm::vec4));
     std::memcpy(out_nrm, nrm.data(), npx * sizeof(glm::vec4));

@@ -45,6 +45,7 @@ int main(int argc, char** argv) {
         std::fwrite(&frames, 4, 1, o);
         std::fwrite(&maxp, 8, 1, o);
         fluidmarch::VisualizationSettings s;
+        s.EnableAnisotropy = false;  // the isotropic march, compared with the oracle's
         s.MaxSteps = hdr[2];
         s.StepSize = par[1];
         s.IsoDensity = par[2];

@@ -33,6 +33,7 @@ int main(int argc, char** argv) {
         fluidmarch::RayMarcher marcher(0);
         fluidmarch::Frame frame(marcher.context(), xyz.data(), (size_t)n, par[0]);
         fluidmarch::VisualizationSettings s;
+        s.EnableAnisotropy = false;  // the isotropic march, compared with the oracle's
         s.MaxSteps = hdr[3];
         s.StepSize = par[1];
         s.IsoDensity = par[2];

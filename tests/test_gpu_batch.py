@@ -116,6 +116,50 @@ def test_batch_view_matches_oracle(fmlib, ctx, small_batch, oracle_lib):
     b.close()
 
 
+def test_bench_batch_every_view_matches_oracle(fmlib, ctx, oracle_lib):
+    """The benchmark's batch (64 sloshing-family scenes, 50k..2M particles, 146 views at 640x480 /
+    1280x720 / 1920x1080, exact skip, 8 bisections) in one graph launch with the work split its
+    autotuner picks (8x4 tiles, deferral after 64 sums): in every view, a seeded sample of 1,000 started pixels and 200 pixels anywhere bit-exact against
+    the oracle's march of that view from the batch's start depths."""
+    bs = scenes.batch_scenes()
+    keep, views, outs, where = [], [], [], []
+    for sc in bs:
+        s = fmlib.Scene(ctx, sc.xyz, sc.support)
+        keep.append(s)
+        p = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, sc.bisect, fmlib.FM_SKIP_EXACT)
+        for cam in sc.cameras:
+            o = device_outputs(cam)
+            outs.append(o)
+            views.append(fmlib.View(s, cam, p, **o))
+            where.append((sc, cam))
+    assert len(views) == 146
+    b = fmlib.Batch(ctx, views, dict(tile_width=8, tiles_per_claim=1, defer_iters=64))
+    b.run()
+    ctx.sync()
+    rng = np.random.default_rng(146)
+    frames = {}
+    checked = 0
+    for o, (sc, cam) in zip(outs, where):
+        if id(sc) not in frames:
+            frames.clear()  # views of a scene are consecutive: keep one oracle frame at a time
+            frames[id(sc)] = O.build_frame(sc.xyz, sc.support)
+        fr = frames[id(sc)]
+        z = o["start_depth"].cpu().numpy()
+        started = np.nonzero(z < 1)[0]
+        assert started.size > 1000
+        pix = np.unique(np.concatenate([rng.choice(started, 1000, replace=False),
+                                        rng.integers(0, cam.width * cam.height, 200)])).astype(np.int64)
+        idx = torch.from_numpy(pix).cuda()
+        g = {k: o[k].index_select(0, idx).cpu().numpy() for k in ("position", "normal", "depth", "colour")}
+        ref = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, sc.bisect, z, pixels=pix)
+        assert_same(g, {k: ref[k][pix] for k in g}, f"view {checked} ({cam.width}x{cam.height}, {sc.n} particles)")
+        checked += 1
+    assert checked == 146
+    b.close()
+    for s in keep:
+        s.close()
+
+
 @pytest.mark.parametrize("cfg", [
     dict(tile_width=1), dict(tile_width=2), dict(tile_width=4), dict(tile_width=16), dict(tile_width=32),
     dict(tile_width=8, tiles_per_claim=4), dict(tile_width=8, defer_iters=1), dict(tile_width=8, defer_iters=4096),

@@ -1,9 +1,11 @@
 """Learned proposal and batching at scale: 4M-particle scenes at 3840x2160.
 
 Every learned view of the batch is judged against the plain march of the same
-view (hit masks identical, depth within 1e-4 of the scene extent), and a
-sample of its hit pixels is checked against the FP64 re-evaluation of the
-march (the oracle's FP64 twin, from the same splatted start depths).
+view (hit masks identical, depth within 1e-4 of the scene extent); the plain
+march of every view equals the FP32 oracle bit for bit on 1,000 seeded
+started pixels, and a sample of the learned view's hit pixels is checked
+against the FP64 re-evaluation of the march (the oracle's FP64 twin, from the
+same splatted start depths).
 
 By default the test renders 2 scenes x 2 views at 3840x2160 with a short
 fine-tuning; FM_SCALE=full renders the whole workload (8 scenes x 16 views,
@@ -59,6 +61,12 @@ def test_learned_batch_at_scale(fmlib, ctx):
                 j = i * views + k
                 dl = sr.depth_learned[j].cpu().numpy()
                 z = sr.start_depth[j].cpu().numpy()
+                # the plain batch's hit distances bit-exact against the FP32 oracle on 1,000 started pixels
+                started = np.nonzero(z < 1)[0]
+                p32 = np.sort(rng.choice(started, min(1000, started.size), replace=False)).astype(np.int64)
+                o32 = O.march(fr, cam, st["iso"], st["step"], st["max_steps"], 8, z, pixels=p32, want_colour=False)
+                dp = sr.depth_plain[j].cpu().numpy()
+                fp32_diff = int(np.sum(dp[p32].view(np.uint32) != o32["depth"][p32].view(np.uint32)))
                 pix = np.sort(rng.choice(np.nonzero(dl > 0)[0], 64, replace=False))
                 o64 = O.march(fr, cam, st["iso"], st["step"], st["max_steps"], 8, z, pixels=pix, precision=64,
                               want_colour=False)
@@ -68,7 +76,8 @@ def test_learned_batch_at_scale(fmlib, ctx):
                 n2 = o64["normal"][pix][both, :3].astype(np.float64)
                 c = np.sum(n1 * n2, 1) / np.linalg.norm(n1, axis=1) / np.linalg.norm(n2, axis=1)
                 ang = np.degrees(np.arccos(np.clip(c, -1, 1)))
-                fp64.append({"view": j, "sampled": int(pix.size), "hit_fp64": int(both.sum()),
+                fp64.append({"view": j, "fp32_sampled": int(p32.size), "fp32_depth_bits_differ": fp32_diff,
+                             "sampled": int(pix.size), "hit_fp64": int(both.sum()),
                              "within_1e-4_extent": float(np.mean(derr <= 1e-4)),
                              "max_depth_err_extent": float(derr.max()) if derr.size else 0.0,
                              "max_normal_deg": float(ang.max()) if ang.size else 0.0})
@@ -88,6 +97,8 @@ def test_learned_batch_at_scale(fmlib, ctx):
             assert r["mask_mismatch"] == 0, f"view {j}: {r}"
             assert r["hits_within_tol"] >= 0.99, f"view {j}: {r}"
         assert rep["judge_all_views"]["within_tol"] >= 0.999
+        # the plain march of every view equals the FP32 oracle bit for bit on its sampled pixels
+        assert all(f["fp32_depth_bits_differ"] == 0 for f in fp64), [f for f in fp64 if f["fp32_depth_bits_differ"]]
         # a sampled hit may miss in FP64 only when its density sits within 1e-3 of the iso value
         assert sum(f["hit_fp64"] for f in fp64) >= 0.99 * sum(f["sampled"] for f in fp64)
         assert within >= 0.99

@@ -117,6 +117,37 @@ def test_march_bitwise_vs_reference(which, box_mode):
     assert (a["position"][:, 3] == 1).sum() > 100
 
 
+@needs_ref
+def test_neighbour_clamp_is_where_reference_and_restatement_part():
+    """The reference keeps at most MAX_NEIGHBORS = 8192 neighbours per sample (RayMarcher.cpp:14,312);
+    the restatement (and the GPU march) sums every particle within the support radius.  A cluster of
+    particles much smaller than the support radius puts all of them in range of the samples near it:
+    with 8192 particles the two agree bit for bit, with 9000 the reference sums only the first 8192 of
+    its neighbour list and its hit points and normals differ."""
+    H = 0.1
+    cam = scenes.make_camera((0.0, 0.0, -1.0), (0.0, 0.0, 0.0), 17, 17)
+    rng = np.random.default_rng(11)
+    w06 = 2.0 * sigma(H) * (1.0 - 0.6) ** 3  # W at q = 0.6
+    results = {}
+    for m in (8192, 9000):
+        xyz = rng.uniform(-0.005, 0.005, (m, 3)).astype(np.float32)
+        iso = float(np.float32(m * w06))  # crossing near 0.6 H from the cluster, every particle in range
+        fr = O.build_frame(xyz, H)
+        depth = O.splat(xyz, H, cam)
+        a = O.ref_march(xyz, H, cam, depth, 200, 0.005, iso)
+        b = O.march(fr, cam, iso, 0.005, 200, 0, depth, threads=2)
+        last = cam.width * cam.height - 1
+        same = True
+        for k in ("position", "normal"):
+            x = b[k].copy()
+            x[last] = 0
+            same &= np.array_equal(a[k].view(np.uint32), x.view(np.uint32))
+        hits = int((b["position"][:, 3] == 1).sum())
+        assert hits > 0
+        results[m] = same
+    assert results == {8192: True, 9000: False}
+
+
 # ---- golden vectors written by the reference --------------------------------
 
 class _Cam:

@@ -1,14 +1,14 @@
 """fm_grid_build_noalloc: the grid build for callers that cannot allocate.
 
 Some callers must not call cudaMalloc (a renderer that reserves its memory up
-front, a plugin inside a host application's memory budget, work recorded into
-a CUDA graph).  For them the library has one entry point that allocates
-nothing: the caller passes the input and every output buffer, and the build's
-scratch lives in a fixed device array inside the library.  This test calls it
-through the C ABI twice in a row (the second call finds the first call's
-leftovers in the shared scratch) and checks that its output equals, bit for
-bit, what the regular entry point (fm_scene_create) builds for the same
-particles.  The file is named so that pytest collects it last.
+front, a plugin inside a host application's memory budget).  For them the
+library has one entry point that allocates nothing: the caller passes the
+input and every output buffer, and the build's scratch lives in a fixed device
+array inside the library.  These tests call it through the C ABI several times
+in a row (each call finds the previous call's leftovers in the shared scratch)
+and check that its output equals, bit for bit, what the regular entry point
+(fm_scene_create) builds for the same particles, for sort keys of three, two
+and one radix pass.  The file is named so that pytest collects it last.
 """
 
 import ctypes
@@ -39,13 +39,29 @@ def _build_noalloc(fmlib, torch, xyz_np, support, capacity=None):
     return rc, info, sorted_xyzw, cell, perm, sub
 
 
-def test_noalloc_grid_build_matches_scene_create(fmlib, ctx):
-    torch = pytest.importorskip("torch")
-    # two calls in a row, different sizes: the second sees the first one's scratch contents
+def _cases():
+    """(xyz, support, radix passes): sloshing frames of 8 * n_cells > 2^16 keys (three 8-bit passes), a
+    small scene of 8 * n_cells <= 2^16 (two) and a cluster inside 3x3x3 cells (one)."""
+    out = []
     for seed, n in ((101, 300_000), (102, 120_000)):
         sc = scenes.sloshing(seed=seed, n=n, h=0.02 * (1_000_000 / n) ** (1 / 3), width=8, height=8)
+        out.append((sc.xyz, sc.support, 3))
+    sc = scenes.small_scene(seed=104, n=30_000)
+    out.append((sc.xyz, sc.support, 2))
+    rng = np.random.default_rng(105)
+    out.append((rng.uniform(0.0, 0.09, (5000, 3)).astype(np.float32), 0.1, 1))
+    return out
+
+
+def test_noalloc_grid_build_matches_scene_create(fmlib, ctx):
+    torch = pytest.importorskip("torch")
+    # calls in a row, different sizes: each sees the previous one's scratch contents
+    for xyz, support, passes in _cases():
+        sc = scenes.Scene("noalloc", xyz, support, 1.0, 0.01, 8, 0)
         rc, info, srt, cell, perm, sub = _build_noalloc(fmlib, torch, sc.xyz, sc.support)
         assert rc == fmlib.FM_OK
+        nkeys = 8 * int(info.n_cells)
+        assert (nkeys - 1).bit_length() <= 8 * passes and (passes == 1 or (nkeys - 1).bit_length() > 8 * passes - 8)
         ref = fmlib.Scene(ctx, sc.xyz, sc.support)
         g = ref.grid()
         d = ref.download()
@@ -68,4 +84,30 @@ def test_noalloc_rejects_sizes_beyond_its_limits(fmlib, ctx):
     # more particles than the scratch array is sized for
     big = np.zeros(((1 << 21) + 1, 3), np.float32)
     rc, *_ = _build_noalloc(fmlib, torch, big, 0.1, capacity=9)
+    assert rc == fmlib.FM_ERR_INVALID
+    # more cells than it is sized for: a unit cube at a support radius of 0.005 (~8 M cells)
+    rng = np.random.default_rng(106)
+    spread = rng.uniform(0.0, 1.0, (1000, 3)).astype(np.float32)
+    rc, info, *_ = _build_noalloc(fmlib, torch, spread, 0.005, capacity=9)
+    assert rc == fmlib.FM_ERR_INVALID and int(info.n_cells) > (1 << 21)
+
+
+def test_noalloc_rejects_host_pointers(fmlib, ctx):
+    """Buffers the GPU cannot use as device memory are refused before any launch."""
+    torch = pytest.importorskip("torch")
+    L = fmlib.load()
+    sc = scenes.small_scene(seed=107, n=2000)
+    n = sc.n
+    xyz = torch.from_numpy(sc.xyz).cuda()
+    srt = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    cell = torch.zeros(n, dtype=torch.int32, device="cuda")
+    perm = torch.zeros(n, dtype=torch.int32, device="cuda")
+    host_sub = np.zeros(8 * 400_000 + 1, np.uint32)
+    info = fmlib.CGridInfo()
+    torch.cuda.synchronize()
+    rc = L.fm_grid_build_noalloc(xyz.data_ptr(), n, 3, float(sc.support), srt.data_ptr(), cell.data_ptr(),
+                                 perm.data_ptr(), host_sub.ctypes.data, host_sub.size, ctypes.byref(info), None)
+    assert rc == fmlib.FM_ERR_INVALID
+    rc = L.fm_grid_build_noalloc(sc.xyz.ctypes.data, n, 3, float(sc.support), srt.data_ptr(), cell.data_ptr(),
+                                 perm.data_ptr(), host_sub.ctypes.data, host_sub.size, ctypes.byref(info), None)
     assert rc == fmlib.FM_ERR_INVALID
