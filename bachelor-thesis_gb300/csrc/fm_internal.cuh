@@ -37,6 +37,7 @@ struct GridDev {
     const uint32_t* __restrict__ sub;     // 8 * n_cells + 1 sub-cell starts; cell c = [sub[8c], sub[8c+8])
     const float* __restrict__ bound;      // per bound box density upper bound (FM_SKIP_EXACT) or null
     const uint8_t* __restrict__ flag;     // per-cell reference skip flag (FM_SKIP_REFERENCE) or null
+    float zlo[3], zhi[3];                 // zero-density box: outside it no particle is within the support radius
 };
 
 // Cubic spline constants, Kernel.cpp:8-14 (h = support radius).
@@ -150,6 +151,24 @@ __device__ __forceinline__ bool outside_forever(const GridDev& g, float px, floa
         if (f < -2.0f && s[a] <= 0.0f) return true;
     }
     return false;
+}
+
+// The grid spans the particles' bounding box padded by the support radius H
+// (Dataset.cpp:89-92), so a sample farther than H beyond that box on some axis
+// has no particle within H: its FP32 density is exactly 0 (every term's
+// squared distance rounds to at least H^2).  zlo / zhi are the padded box grown
+// by a slack of 1e-4 H + 1e-6 max|coordinate|, which covers the rounding of the
+// padding, of the differences and of the squared distances.
+__device__ __forceinline__ bool zero_density(const GridDev& g, float px, float py, float pz) {
+    return px < g.zlo[0] || px > g.zhi[0] || py < g.zlo[1] || py > g.zhi[1] || pz < g.zlo[2] || pz > g.zhi[2];
+}
+
+// True when p is outside the zero-density box on an axis and the step moves
+// further out on it: every later sample has density exactly 0.
+__device__ __forceinline__ bool leaving_zero_box(const GridDev& g, float px, float py, float pz, float sx, float sy,
+                                                 float sz) {
+    return (px > g.zhi[0] && sx >= 0.0f) || (px < g.zlo[0] && sx <= 0.0f) || (py > g.zhi[1] && sy >= 0.0f) ||
+           (py < g.zlo[1] && sy <= 0.0f) || (pz > g.zhi[2] && sz >= 0.0f) || (pz < g.zlo[2] && sz <= 0.0f);
 }
 
 // ---- host-side objects ------------------------------------------------------

@@ -272,6 +272,133 @@ __global__ void k_radix_scatter(const uint32_t* __restrict__ keys_in, const uint
     }
 }
 
+// ---- counting sort seeded by the key histogram ----------------------------
+// The key histogram k_cells counts, scanned, gives every key its segment
+// [sub[k], sub[k+1]).  k_scatter drops each particle's index into a free slot
+// of its segment (counts[k] counts down as slots are taken, so the order
+// inside a segment is arbitrary and counts ends at 0); k_segsort_gather then
+// sorts each segment by input index, which restores exactly the stable order
+// (cell, sub-cell, input index), and gathers the positions.  Segments longer
+// than kShortSeg go to a list that k_long_segsort sorts a block per segment.
+constexpr uint32_t kShortSeg = 32;
+
+__global__ void k_scatter(const uint32_t* __restrict__ key, uint64_t n, const uint32_t* __restrict__ sub,
+                          uint32_t* __restrict__ counts, uint32_t* __restrict__ slots) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint32_t k = key[i];
+    const uint32_t left = atomicSub(&counts[k], 1u);  // 1 .. count
+    slots[sub[k] + left - 1u] = (uint32_t)i;
+}
+
+// One thread per key: sort a short segment of indices (insertion sort in
+// registers), write the sorted indices and gather the positions; append a long
+// one to long_keys.
+__global__ void k_segsort_gather(const float* __restrict__ xyz, uint32_t stride, uint64_t nkeys,
+                                 const uint32_t* __restrict__ sub, const uint32_t* __restrict__ slots,
+                                 uint32_t* __restrict__ perm, float4* __restrict__ pts,
+                                 uint32_t* __restrict__ long_keys, uint32_t* __restrict__ n_long) {
+    uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (k >= nkeys) return;
+    const uint32_t b = sub[k], m = sub[k + 1] - b;
+    if (m == 0) return;
+    if (m > kShortSeg) {
+        long_keys[atomicAdd(n_long, 1u)] = (uint32_t)k;
+        return;
+    }
+    uint32_t v[kShortSeg];
+    for (uint32_t j = 0; j < m; ++j) {
+        const uint32_t x = slots[b + j];
+        uint32_t t = j;
+        while (t > 0 && v[t - 1] > x) {
+            v[t] = v[t - 1];
+            --t;
+        }
+        v[t] = x;
+    }
+    for (uint32_t j = 0; j < m; ++j) {
+        const float* p = xyz + (uint64_t)v[j] * stride;
+        perm[b + j] = v[j];
+        pts[b + j] = make_float4(p[0], p[1], p[2], 0.0f);
+    }
+}
+
+// One block per long segment (grid-stride over the list): a stable LSD radix
+// sort of the segment's indices, 8 bits per pass, ping-ponging between the
+// segment's range of `slots` and of `tmp`, then the gather.  The indices are
+// distinct, so the sorted segment is unique.
+constexpr int kLongThreads = 256;
+
+__global__ void __launch_bounds__(kLongThreads) k_long_segsort(const float* __restrict__ xyz, uint32_t stride,
+                                                               const uint32_t* __restrict__ sub,
+                                                               uint32_t* __restrict__ slots, uint32_t* __restrict__ tmp,
+                                                               const uint32_t* __restrict__ long_keys,
+                                                               const uint32_t* __restrict__ n_long, int passes,
+                                                               uint32_t* __restrict__ perm, float4* __restrict__ pts) {
+    __shared__ uint32_t s_base[256];
+    __shared__ uint32_t s_w[kLongThreads / kWarp][256];
+    const int t = threadIdx.x, l = t % kWarp, w = t / kWarp;
+    const uint32_t lt = (1u << l) - 1u;
+    const uint32_t nl = *n_long;
+    for (uint32_t e = blockIdx.x; e < nl; e += gridDim.x) {
+        const uint32_t k = long_keys[e];
+        const uint32_t b = sub[k], m = sub[k + 1] - b;
+        uint32_t* src = slots + b;
+        uint32_t* dst = tmp + b;
+        for (int p = 0; p < passes; ++p) {
+            const int shift = 8 * p;
+            s_base[t] = 0;
+            __syncthreads();
+            for (uint32_t j = t; j < m; j += kLongThreads) atomicAdd(&s_base[(src[j] >> shift) & 255u], 1u);
+            __syncthreads();
+            if (t == 0) {  // exclusive scan of the 256 digit counts
+                uint32_t run = 0;
+                for (int d = 0; d < 256; ++d) {
+                    const uint32_t c = s_base[d];
+                    s_base[d] = run;
+                    run += c;
+                }
+            }
+            __syncthreads();
+            for (uint32_t j0 = 0; j0 < m; j0 += kLongThreads) {
+                const uint32_t j = j0 + t;
+                const bool valid = j < m;
+                const uint32_t x = valid ? src[j] : 0u;
+                const uint32_t d = valid ? ((x >> shift) & 255u) : (0x10000u + l);
+#pragma unroll
+                for (int q = 0; q < kLongThreads / kWarp; ++q) s_w[q][t] = 0;
+                __syncthreads();
+                const uint32_t peers = __match_any_sync(0xffffffffu, d);
+                const uint32_t rank = __popc(peers & lt);
+                if (valid && rank == 0) s_w[w][d] = __popc(peers);
+                __syncthreads();
+                uint32_t run = 0;  // thread t: prefix over warps of digit t
+#pragma unroll
+                for (int q = 0; q < kLongThreads / kWarp; ++q) {
+                    const uint32_t c = s_w[q][t];
+                    s_w[q][t] = run;
+                    run += c;
+                }
+                __syncthreads();
+                if (valid) dst[s_base[d] + s_w[w][d] + rank] = x;
+                __syncthreads();
+                s_base[t] += run;
+                __syncthreads();
+            }
+            uint32_t* sw = src;
+            src = dst;
+            dst = sw;
+        }
+        for (uint32_t j = t; j < m; j += kLongThreads) {
+            const uint32_t x = src[j];
+            const float* q = xyz + (uint64_t)x * stride;
+            perm[b + j] = x;
+            pts[b + j] = make_float4(q[0], q[1], q[2], 0.0f);
+        }
+        __syncthreads();
+    }
+}
+
 __global__ void k_gather(const float* __restrict__ xyz, uint64_t n, uint32_t stride, const uint32_t* __restrict__ perm,
                          float4* __restrict__ out) {
     uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
@@ -426,6 +553,13 @@ GridDev grid_dev(const fm_scene* s) {
     g.nsub = (uint32_t)(8 * s->ncells + 1);
     g.bound = s->bound_valid ? s->d_bound : nullptr;
     g.flag = s->flag_valid ? s->d_flag : nullptr;
+    float amax = 0.0f;
+    for (int a = 0; a < 3; ++a) amax = std::max(amax, std::max(std::fabs(s->min[a]), std::fabs(s->max[a])));
+    const float slack = 1.0e-4f * s->support + 1.0e-6f * amax;
+    for (int a = 0; a < 3; ++a) {
+        g.zlo[a] = s->min[a] - slack;
+        g.zhi[a] = s->max[a] + slack;
+    }
     return g;
 }
 
@@ -494,49 +628,34 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     GridParams gp;
     for (int a = 0; a < 3; ++a) { gp.min[a] = s->min[a]; gp.dims[a] = s->dims[a]; }
     gp.inv = s->inv;
-    const uint64_t nblk = (n + kSortTile - 1) / kSortTile;
-    const uint64_t hist_n = 256 * nblk;
-    const uint64_t scan_n = std::max<uint64_t>(nkeys + 1, hist_n);
-    if (!ensure_buf(ctx->scratch[1], (nkeys + 1) * sizeof(uint32_t)) ||  // counts
-        !ensure_buf(ctx->scratch[2], n * sizeof(uint32_t)) ||            // keys b
-        !ensure_buf(ctx->scratch[3], n * sizeof(uint32_t)) ||            // vals b
-        !ensure_buf(ctx->scratch[4], n * sizeof(uint32_t)) ||            // keys a
-        !ensure_buf(ctx->scratch[5], hist_n * sizeof(uint32_t)) ||       // hist
-        !ensure_buf(ctx->scratch[6], scan_tmp_words(scan_n) * sizeof(uint32_t)) ||
+    if (!ensure_buf(ctx->scratch[1], (nkeys + 2) * sizeof(uint32_t)) ||  // key counts + long-segment count
+        !ensure_buf(ctx->scratch[2], n * sizeof(uint32_t)) ||            // slots
+        !ensure_buf(ctx->scratch[3], n * sizeof(uint32_t)) ||            // long-segment sort temporaries
+        !ensure_buf(ctx->scratch[4], n * sizeof(uint32_t)) ||            // long-segment keys
+        !ensure_buf(ctx->scratch[6], scan_tmp_words(nkeys + 1) * sizeof(uint32_t)) ||
         !ensure_buf(ctx->scratch[7], n * sizeof(uint32_t)))              // keys (input order)
         return set_err(ctx, FM_ERR_OOM, "grid build scratch allocation failed");
     uint32_t* counts = (uint32_t*)ctx->scratch[1].p;
+    uint32_t* n_long = counts + nkeys + 1;
+    uint32_t* slots = (uint32_t*)ctx->scratch[2].p;
     uint32_t* keys0 = (uint32_t*)ctx->scratch[7].p;
-    FM_CUDA(ctx, cudaMemsetAsync(counts, 0, (nkeys + 1) * sizeof(uint32_t), st));
-    k_cells<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_xyz, n, stride, gp, s->d_cell, keys0, counts);
+    FM_CUDA(ctx, cudaMemsetAsync(counts, 0, (nkeys + 2) * sizeof(uint32_t), st));
+    const unsigned pblocks = (unsigned)((n + 255) / 256);
+    k_cells<<<pblocks, 256, 0, st>>>(d_xyz, n, stride, gp, s->d_cell, keys0, counts);
     FM_CUDA(ctx, cudaGetLastError());
     uint32_t* tmp = (uint32_t*)ctx->scratch[6].p;
     exclusive_scan(counts, s->d_sub, nkeys + 1, tmp, st);
     FM_CUDA(ctx, cudaGetLastError());
-    // 4. stable LSD radix sort of (key, index)
-    int bits = 1;
-    while (bits < 32 && ((nkeys - 1) >> bits)) ++bits;
-    const uint32_t* kin = keys0;
-    const uint32_t* vin = nullptr;
-    uint32_t* kbuf[2] = {(uint32_t*)ctx->scratch[4].p, (uint32_t*)ctx->scratch[2].p};
-    uint32_t* vbuf[2] = {s->d_perm, (uint32_t*)ctx->scratch[3].p};
-    uint32_t* hist = (uint32_t*)ctx->scratch[5].p;
-    const int passes = (bits + 7) / 8;
-    // the last pass must land its values in s->d_perm
-    int cur = (passes % 2 == 1) ? 0 : 1;
-    for (int p = 0; p < passes; ++p) {
-        const int shift = 8 * p;
-        k_radix_hist<<<(unsigned)nblk, kSortThreads, 0, st>>>(kin, n, shift, (uint32_t)nblk, hist);
-        exclusive_scan(hist, hist, hist_n, tmp, st);
-        k_radix_scatter<<<(unsigned)nblk, kSortThreads, 0, st>>>(kin, vin, kbuf[cur], vbuf[cur], n, shift,
-                                                               (uint32_t)nblk, hist);
-        FM_CUDA(ctx, cudaGetLastError());
-        kin = kbuf[cur];
-        vin = vbuf[cur];
-        cur ^= 1;
-    }
-    // 5. gather sorted float4 positions
-    k_gather<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(d_xyz, n, stride, s->d_perm, s->d_pts);
+    // 4. counting sort: scatter into the key segments, sort each by input index, gather
+    k_scatter<<<pblocks, 256, 0, st>>>(keys0, n, s->d_sub, counts, slots);
+    k_segsort_gather<<<(unsigned)((nkeys + 255) / 256), 256, 0, st>>>(d_xyz, stride, nkeys, s->d_sub, slots,
+                                                                      s->d_perm, s->d_pts,
+                                                                      (uint32_t*)ctx->scratch[4].p, n_long);
+    int ibits = 1;
+    while (ibits < 32 && ((n - 1) >> ibits)) ++ibits;
+    k_long_segsort<<<(unsigned)ctx->sm_count, kLongThreads, 0, st>>>(
+        d_xyz, stride, s->d_sub, slots, (uint32_t*)ctx->scratch[3].p, (const uint32_t*)ctx->scratch[4].p, n_long,
+        (ibits + 7) / 8, s->d_perm, s->d_pts);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }

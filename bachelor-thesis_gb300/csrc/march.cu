@@ -401,8 +401,11 @@ __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc&
             r.p[2] = r.p[2] + r.s[2];
             ++r.i;
             if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2], a.status);
-            if (!locate(a.g, r.p[0], r.p[1], r.p[2], L)) {
-                if (outside_forever(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2])) {
+            if (zero_density(a.g, r.p[0], r.p[1], r.p[2]) || !locate(a.g, r.p[0], r.p[1], r.p[2], L)) {
+                // density exactly 0 here; with iso > 0 no later sample of a ray leaving the
+                // zero-density box can hit
+                if ((a.iso > 0.0f && leaving_zero_box(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2])) ||
+                    outside_forever(a.g, r.p[0], r.p[1], r.p[2], r.s[0], r.s[1], r.s[2])) {
                     // every later sample has density 0; an interval still needs its prefix
                     r.phase = kDone;
                     if (LEARNED && r.mode == kInterval) {
@@ -426,7 +429,7 @@ __device__ __forceinline__ bool prepare(const MarchArgs& a, Ray& r, Loc& L, Acc&
             r.e[0] = (r.q[0] + r.p[0]) * 0.5f;
             r.e[1] = (r.q[1] + r.p[1]) * 0.5f;
             r.e[2] = (r.q[2] + r.p[2]) * 0.5f;
-            if (!locate(a.g, r.e[0], r.e[1], r.e[2], L)) {
+            if (zero_density(a.g, r.e[0], r.e[1], r.e[2]) || !locate(a.g, r.e[0], r.e[1], r.e[2], L)) {
                 if (STATS && cnt) acc.evals++;
                 apply<LEARNED>(a, r, 0.0f);
                 continue;

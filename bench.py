@@ -573,7 +573,8 @@ def run_grid(args, fm, torch, ctx, ext, sc, flush, peak):
                      "achieved_gbs": alg / ms / 1e6, "frac_of_hbm_peak": alg / ms / 1e6 / peak}
         del xyz_d
     res["note"] = ("fm_scene_update from device positions: k_aabb, read-back of the bounds for the grid size, "
-                   "cell keys, 8-bit radix passes, sorted gather; median of the builds, each after an L2 flush")
+                   "cell keys and key histogram, its scan, counting scatter, per-sub-cell sort by input index "
+                   "with the gather; median of the builds, each after an L2 flush")
     return res
 
 

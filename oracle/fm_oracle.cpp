@@ -184,6 +184,25 @@ template <typename T> inline bool sample_cell(const OrcGrid& g, V3<T> p, int& cx
 
 struct EvalStats { int64_t evals = 0; int64_t candidates = 0; };
 
+// The grid is the particles' box padded by the support radius H
+// (Dataset.cpp:89-92), so farther than H beyond that box (plus a rounding
+// slack of 1e-4 H + 1e-6 max|coordinate|) no particle is within H and the
+// density is exactly 0.  True when p is out there on an axis the step moves
+// further out on: with iso > 0 no later sample can hit.
+template <typename T> inline bool leaving_zero_box(const OrcGrid& g, V3<T> p, V3<T> s) {
+    float amax = 0.0f;
+    for (int a = 0; a < 3; ++a) amax = std::max(amax, std::max(std::fabs(g.min[a]), std::fabs(g.max[a])));
+    const float H = g.cell;
+    const float slack = 1.0e-4f * H + 1.0e-6f * amax;
+    const T pa[3] = {p.x, p.y, p.z}, sa[3] = {s.x, s.y, s.z};
+    for (int a = 0; a < 3; ++a) {
+        const float lo = g.min[a] - slack, hi = g.max[a] + slack;
+        if (pa[a] > T(hi) && sa[a] >= T(0)) return true;
+        if (pa[a] < T(lo) && sa[a] <= T(0)) return true;
+    }
+    return false;
+}
+
 // floor((p - min) * inv) leaves [-2, dims + 1] on an axis and the step moves
 // further out on it (monotone FP addition): all later densities are 0.
 template <typename T> inline bool outside_forever(const OrcGrid& g, V3<T> p, V3<T> s) {
@@ -403,9 +422,10 @@ void march_pixel(const Scene& s, const OrcCamera& cam, const OrcParams& P, const
                     p = V3<T>{T(pf.x), T(pf.y), T(pf.z)};
                 }
             }
-            // Past the grid's evaluation range on an axis the step moves away from:
-            // every later sample has density 0, so stop (same outputs as marching on).
-            if (outside_forever(s.g, p, step)) break;
+            // Past the grid's evaluation range, or (iso > 0) past the zero-density box, on an
+            // axis the step moves away from: every later sample has density 0, so stop (same
+            // outputs as marching on).
+            if (outside_forever(s.g, p, step) || (P.iso > 0.0f && leaving_zero_box(s.g, p, step))) break;
             T rho = density(s, k, p, st);
             if (rho >= T(P.iso)) {
                 if (kf >= 0 && i == ks) { restart = true; break; }

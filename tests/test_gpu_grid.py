@@ -57,11 +57,27 @@ def test_grid_all_in_one_cell_and_duplicates(fmlib, ctx):
 
 
 def test_grid_many_cells(fmlib, ctx):
-    """More than 2^16 cells: three radix passes."""
+    """More than 2^16 cells (636k), sparse: most sub-cells hold 0 or 1 particle."""
     rng = np.random.default_rng(3)
     xyz = rng.uniform(0.0, 1.0, size=(300000, 3)).astype(np.float32)
     g = check_grid(fmlib, ctx, xyz, 0.012)
     assert g["n_cells"] > (1 << 16)
+
+
+def test_grid_segment_lengths(fmlib, ctx):
+    """Sub-cells holding 1 .. 32 particles (sorted by one thread), 33 .. 4,000 and 60,000 (sorted by a
+    block, radix passes over the input indices), in scrambled input order."""
+    rng = np.random.default_rng(4)
+    parts = [rng.uniform(0.0, 2.0, (20000, 3))]
+    for m in (33, 64, 257, 4000):
+        parts.append(rng.uniform(0.0, 2.0, 3) + rng.uniform(0.0, 0.01, (m, 3)))
+    parts.append(np.repeat(rng.uniform(0.0, 2.0, (1, 3)), 60000, axis=0))
+    xyz = np.concatenate(parts).astype(np.float32)
+    rng.shuffle(xyz)
+    fr = O.build_frame(xyz, 0.1)
+    seg = np.diff(fr.sub_start)
+    assert seg.max() >= 60000 and np.sum((seg > 32) & (seg < 60000)) >= 4
+    check_grid(fmlib, ctx, xyz, 0.1)
 
 
 def test_scene_update_rebuilds(fmlib, ctx):

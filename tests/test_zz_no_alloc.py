@@ -40,28 +40,30 @@ def _build_noalloc(fmlib, torch, xyz_np, support, capacity=None):
 
 
 def _cases():
-    """(xyz, support, radix passes): sloshing frames of 8 * n_cells > 2^16 keys (three 8-bit passes), a
-    small scene of 8 * n_cells <= 2^16 (two) and a cluster inside 3x3x3 cells (one)."""
+    """(xyz, support): sort keys of three 8-bit radix passes (a 300k-particle sloshing frame on the 1M
+    frame's grid, 8 * n_cells > 2^16), two (a 120k-particle frame with its scaled support radius, and a
+    small scene) and one (a cluster inside 3x3x3 cells)."""
     out = []
-    for seed, n in ((101, 300_000), (102, 120_000)):
-        sc = scenes.sloshing(seed=seed, n=n, h=0.02 * (1_000_000 / n) ** (1 / 3), width=8, height=8)
-        out.append((sc.xyz, sc.support, 3))
+    sc = scenes.sloshing(seed=101, n=300_000, h=0.02, width=8, height=8)
+    out.append((sc.xyz, sc.support))
+    sc = scenes.sloshing(seed=102, n=120_000, h=0.02 * (1_000_000 / 120_000) ** (1 / 3), width=8, height=8)
+    out.append((sc.xyz, sc.support))
     sc = scenes.small_scene(seed=104, n=30_000)
-    out.append((sc.xyz, sc.support, 2))
+    out.append((sc.xyz, sc.support))
     rng = np.random.default_rng(105)
-    out.append((rng.uniform(0.0, 0.09, (5000, 3)).astype(np.float32), 0.1, 1))
+    out.append((rng.uniform(0.0, 0.09, (5000, 3)).astype(np.float32), 0.1))
     return out
 
 
 def test_noalloc_grid_build_matches_scene_create(fmlib, ctx):
     torch = pytest.importorskip("torch")
     # calls in a row, different sizes: each sees the previous one's scratch contents
-    for xyz, support, passes in _cases():
+    passes = set()
+    for xyz, support in _cases():
         sc = scenes.Scene("noalloc", xyz, support, 1.0, 0.01, 8, 0)
         rc, info, srt, cell, perm, sub = _build_noalloc(fmlib, torch, sc.xyz, sc.support)
         assert rc == fmlib.FM_OK
-        nkeys = 8 * int(info.n_cells)
-        assert (nkeys - 1).bit_length() <= 8 * passes and (passes == 1 or (nkeys - 1).bit_length() > 8 * passes - 8)
+        passes.add((max(1, (8 * int(info.n_cells) - 1).bit_length()) + 7) // 8)
         ref = fmlib.Scene(ctx, sc.xyz, sc.support)
         g = ref.grid()
         d = ref.download()
@@ -73,6 +75,7 @@ def test_noalloc_grid_build_matches_scene_create(fmlib, ctx):
         assert np.array_equal(srt.cpu().numpy().view(np.uint32), d["sorted"].view(np.uint32))
         starts = sub.cpu().numpy().view(np.uint32)[: 8 * g["n_cells"] + 1 : 8]
         assert np.array_equal(starts, d["start"])
+    assert passes == {1, 2, 3}
 
 
 def test_noalloc_rejects_sizes_beyond_its_limits(fmlib, ctx):
