@@ -178,6 +178,10 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->prop_scratch.p);
     cudaFree(ctx->prop_low.p);
     cudaFree(ctx->prop_judge.p);
+    cudaFree(ctx->judge_z.p);
+    cudaFree(ctx->judge_ref.p);
+    cudaFree(ctx->judge_test.p);
+    cudaFree(ctx->judge_acc.p);
     if (ctx->h_pinned_small) cudaFreeHost(ctx->h_pinned_small);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
@@ -557,10 +561,16 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     o.nrm = (float4*)dev[1];
     o.depth = (float*)dev[2];
     o.col = (float4*)dev[3];
+    const bool judge = (p->flags & FM_MARCH_PROPOSAL) && ctx->judge_stride > 0;
+    if (judge && !o.depth) {  // the judge compares hit distances: the learned march writes them here
+        if (!grow_buf(ctx->judge_test, npx * 4)) return set_err(ctx, FM_ERR_OOM, "judge buffer allocation failed");
+        o.depth = (float*)ctx->judge_test.p;
+    }
     if (ctx->stats_enabled) FM_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, fm::kStatSlots * sizeof(unsigned long long), st));
     if (p->flags & FM_MARCH_ANISOTROPIC) rc = launch_march_aniso(ctx, s, cam, p, &ctx->aniso, o, st);
     else rc = launch_march(ctx, s, cam, p, o, st);
     if (rc) return rc;
+    if (judge && (rc = judge_learned(ctx, sm, cam, p, z, o.depth, st)) != FM_OK) return rc;
     if (host) {
         for (int i = 0; i < 4; ++i)
             if (user[i] && !direct[i])

@@ -229,6 +229,13 @@ struct fm_ctx {
     // intervals, occupancy counts, low-resolution depth, judge counters
     fm_proposal* proposal = nullptr;
     fm::DevBuf prop_ivl, prop_scratch, prop_low, prop_judge;
+    // per-frame judge of learned marches (fm_set_judge): sample stride, depth
+    // tolerance, frames judged so far (seeds the sample), sample start plane,
+    // plain-march and learned-march hit distances, counters
+    uint32_t judge_stride = 0;
+    float judge_tol = 0.0f;
+    uint64_t judge_seq = 0;
+    fm::DevBuf judge_z, judge_ref, judge_test, judge_acc;
     fm::DevBuf file_rec, file_xyz;  // particle-file loader: point records, gathered positions
     fm::DevBuf blur_in, blur_out;   // depth blur staging for host buffers
     // live scenes of this context; fm_destroy frees the ones still alive
@@ -423,6 +430,10 @@ void destroy_batches(fm_ctx* ctx);
 int ensure_occupancy(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
 int launch_features(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const float* zbuf, float* feat, float* t0,
                     cudaStream_t st);
+// Per-frame judge (fm_set_judge): plain march of a pixel sample next to a
+// learned march whose start depths are z and hit distances learned_depth.
+int judge_learned(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const float* z,
+                  const float* learned_depth, cudaStream_t st);
 int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const fm_proposal* pr,
                    const float* zbuf, int2* ivl, float2* raw, cudaStream_t st);
 // Batched proposal: per-view blocks (propose_view) laid out by the caller.

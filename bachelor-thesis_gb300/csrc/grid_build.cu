@@ -277,9 +277,10 @@ __global__ void k_radix_scatter(const uint32_t* __restrict__ keys_in, const uint
 // [sub[k], sub[k+1]).  k_scatter drops each particle's index into a free slot
 // of its segment (counts[k] counts down as slots are taken, so the order
 // inside a segment is arbitrary and counts ends at 0); k_segsort_gather then
-// sorts each segment by input index, which restores exactly the stable order
-// (cell, sub-cell, input index), and gathers the positions.  Segments longer
-// than kShortSeg go to a list that k_long_segsort sorts a block per segment.
+// sorts each segment by input index (a warp per segment), which restores
+// exactly the stable order (cell, sub-cell, input index), and gathers the
+// positions.  Segments longer than kShortSeg go to a list that k_long_segsort
+// sorts a block per segment.
 constexpr uint32_t kShortSeg = 32;
 
 __global__ void k_scatter(const uint32_t* __restrict__ key, uint64_t n, const uint32_t* __restrict__ sub,
@@ -291,35 +292,30 @@ __global__ void k_scatter(const uint32_t* __restrict__ key, uint64_t n, const ui
     slots[sub[k] + left - 1u] = (uint32_t)i;
 }
 
-// One thread per key: sort a short segment of indices (insertion sort in
-// registers), write the sorted indices and gather the positions; append a long
-// one to long_keys.
+// One warp per key: a short segment's indices are distinct, so lane l's rank in
+// the sorted segment is the number of the segment's indices below its own
+// (compared through shuffles); the lane writes its index and gathers its
+// position there.  A long segment goes to long_keys.
 __global__ void k_segsort_gather(const float* __restrict__ xyz, uint32_t stride, uint64_t nkeys,
                                  const uint32_t* __restrict__ sub, const uint32_t* __restrict__ slots,
                                  uint32_t* __restrict__ perm, float4* __restrict__ pts,
                                  uint32_t* __restrict__ long_keys, uint32_t* __restrict__ n_long) {
-    uint64_t k = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (k >= nkeys) return;
-    const uint32_t b = sub[k], m = sub[k + 1] - b;
+    const uint64_t k = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
+    const uint32_t l = threadIdx.x % kWarp;
+    if (k >= nkeys) return;  // warp-uniform
+    const uint32_t b = __ldg(sub + k), m = __ldg(sub + k + 1) - b;
     if (m == 0) return;
     if (m > kShortSeg) {
-        long_keys[atomicAdd(n_long, 1u)] = (uint32_t)k;
+        if (l == 0) long_keys[atomicAdd(n_long, 1u)] = (uint32_t)k;
         return;
     }
-    uint32_t v[kShortSeg];
-    for (uint32_t j = 0; j < m; ++j) {
-        const uint32_t x = slots[b + j];
-        uint32_t t = j;
-        while (t > 0 && v[t - 1] > x) {
-            v[t] = v[t - 1];
-            --t;
-        }
-        v[t] = x;
-    }
-    for (uint32_t j = 0; j < m; ++j) {
-        const float* p = xyz + (uint64_t)v[j] * stride;
-        perm[b + j] = v[j];
-        pts[b + j] = make_float4(p[0], p[1], p[2], 0.0f);
+    const uint32_t v = l < m ? slots[b + l] : 0xffffffffu;
+    uint32_t rank = 0;
+    for (uint32_t t = 0; t < m; ++t) rank += __shfl_sync(0xffffffffu, v, (int)t) < v ? 1u : 0u;
+    if (l < m) {
+        const float* p = xyz + (uint64_t)v * stride;
+        perm[b + rank] = v;
+        pts[b + rank] = make_float4(p[0], p[1], p[2], 0.0f);
     }
 }
 
@@ -648,7 +644,7 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     FM_CUDA(ctx, cudaGetLastError());
     // 4. counting sort: scatter into the key segments, sort each by input index, gather
     k_scatter<<<pblocks, 256, 0, st>>>(keys0, n, s->d_sub, counts, slots);
-    k_segsort_gather<<<(unsigned)((nkeys + 255) / 256), 256, 0, st>>>(d_xyz, stride, nkeys, s->d_sub, slots,
+    k_segsort_gather<<<(unsigned)((nkeys * kWarp + 255) / 256), 256, 0, st>>>(d_xyz, stride, nkeys, s->d_sub, slots,
                                                                       s->d_perm, s->d_pts,
                                                                       (uint32_t*)ctx->scratch[4].p, n_long);
     int ibits = 1;

@@ -774,6 +774,60 @@ __global__ void k_judge(const float* __restrict__ dref, const float* __restrict_
     }
 }
 
+// Per-frame judge: the sample of a frame is every started pixel of the 8x4
+// pixel blocks (one march tile each) whose hashed block index (lowbias32 of
+// index ^ seed) is 0 modulo the stride, so the sampled rays march together.
+__device__ __forceinline__ bool judge_sampled(uint64_t i, uint32_t width, uint32_t seed, uint32_t stride) {
+    const uint32_t px = (uint32_t)(i % width), py = (uint32_t)(i / width);
+    uint32_t x = ((py >> 2) * ((width + 7u) >> 3) + (px >> 3)) ^ seed;
+    x ^= x >> 16;
+    x *= 0x7feb352du;
+    x ^= x >> 15;
+    x *= 0x846ca68bu;
+    x ^= x >> 16;
+    return x % stride == 0u;
+}
+
+// Start plane of the sample: the learned march's start depth where sampled, 1 (no ray) elsewhere.
+__global__ void k_judge_starts(const float* __restrict__ z, float* __restrict__ zs, uint64_t n, uint32_t width,
+                               uint32_t seed, uint32_t stride) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i < n) zs[i] = judge_sampled(i, width, seed, stride) ? z[i] : 1.0f;
+}
+
+// acc: frames, sampled, hits_ref, hits_test, mask_mismatch, within_tol, max |error| bits.
+__global__ void k_judge_sample(const float* __restrict__ zs, const float* __restrict__ dref,
+                               const float* __restrict__ dtest, uint64_t n, float tol,
+                               unsigned long long* __restrict__ acc) {
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    bool s = false, hr = false, ht = false, within = false;
+    float err = 0.0f;
+    if (i < n && zs[i] != 1.0f) {
+        s = true;
+        const float a = dref[i], b = dtest[i];
+        hr = a > 0.0f;
+        ht = b > 0.0f;
+        if (hr && ht) {
+            err = fabsf(b - a);
+            within = err <= tol;
+        }
+    }
+    const unsigned m_s = __ballot_sync(0xffffffffu, s), m_hr = __ballot_sync(0xffffffffu, hr);
+    const unsigned m_ht = __ballot_sync(0xffffffffu, ht), m_mis = __ballot_sync(0xffffffffu, hr != ht);
+    const unsigned m_in = __ballot_sync(0xffffffffu, within);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) err = fmaxf(err, __shfl_xor_sync(0xffffffffu, err, o));
+    if ((threadIdx.x & 31) == 0 && m_s) {
+        atomicAdd(acc + 1, (unsigned long long)__popc(m_s));
+        if (m_hr) atomicAdd(acc + 2, (unsigned long long)__popc(m_hr));
+        if (m_ht) atomicAdd(acc + 3, (unsigned long long)__popc(m_ht));
+        if (m_mis) atomicAdd(acc + 4, (unsigned long long)__popc(m_mis));
+        if (m_in) atomicAdd(acc + 5, (unsigned long long)__popc(m_in));
+        if (err > 0.0f) atomicMax(acc + 6, (unsigned long long)__float_as_uint(err));
+    }
+    if (i == 0) atomicAdd(acc + 0, 1ull);
+}
+
 // Host FP32 -> BF16, round to nearest even (NaN kept quiet).
 uint16_t to_bf16(float f) {
     uint32_t u;
@@ -966,6 +1020,36 @@ int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_marc
     return FM_OK;
 }
 
+int judge_learned(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const float* z,
+                  const float* learned_depth, cudaStream_t st) {
+    const uint64_t npx = (uint64_t)cam->width * cam->height;
+    const bool fresh = ctx->judge_acc.p == nullptr;
+    if (!grow_buf(ctx->judge_z, npx * 4) || !grow_buf(ctx->judge_ref, npx * 4) || !grow_buf(ctx->judge_acc, 64))
+        return set_err(ctx, FM_ERR_OOM, "judge buffer allocation failed");
+    unsigned long long* acc = (unsigned long long*)ctx->judge_acc.p;
+    if (fresh) FM_CUDA(ctx, cudaMemsetAsync(acc, 0, 64, st));
+    const uint32_t seed = (uint32_t)(ctx->judge_seq++ * 0x9E3779B9ull);
+    const unsigned blocks = (unsigned)((npx + 255) / 256);
+    float* zs = (float*)ctx->judge_z.p;
+    float* dref = (float*)ctx->judge_ref.p;
+    k_judge_starts<<<blocks, 256, 0, st>>>(z, zs, npx, (uint32_t)cam->width, seed, ctx->judge_stride);
+    FM_CUDA(ctx, cudaGetLastError());
+    // the plain march of the sample: same settings, its own start plane and hit distances
+    fm_march_params q = *p;
+    q.flags = FM_MARCH_EXTERNAL_DEPTH;
+    MarchOutDev o{};
+    o.start_depth = zs;
+    o.depth = dref;
+    const int stats = ctx->stats_enabled;
+    ctx->stats_enabled = 0;  // the counters describe the learned march
+    const int rc = launch_march(ctx, s, cam, &q, o, st);
+    ctx->stats_enabled = stats;
+    if (rc) return rc;
+    k_judge_sample<<<blocks, 256, 0, st>>>(zs, dref, learned_depth, npx, ctx->judge_tol, acc);
+    FM_CUDA(ctx, cudaGetLastError());
+    return FM_OK;
+}
+
 }  // namespace fm
 
 using namespace fm;
@@ -1107,6 +1191,38 @@ int fm_judge(fm_ctx* ctx, const float* depth_ref, const float* depth_test, uint6
     const unsigned int mb = (unsigned int)(h[4] & 0xffffffffu);
     std::memcpy(&r.max_err, &mb, 4);
     r.tol = tol;
+    *out = r;
+    return FM_OK;
+}
+
+int fm_set_judge(fm_ctx* ctx, uint32_t stride, float tol) {
+    if (!ctx) return FM_ERR_INVALID;
+    if (!(tol >= 0.0f) || !std::isfinite(tol)) return set_err(ctx, FM_ERR_INVALID, "tolerance must be finite and >= 0");
+    ctx->judge_stride = stride;
+    ctx->judge_tol = tol;
+    return FM_OK;
+}
+
+int fm_judge_frames(fm_ctx* ctx, fm_frame_judge* out, int reset) {
+    if (!ctx) return FM_ERR_INVALID;
+    if (!out) return set_err(ctx, FM_ERR_INVALID, "NULL argument");
+    cudaSetDevice(ctx->device);
+    fm_frame_judge r{};
+    r.tol = ctx->judge_tol;
+    if (ctx->judge_acc.p) {
+        unsigned long long h[7];
+        FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        FM_CUDA(ctx, cudaMemcpy(h, ctx->judge_acc.p, sizeof(h), cudaMemcpyDeviceToHost));
+        r.frames = h[0];
+        r.sampled = h[1];
+        r.hits_ref = h[2];
+        r.hits_test = h[3];
+        r.mask_mismatch = h[4];
+        r.within_tol = h[5];
+        const unsigned int mb = (unsigned int)(h[6] & 0xffffffffu);
+        std::memcpy(&r.max_err, &mb, 4);
+        if (reset) FM_CUDA(ctx, cudaMemset(ctx->judge_acc.p, 0, 64));
+    }
     *out = r;
     return FM_OK;
 }

@@ -42,7 +42,7 @@ EXPORTS = [
     "fm_set_tile_config", "fm_get_tile_config", "fm_batch_create", "fm_batch_run", "fm_batch_refresh",
     "fm_batch_autotune", "fm_batch_info_get", "fm_batch_destroy", "fm_march_batch",
     "fm_proposal_create", "fm_proposal_destroy", "fm_set_proposal", "fm_proposal_features", "fm_proposal_intervals",
-    "fm_judge", "fm_trainer_create", "fm_trainer_destroy", "fm_trainer_step", "fm_trainer_predict",
+    "fm_judge", "fm_set_judge", "fm_judge_frames", "fm_trainer_create", "fm_trainer_destroy", "fm_trainer_step", "fm_trainer_predict",
     "fm_trainer_params", "fm_density", "fm_set_anisotropy",
     "fm_trainer_get_state", "fm_trainer_set_state", "fm_selftest_wait_timeout", "fm_depth_blur", "fm_bgeo_read", "fm_gunzip", "fm_scene_create_bgeo", "fm_dataset_open", "fm_dataset_frames", "fm_dataset_path",
     "fm_dataset_frame_info", "fm_dataset_max_particles", "fm_dataset_read", "fm_dataset_scene",
@@ -106,6 +106,11 @@ class CMarchStats(C.Structure):
 
 class CJudge(C.Structure):
     _fields_ = [("pixels", C.c_uint64), ("hits_ref", C.c_uint64), ("hits_test", C.c_uint64),
+                ("mask_mismatch", C.c_uint64), ("within_tol", C.c_uint64), ("max_err", C.c_float), ("tol", C.c_float)]
+
+
+class CFrameJudge(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("sampled", C.c_uint64), ("hits_ref", C.c_uint64), ("hits_test", C.c_uint64),
                 ("mask_mismatch", C.c_uint64), ("within_tol", C.c_uint64), ("max_err", C.c_float), ("tol", C.c_float)]
 
 
@@ -188,6 +193,8 @@ def load(path: str = LIB_PATH) -> C.CDLL:
     L.fm_proposal_features.argtypes = [vp, vp, C.POINTER(CCamera), vp, vp, vp, vp]
     L.fm_proposal_intervals.argtypes = [vp, vp, C.POINTER(CCamera), C.POINTER(CMarchParams), vp, vp, vp, vp]
     L.fm_judge.argtypes = [vp, vp, vp, C.c_uint64, C.c_float, C.POINTER(CJudge), vp]
+    L.fm_set_judge.argtypes = [vp, C.c_uint32, C.c_float]
+    L.fm_judge_frames.argtypes = [vp, C.POINTER(CFrameJudge), C.c_int]
     L.fm_trainer_create.argtypes = [vp, C.c_uint64, vp, C.POINTER(vp)]
     L.fm_trainer_destroy.argtypes = [vp]
     L.fm_trainer_destroy.restype = None
@@ -288,6 +295,18 @@ class Context:
         c = CTileConfig(int(tile_width), int(tiles_per_claim), int(defer_iters), int(long_queue), int(defer_lanes),
                         int(regroup_iters))
         self.check(self.L.fm_set_tile_config(self.h, C.byref(c)))
+
+    def set_judge(self, stride: int, tol: float):
+        """Judge every learned march: the plain march of a 1-in-`stride` pixel sample, compared on the
+        device (hit masks, hit distances within `tol`); stride 0 turns it off."""
+        self.check(self.L.fm_set_judge(self.h, int(stride), float(tol)))
+
+    def judge_frames(self, reset: bool = False) -> dict:
+        """What the per-frame judge accumulated since the last reset."""
+        r = CFrameJudge()
+        self.check(self.L.fm_judge_frames(self.h, C.byref(r), 1 if reset else 0))
+        return {k: (float(getattr(r, k)) if k in ("max_err", "tol") else int(getattr(r, k))) for k, _ in
+                CFrameJudge._fields_}
 
     def host_array(self, shape, dtype=np.float32) -> np.ndarray:
         """A numpy array in page-locked host memory of this context (fm_host_alloc).

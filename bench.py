@@ -23,8 +23,11 @@ e2e    the same frame through the C ABI with pinned HOST buffers: particle
        RayMarcher.cpp:67 does) on a bounded random pixel sample per step.
 learned  the same frame with the learned hit-interval proposal
        (FM_MARCH_PROPOSAL, weights fluidmarch/proposal_sloshing.npz), timed the
-       same way, and its depth error judged against the plain march of the
-       same frame (hit masks, |depth difference| <= 1e-4 x scene extent).
+       same way; every timed frame includes the per-frame judge (fm_set_judge:
+       the plain march of a 1-in-64 sample of 8x4 pixel blocks compared on the
+       device), and
+       the last frame is also judged whole against the plain march of the same
+       frame (hit masks, |depth difference| <= 1e-4 x scene extent).
 batch  64 scenes of the sloshing family (50k..2M particles, 1-4 views each
        at 640x480 / 1280x720 / 1920x1080) in one graph launch per frame.
 anisotropic  the same frame with the reference's default marcher
@@ -340,14 +343,21 @@ def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, pla
         fm.splat_depth(scene, cam, lo["start_depth"])
         fm.march(scene, cam, P_l, lo["position"], lo["normal"], lo["depth"], lo["colour"], lo["start_depth"])
 
+    extent = float((sc.xyz.max(0) - sc.xyz.min(0)).max())
+    tol = 1e-4 * extent
     ctx.set_stats(True)
     frame()
     ctx.sync()
     st = ctx.stats()
     ctx.set_stats(False)
+    # every timed learned frame is judged: the plain march of a 1-in-64 sample of 8x4 pixel blocks
+    # (a different one each frame), compared on the device
+    judge_stride = 64
+    ctx.set_judge(judge_stride, tol)
     for _ in range(args.warmup):
         frame()
     ctx.sync()
+    ctx.judge_frames(reset=True)
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     with torch.cuda.stream(ext):
         for e0, e1 in ev:
@@ -357,8 +367,8 @@ def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, pla
             e1.record(ext)
         ext.synchronize()
     ms = sum(a.elapsed_time(b) for a, b in ev) / args.steps
-    extent = float((sc.xyz.max(0) - sc.xyz.min(0)).max())
-    tol = 1e-4 * extent
+    jf = ctx.judge_frames(reset=True)
+    ctx.set_judge(0, 0.0)
     j = fm.judge(ctx, out["depth"], lo["depth"], tol)
     # the plain march without empty-space skipping (the reference's loop) and with
     # the reference's own skip flags, for comparison (a few frames each)
@@ -387,6 +397,10 @@ def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, pla
             "plain_skip_off_ms_per_frame": float(np.mean(off)), "vs_plain_skip_off": float(np.mean(off)) / ms,
             "plain_reference_skip_ms_per_frame": ref_skip, "vs_plain_reference_skip": ref_skip / ms,
             "depth_tol": tol, "judge": j, "hits_within_tol": j["within_tol"] / max(1, j["hits_ref"]),
+            "per_frame_judge": dict(jf, stride=judge_stride,
+                                    hits_within_tol=jf["within_tol"] / max(1, jf["hits_ref"]),
+                                    note="inside every timed learned frame: plain march of a 1-in-stride sample of "
+                                         "8x4 pixel blocks, compared with the learned march on the device"),
             "mask_identical": j["mask_mismatch"] == 0,
             "margins_support_radii": [margin_lo, margin_hi], "min_near_support_radii": min_near,
             "counters": {k: st[k] for k in ("evals", "proposed", "fallbacks", "deferred")},

@@ -412,6 +412,31 @@ typedef struct fm_judge_result {
 int fm_judge(fm_ctx* ctx, const float* depth_ref, const float* depth_test, uint64_t n, float tol,
              fm_judge_result* out, void* stream);
 
+/* Per-frame judge of the learned march.  No counterpart in the reference (the
+ * learned proposal is an addition).  With stride > 0, every FM_MARCH_PROPOSAL
+ * march of this context also marches the started rays of a pixel sample
+ * (about 1 in `stride` 8x4 pixel blocks, drawn by a hash of the block index
+ * and a frame counter, so every frame judges other pixels) with the plain march -- same
+ * iso, step, steps, bisection and skip mode -- right after the learned march on
+ * the same stream, and compares their hit distances with the learned march's
+ * on the device: hit-mask mismatches, hits within `tol` (world units) and the
+ * largest difference accumulate until fm_judge_frames reads them.  The cost is
+ * part of the learned march.  stride 0 turns the judge off. */
+int fm_set_judge(fm_ctx* ctx, uint32_t stride, float tol);
+typedef struct fm_frame_judge {
+    uint64_t frames;         /* learned marches judged since the last reset */
+    uint64_t sampled;        /* started rays in the samples */
+    uint64_t hits_ref;       /* of those, hits of the plain march */
+    uint64_t hits_test;      /* hits of the learned march */
+    uint64_t mask_mismatch;  /* hit in one march and missed in the other */
+    uint64_t within_tol;     /* hit in both with |depth difference| <= tol */
+    float max_err;           /* largest |depth difference| over rays hit in both */
+    float tol;
+} fm_frame_judge;
+/* What the per-frame judge accumulated (waits for the context's work);
+ * reset != 0 clears it afterwards. */
+int fm_judge_frames(fm_ctx* ctx, fm_frame_judge* out, int reset);
+
 /* Training of the proposal: FP32 forward, backward and Adam kernels.  Loss:
  * pinball (quantile) loss of near at quantile tau_lo and of far at tau_hi
  * against the first-hit distance (support radii past the ray start). */

@@ -335,3 +335,64 @@ def test_judge(fmlib, ctx):
     assert r["mask_mismatch"] == 277
     assert r["within_tol"] == int((both & (err <= np.float32(1e-4))).sum())
     assert r["max_err"] == pytest.approx(float(err[both].max()), rel=1e-6)
+
+
+def _judge_sample(width, height, seq, stride):
+    """The per-frame judge's sample of frame `seq`: pixels of the 8x4 blocks whose index, hashed with
+    lowbias32 after an xor with the frame's seed, is 0 modulo the stride."""
+    py, px = np.divmod(np.arange(width * height, dtype=np.uint64), np.uint64(width))
+    blk = (py >> np.uint64(2)) * np.uint64((width + 7) // 8) + (px >> np.uint64(3))
+    x = ((blk ^ np.uint64((seq * 0x9E3779B9) & 0xFFFFFFFF)) & np.uint64(0xFFFFFFFF)).astype(np.uint32)
+    with np.errstate(over="ignore"):
+        x ^= x >> np.uint32(16)
+        x *= np.uint32(0x7FEB352D)
+        x ^= x >> np.uint32(15)
+        x *= np.uint32(0x846CA68B)
+        x ^= x >> np.uint32(16)
+    return x % np.uint32(stride) == 0
+
+
+def test_per_frame_judge(fmlib, scene_setup):
+    """fm_set_judge: every learned march also marches a changing sample of 8x4 pixel blocks plainly and compares the
+    hit distances on the device; the accumulated counts equal a host count over the same samples."""
+    sc, cam, _, _ = scene_setup
+    ctx = fmlib.Context(0)
+    s = fmlib.Scene(ctx, sc.xyz, sc.support)
+    prop = fmlib.Proposal(ctx, random_params(12, bias_scale=1.0))
+    fmlib.set_proposal(ctx, prop)
+    stride, frames = 4, 3
+    tol = 1e-4 * float(np.max(sc.xyz.max(0) - sc.xyz.min(0)))
+    ctx.set_judge(stride, tol)
+    plain = fmlib.render(s, cam, fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, 8, 1))
+    p = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, 8, 1, proposal=True)
+    outs = [fmlib.render(s, cam, p) for _ in range(frames)]
+    j = ctx.judge_frames(reset=True)
+    npx = cam.width * cam.height
+    ref = plain["depth"]
+    started = plain["start_depth"] < 1
+    want = dict(frames=frames, sampled=0, hits_ref=0, hits_test=0, mask_mismatch=0, within_tol=0)
+    max_err = 0.0
+    for k, o in enumerate(outs):
+        m = _judge_sample(cam.width, cam.height, k, stride) & started
+        hr, ht = ref[m] > 0, o["depth"][m] > 0
+        both = hr & ht
+        err = np.abs(o["depth"][m][both] - ref[m][both])
+        want["sampled"] += int(m.sum())
+        want["hits_ref"] += int(hr.sum())
+        want["hits_test"] += int(ht.sum())
+        want["mask_mismatch"] += int((hr != ht).sum())
+        want["within_tol"] += int((err <= np.float32(tol)).sum())
+        max_err = max(max_err, float(err.max()) if err.size else 0.0)
+    assert {k: j[k] for k in want} == want
+    assert j["max_err"] == pytest.approx(max_err, abs=0.0)
+    assert want["sampled"] > 3 * 0.1 * started.sum() and want["hits_ref"] > 100
+    assert ctx.judge_frames()["frames"] == 0  # reset
+    ctx.set_judge(0, 0.0)
+    fmlib.render(s, cam, p)
+    assert ctx.judge_frames()["frames"] == 0  # off
+    with pytest.raises(fmlib.FmError):
+        ctx.set_judge(4, float("nan"))
+    fmlib.set_proposal(ctx, None)
+    prop.close()
+    s.close()
+    ctx.close()
