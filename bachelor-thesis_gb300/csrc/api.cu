@@ -145,6 +145,7 @@ static void scene_free(fm_scene* s) {
     cudaFree(s->d_perm);
     cudaFree(s->d_sub);
     cudaFree(s->d_bound);
+    cudaFree(s->coarse.p);
     cudaFree(s->d_flag);
     cudaFree(s->d_occ);
     delete s;
@@ -496,6 +497,7 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     const bool overlap = p->skip_mode == FM_SKIP_EXACT && !external && bound_stale(sm, p->iso_density);
     if (p->skip_mode == FM_SKIP_EXACT && !overlap && (rc = ensure_bound(ctx, sm, st, p->iso_density)) != FM_OK)
         return rc;
+
     if (p->skip_mode == FM_SKIP_REFERENCE && (rc = ensure_flags(ctx, sm, st)) != FM_OK) return rc;
     MarchOutDev o{};
     const bool host = mem == FM_MEM_HOST;
@@ -529,6 +531,12 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     }
     o.start_depth = z;
     o.ivl = nullptr;
+    if (p->skip_mode == FM_SKIP_EXACT) {
+        // the table is built (on st, or on the side stream joined into st): one
+        // read a second time gets its shell boxes refined first
+        if (sm->bound_uses > 0 && (rc = refine_bound(ctx, sm, st)) != FM_OK) return rc;
+        sm->bound_uses++;
+    }
     if (p->flags & FM_MARCH_PROPOSAL) {
         if (p->skip_mode == FM_SKIP_REFERENCE)
             return set_err(ctx, FM_ERR_INVALID, "FM_MARCH_PROPOSAL marches the plain sample lattice: skip mode must be off or exact");

@@ -19,7 +19,8 @@
 namespace fm {
 
 constexpr int kWarp = 32;
-constexpr int kBoundBoxes = 64;         // exact-skip bound boxes per cell (4 x 4 x 4)
+constexpr int kBoundDiv = 8;            // exact-skip bound boxes per cell and axis
+constexpr int kBoundBoxes = kBoundDiv * kBoundDiv * kBoundDiv;
 constexpr int kProposalOcc = 64;        // occupancy grid resolution of the proposal
 constexpr int kProposalFeatures = FM_PROPOSAL_FEATURES;
 constexpr int kProposalParams = FM_PROPOSAL_PARAMS;
@@ -268,7 +269,10 @@ struct fm_scene {
     uint32_t* d_cell = nullptr;    // cell of each input particle
     uint32_t* d_perm = nullptr;    // input index of each sorted particle
     uint32_t* d_sub = nullptr;     // 8 * ncells + 1 sub-cell starts
-    float* d_bound = nullptr;      // exact-skip bound table, 4x4x4 boxes per cell (lazy)
+    float* d_bound = nullptr;      // exact-skip bound table, 8x8x8 boxes per cell (lazy)
+    fm::DevBuf coarse;             // its 4x4x4 first level (64 bounds per cell)
+    bool bound_fine = false;       // the shell boxes are refined (a second march of the same build)
+    uint32_t bound_uses = 0;       // marches that read the table since it was built
     uint8_t* d_flag = nullptr;     // per-cell reference flag (lazy)
     bool bound_valid = false;      // built by the first exact-skip march after a build
     float bound_iso = 0.0f;        // the bound table holds +inf for boxes whose sum reached it
@@ -285,6 +289,8 @@ int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride);
 // Lazily built skip tables, launched on `st` (valid for every later launch
 // on that stream; other streams must order after it).
 int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st, float iso);
+// Refine the shell boxes of a built table (once per build; a no-op otherwise).
+int refine_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
 bool bound_stale(const fm_scene* s, float iso);
 int ensure_flags(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
 GridDev grid_dev(const fm_scene* s);

@@ -403,7 +403,7 @@ __global__ void k_gather(const float* __restrict__ xyz, uint64_t n, uint32_t str
     out[k] = make_float4(p[0], p[1], p[2], 0.0f);
 }
 
-// Exact-skip bound table: 4x4x4 boxes per cell.
+// Exact-skip bound table, first level: 4x4x4 boxes per cell.
 // Upper bound of the density any sample inside a bound box can reach.  Every
 // cell is divided into 4x4x4 bound boxes (a quarter cell per axis); a box's
 // bound is the sum over the particles of the cell's 27-neighbourhood (the
@@ -428,7 +428,8 @@ __global__ void k_gather(const float* __restrict__ xyz, uint64_t n, uint32_t str
 constexpr int kBoundWarps = 8;
 
 __global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, KernelDev k, float slack, float thr,
-                                                                     float* __restrict__ bound) {
+                                                                     float* __restrict__ bound,
+                                                                     float* __restrict__ fine) {
     __shared__ float4 s_pts[kBoundWarps][kWarp];
     const uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
     const uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
@@ -494,8 +495,116 @@ __global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_bound4(GridDev g, 
     for (int h = 0; h < 2; ++h) {
         const float a = h ? acc1 : acc0;
         const float up = a * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
-        bound[(uint64_t)kBoundBoxes * c + l + 32 * h] =
-            reached ? __int_as_float(0x7f800000) : ((cnt == 0 || a == 0.0f) ? 0.0f : up);
+        const float v = reached ? __int_as_float(0x7f800000) : ((cnt == 0 || a == 0.0f) ? 0.0f : up);
+        bound[64 * c + l + 32 * h] = v;
+        // the 8x8x8 table: each of the box's eight eighths starts with its bound
+        const int cbx = l + 32 * h, cx = cbx & 3, cy = (cbx >> 2) & 3, cz = cbx >> 4;
+        float* fb = fine + (uint64_t)kBoundBoxes * c;
+#pragma unroll
+        for (int f = 0; f < 8; ++f) fb[(2 * cx + (f & 1)) + 8 * (2 * cy + ((f >> 1) & 1)) + 64 * (2 * cz + (f >> 2))] = v;
+    }
+}
+
+// Refinement of the bound table (8x8x8 boxes per cell, an eighth of a cell per
+// axis) from its 4x4x4 first level `coarse`: k_cell_bound4 gave every eighth
+// its box's bound, which stays where that is below `thr` (skipped either way),
+// +inf (the cell reached thr) or 0 (no particle within reach); the eighths of
+// "shell" boxes (thr <= bound < +inf: near the iso surface, where most
+// evaluated samples lie) get their own sums, with the same slack and margin.
+// One warp per cell: the fine boxes to sum are taken 32 at a time, one per
+// lane, and each round streams the cell's 27-neighbourhood through shared
+// memory as k_cell_bound4 does; a round stops once all its boxes reached thr.
+// Fine box b = ix + 8 iy + 64 iz; coarse box (ix, iy, iz) / 2.
+__global__ void __launch_bounds__(kWarp * kBoundWarps) k_cell_refine8(GridDev g, KernelDev k, float slack, float thr,
+                                                                      const float* __restrict__ coarse,
+                                                                      float* __restrict__ bound) {
+    __shared__ float4 s_pts[kBoundWarps][kWarp];
+    const uint64_t ncells = (uint64_t)g.dims[0] * g.dims[1] * g.dims[2];
+    const uint64_t c = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
+    const int l = threadIdx.x % kWarp;
+    if (c >= ncells) return;  // warp-uniform
+    float4* sp = s_pts[threadIdx.x / kWarp];
+    const float* cb = coarse + 64 * c;
+    float* fb = bound + (uint64_t)kBoundBoxes * c;
+    // coarse boxes l and l + 32: shell or not (the others' eighths already hold their bound)
+    uint64_t shell = 0;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float v = cb[l + 32 * h];
+        const bool sh = v >= thr && v < __int_as_float(0x7f800000);
+        shell |= (uint64_t)__ballot_sync(0xffffffffu, sh) << (32 * h);
+    }
+    if (!shell) return;
+    const int cc[3] = {(int)(c % (uint64_t)g.dims[0]), (int)((c / (uint64_t)g.dims[0]) % (uint64_t)g.dims[1]),
+                       (int)(c / ((uint64_t)g.dims[0] * g.dims[1]))};
+    const int x0 = max(cc[0] - 1, 0), x1 = min(cc[0] + 1, g.dims[0] - 1);
+    constexpr uint64_t kRowOrder = 0xa82091645ull;  // centre row first, then face neighbours, then diagonals
+    uint32_t cnt = 0;  // candidates of the 27-neighbourhood (for the margin)
+    for (int r = 0; r < 9; ++r) {
+        const int code = (int)((kRowOrder >> (4 * r)) & 15u);
+        const int y = cc[1] + (code & 3) - 1, z = cc[2] + (code >> 2) - 1;
+        if (y < 0 || y >= g.dims[1] || z < 0 || z >= g.dims[2]) continue;
+        const uint64_t row = ((uint64_t)z * g.dims[1] + y) * g.dims[0];
+        cnt += g.sub[8 * (row + x1) + 8] - g.sub[8 * (row + x0)];
+    }
+    const int nfine = 8 * __popcll(shell);
+    for (int f0 = 0; f0 < nfine; f0 += kWarp) {
+        // this lane's fine box: the (f0 + l)-th of the shell boxes' fine boxes
+        const int f = f0 + l;
+        const bool live = f < nfine;
+        int fbx = 0;
+        if (live) {
+            uint64_t m = shell;
+            for (int i = 0; i < (f >> 3); ++i) m &= m - 1;  // drop the lowest (f / 8) shell boxes
+            const int cbx = __ffsll((long long)m) - 1;
+            const int cx = cbx & 3, cy = (cbx >> 2) & 3, cz = cbx >> 4, sub = f & 7;
+            fbx = (2 * cx + (sub & 1)) + 8 * (2 * cy + ((sub >> 1) & 1)) + 64 * (2 * cz + (sub >> 2));
+        }
+        const int ib[3] = {fbx & 7, (fbx >> 3) & 7, fbx >> 6};
+        float lo[3], hi[3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            lo[a] = g.min[a] + ((float)cc[a] + 0.125f * (float)ib[a]) * g.cell - slack;
+            hi[a] = g.min[a] + ((float)cc[a] + 0.125f * (float)(ib[a] + 1)) * g.cell + slack;
+        }
+        float acc = 0.0f;
+        bool reached = false;
+        for (int r = 0; r < 9 && !reached; ++r) {
+            const int code = (int)((kRowOrder >> (4 * r)) & 15u);
+            const int y = cc[1] + (code & 3) - 1, z = cc[2] + (code >> 2) - 1;
+            if (y < 0 || y >= g.dims[1] || z < 0 || z >= g.dims[2]) continue;
+            const uint64_t row = ((uint64_t)z * g.dims[1] + y) * g.dims[0];
+            const uint32_t b = g.sub[8 * (row + x0)], e = g.sub[8 * (row + x1) + 8];
+            for (uint32_t j0 = b; j0 < e; j0 += kWarp) {
+                const uint32_t j = j0 + (uint32_t)l;
+                const float4 mine = j < e ? g.pts[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const int m = (int)min(e - j0, (uint32_t)kWarp);
+                __syncwarp();
+                sp[l] = mine;
+                __syncwarp();
+                for (int t = 0; t < m; ++t) {
+                    const float4 qv = sp[t];
+                    const float q[3] = {qv.x, qv.y, qv.z};
+                    float d2 = 0.0f;
+#pragma unroll
+                    for (int a = 0; a < 3; ++a) {
+                        const float d = fmaxf(fmaxf(lo[a] - q[a], q[a] - hi[a]), 0.0f);
+                        d2 += d * d;
+                    }
+                    if (d2 < k.h2) acc += w_in(k, d2);
+                }
+                if (__all_sync(0xffffffffu, !live || acc >= thr)) {
+                    reached = true;
+                    break;
+                }
+            }
+        }
+        if (live) {
+            const float eps = 5.9604645e-8f;  // 2^-24
+            const float n = (float)cnt;
+            const float up = acc * (1.0f + 16.0f * eps) * (1.0f + 4.0f * n * eps) + 32.0f * n * eps * k.sig;
+            fb[fbx] = reached ? __int_as_float(0x7f800000) : (acc == 0.0f ? 0.0f : up);
+        }
     }
 }
 
@@ -664,19 +773,42 @@ static float bound_thr(float iso) { return (iso > 0.0f && std::isfinite(iso)) ? 
 
 bool bound_stale(const fm_scene* s, float iso) { return !(s->bound_valid && bound_thr(iso) <= s->bound_iso); }
 
+static float bound_slack(const fm_scene* s) {
+    float amax = 0.0f;
+    for (int a = 0; a < 3; ++a) amax = std::max(amax, std::max(std::fabs(s->min[a]), std::fabs(s->max[a])));
+    return 1.0e-4f * s->support + 1.0e-6f * amax;
+}
+
 int ensure_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st, float iso) {
     const float thr = bound_thr(iso);
     if (!bound_stale(s, iso)) return FM_OK;
+    if (!ensure_buf(s->coarse, s->ncells * 64 * sizeof(float)))
+        return set_err(ctx, FM_ERR_OOM, "bound table allocation failed");
     GridDev g = grid_dev(s);
     KernelDev k = make_kernel(s->support);
-    float amax = 0.0f;
-    for (int a = 0; a < 3; ++a) amax = std::max(amax, std::max(std::fabs(s->min[a]), std::fabs(s->max[a])));
-    float slack = 1.0e-4f * s->support + 1.0e-6f * amax;
     const uint64_t blocks = (s->ncells + kBoundWarps - 1) / kBoundWarps;
-    k_cell_bound4<<<(unsigned)blocks, kWarp * kBoundWarps, 0, st>>>(g, k, slack, thr, s->d_bound);
+    k_cell_bound4<<<(unsigned)blocks, kWarp * kBoundWarps, 0, st>>>(g, k, bound_slack(s), thr, (float*)s->coarse.p,
+                                                                    s->d_bound);
     FM_CUDA(ctx, cudaGetLastError());
     s->bound_valid = true;
     s->bound_iso = thr;
+    s->bound_fine = false;
+    s->bound_uses = 0;
+    return FM_OK;
+}
+
+// The refinement costs a few times the first level's build and pays back in
+// the marches that follow, so it is made when a table is used a second time
+// (a scene marched again without a rebuild) or by a batch.
+int refine_bound(fm_ctx* ctx, fm_scene* s, cudaStream_t st) {
+    if (!s->bound_valid || s->bound_fine) return FM_OK;
+    GridDev g = grid_dev(s);
+    KernelDev k = make_kernel(s->support);
+    const uint64_t blocks = (s->ncells + kBoundWarps - 1) / kBoundWarps;
+    k_cell_refine8<<<(unsigned)blocks, kWarp * kBoundWarps, 0, st>>>(g, k, bound_slack(s), s->bound_iso,
+                                                                     (const float*)s->coarse.p, s->d_bound);
+    FM_CUDA(ctx, cudaGetLastError());
+    s->bound_fine = true;
     return FM_OK;
 }
 

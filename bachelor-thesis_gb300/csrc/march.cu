@@ -9,9 +9,9 @@
 //                  p; hit at the first sample with rho >= iso      (:276-343)
 //   skip           FM_SKIP_REFERENCE: the reference's flag/jump loop
 //                  (:281-306, intersectAABB :51-62);  FM_SKIP_EXACT: samples in
-//                  bound boxes (a quarter cell per axis) whose density upper
-//                  bound is below iso are stepped over without evaluating, so
-//                  results equal skip-off exactly
+//                  bound boxes (an eighth of a cell per axis) whose density
+//                  upper bound is below iso are stepped over without
+//                  evaluating, so results equal skip-off exactly
 //   refinement     bisection between the last outside and first inside sample
 //   normal         normalize(sum_j gradW(x_j - p_hit)) (:332-338, Kernel.cpp:34-52)
 //   shading        composition.frag:132-184 fused into the epilogue
@@ -90,7 +90,7 @@ __device__ __forceinline__ bool locate(const GridDev& g, float px, float py, flo
     return true;
 }
 
-// Exact-skip bound of the bound box that holds a located sample (1/4 cell per
+// Exact-skip bound of the bound box that holds a located sample (1/8 cell per
 // axis; u < 1 inside the grid, clamped all the same): no sample in
 // the box reaches a density above it, and 0 means no particle lies within the
 // support radius of the box.  +inf for a cell outside the grid.
@@ -99,9 +99,9 @@ __device__ __forceinline__ float box_bound(const GridDev& g, const Loc& L) {
         return __int_as_float(0x7f800000);
     const uint32_t c = (uint32_t)L.c[0] + (uint32_t)L.c[1] * (uint32_t)g.dims[0] +
                        (uint32_t)L.c[2] * (uint32_t)g.dims[0] * (uint32_t)g.dims[1];
-    const uint32_t bx = min((uint32_t)(4.0f * L.u[0]), 3u), by = min((uint32_t)(4.0f * L.u[1]), 3u),
-                   bz = min((uint32_t)(4.0f * L.u[2]), 3u);
-    return __ldg(g.bound + (uint64_t)kBoundBoxes * c + (bx | (by << 2) | (bz << 4)));
+    const uint32_t bx = min((uint32_t)(8.0f * L.u[0]), 7u), by = min((uint32_t)(8.0f * L.u[1]), 7u),
+                   bz = min((uint32_t)(8.0f * L.u[2]), 7u);
+    return __ldg(g.bound + (uint64_t)kBoundBoxes * c + (bx | (by << 3) | (bz << 6)));
 }
 
 // Squared distance (cell units) from fraction u to the half-cell slab [lo, lo + 0.5].

@@ -186,11 +186,11 @@ def march_roofline(st, g, npx, march_ms, peak, peak_kind):
 
     HBM: the bytes the march has to move between HBM and the SMs once per frame -- the cell-sorted
     particles (16 B each), the sub-cell start table (4 B x (8 n_cells + 1)), the exact-skip bound table
-    (4 B x 64 n_cells), the start depths (4 B per pixel) and the four output planes (position, normal,
+    (4 B x 512 n_cells), the start depths (4 B per pixel) and the four output planes (position, normal,
     colour 16 B, hit distance 4 B per pixel) -- over the stage's time.  The candidate stream the
     reference's loop implies (16 B for every particle in the 27 cells of every density evaluation,
     RayMarcher.cpp:308-325) is served from L1/L2 and reported beside it, not as an HBM figure."""
-    hbm_bytes = 16 * g["n_particles"] + 4 * (8 * g["n_cells"] + 1) + 4 * 64 * g["n_cells"] + (4 + 52) * npx
+    hbm_bytes = 16 * g["n_particles"] + 4 * (8 * g["n_cells"] + 1) + 4 * 512 * g["n_cells"] + (4 + 52) * npx
     t = march_ms / 1000.0
     achieved = hbm_bytes / t / 1e9
     prof = profiled_march()

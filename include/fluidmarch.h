@@ -57,11 +57,12 @@ extern "C" {
 
 /* skip modes (march parameter) */
 #define FM_SKIP_OFF 0        /* evaluate the density at every sample (reference parity gate) */
-#define FM_SKIP_EXACT 1      /* skip samples whose bound box (a quarter cell per axis) has a
-                                density upper bound below iso; same samples, same results
-                                as FM_SKIP_OFF.  The scene's bound table is built by its
-                                first such march and serves marches at that iso or a lower
-                                one; a march at a higher iso builds it again. */
+#define FM_SKIP_EXACT 1      /* skip samples whose bound box (an eighth of a cell per axis) has
+                                a density upper bound below iso; same results as FM_SKIP_OFF.
+                                The scene's bound table is built by its first such march
+                                (boxes of a quarter cell), refined where it lies near the iso
+                                surface by the second, and serves marches at that iso or a
+                                lower one; a march at a higher iso builds it again. */
 #define FM_SKIP_REFERENCE 2  /* the reference's skip: flag = own-cell count * W0 > 1, jump to the
                                 cell's exit plus one step (RayMarcher.cpp:281-306) */
 

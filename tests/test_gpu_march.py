@@ -322,54 +322,66 @@ def test_density_probe_bitwise(fmlib, ctx):
 
 
 def test_bound_table_on_reuse(fmlib, ctx):
-    """The scene's first exact-skip march builds the bound table, the next reuses it: the same samples
-    skipped, the oracle's bits both times."""
+    """The scene's first exact-skip march builds the bound table's 4x4x4 level, the second refines its
+    shell boxes into eighths and skips more samples, the third reuses the refined table: the oracle's
+    bits every time."""
     sc = scenes.small_scene(seed=23, n=20000, width=128, height=96)
     cam = sc.cameras[0]
     s = fmlib.Scene(ctx, sc.xyz, sc.support)
     p = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_EXACT)
     ctx.set_stats(True)
     try:
-        first = fmlib.render(s, cam, p)
-        st1 = ctx.stats()
-        second = fmlib.render(s, cam, p)
-        st2 = ctx.stats()
+        runs = []
+        for _ in range(3):
+            runs.append((fmlib.render(s, cam, p), ctx.stats()))
     finally:
         ctx.set_stats(False)
     fr = O.build_frame(sc.xyz, sc.support)
     o = O.march(fr, cam, sc.iso, sc.step, sc.max_steps, 8, O.splat(sc.xyz, sc.support, cam))
-    for g in (first, second):
+    for g, _ in runs:
         for k in ("position", "normal", "depth", "colour"):
             assert np.array_equal(bits(g[k]), bits(o[k])), k
-    assert st1["skipped"] > 0 and (st2["skipped"], st2["evals"]) == (st1["skipped"], st1["evals"])
+    (_, st1), (_, st2), (_, st3) = runs
+    assert st1["skipped"] > 0
+    assert st2["skipped"] > st1["skipped"] and st2["evals"] < st1["evals"]
+    assert (st3["skipped"], st3["evals"]) == (st2["skipped"], st2["evals"])
     s.close()
 
 
 def test_bound_table_follows_iso(fmlib, ctx):
     """The bound table stops summing a cell once every box reached the iso density of the march that
-    built it (+inf there): marches at that iso or a lower one reuse it, a march at a higher iso builds
-    it again.  Every march equals the march without skipping bit for bit, and a march skips the same
-    samples whether the table was built at its own iso or at a higher one."""
+    built it (+inf there), and refines the boxes whose bound lies between that iso and +inf: marches at
+    that iso or a lower one reuse it, a march at a higher iso builds it again.  Every march equals the
+    march without skipping bit for bit; a march at the table's own iso skips at least as many samples
+    as one at that iso reading a table built for a higher iso."""
     sc = scenes.small_scene(seed=29, n=20000, width=128, height=96)
     cam = sc.cameras[0]
-    s = fmlib.Scene(ctx, sc.xyz, sc.support)
     ctx.set_stats(True)
-    seen = {}
+    own = {}
     try:
-        # tables: built at iso, reused (iso, iso / 2), built at 2 iso, reused (iso), built at 3 iso,
-        # reused (iso / 2, 2 iso)
-        for iso in (sc.iso, sc.iso, 0.5 * sc.iso, 2.0 * sc.iso, sc.iso, 3.0 * sc.iso, 0.5 * sc.iso, 2.0 * sc.iso):
+        for iso in (sc.iso, 0.5 * sc.iso, 2.0 * sc.iso):
+            s = fmlib.Scene(ctx, sc.xyz, sc.support)
+            p = fmlib.MarchParams(iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_EXACT)
+            for _ in range(2):  # built at this iso, then refined
+                fmlib.render(s, cam, p)
+            own[iso] = ctx.stats()["skipped"]
+            s.close()
+        s = fmlib.Scene(ctx, sc.xyz, sc.support)
+        # tables: built at iso and refined, reused (iso / 2), built at 2 iso and refined, reused (iso),
+        # built at 3 iso, reused (iso / 2, 2 iso)
+        for iso in (sc.iso, sc.iso, 0.5 * sc.iso, 2.0 * sc.iso, 2.0 * sc.iso, sc.iso, 3.0 * sc.iso, 0.5 * sc.iso,
+                    2.0 * sc.iso):
             ref = fmlib.render(s, cam, fmlib.MarchParams(iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_OFF))
             got = fmlib.render(s, cam, fmlib.MarchParams(iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_EXACT))
             st = ctx.stats()
             for k in ("position", "normal", "depth", "colour"):
                 assert np.array_equal(bits(got[k]), bits(ref[k])), (iso, k)
-            key = (st["skipped"], st["evals"])
-            assert seen.setdefault(iso, key) == key, iso
-        assert seen[sc.iso][0] > 0
+            if iso in own:
+                assert st["skipped"] <= own[iso], iso
+        assert own[sc.iso] > 0
+        s.close()
     finally:
         ctx.set_stats(False)
-    s.close()
 
 
 def test_outputs_in_library_pinned_memory(fmlib, ctx):
