@@ -110,11 +110,17 @@ __device__ __forceinline__ float slab_d2(float u, float lo) {
     return d * d;
 }
 
-// Walk, in canonical order, the sorted ranges of the sub-cells within reach of
-// the sample at L.  Warp-uniform: every lane gets the same (b, e) sequence.
-// Lane l < 24 tests sub-cell (l & 7) of cell cx - 1 + (l >> 3) in each row.
+// Walk, in canonical order, the particles of the sub-cells within reach of the
+// sample at L (warp-uniform: every lane sees the same sequence), packed: per
+// row, the reachable sub-cells' particles
+// are numbered consecutively (sub-cell order, then sorted order) and handed
+// out 32 at a time, lane l taking number v0 + l; f(q, ok) gets the lane's
+// particle (ok false past the row's end).  The particles of the next 32 are
+// loaded before f runs on the current ones.  Lane l < 24 owns sub-cell l of
+// the row (cell cx - 1 + (l >> 3), sub-cell l & 7) and its range; a number's
+// owner is found by a binary search over the lanes' running counts.
 template <bool STATS, typename F>
-__device__ __forceinline__ void for_ranges_warp(const GridDev& g, const Loc& L, float T, int lane, Acc& acc, bool cnt,
+__device__ __forceinline__ void for_packed_warp(const GridDev& g, const Loc& L, float T, int lane, Acc& acc, bool cnt,
                                                 F&& f) {
     const int W = g.dims[0], Hd = g.dims[1], D = g.dims[2];
     const int ci = lane >> 3, sb = lane & 7;
@@ -131,27 +137,55 @@ __device__ __forceinline__ void for_ranges_warp(const GridDev& g, const Loc& L, 
             const int y = L.c[1] - 1 + dy;
             if (y < 0 || y >= Hd) continue;
             const float dy2 = slab_d2(L.u[1], -1.0f + 0.5f * (float)(2 * dy + ((sb >> 1) & 1)));
-            uint32_t m = __ballot_sync(kFull, lane_ok && (dx2 + dy2 + dz2 < T));
+            const bool reach = lane_ok && (dx2 + dy2 + dz2 < T);
+            if (!__any_sync(kFull, reach)) continue;
             const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
-            // base wraps below 0 when row + cx == 0; then only bits >= 8 are set and
-            // base + s wraps back into range.  Indices are formed in uint32 first.
-            const uint32_t base = 8u * (row + (uint32_t)L.c[0]) - 8u;
             if (STATS && cnt) {
                 const int x0 = max(L.c[0] - 1, 0), x1 = min(L.c[0] + 1, W - 1);
                 if (x0 <= x1) acc.cand += __ldg(g.sub + 8u * (row + (uint32_t)x1) + 8u) - __ldg(g.sub + 8u * (row + (uint32_t)x0));
             }
-            while (m) {
-                const int s = __ffs(m) - 1;
-                const int t = __ffs(~(m >> s)) - 1;  // length of the run of set bits at s
-                m &= ~(((1u << t) - 1u) << s);
-                const uint32_t i0 = base + (uint32_t)s, i1 = i0 + (uint32_t)t;
-                if (i1 >= g.nsub) {  // cannot happen for a consistent table; never read past it
-                    acc.bad = true;
-                    continue;
+            // base wraps below 0 when row + cx == 0 (then lanes 0-7 are out of the grid);
+            // indices are formed in uint32 and loads past the table are never made
+            const uint32_t base = 8u * (row + (uint32_t)L.c[0]) - 8u;
+            const uint32_t il = base + (uint32_t)lane;
+            const uint32_t st = (lane <= 24 && il < g.nsub) ? __ldg(g.sub + il) : 0u;
+            const uint32_t en = __shfl_down_sync(kFull, st, 1);
+            const uint32_t c = reach ? en - st : 0u;
+            uint32_t incl = c;
+#pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint32_t t = __shfl_up_sync(kFull, incl, o);
+                if (lane >= o) incl += t;
+            }
+            const uint32_t excl = incl - c;
+            const uint32_t N = __shfl_sync(kFull, incl, 31);
+            if (STATS && cnt) acc.tested += N;
+            // particle of number v: owner lane = number of lanes whose running count is <= v
+            auto particle = [&](uint32_t v) -> uint32_t {
+                int o = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const uint32_t it = __shfl_sync(kFull, incl, o + step - 1);
+                    if (it <= v) o += step;
                 }
-                const uint32_t b = __ldg(g.sub + i0), e = __ldg(g.sub + i1);
-                if (STATS && cnt) acc.tested += e - b;
-                f(b, e);
+                const uint32_t s0 = __shfl_sync(kFull, st, o & 31), e0 = __shfl_sync(kFull, excl, o & 31);
+                return s0 + (v - e0);
+            };
+            uint32_t v = (uint32_t)lane;
+            bool ok = v < N;
+            uint32_t j = particle(v);
+            float4 q = ok ? __ldg(g.pts + j) : make_float4(0.f, 0.f, 0.f, 0.f);
+            for (uint32_t v0 = 0; v0 < N; v0 += 32) {
+                const uint32_t vn = v0 + 32u + (uint32_t)lane;
+                const bool okn = vn < N;
+                float4 qn = make_float4(0.f, 0.f, 0.f, 0.f);
+                if (v0 + 32u < N) {
+                    const uint32_t jn = particle(vn);
+                    if (okn) qn = __ldg(g.pts + jn);
+                }
+                f(q, ok);
+                q = qn;
+                ok = okn;
             }
         }
     }
@@ -188,18 +222,14 @@ __device__ __forceinline__ float density_warp(const GridDev& g, const KernelDev&
                                               float pz, float T, int lane, Acc& acc, bool cnt, float* red) {
     if (STATS && cnt) acc.evals++;
     float rho = 0.0f;
-    for_ranges_warp<STATS>(g, L, T, lane, acc, cnt, [&](uint32_t b, uint32_t e) {
-        for (uint32_t j0 = b; j0 < e; j0 += 32) {
-            const uint32_t j = j0 + (uint32_t)lane;
-            float w = 0.0f;
-            if (j < e) {
-                const float4 q = __ldg(g.pts + j);
-                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-                const float d2 = dot3(rx, ry, rz, rx, ry, rz);
-                if (d2 < k.h2) w = w_in(k, d2);
-            }
-            rho = ordered_sum32(red, lane, w, rho);
+    for_packed_warp<STATS>(g, L, T, lane, acc, cnt, [&](const float4& q, bool ok) {
+        float w = 0.0f;
+        if (ok) {
+            const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+            const float d2 = dot3(rx, ry, rz, rx, ry, rz);
+            if (d2 < k.h2) w = w_in(k, d2);
         }
+        rho = ordered_sum32(red, lane, w, rho);
     });
     return rho;
 }
@@ -546,12 +576,208 @@ __device__ __forceinline__ void union_stream(const GridDev& g, bool mine, const 
     if (pending) acc.bad = true;  // unreachable: every pass retires its leader
 }
 
+#ifndef FM_STAGE_TMA
+#define FM_STAGE_TMA 0
+#endif
+
+#if FM_STAGE_TMA
+// Staged variant of the union stream (measured against the plain loads): each
+// union row's particle span -- first to last reached sub-cell, contiguous in
+// the sorted array -- is copied into the warp's shared memory by
+// cp.async.bulk in chunks of kStageCh particles, two buffers per warp, each
+// with its own mbarrier; the next chunk of the row is in flight while the
+// lanes read the current one.  Waits are bounded: after kStageWaitLimit polls
+// the status word gets bit 16 and the chunk is read as it is (the results of
+// that launch are then reported as invalid).
+constexpr int kStageCh = 128;
+constexpr uint32_t kStageWaitLimit = 1u << 22;
+__shared__ __align__(128) float4 g_stage[kThreads / 32][2][kStageCh];
+__shared__ __align__(8) uint64_t g_stage_bar[kThreads / 32][2];
+__shared__ uint32_t g_stage_phase[kThreads / 32];
+
+__device__ __forceinline__ void stage_init() {
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        for (int b = 0; b < 2; ++b)
+            asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&g_stage_bar[w][b]))
+                         : "memory");
+        g_stage_phase[w] = 0u;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncwarp();
+}
+
+// Lane 0: copy n particles from src into buffer b of this warp.
+__device__ __forceinline__ void stage_issue(int w, int b, const float4* src, uint32_t n) {
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&g_stage_bar[w][b]);
+    const uint32_t dst = (uint32_t)__cvta_generic_to_shared(&g_stage[w][b][0]);
+    const uint32_t bytes = n * 16u;
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool stage_wait(int w, int b, uint32_t parity) {
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&g_stage_bar[w][b]);
+    for (uint32_t i = 0; i < kStageWaitLimit; ++i) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(bar), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// As union_stream, but f(pred, src, n) gets n particles in shared memory.
+template <bool STATS, typename F>
+__device__ __forceinline__ void union_stream_staged(const GridDev& g, bool mine, const Loc& L, float T, Acc& acc,
+                                                    unsigned int* status, F&& f) {
+    float ax[6];
+#pragma unroll
+    for (int i = 0; i < 6; ++i) ax[i] = slab_d2(L.u[0], -1.0f + 0.5f * (float)i);
+    const int W = g.dims[0], Hd = g.dims[1], D = g.dims[2];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    uint32_t ph = g_stage_phase[w];
+    uint32_t pending = __ballot_sync(kFull, mine);
+    for (int pass = 0; pending && pass < 32; ++pass) {
+        const bool cand = (pending >> lane) & 1u;
+        const int lead = __ffs(pending) - 1;
+        const int lx = __shfl_sync(kFull, L.c[0], lead), ly = __shfl_sync(kFull, L.c[1], lead),
+                  lz = __shfl_sync(kFull, L.c[2], lead);
+        const bool near = cand && abs(L.c[0] - lx) <= 1 && abs(L.c[1] - ly) <= 1 && abs(L.c[2] - lz) <= 1;
+        const int gx = __reduce_min_sync(kFull, near ? L.c[0] : 0x7fffffff);
+        const int gy = __reduce_min_sync(kFull, near ? L.c[1] : 0x7fffffff);
+        const int gz = __reduce_min_sync(kFull, near ? L.c[2] : 0x7fffffff);
+        const bool in = near && L.c[0] - gx <= 1 && L.c[1] - gy <= 1 && L.c[2] - gz <= 1;
+        pending &= ~__ballot_sync(kFull, in);
+        if (STATS && in) {
+            const int x0 = max(L.c[0] - 1, 0), x1 = min(L.c[0] + 1, W - 1);
+            if (x0 <= x1)
+                for (int z = max(L.c[2] - 1, 0); z <= min(L.c[2] + 1, D - 1); ++z)
+                    for (int y = max(L.c[1] - 1, 0); y <= min(L.c[1] + 1, Hd - 1); ++y) {
+                        const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
+                        acc.cand += __ldg(g.sub + 8u * (row + (uint32_t)x1) + 8u) - __ldg(g.sub + 8u * (row + (uint32_t)x0));
+                    }
+        }
+#pragma unroll 1
+        for (int zz = 0; zz < 4; ++zz) {
+            const int z = gz - 1 + zz;
+            if (z < 0 || z >= D) continue;
+#pragma unroll 1
+            for (int yy = 0; yy < 4; ++yy) {
+                const int y = gy - 1 + yy;
+                if (y < 0 || y >= Hd) continue;
+                const uint32_t own = in ? own_row_mask(g, L, ax, y, z, gx, T) : 0u;
+                const uint32_t uni = __reduce_or_sync(kFull, own);
+                if (!uni) continue;
+                const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
+                const uint32_t base = 8u * (row + (uint32_t)gx) - 8u;
+                const uint32_t il = base + (uint32_t)lane;
+                const uint32_t mystart = il < g.nsub ? __ldg(g.sub + il) : 0u;
+                const uint32_t i32 = base + 32u;
+                const uint32_t start32 = i32 < g.nsub ? __ldg(g.sub + i32) : 0u;
+                if ((uni >> 31) && i32 >= g.nsub) acc.bad = true;
+                const int first = __ffs(uni) - 1, last = 31 - __clz(uni);
+                const uint32_t B = __shfl_sync(kFull, mystart, first);
+                const uint32_t nx = __shfl_sync(kFull, mystart, (last + 1) & 31);
+                const uint32_t E = last == 31 ? start32 : nx;
+                if (E <= B) continue;
+                const uint32_t nch = (E - B + kStageCh - 1) / kStageCh;
+                if (lane == 0) stage_issue(w, 0, g.pts + B, min(E - B, (uint32_t)kStageCh));
+                uint32_t rem = uni;
+                int u = __ffs(rem) - 1;
+                rem &= rem - 1u;
+                uint32_t rb = __shfl_sync(kFull, mystart, u);
+                uint32_t rn = __shfl_sync(kFull, mystart, (u + 1) & 31);
+                uint32_t re = u == 31 ? start32 : rn;
+                bool pred = (own >> u) & 1u;
+                bool more = true;
+                for (uint32_t kc = 0; kc < nch; ++kc) {
+                    const int bf = (int)(kc & 1u);
+                    const uint32_t cb = B + kc * (uint32_t)kStageCh;
+                    const uint32_t ce = min(E, cb + (uint32_t)kStageCh);
+                    if (kc + 1 < nch) {
+                        __syncwarp();  // the other buffer's chunk (kc - 1) is read by every lane
+                        if (lane == 0)
+                            stage_issue(w, bf ^ 1, g.pts + ce, min(E - ce, (uint32_t)kStageCh));
+                    }
+                    if (!stage_wait(w, bf, (ph >> bf) & 1u)) atomicOr(status, 16u);
+                    ph ^= 1u << bf;
+                    const float4* buf = &g_stage[w][bf][0];
+                    while (more && rb < ce) {
+                        const uint32_t j0 = max(rb, cb), j1 = min(re, ce);
+                        if (STATS && j1 > j0) {
+                            if (pred) acc.tested += j1 - j0;
+                            if (lane == 0) acc.streamed += j1 - j0;
+                        }
+                        if (j1 > j0) f(pred, buf + (j0 - cb), j1 - j0);
+                        if (re > ce) break;  // the run goes on in the next chunk
+                        if (!rem) {
+                            more = false;
+                            break;
+                        }
+                        u = __ffs(rem) - 1;
+                        rem &= rem - 1u;
+                        rb = __shfl_sync(kFull, mystart, u);
+                        rn = __shfl_sync(kFull, mystart, (u + 1) & 31);
+                        re = u == 31 ? start32 : rn;
+                        pred = (own >> u) & 1u;
+                    }
+                }
+                __syncwarp();  // buffers free before the next row's copy
+            }
+        }
+    }
+    if (pending) acc.bad = true;
+    if (lane == 0) g_stage_phase[w] = ph;
+    __syncwarp();
+}
+#endif
+
 template <bool STATS>
 __device__ __forceinline__ float union_density(const MarchArgs& a, bool mine, const Loc& L, const float e[3], Acc& acc) {
     if (STATS && mine) acc.evals++;
     const float px = e[0], py = e[1], pz = e[2];
     const KernelDev& k = a.k;
     float rho = 0.0f;
+#if FM_STAGE_TMA
+    union_stream_staged<STATS>(a.g, mine, L, a.cull, acc, a.status, [&](bool pred, const float4* src, uint32_t n) {
+        uint32_t j = 0;
+        for (; j + 4 <= n; j += 4) {
+            const float4 q0 = src[j], q1 = src[j + 1], q2 = src[j + 2], q3 = src[j + 3];
+            if (pred) {
+                const float r0x = q0.x - px, r0y = q0.y - py, r0z = q0.z - pz;
+                const float r1x = q1.x - px, r1y = q1.y - py, r1z = q1.z - pz;
+                const float r2x = q2.x - px, r2y = q2.y - py, r2z = q2.z - pz;
+                const float r3x = q3.x - px, r3y = q3.y - py, r3z = q3.z - pz;
+                const float d0 = dot3(r0x, r0y, r0z, r0x, r0y, r0z);
+                const float d1 = dot3(r1x, r1y, r1z, r1x, r1y, r1z);
+                const float d2 = dot3(r2x, r2y, r2z, r2x, r2y, r2z);
+                const float d3 = dot3(r3x, r3y, r3z, r3x, r3y, r3z);
+                if (d0 < k.h2) rho = rho + w_in(k, d0);
+                if (d1 < k.h2) rho = rho + w_in(k, d1);
+                if (d2 < k.h2) rho = rho + w_in(k, d2);
+                if (d3 < k.h2) rho = rho + w_in(k, d3);
+            }
+        }
+        for (; j < n; ++j) {
+            const float4 q = src[j];
+            if (pred) {
+                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+                const float d = dot3(rx, ry, rz, rx, ry, rz);
+                if (d < k.h2) rho = rho + w_in(k, d);
+            }
+        }
+    });
+    return rho;
+#endif
     union_stream<STATS>(a.g, mine, L, a.cull, acc, [&](bool pred, uint32_t b, uint32_t e_) {
         uint32_t j = b;
         for (; j + 4 <= e_; j += 4) {
@@ -662,12 +888,10 @@ __device__ __forceinline__ void grad_warp(const GridDev& g, const KernelDev& k, 
     Loc L;
     if (STATS && cnt) acc.evals++;
     if (!locate(g, px, py, pz, L)) return;
-    for_ranges_warp<STATS>(g, L, T, lane, acc, cnt, [&](uint32_t b, uint32_t e) {
-        for (uint32_t j0 = b; j0 < e; j0 += 32) {
-            const uint32_t j = j0 + (uint32_t)lane;
+    for_packed_warp<STATS>(g, L, T, lane, acc, cnt, [&](const float4& q, bool ok) {
+        {
             float tx = 0.0f, ty = 0.0f, tz = 0.0f;
-            if (j < e) {
-                const float4 q = __ldg(g.pts + j);
+            if (ok) {
                 const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
                 const float q2 = dot3(rx, ry, rz, rx, ry, rz);
                 if (q2 < k.h2 && q2 > 0.0f) gradw_term(k, rx, ry, rz, q2, tx, ty, tz);
@@ -891,6 +1115,9 @@ template <bool STATS, bool BATCH, bool LEARNED>
 __global__ void __launch_bounds__(kThreads, LEARNED ? 4 : 3)
     k_march(const MarchArgs a, const MarchArgs* __restrict__ views, const uint32_t* __restrict__ tile_pfx, int nviews) {
     const int lane = threadIdx.x & 31;
+#if FM_STAGE_TMA
+    stage_init();
+#endif
     Acc acc;
     uint64_t rays = 0, started_n = 0, hits = 0;
     const unsigned total = (unsigned)a.ntiles, claim = (unsigned)a.claim;
@@ -963,6 +1190,9 @@ __global__ void k_queue_scatter(const MarchArgs a, const MarchArgs* __restrict__
 template <bool STATS, bool BATCH, bool LEARNED>
 __global__ void __launch_bounds__(kThreads, 4) k_regroup(const MarchArgs a, const MarchArgs* __restrict__ views) {
     const int lane = threadIdx.x & 31;
+#if FM_STAGE_TMA
+    stage_init();
+#endif
     Acc acc;
     uint64_t hits = 0;
     const unsigned n = min(*(volatile unsigned int*)a.q_tail, a.q_cap);
