@@ -165,6 +165,7 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->d_stats);
     cudaFree(ctx->d_work);
     cudaFree(ctx->longq.p);
+    cudaFree(ctx->aniso_list.p);
     cudaFree(ctx->longq2.p);
     cudaFree(ctx->rg_keys.p);
     cudaFree(ctx->rg_tmp.p);

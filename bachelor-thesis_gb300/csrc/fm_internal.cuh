@@ -219,6 +219,7 @@ struct fm_ctx {
     // long-ray queue of the march (64 B per entry, long_queue_entries(pixels)
     // entries for the largest view so far)
     fm::DevBuf longq;
+    fm::DevBuf aniso_list;  // started pixels of an anisotropic march (one ray per claim)
     // regrouped second pass: second queue, sort counters, scan temporaries, order
     fm::DevBuf longq2, rg_keys, rg_tmp, rg_order;
     // splat depth tile maxima (4 B per 8x8 tile) and the list of particles that

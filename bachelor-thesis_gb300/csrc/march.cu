@@ -1714,6 +1714,71 @@ struct AnisoCount {
     uint64_t evals = 0, hits = 0, rays = 0, started = 0, skipped = 0;
 };
 
+// One started ray (pixel idx) of view `a`, marched with the whole warp.
+template <bool STATS>
+__device__ __forceinline__ void aniso_ray(const MarchArgs& a, const AnisoDev& an, uint64_t idx, int lane,
+                                          AnisoCount& c) {
+    const int px = (int)(idx % (uint64_t)a.W), py = (int)(idx / (uint64_t)a.W);
+    float p[3], s[3];
+    ray_setup(a, px, py, a.zbuf[idx], p, s);
+    float q[3] = {p[0], p[1], p[2]};
+    float G[3][3], detG = 0.0f, rho = 0.0f;
+    bool hit = false;
+    for (int i = 0; i < a.max_steps; ++i) {
+        p[0] = p[0] + s[0];
+        p[1] = p[1] + s[1];
+        p[2] = p[2] + s[2];
+        if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p[0], p[1], p[2], s[0], s[1], s[2], a.status);
+        if (outside_forever(a.g, p[0], p[1], p[2], s[0], s[1], s[2])) break;
+        if (a.iso > 0.0f && zero_density(a.g, p[0], p[1], p[2])) {
+            // no particle within the support radius: the anisotropic density (its
+            // terms need |r| < H) is exactly 0, below iso; leaving the box for good ends the ray
+            if (leaving_zero_box(a.g, p[0], p[1], p[2], s[0], s[1], s[2])) break;
+            if (STATS) c.skipped++;
+            q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+            continue;
+        }
+        if (a.skip_mode == FM_SKIP_EXACT && a.iso > 0.0f) {
+            // no particle within the support radius of the sample's bound box:
+            // the anisotropic density is exactly 0
+            Loc L;
+            if (locate(a.g, p[0], p[1], p[2], L) && box_bound(a.g, L) == 0.0f) {
+                if (STATS) c.skipped++;
+                q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+                continue;
+            }
+        }
+        if (STATS) c.evals++;
+        aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
+        if (rho >= a.iso) {
+            hit = true;
+            break;
+        }
+        q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
+    }
+    float n0 = 0.f, n1 = 0.f, n2 = 0.f;
+    if (hit) {
+        for (int b = 0; b < a.bisect; ++b) {
+            const float m[3] = {(q[0] + p[0]) * 0.5f, (q[1] + p[1]) * 0.5f, (q[2] + p[2]) * 0.5f};
+            if (STATS) c.evals++;
+            aniso_eval(a.g, an, m[0], m[1], m[2], lane, G, detG, rho);
+            if (rho >= a.iso) { p[0] = m[0]; p[1] = m[1]; p[2] = m[2]; }
+            else { q[0] = m[0]; q[1] = m[1]; q[2] = m[2]; }
+        }
+        // RayMarcher.cpp:411-416: the gradient sum with the G of the hit point
+        if (STATS) c.evals++;
+        aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
+        float gx, gy, gz;
+        aniso_grad(a.g, an, p[0], p[1], p[2], lane, G, detG, gx, gy, gz);
+        const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
+        n0 = gx * gi;
+        n1 = gy * gi;
+        n2 = gz * gi;
+        if (STATS) c.hits++;
+    }
+    if (lane == 0) write_pixel(a, idx, px, py, hit, p[0], p[1], p[2], n0, n1, n2);
+}
+
 // One chunk of 32 consecutive pixels of view `a` (from pixel `base`): the
 // started rays among them are marched one after the other with the whole warp.
 template <bool STATS>
@@ -1732,84 +1797,58 @@ __device__ __forceinline__ void aniso_chunk(const MarchArgs& a, const AnisoDev& 
     while (todo) {
         const int src = __ffs(todo) - 1;
         todo &= todo - 1u;
-        const uint64_t idx = base + (uint64_t)src;
-        const int px = (int)(idx % (uint64_t)a.W), py = (int)(idx / (uint64_t)a.W);
-        float p[3], s[3];
-        ray_setup(a, px, py, a.zbuf[idx], p, s);
-        float q[3] = {p[0], p[1], p[2]};
-        float G[3][3], detG = 0.0f, rho = 0.0f;
-        bool hit = false;
-        for (int i = 0; i < a.max_steps; ++i) {
-            p[0] = p[0] + s[0];
-            p[1] = p[1] + s[1];
-            p[2] = p[2] + s[2];
-            if (a.skip_mode == FM_SKIP_REFERENCE) ref_skip(a.g, p[0], p[1], p[2], s[0], s[1], s[2], a.status);
-            if (outside_forever(a.g, p[0], p[1], p[2], s[0], s[1], s[2])) break;
-            if (a.skip_mode == FM_SKIP_EXACT && a.iso > 0.0f) {
-                // no particle within the support radius of the sample's bound box:
-                // the anisotropic density (its terms need |r| < H) is exactly 0
-                Loc L;
-                if (locate(a.g, p[0], p[1], p[2], L) && box_bound(a.g, L) == 0.0f) {
-                    if (STATS) c.skipped++;
-                    q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
-                    continue;
-                }
-            }
-            if (STATS) c.evals++;
-            aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
-            if (rho >= a.iso) {
-                hit = true;
-                break;
-            }
-            q[0] = p[0]; q[1] = p[1]; q[2] = p[2];
-        }
-        float n0 = 0.f, n1 = 0.f, n2 = 0.f;
-        if (hit) {
-            for (int b = 0; b < a.bisect; ++b) {
-                const float m[3] = {(q[0] + p[0]) * 0.5f, (q[1] + p[1]) * 0.5f, (q[2] + p[2]) * 0.5f};
-                if (STATS) c.evals++;
-                aniso_eval(a.g, an, m[0], m[1], m[2], lane, G, detG, rho);
-                if (rho >= a.iso) { p[0] = m[0]; p[1] = m[1]; p[2] = m[2]; }
-                else { q[0] = m[0]; q[1] = m[1]; q[2] = m[2]; }
-            }
-            // RayMarcher.cpp:411-416: the gradient sum with the G of the hit point
-            if (STATS) c.evals++;
-            aniso_eval(a.g, an, p[0], p[1], p[2], lane, G, detG, rho);
-            float gx, gy, gz;
-            aniso_grad(a.g, an, p[0], p[1], p[2], lane, G, detG, gx, gy, gz);
-            const float gi = 1.0f / sqrtf(dot3(gx, gy, gz, gx, gy, gz));
-            n0 = gx * gi;
-            n1 = gy * gi;
-            n2 = gz * gi;
-            if (STATS) c.hits++;
-        }
-        if (lane == src) write_pixel(a, idx, px, py, hit, p[0], p[1], p[2], n0, n1, n2);
+        aniso_ray<STATS>(a, an, base + (uint64_t)src, lane, c);
+    }
+}
+
+// Single view: the started pixels into a list (in any order) for k_march_aniso
+// to take one ray at a time, so the launch does not end on a chunk of many long
+// rays; pixels without a ray start get their miss outputs here.
+template <bool STATS>
+__global__ void k_aniso_starts(const MarchArgs a, uint32_t* __restrict__ list, unsigned int* __restrict__ n_list) {
+    const uint64_t npx = (uint64_t)a.W * (uint64_t)a.Hh;
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    const bool valid = i < npx;
+    const bool started = valid && a.zbuf[i] != 1.0f;
+    const uint32_t m = __ballot_sync(kFull, started);
+    const int lane = threadIdx.x & 31;
+    uint32_t base = 0;
+    if (lane == 0 && m) base = atomicAdd(n_list, (unsigned)__popc(m));
+    base = __shfl_sync(kFull, base, 0);
+    if (started) list[base + __popc(m & ((1u << lane) - 1u))] = (uint32_t)i;
+    else if (valid) write_pixel(a, i, (int)(i % (uint64_t)a.W), (int)(i / (uint64_t)a.W), false, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f);
+    if (STATS) {
+        const uint32_t v = __ballot_sync(kFull, valid);
+        if (lane == 0 && v) atomicAdd(a.stats + 0, (unsigned long long)__popc(v));
+        if (lane == 0 && m) atomicAdd(a.stats + 1, (unsigned long long)__popc(m));
     }
 }
 
 // Persistent warps take chunks of 32 consecutive pixels from a counter.
 // BATCH: chunk t belongs to view find_view(pfx, t) of `views` / `aviews`
 // (views without anisotropic rays own no chunks); otherwise to view `a`.
+// Single view (list != null): warps take one started ray at a time from the
+// list k_aniso_starts wrote.
 template <bool STATS, bool BATCH>
 __global__ void __launch_bounds__(kThreads)
     k_march_aniso(const __grid_constant__ MarchArgs a, const __grid_constant__ AnisoDev an,
                   const MarchArgs* __restrict__ views, const AnisoDev* __restrict__ aviews,
-                  const uint32_t* __restrict__ pfx, int nviews, uint32_t nchunks) {
+                  const uint32_t* __restrict__ pfx, int nviews, uint32_t nchunks, const uint32_t* __restrict__ list,
+                  const unsigned int* __restrict__ n_list) {
     const int lane = threadIdx.x & 31;
     AnisoCount c;
-    const uint64_t npx = (uint64_t)a.W * (uint64_t)a.Hh;
+    const unsigned nl = BATCH ? 0u : *n_list;
     for (;;) {
-        unsigned chunk = 0;
-        if (lane == 0) chunk = atomicAdd(a.tile_counter, 1u);
-        chunk = __shfl_sync(kFull, chunk, 0);
+        unsigned k = 0;
+        if (lane == 0) k = atomicAdd(a.tile_counter, 1u);
+        k = __shfl_sync(kFull, k, 0);
         if (BATCH) {
-            if (chunk >= nchunks) break;
-            const int v = find_view(pfx, nviews, chunk);
-            aniso_chunk<STATS>(views[v], aviews[v], (uint64_t)(chunk - __ldg(pfx + v)) * 32u, lane, c);
+            if (k >= nchunks) break;
+            const int v = find_view(pfx, nviews, k);
+            aniso_chunk<STATS>(views[v], aviews[v], (uint64_t)(k - __ldg(pfx + v)) * 32u, lane, c);
         } else {
-            const uint64_t base = (uint64_t)chunk * 32u;
-            if (base >= npx) break;
-            aniso_chunk<STATS>(a, an, base, lane, c);
+            if (k >= nl) break;
+            aniso_ray<STATS>(a, an, (uint64_t)__ldg(list + k), lane, c);
         }
     }
     if (STATS) {
@@ -1849,12 +1888,18 @@ AnisoDev make_aniso(const fm_scene* s, const fm_aniso_params* ap) {
 
 template <bool STATS, bool BATCH>
 int launch_aniso_variant(fm_ctx* ctx, const MarchArgs& a, const AnisoDev& an, const MarchArgs* views,
-                         const AnisoDev* aviews, const uint32_t* pfx, int nviews, uint32_t nchunks, cudaStream_t st) {
+                         const AnisoDev* aviews, const uint32_t* pfx, int nviews, uint32_t nchunks, uint32_t* list,
+                         unsigned int* n_list, cudaStream_t st) {
+    if (!BATCH) {
+        const uint64_t npx = (uint64_t)a.W * (uint64_t)a.Hh;
+        k_aniso_starts<STATS><<<(unsigned)((npx + 255) / 256), 256, 0, st>>>(a, list, n_list);
+        FM_CUDA(ctx, cudaGetLastError());
+    }
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_march_aniso<STATS, BATCH>, kThreads, 0);
     if (per_sm < 1) per_sm = 1;
     const unsigned blocks = (unsigned)(ctx->sm_count * per_sm);
-    k_march_aniso<STATS, BATCH><<<blocks, kThreads, 0, st>>>(a, an, views, aviews, pfx, nviews, nchunks);
+    k_march_aniso<STATS, BATCH><<<blocks, kThreads, 0, st>>>(a, an, views, aviews, pfx, nviews, nchunks, list, n_list);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }
@@ -1875,9 +1920,9 @@ int launch_march_aniso_batch(fm_ctx* ctx, const MarchArgs& a, const MarchArgs* d
     std::memset(&none, 0, sizeof(none));
     if (a.stats)
         return launch_aniso_variant<true, true>(ctx, a, none, d_views, (const AnisoDev*)d_aviews, d_pfx, nviews,
-                                                nchunks, st);
+                                                nchunks, nullptr, nullptr, st);
     return launch_aniso_variant<false, true>(ctx, a, none, d_views, (const AnisoDev*)d_aviews, d_pfx, nviews, nchunks,
-                                             st);
+                                             nullptr, nullptr, st);
 }
 
 int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
@@ -1887,10 +1932,16 @@ int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, con
     a.status = ctx->d_status;
     unsigned int* slot = ctx->d_work + (ctx->work_slot++ % kWorkSlots) * 32;
     a.tile_counter = slot;
-    FM_CUDA(ctx, cudaMemsetAsync(slot, 0, sizeof(unsigned int), st));
+    FM_CUDA(ctx, cudaMemsetAsync(slot, 0, 2 * sizeof(unsigned int), st));
+    const uint64_t npx = (uint64_t)cam->width * (uint64_t)cam->height;
+    if (ctx->aniso_list.bytes < npx * 4) {
+        FM_CUDA(ctx, cudaStreamSynchronize(st));  // the list may be in use by an earlier launch
+        if (!grow_buf(ctx->aniso_list, npx * 4)) return set_err(ctx, FM_ERR_OOM, "ray list allocation failed");
+    }
+    uint32_t* list = (uint32_t*)ctx->aniso_list.p;
     const AnisoDev an = make_aniso(s, ap);
-    if (a.stats) return launch_aniso_variant<true, false>(ctx, a, an, nullptr, nullptr, nullptr, 0, 0, st);
-    return launch_aniso_variant<false, false>(ctx, a, an, nullptr, nullptr, nullptr, 0, 0, st);
+    if (a.stats) return launch_aniso_variant<true, false>(ctx, a, an, nullptr, nullptr, nullptr, 0, 0, list, slot + 1, st);
+    return launch_aniso_variant<false, false>(ctx, a, an, nullptr, nullptr, nullptr, 0, 0, list, slot + 1, st);
 }
 
 int launch_density(fm_ctx* ctx, const fm_scene* s, const float* d_xyz, uint64_t n, uint32_t stride, float* d_out,

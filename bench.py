@@ -326,7 +326,7 @@ def run_reference(args):
     print(json.dumps(line))
 
 
-def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, plain_ms):
+def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, plain_ms, plain_st):
     """The learned-proposal march of the same frame, timed like the plain one, judged against it."""
     from fluidmarch import proposal as PR
 
@@ -388,6 +388,23 @@ def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, pla
                 ts.append(e0.elapsed_time(e1))
         return float(np.mean(ts))
 
+    # where proposed rays go: intervals of this frame against the plain march's hit mask
+    iv = torch.zeros((npx, 2), dtype=torch.int32, device=dev)
+    fm.proposal_intervals(scene, cam, P_l, lo["start_depth"], iv)
+    ctx.sync()
+    started = lo["start_depth"] < 1
+    proposed = (iv[:, 1] > 0) & started
+    plain_hit = out["depth"] > 0
+    # no proposal can remove a hit ray's crossing sample, its bisections or its normal
+    floor = plain_st["hits"] * (sc.bisect + 2)
+    causes = {"proposed": int(proposed.sum().item()),
+              "proposed_plain_misses": int((proposed & ~plain_hit).sum().item()),
+              "proposed_plain_hits": int((proposed & plain_hit).sum().item()),
+              "plain_evals": plain_st["evals"], "learned_evals": st["evals"],
+              "evals_floor_hits_x_bisect_plus_2": floor,
+              "max_vs_plain_by_evaluations": plain_st["evals"] / max(1, floor),
+              "note": "a ray the plain march misses has no crossing in any interval and always falls back; "
+                      "a perfect, free proposal still evaluates each hit's crossing, bisections and normal"}
     off = [timed_plain(fm.FM_SKIP_OFF)]
     ref_skip = timed_plain(fm.FM_SKIP_REFERENCE)
     fm.set_proposal(ctx, None)
@@ -404,6 +421,7 @@ def run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, pla
             "mask_identical": j["mask_mismatch"] == 0,
             "margins_support_radii": [margin_lo, margin_hi], "min_near_support_radii": min_near,
             "counters": {k: st[k] for k in ("evals", "proposed", "fallbacks", "deferred")},
+            "fallback_causes": causes,
             "proposal": {"weights": "fluidmarch/proposal_sloshing.npz", "train_scenes": meta.get("train_scenes"),
                          "heldout_scenes": meta.get("heldout_scenes"), "heldout": meta.get("heldout")}}
 
@@ -755,7 +773,7 @@ def run_ours(args):
 
     learned = None
     if rank == 0 and not args.no_learned:
-        learned = run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, total_ms / args.steps)
+        learned = run_learned(args, fm, torch, ctx, ext, scene, sc, cam, out, flush, skip, total_ms / args.steps, st)
     batch = None
     if rank == 0 and not args.no_batch:
         batch = run_batch(args, fm, torch, ctx, ext, dev)
