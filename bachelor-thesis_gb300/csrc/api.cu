@@ -122,7 +122,9 @@ int fm_create(fm_ctx** out, int device) {
     }
     if (cudaStreamCreateWithFlags(&ctx->side, cudaStreamNonBlocking) != cudaSuccess ||
         cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+        cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_jfork, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&ctx->ev_jjoin, cudaEventDisableTiming) != cudaSuccess) {
         fm_destroy(ctx);
         return FM_ERR_CUDA;
     }
@@ -184,9 +186,12 @@ void fm_destroy(fm_ctx* ctx) {
     cudaFree(ctx->judge_ref.p);
     cudaFree(ctx->judge_test.p);
     cudaFree(ctx->judge_acc.p);
+    cudaFree(ctx->judge_longq.p);
     if (ctx->h_pinned_small) cudaFreeHost(ctx->h_pinned_small);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->ev_jfork) cudaEventDestroy(ctx->ev_jfork);
+    if (ctx->ev_jjoin) cudaEventDestroy(ctx->ev_jjoin);
     if (ctx->side) cudaStreamDestroy(ctx->side);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -576,10 +581,25 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
         o.depth = (float*)ctx->judge_test.p;
     }
     if (ctx->stats_enabled) FM_CUDA(ctx, cudaMemsetAsync(ctx->d_stats, 0, fm::kStatSlots * sizeof(unsigned long long), st));
+    if (judge) {
+        // the judge's sample march runs on the side stream next to the learned march
+        FM_CUDA(ctx, cudaEventRecord(ctx->ev_jfork, st));
+        FM_CUDA(ctx, cudaStreamWaitEvent(ctx->side, ctx->ev_jfork, 0));
+        rc = judge_start(ctx, sm, cam, p, z, ctx->side);
+        // whatever it returned, st waits for what reached the side stream
+        FM_CUDA(ctx, cudaEventRecord(ctx->ev_jjoin, ctx->side));
+        if (rc) {
+            FM_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_jjoin, 0));
+            return rc;
+        }
+    }
     if (p->flags & FM_MARCH_ANISOTROPIC) rc = launch_march_aniso(ctx, s, cam, p, &ctx->aniso, o, st);
     else rc = launch_march(ctx, s, cam, p, o, st);
+    if (judge) {
+        FM_CUDA(ctx, cudaStreamWaitEvent(st, ctx->ev_jjoin, 0));
+        if (!rc) rc = judge_finish(ctx, o.depth, npx, st);
+    }
     if (rc) return rc;
-    if (judge && (rc = judge_learned(ctx, sm, cam, p, z, o.depth, st)) != FM_OK) return rc;
     if (host) {
         for (int i = 0; i < 4; ++i)
             if (user[i] && !direct[i])

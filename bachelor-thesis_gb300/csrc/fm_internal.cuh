@@ -238,6 +238,8 @@ struct fm_ctx {
     float judge_tol = 0.0f;
     uint64_t judge_seq = 0;
     fm::DevBuf judge_z, judge_ref, judge_test, judge_acc;
+    fm::DevBuf judge_longq;  // the sample march's long-ray queue (it runs next to the learned march)
+    cudaEvent_t ev_jfork = nullptr, ev_jjoin = nullptr;
     fm::DevBuf file_rec, file_xyz;  // particle-file loader: point records, gathered positions
     fm::DevBuf blur_in, blur_out;   // depth blur staging for host buffers
     // live scenes of this context; fm_destroy frees the ones still alive
@@ -406,8 +408,10 @@ inline uint64_t long_queue_entries(uint64_t pixels, uint32_t limit = 0) {
 // launch-wide fields with ntiles = total tiles.
 int launch_march_kernels(fm_ctx* ctx, const MarchArgs& launch, const MarchArgs* d_views, const uint32_t* d_tile_pfx,
                          int nviews, cudaStream_t st);
+// queue: a long-ray queue of the caller's for this launch (then no regrouped
+// pass), so that it can run next to another march of the context.
 int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
-                 const MarchOutDev& o, cudaStream_t st);
+                 const MarchOutDev& o, cudaStream_t st, DevBuf* queue = nullptr);
 // The anisotropic march (march.cu), warp per ray.
 int launch_march_aniso(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
                        const fm_aniso_params* ap, const MarchOutDev& o, cudaStream_t st);
@@ -437,10 +441,13 @@ void destroy_batches(fm_ctx* ctx);
 int ensure_occupancy(fm_ctx* ctx, fm_scene* s, cudaStream_t st);
 int launch_features(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const float* zbuf, float* feat, float* t0,
                     cudaStream_t st);
-// Per-frame judge (fm_set_judge): plain march of a pixel sample next to a
-// learned march whose start depths are z and hit distances learned_depth.
-int judge_learned(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const float* z,
-                  const float* learned_depth, cudaStream_t st);
+// Per-frame judge (fm_set_judge): judge_start enqueues the plain march of a
+// pixel sample of a learned march whose start depths are z (on a stream of its
+// own, next to the learned march); judge_finish, once both are done, compares
+// the sample's hit distances with the learned ones.
+int judge_start(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const float* z,
+                cudaStream_t st);
+int judge_finish(fm_ctx* ctx, const float* learned_depth, uint64_t npx, cudaStream_t st);
 int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const fm_proposal* pr,
                    const float* zbuf, int2* ivl, float2* raw, cudaStream_t st);
 // Batched proposal: per-view blocks (propose_view) laid out by the caller.

@@ -1954,7 +1954,7 @@ int launch_density(fm_ctx* ctx, const fm_scene* s, const float* d_xyz, uint64_t 
 }
 
 int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_march_params* p,
-                 const MarchOutDev& o, cudaStream_t st) {
+                 const MarchOutDev& o, cudaStream_t st, DevBuf* queue) {
     MarchArgs a = march_view_args(s, cam, p, o, ctx->tile);
     a.stats = ctx->stats_enabled ? ctx->d_stats : nullptr;
     a.status = ctx->d_status;
@@ -1970,19 +1970,20 @@ int launch_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_
     a.q2_head = slot + 5;
     FM_CUDA(ctx, cudaMemsetAsync(slot, 0, 6 * sizeof(unsigned int), st));
     const uint64_t entries = long_queue_entries((uint64_t)cam->width * (uint64_t)cam->height, ctx->tile.qlimit);
-    const bool regroup = ctx->tile.cap2 > 0;
+    const bool regroup = ctx->tile.cap2 > 0 && !queue;
+    DevBuf& longq = queue ? *queue : ctx->longq;
     const uint64_t nkeys = (uint64_t)a.ntiles + 1;
-    const bool small = ctx->longq.bytes < entries * 64 ||
+    const bool small = longq.bytes < entries * 64 ||
                        (regroup && (ctx->longq2.bytes < entries * 64 || ctx->rg_order.bytes < entries * 4 ||
                                     ctx->rg_keys.bytes < nkeys * 4 || ctx->rg_tmp.bytes < scan_words(nkeys) * 4));
     if (small) {
         FM_CUDA(ctx, cudaStreamSynchronize(st));  // the buffers may be in use by an earlier launch
-        if (!grow_buf(ctx->longq, entries * 64) ||
+        if (!grow_buf(longq, entries * 64) ||
             (regroup && (!grow_buf(ctx->longq2, entries * 64) || !grow_buf(ctx->rg_order, entries * 4) ||
                          !grow_buf(ctx->rg_keys, nkeys * 4) || !grow_buf(ctx->rg_tmp, scan_words(nkeys) * 4))))
             return set_err(ctx, FM_ERR_OOM, "long-ray queue allocation failed");
     }
-    a.longq = (float4*)ctx->longq.p;
+    a.longq = (float4*)longq.p;
     a.q_cap = (unsigned int)entries;
     if (regroup) {
         a.longq2 = (float4*)ctx->longq2.p;

@@ -356,9 +356,11 @@ struct ProposeArgs {
 };
 
 // Hidden layer epilogue: TMEM columns [c0, c0 + 64) of this row -> bias + GELU -> BF16 A tile.
-__device__ __forceinline__ void hidden_epilogue(uint32_t tmem_row, uint32_t c0, const float* bias, uint8_t* a2,
-                                                int row) {
-#pragma unroll
+// One copy for both hidden layers, a loop over four groups of 16 columns: the
+// kernel's code stays small (instruction fetch was its top stall).
+__device__ __noinline__ void hidden_epilogue(uint32_t tmem_row, uint32_t c0, const float* bias, uint8_t* a2,
+                                             int row) {
+#pragma unroll 1
     for (int q = 0; q < 4; ++q) {
         float v[16];
         tmem_ld16(tmem_row + c0 + 16 * q, v);
@@ -1020,32 +1022,37 @@ int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_marc
     return FM_OK;
 }
 
-int judge_learned(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const float* z,
-                  const float* learned_depth, cudaStream_t st) {
+int judge_start(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_march_params* p, const float* z,
+                cudaStream_t st) {
     const uint64_t npx = (uint64_t)cam->width * cam->height;
     const bool fresh = ctx->judge_acc.p == nullptr;
     if (!grow_buf(ctx->judge_z, npx * 4) || !grow_buf(ctx->judge_ref, npx * 4) || !grow_buf(ctx->judge_acc, 64))
         return set_err(ctx, FM_ERR_OOM, "judge buffer allocation failed");
-    unsigned long long* acc = (unsigned long long*)ctx->judge_acc.p;
-    if (fresh) FM_CUDA(ctx, cudaMemsetAsync(acc, 0, 64, st));
+    if (fresh) FM_CUDA(ctx, cudaMemsetAsync(ctx->judge_acc.p, 0, 64, st));
     const uint32_t seed = (uint32_t)(ctx->judge_seq++ * 0x9E3779B9ull);
-    const unsigned blocks = (unsigned)((npx + 255) / 256);
     float* zs = (float*)ctx->judge_z.p;
-    float* dref = (float*)ctx->judge_ref.p;
-    k_judge_starts<<<blocks, 256, 0, st>>>(z, zs, npx, (uint32_t)cam->width, seed, ctx->judge_stride);
+    k_judge_starts<<<(unsigned)((npx + 255) / 256), 256, 0, st>>>(z, zs, npx, (uint32_t)cam->width, seed,
+                                                                   ctx->judge_stride);
     FM_CUDA(ctx, cudaGetLastError());
-    // the plain march of the sample: same settings, its own start plane and hit distances
+    // the plain march of the sample: same settings, its own start plane, hit
+    // distances and long-ray queue
     fm_march_params q = *p;
     q.flags = FM_MARCH_EXTERNAL_DEPTH;
     MarchOutDev o{};
     o.start_depth = zs;
-    o.depth = dref;
+    o.depth = (float*)ctx->judge_ref.p;
     const int stats = ctx->stats_enabled;
     ctx->stats_enabled = 0;  // the counters describe the learned march
-    const int rc = launch_march(ctx, s, cam, &q, o, st);
+    const int rc = launch_march(ctx, s, cam, &q, o, st, &ctx->judge_longq);
     ctx->stats_enabled = stats;
-    if (rc) return rc;
-    k_judge_sample<<<blocks, 256, 0, st>>>(zs, dref, learned_depth, npx, ctx->judge_tol, acc);
+    return rc;
+}
+
+int judge_finish(fm_ctx* ctx, const float* learned_depth, uint64_t npx, cudaStream_t st) {
+    k_judge_sample<<<(unsigned)((npx + 255) / 256), 256, 0, st>>>((const float*)ctx->judge_z.p,
+                                                                   (const float*)ctx->judge_ref.p, learned_depth, npx,
+                                                                   ctx->judge_tol,
+                                                                   (unsigned long long*)ctx->judge_acc.p);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
 }
@@ -1211,7 +1218,7 @@ int fm_judge_frames(fm_ctx* ctx, fm_frame_judge* out, int reset) {
     r.tol = ctx->judge_tol;
     if (ctx->judge_acc.p) {
         unsigned long long h[7];
-        FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+        FM_CUDA(ctx, cudaDeviceSynchronize());  // judged marches may run on any stream
         FM_CUDA(ctx, cudaMemcpy(h, ctx->judge_acc.p, sizeof(h), cudaMemcpyDeviceToHost));
         r.frames = h[0];
         r.sampled = h[1];
