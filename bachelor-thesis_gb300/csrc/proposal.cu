@@ -81,10 +81,13 @@ constexpr uint32_t kSmBias = kSmW3 + kN3 * kH * 2;  // 130 floats
 constexpr uint32_t kSmBar = kSmBias + 544;          // mbarrier (8 B)
 constexpr uint32_t kSmTmem = kSmBar + 8;            // TMEM base address
 constexpr uint32_t kSmUsed = kSmTmem + 8;
-// Requested dynamic shared memory: more than a quarter of the SM's 228 KB, so
-// at most 4 CTAs share an SM and their 4 x 128 TMEM columns always fit.
-constexpr uint32_t kSmRequest = 60 * 1024;
-constexpr uint32_t kTmemCols = 128;
+// Requested dynamic shared memory: more than a sixth of the SM's 228 KB, so
+// at most 5 CTAs share an SM and their 5 x 64 TMEM columns always fit in 512.
+// The three layers' accumulators share the same 64 columns: a layer's MMA is
+// issued only after the previous epilogue has read them back.
+constexpr uint32_t kSmRequest = 40 * 1024;
+constexpr uint32_t kTmemCols = 64;
+constexpr int kCtasPerSm = 5;          // persistent grid: CTAs resident per SM
 constexpr uint32_t kWaitLimit = 1u << 22;  // mbarrier polls before giving up
 static_assert(kSmUsed <= kSmRequest, "shared memory image");
 
@@ -421,7 +424,7 @@ __device__ __forceinline__ bool propose_tile(const ProposeView& pv, uint64_t lt,
     if (!ok) return false;
     tc_after();
     hidden_epilogue(c.tmem_row, 0, bias, a2, tid);
-    // layer 2: D[:, 64:128) = H1 (128 x 64) * W2^T
+    // layer 2: D[:, 0:64) = H1 (128 x 64) * W2^T (epilogue 1 has read layer 1's D)
     fence_async_smem();
     tc_before();
     __syncthreads();
@@ -429,7 +432,7 @@ __device__ __forceinline__ bool propose_tile(const ProposeView& pv, uint64_t lt,
     if (tid == 0) {
 #pragma unroll
         for (int kk = 0; kk < kH / 16; ++kk)
-            mma_bf16(c.tmem + kH, mdesc(a2s + 256 * kk, 128, (kH / 8) * 128),
+            mma_bf16(c.tmem, mdesc(a2s + 256 * kk, 128, (kH / 8) * 128),
                      mdesc(w2s + 256 * kk, 128, (kH / 8) * 128), idesc_bf16(kH), kk > 0 ? 1u : 0u);
         mma_commit(c.bar);
     }
@@ -437,7 +440,7 @@ __device__ __forceinline__ bool propose_tile(const ProposeView& pv, uint64_t lt,
     phase ^= 1;
     if (!ok) return false;
     tc_after();
-    hidden_epilogue(c.tmem_row, kH, bias + kH, a2, tid);
+    hidden_epilogue(c.tmem_row, 0, bias + kH, a2, tid);
     // layer 3: D[:, 0:16) = H2 (128 x 64) * W3^T (rows 2..15 of W3 are zero)
     fence_async_smem();
     tc_before();
@@ -973,7 +976,7 @@ int launch_propose_batch(fm_ctx* ctx, const ProposeBatchDev& b, cudaStream_t st)
     a.bias = b.bias;
     a.status = ctx->d_status;
     FM_CUDA(ctx, cudaFuncSetAttribute(k_propose<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmRequest));
-    uint64_t grid = (uint64_t)ctx->sm_count * 4;
+    uint64_t grid = (uint64_t)ctx->sm_count * kCtasPerSm;
     if (grid > b.ntiles) grid = b.ntiles;
     if (grid) k_propose<true><<<(unsigned)grid, kRows, kSmRequest, st>>>(a);
     if (b.nblk)
@@ -1013,7 +1016,7 @@ int launch_propose(fm_ctx* ctx, fm_scene* s, const fm_camera* cam, const fm_marc
     a.bias = pr->d_bias;
     a.status = ctx->d_status;
     FM_CUDA(ctx, cudaFuncSetAttribute(k_propose<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmRequest));
-    uint64_t grid = (uint64_t)ctx->sm_count * 4;
+    uint64_t grid = (uint64_t)ctx->sm_count * kCtasPerSm;
     if (grid > a.ntiles) grid = a.ntiles;
     k_propose<false><<<(unsigned)grid, kRows, kSmRequest, st>>>(a);
     const uint64_t nblk = ivl_blocks(cam->width, cam->height);
