@@ -216,6 +216,10 @@ struct fm_ctx {
     fm_march_stats last_stats{};
     // scratch for grid builds
     fm::DevBuf scratch[8];
+    // the key counts and the bounds accumulator of a grid build return to their
+    // initial state at the end of every build; they are set again when they
+    // were reallocated or a build stopped in between
+    bool grid_scratch_dirty = true;
     // long-ray queue of the march (64 B per entry, long_queue_entries(pixels)
     // entries for the largest view so far)
     fm::DevBuf longq;

@@ -112,11 +112,7 @@ struct GridParams {
 // Per-particle cell (QueryDensityGrid formula; coordinates clamped into the
 // grid, which the support-radius padding guarantees for finite input), the
 // sort key cell * 8 + sub-cell, and the key histogram.
-__global__ void k_cells(const float* __restrict__ xyz, uint64_t n, uint32_t stride, GridParams g,
-                        uint32_t* __restrict__ cell, uint32_t* __restrict__ key, uint32_t* __restrict__ count) {
-    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const float* p = xyz + i * stride;
+__device__ __forceinline__ uint32_t cell_key(const float* p, const GridParams& g, uint32_t& lin) {
     int c[3];
     uint32_t sub = 0;
 #pragma unroll
@@ -126,12 +122,198 @@ __global__ void k_cells(const float* __restrict__ xyz, uint64_t n, uint32_t stri
         c[a] = min(max(v, 0), g.dims[a] - 1);
         if (f - (float)c[a] >= 0.5f) sub |= 1u << a;
     }
-    uint32_t lin = (uint32_t)c[0] + (uint32_t)c[1] * (uint32_t)g.dims[0] +
-                   (uint32_t)c[2] * (uint32_t)g.dims[0] * (uint32_t)g.dims[1];
+    lin = (uint32_t)c[0] + (uint32_t)c[1] * (uint32_t)g.dims[0] +
+          (uint32_t)c[2] * (uint32_t)g.dims[0] * (uint32_t)g.dims[1];
+    return lin * 8u + sub;
+}
+
+__global__ void k_cells(const float* __restrict__ xyz, uint64_t n, uint32_t stride, GridParams g,
+                        uint32_t* __restrict__ cell, uint32_t* __restrict__ key, uint32_t* __restrict__ count) {
+    uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t lin;
+    const uint32_t k = cell_key(xyz + i * stride, g, lin);
     cell[i] = lin;
-    uint32_t k = lin * 8u + sub;
     key[i] = k;
     atomicAdd(&count[k], 1u);
+}
+
+// ---- single-sync build: grid parameters computed on the device ------------
+// The bounds pass accumulates the AABB into the bounds words; a one-thread
+// pass turns those into the grid (the reference's FP32 order,
+// Dataset.cpp:89-104: max + pad, min - pad, ceil(extent / cell), 1 / cell;
+// device division and ceil are IEEE-exact like the host's), checks it against
+// the cell capacity the host launched the rest of the build for and writes a
+// record.  Every later pass reads the record (through L1: one line that all
+// threads read) and does nothing unless status is kGridOk; the host reads it
+// once, after the build.
+enum : uint32_t { kGridOk = 0, kGridNonFinite = 1, kGridExtent = 2, kGridTooMany = 3, kGridOverCapacity = 4 };
+
+struct GridInfo {
+    GridParams g;
+    uint32_t status;
+    float max[3];
+    uint32_t ncells;
+    uint32_t n_long;  // segments longer than kShortSeg, listed by k_segsort_gather
+};
+
+// Bounds words: [0..2] ordered min, [3..5] ordered max, [6] non-finite
+// coordinates.  Between builds they hold (~0, ~0, ~0, 0, 0, 0, 0): the record
+// pass puts them back once it has read them.
+constexpr int kBoundsThreads = 256;
+
+__device__ void reset_bounds(uint32_t* mm) {
+    for (int a = 0; a < 3; ++a) {
+        mm[a] = 0xffffffffu;
+        mm[3 + a] = 0u;
+    }
+    mm[6] = 0u;
+}
+
+__device__ GridInfo grid_from_bounds(const uint32_t* mm, float support, uint64_t capacity) {
+    uint32_t h[7];
+    for (int a = 0; a < 7; ++a) h[a] = mm[a];
+    GridInfo gi;
+    gi.status = h[6] ? kGridNonFinite : kGridOk;
+    gi.n_long = 0;
+    gi.ncells = 0;
+    const float pad = 1.0f * support, cell = 1.0f * support;
+    uint64_t ncells = 1;
+    for (int a = 0; a < 3; ++a) {
+        const float lo = ord2f(h[a]), hi = ord2f(h[3 + a]);
+        gi.max[a] = hi + pad;
+        gi.g.min[a] = lo - pad;
+        const float ext = gi.max[a] - gi.g.min[a];
+        const float d = ceilf(ext / cell);
+        if (!(d >= 1.0f && d < 1.0e6f)) {
+            if (gi.status == kGridOk) gi.status = kGridExtent;
+            gi.g.dims[a] = 1;
+        } else {
+            gi.g.dims[a] = (int)d;
+        }
+        ncells *= (uint64_t)gi.g.dims[a];
+    }
+    gi.g.inv = 1.0f / cell;
+    if (gi.status == kGridOk) {
+        if (ncells > (1ull << 28)) {
+            gi.status = kGridTooMany;
+        } else {
+            gi.ncells = (uint32_t)ncells;
+            if (ncells > capacity) gi.status = kGridOverCapacity;
+        }
+    }
+    return gi;
+}
+
+// Bounds pass over positions with a stride of 3 floats at a 16-byte aligned
+// base (VEC3: the 3n floats read as float4; component c of float4 q holds
+// axis (q + c) % 3, and the grid stride is a multiple of 3 float4s, so all of
+// a thread's float4s share q % 3 and the axes are rotated into place once at
+// the end) or any stride (one float per load).
+template <bool VEC3>
+__global__ void __launch_bounds__(kBoundsThreads)
+    k_grid_bounds(const float* __restrict__ xyz, uint64_t n, uint32_t stride, uint32_t* __restrict__ mm) {
+    float mn[3] = {INFINITY, INFINITY, INFINITY}, mx[3] = {-INFINITY, -INFINITY, -INFINITY};
+    uint32_t bad = 0;
+    const uint64_t t0 = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x, step = (uint64_t)gridDim.x * blockDim.x;
+    if (VEC3) {
+        const uint64_t nf = 3 * n, nq = nf / 4;
+        float smn[3] = {INFINITY, INFINITY, INFINITY}, smx[3] = {-INFINITY, -INFINITY, -INFINITY};
+        for (uint64_t q = t0; q < nq; q += step) {
+            const float4 v = __ldg(reinterpret_cast<const float4*>(xyz) + q);
+            const float c[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+                const int sl = j == 3 ? 0 : j;
+                if (!isfinite(c[j])) { bad++; continue; }
+                smn[sl] = fminf(smn[sl], c[j]);
+                smx[sl] = fmaxf(smx[sl], c[j]);
+            }
+        }
+        const uint32_t r = (uint32_t)(t0 % 3);
+#pragma unroll
+        for (int sl = 0; sl < 3; ++sl) {
+            const uint32_t a = (r + (uint32_t)sl) % 3u;
+            // axis a, unrolled into selects (no indexed register arrays)
+            mn[0] = a == 0 ? smn[sl] : mn[0]; mx[0] = a == 0 ? smx[sl] : mx[0];
+            mn[1] = a == 1 ? smn[sl] : mn[1]; mx[1] = a == 1 ? smx[sl] : mx[1];
+            mn[2] = a == 2 ? smn[sl] : mn[2]; mx[2] = a == 2 ? smx[sl] : mx[2];
+        }
+        for (uint64_t j = 4 * nq + t0; j < nf; j += step) {  // the last nf % 4 floats
+            const float v = xyz[j];
+            const uint32_t a = (uint32_t)(j % 3);
+            if (!isfinite(v)) { bad++; continue; }
+            if (a == 0) { mn[0] = fminf(mn[0], v); mx[0] = fmaxf(mx[0], v); }
+            if (a == 1) { mn[1] = fminf(mn[1], v); mx[1] = fmaxf(mx[1], v); }
+            if (a == 2) { mn[2] = fminf(mn[2], v); mx[2] = fmaxf(mx[2], v); }
+        }
+    } else {
+        for (uint64_t i = t0; i < n; i += step) {
+            const float* p = xyz + i * stride;
+#pragma unroll
+            for (int a = 0; a < 3; ++a) {
+                const float v = p[a];
+                if (!isfinite(v)) { bad++; continue; }
+                mn[a] = fminf(mn[a], v);
+                mx[a] = fmaxf(mx[a], v);
+            }
+        }
+    }
+    __shared__ uint32_t s[7][kBoundsThreads / kWarp];
+    uint32_t k[7];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) { k[a] = f2ord(mn[a]); k[3 + a] = f2ord(mx[a]); }
+    k[6] = bad;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int a = 0; a < 3; ++a) {
+            k[a] = min(k[a], __shfl_xor_sync(0xffffffffu, k[a], o));
+            k[3 + a] = max(k[3 + a], __shfl_xor_sync(0xffffffffu, k[3 + a], o));
+        }
+        k[6] += __shfl_xor_sync(0xffffffffu, k[6], o);
+    }
+    const int w = threadIdx.x / kWarp, l = threadIdx.x % kWarp;
+    if (l == 0)
+        for (int a = 0; a < 7; ++a) s[a][w] = k[a];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int j = 1; j < kBoundsThreads / kWarp; ++j) {
+            for (int a = 0; a < 3; ++a) {
+                k[a] = min(k[a], s[a][j]);
+                k[3 + a] = max(k[3 + a], s[3 + a][j]);
+            }
+            k[6] += s[6][j];
+        }
+        for (int a = 0; a < 3; ++a) {
+            atomicMin(&mm[a], k[a]);
+            atomicMax(&mm[3 + a], k[3 + a]);
+        }
+        if (k[6]) atomicAdd(&mm[6], k[6]);
+    }
+}
+
+__global__ void k_grid_record(uint32_t* __restrict__ mm, float support, uint64_t capacity,
+                              GridInfo* __restrict__ info) {
+    *info = grid_from_bounds(mm, support, capacity);
+    reset_bounds(mm);
+}
+
+// Cell pass: per particle the cell, the key and its rank among the particles
+// of its key (the histogram's atomic returns it; the order of equal keys is
+// arbitrary here and fixed by the segment sort).
+__global__ void k_cells_info(const float* __restrict__ xyz, uint64_t n, uint32_t stride,
+                             const GridInfo* __restrict__ info, uint32_t* __restrict__ cell,
+                             uint32_t* __restrict__ key, uint32_t* __restrict__ rank, uint32_t* __restrict__ count) {
+    if (info->status != kGridOk) return;
+    const uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const GridParams g = info->g;
+    uint32_t lin;
+    const uint32_t k = cell_key(xyz + i * stride, g, lin);
+    cell[i] = lin;
+    key[i] = k;
+    rank[i] = atomicAdd(&count[k], 1u);
 }
 
 // ---- exclusive scan (uint32), multi-level ---------------------------------
@@ -180,6 +362,32 @@ __global__ void k_scan_add(uint32_t* __restrict__ out, uint64_t n, const uint32_
     out[i] += tile_offsets[i / kScanTile];
 }
 
+// Second pass of a two-launch scan: the block adds the sum of all earlier
+// tiles' totals (read from tile_sums and reduced by the block itself: at most
+// kScanDirectTiles of them) to its 256 items, all inside one tile.
+constexpr uint64_t kScanDirectTiles = 2048;
+constexpr int kScanAddThreads = 256;
+static_assert(kScanTile % kScanAddThreads == 0, "an add block stays inside one tile");
+
+__global__ void __launch_bounds__(kScanAddThreads)
+    k_scan_add_sums(uint32_t* __restrict__ out, uint64_t n, const uint32_t* __restrict__ tile_sums) {
+    __shared__ uint32_t s_part[kScanAddThreads / kWarp];
+    const uint64_t i0 = (uint64_t)blockIdx.x * kScanAddThreads;
+    const uint32_t tile = (uint32_t)(i0 / kScanTile);
+    uint32_t part = 0;
+    for (uint32_t j = threadIdx.x; j < tile; j += kScanAddThreads) part += tile_sums[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+    const int w = threadIdx.x / kWarp, l = threadIdx.x % kWarp;
+    if (l == 0) s_part[w] = part;
+    __syncthreads();
+    uint32_t off = 0;
+#pragma unroll
+    for (int j = 0; j < kScanAddThreads / kWarp; ++j) off += s_part[j];
+    const uint64_t i = i0 + threadIdx.x;
+    if (i < n) out[i] += off;
+}
+
 // Words of temporary storage exclusive_scan needs for n items.
 uint64_t scan_tmp_words(uint64_t n) {
     uint64_t w = 0;
@@ -200,6 +408,11 @@ void exclusive_scan(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* tmp
     uint32_t* sums = tmp;
     uint32_t* offs = tmp + tiles + 32;
     k_scan_tile<<<(unsigned)tiles, kScanThreads, 0, st>>>(in, out, n, sums);
+    if (tiles <= kScanDirectTiles) {
+        k_scan_add_sums<<<(unsigned)((n + kScanAddThreads - 1) / kScanAddThreads), kScanAddThreads, 0, st>>>(out, n,
+                                                                                                            sums);
+        return;
+    }
     exclusive_scan(sums, offs, tiles, offs + tiles + 32, st);
     k_scan_add<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(out, n, offs);
 }
@@ -273,86 +486,106 @@ __global__ void k_radix_scatter(const uint32_t* __restrict__ keys_in, const uint
 }
 
 // ---- counting sort seeded by the key histogram ----------------------------
-// The key histogram k_cells counts, scanned, gives every key its segment
-// [sub[k], sub[k+1]).  k_scatter drops each particle's index into a free slot
-// of its segment (counts[k] counts down as slots are taken, so the order
-// inside a segment is arbitrary and counts ends at 0); k_segsort_gather then
-// sorts each segment by input index (a warp per segment), which restores
-// exactly the stable order (cell, sub-cell, input index), and gathers the
-// positions.  Segments longer than kShortSeg go to a list that k_long_segsort
-// sorts a block per segment.
-constexpr uint32_t kShortSeg = 32;
+// The key histogram the cell pass counts, scanned, gives every key its
+// segment [sub[k], sub[k+1]); the histogram's atomics gave every particle a
+// rank among the particles of its key.  k_scatter puts (input index, key) at
+// sub[k] + rank, so the order inside a segment is arbitrary; k_segsort_gather
+// then sorts each segment by input index (a thread per slot), which restores
+// exactly the stable order (cell, sub-cell, input index), gathers the
+// positions and zeroes the key counts for the next build.  Segments longer
+// than kShortSeg go to a list that k_long_segsort sorts a block per segment.
+constexpr uint32_t kShortSeg = 2 * kWarp;
 
-__global__ void k_scatter(const uint32_t* __restrict__ key, uint64_t n, const uint32_t* __restrict__ sub,
-                          uint32_t* __restrict__ counts, uint32_t* __restrict__ slots) {
+__global__ void k_scatter(const GridInfo* __restrict__ info, const uint32_t* __restrict__ key,
+                          const uint32_t* __restrict__ rank, uint64_t n, const uint32_t* __restrict__ sub,
+                          uint2* __restrict__ slots) {
+    if (info->status != kGridOk) return;
     uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
     if (i >= n) return;
     const uint32_t k = key[i];
-    const uint32_t left = atomicSub(&counts[k], 1u);  // 1 .. count
-    slots[sub[k] + left - 1u] = (uint32_t)i;
+    slots[sub[k] + rank[i]] = make_uint2((uint32_t)i, k);
 }
 
-// One warp per key: a short segment's indices are distinct, so lane l's rank in
-// the sorted segment is the number of the segment's indices below its own
-// (compared through shuffles); the lane writes its index and gathers its
-// position there.  A long segment goes to long_keys.
-__global__ void k_segsort_gather(const float* __restrict__ xyz, uint32_t stride, uint64_t nkeys,
-                                 const uint32_t* __restrict__ sub, const uint32_t* __restrict__ slots,
-                                 uint32_t* __restrict__ perm, float4* __restrict__ pts,
-                                 uint32_t* __restrict__ long_keys, uint32_t* __restrict__ n_long) {
-    const uint64_t k = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) / kWarp;
-    const uint32_t l = threadIdx.x % kWarp;
-    if (k >= nkeys) return;  // warp-uniform
-    const uint32_t b = __ldg(sub + k), m = __ldg(sub + k + 1) - b;
-    if (m == 0) return;
-    if (m > kShortSeg) {
-        if (l == 0) long_keys[atomicAdd(n_long, 1u)] = (uint32_t)k;
+// One thread per slot: the segment's indices are distinct, so an index's
+// rank in the sorted segment is the number of the segment's indices below it;
+// the thread counts them over its segment's slots (read through L1: the
+// neighbouring threads walk the same lines), writes its index there and
+// gathers its position.  The first slot of a segment zeroes the key's count
+// and, for a long segment, lists it for k_long_segsort; the other slots of a
+// long segment do nothing.
+__global__ void k_segsort_gather(GridInfo* __restrict__ info, const float* __restrict__ xyz, uint32_t stride,
+                                 uint64_t n, const uint32_t* __restrict__ sub, const uint2* __restrict__ slots,
+                                 uint32_t* __restrict__ counts, uint32_t* __restrict__ perm,
+                                 float4* __restrict__ pts, uint32_t* __restrict__ long_keys) {
+    if (info->status != kGridOk) return;
+    const uint64_t p = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+    const uint2 me = __ldg(slots + p);
+    const uint32_t v = me.x, k = me.y;
+    const uint32_t b = __ldg(sub + k), e = __ldg(sub + k + 1);
+    if (p == b) counts[k] = 0;
+    if (e - b > kShortSeg) {
+        if (p == b) long_keys[atomicAdd(&info->n_long, 1u)] = k;
         return;
     }
-    const uint32_t v = l < m ? slots[b + l] : 0xffffffffu;
-    uint32_t rank = 0;
-    for (uint32_t t = 0; t < m; ++t) rank += __shfl_sync(0xffffffffu, v, (int)t) < v ? 1u : 0u;
-    if (l < m) {
-        const float* p = xyz + (uint64_t)v * stride;
-        perm[b + rank] = v;
-        pts[b + rank] = make_float4(p[0], p[1], p[2], 0.0f);
-    }
+    const uint32_t* idx = reinterpret_cast<const uint32_t*>(slots);  // index of slot j at 2 j
+    uint32_t r = 0;
+#pragma unroll 4
+    for (uint32_t j = b; j < e; ++j) r += __ldg(idx + 2 * (uint64_t)j) < v ? 1u : 0u;
+    const float* q = xyz + (uint64_t)v * stride;
+    perm[b + r] = v;
+    pts[b + r] = make_float4(q[0], q[1], q[2], 0.0f);
 }
 
-// One block per long segment (grid-stride over the list): a stable LSD radix
-// sort of the segment's indices, 8 bits per pass, ping-ponging between the
-// segment's range of `slots` and of `tmp`, then the gather.  The indices are
-// distinct, so the sorted segment is unique.
+// One block per long segment (grid-stride over the list): the segment's
+// indices copied out of the slots, a stable LSD radix sort of them, 8 bits per
+// pass, ping-ponging between the segment's ranges of tmp0 and tmp1, then the
+// gather.  The indices are distinct, so the sorted segment is unique.
 constexpr int kLongThreads = 256;
 
 __global__ void __launch_bounds__(kLongThreads) k_long_segsort(const float* __restrict__ xyz, uint32_t stride,
                                                                const uint32_t* __restrict__ sub,
-                                                               uint32_t* __restrict__ slots, uint32_t* __restrict__ tmp,
+                                                               const uint2* __restrict__ slots,
+                                                               uint32_t* __restrict__ tmp0, uint32_t* __restrict__ tmp1,
                                                                const uint32_t* __restrict__ long_keys,
-                                                               const uint32_t* __restrict__ n_long, int passes,
+                                                               const GridInfo* __restrict__ info, int passes,
                                                                uint32_t* __restrict__ perm, float4* __restrict__ pts) {
     __shared__ uint32_t s_base[256];
     __shared__ uint32_t s_w[kLongThreads / kWarp][256];
     const int t = threadIdx.x, l = t % kWarp, w = t / kWarp;
     const uint32_t lt = (1u << l) - 1u;
-    const uint32_t nl = *n_long;
+    const uint32_t nl = info->status == kGridOk ? info->n_long : 0u;
     for (uint32_t e = blockIdx.x; e < nl; e += gridDim.x) {
         const uint32_t k = long_keys[e];
         const uint32_t b = sub[k], m = sub[k + 1] - b;
-        uint32_t* src = slots + b;
-        uint32_t* dst = tmp + b;
+        uint32_t* src = tmp0 + b;
+        uint32_t* dst = tmp1 + b;
+        for (uint32_t j = t; j < m; j += kLongThreads) src[j] = slots[b + j].x;
+        __syncthreads();
         for (int p = 0; p < passes; ++p) {
             const int shift = 8 * p;
             s_base[t] = 0;
             __syncthreads();
             for (uint32_t j = t; j < m; j += kLongThreads) atomicAdd(&s_base[(src[j] >> shift) & 255u], 1u);
             __syncthreads();
-            if (t == 0) {  // exclusive scan of the 256 digit counts
-                uint32_t run = 0;
-                for (int d = 0; d < 256; ++d) {
-                    const uint32_t c = s_base[d];
-                    s_base[d] = run;
-                    run += c;
+            if (w == 0) {  // exclusive scan of the 256 digit counts: 8 per lane, then across the warp
+                uint32_t c[8], sum = 0;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    c[j] = s_base[8 * l + j];
+                    sum += c[j];
+                }
+                uint32_t inc = sum;
+#pragma unroll
+                for (int o = 1; o < kWarp; o <<= 1) {
+                    const uint32_t x = __shfl_up_sync(0xffffffffu, inc, o);
+                    if (l >= o) inc += x;
+                }
+                uint32_t run = inc - sum;
+#pragma unroll
+                for (int j = 0; j < 8; ++j) {
+                    s_base[8 * l + j] = run;
+                    run += c[j];
                 }
             }
             __syncthreads();
@@ -674,95 +907,133 @@ void scan_exclusive(const uint32_t* in, uint32_t* out, uint64_t n, uint32_t* tmp
     exclusive_scan(in, out, n, tmp, st);
 }
 
-int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
+// Cell tables of a scene (sub-cell starts, bound table, reference-skip flags)
+// for at least ncells cells.
+static int grow_cell_tables(fm_ctx* ctx, fm_scene* s, uint64_t ncells) {
+    // a bound table build of an earlier march may still be running on the side stream
+    if (ctx->side) cudaStreamSynchronize(ctx->side);
+    cudaFree(s->d_sub);
+    cudaFree(s->d_bound);
+    cudaFree(s->d_flag);
+    s->d_sub = nullptr; s->d_bound = nullptr; s->d_flag = nullptr;
+    s->cell_capacity = 0;
+    if (cudaMalloc(&s->d_sub, (8 * ncells + 1) * sizeof(uint32_t)) != cudaSuccess ||
+        cudaMalloc(&s->d_bound, ncells * kBoundBoxes * sizeof(float)) != cudaSuccess ||
+        cudaMalloc(&s->d_flag, ncells) != cudaSuccess)
+        return set_err(ctx, FM_ERR_OOM, "cell table allocation failed");
+    s->cell_capacity = ncells;
+    return FM_OK;
+}
+
+// One build, launched for the scene's current cell capacity: the bounds pass
+// (which writes the grid and its status to info) and, when the scene has cell
+// tables, the cell keys, their scan, the counting scatter and the segment
+// sorts, every one of which does nothing unless the grid fits.  No host sync.
+static int launch_build(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride, GridInfo* info) {
     cudaStream_t st = ctx->stream;
     const uint64_t n = s->n;
-    // 1. AABB (exact min/max) -> host
-    if (!ensure_buf(ctx->scratch[0], 64)) return set_err(ctx, FM_ERR_OOM, "scratch allocation failed");
+    const uint64_t cap = s->cell_capacity;
     uint32_t* mm = (uint32_t*)ctx->scratch[0].p;
-    FM_CUDA(ctx, cudaMemsetAsync(mm, 0xff, 3 * sizeof(uint32_t), st));
-    FM_CUDA(ctx, cudaMemsetAsync(mm + 3, 0, 4 * sizeof(uint32_t), st));
-    {
-        unsigned blocks = (unsigned)std::min<uint64_t>((n + 255) / 256, (uint64_t)ctx->sm_count * 8);
-        k_aabb<<<std::max(1u, blocks), 256, 0, st>>>(d_xyz, n, stride, mm);
-        FM_CUDA(ctx, cudaGetLastError());
-    }
-    uint32_t* h = (uint32_t*)ctx->h_pinned_small;
-    FM_CUDA(ctx, cudaMemcpyAsync(h, mm, 7 * sizeof(uint32_t), cudaMemcpyDeviceToHost, st));
-    FM_CUDA(ctx, cudaStreamSynchronize(st));
-    if (h[6] != 0) return set_err(ctx, FM_ERR_INVALID, "particle positions contain non-finite values");
-    // 2. grid parameters, in the reference's FP32 order (Dataset.cpp:89-104)
-    const float H = s->support;
-    const float pad = 1.0f * H;
-    const float cell = 1.0f * H;
-    uint64_t ncells = 1;
-    for (int a = 0; a < 3; ++a) {
-        float mn = ord2f(h[a]), mx = ord2f(h[3 + a]);
-        s->max[a] = mx + pad;
-        s->min[a] = mn - pad;
-        float ext = s->max[a] - s->min[a];
-        float d = std::ceil(ext / cell);
-        if (!(d >= 1.0f && d < 1.0e6f)) return set_err(ctx, FM_ERR_INVALID, "grid extent / support radius out of range");
-        s->dims[a] = (int)d;
-        ncells *= (uint64_t)s->dims[a];
-    }
-    s->inv = 1.0f / cell;
-    if (ncells > (1ull << 28))
-        return set_err(ctx, FM_ERR_INVALID, "grid would exceed 2^28 cells: support radius too small for the extent");
-    s->ncells = ncells;
-    s->bound_valid = false;
-    s->flag_valid = false;
-    s->occ_valid = false;
-    const uint64_t nkeys = 8 * ncells;
-    if (ncells > s->cell_capacity) {
-        // a bound table build of an earlier march may still be running on the side stream
-        if (ctx->side) cudaStreamSynchronize(ctx->side);
-        cudaFree(s->d_sub);
-        cudaFree(s->d_bound);
-        cudaFree(s->d_flag);
-        s->d_sub = nullptr; s->d_bound = nullptr; s->d_flag = nullptr;
-        if (cudaMalloc(&s->d_sub, (nkeys + 1) * sizeof(uint32_t)) != cudaSuccess ||
-            cudaMalloc(&s->d_bound, ncells * kBoundBoxes * sizeof(float)) != cudaSuccess ||
-            cudaMalloc(&s->d_flag, ncells) != cudaSuccess) {
-            s->cell_capacity = 0;
-            return set_err(ctx, FM_ERR_OOM, "cell table allocation failed");
-        }
-        s->cell_capacity = ncells;
-    }
-    // 3. cells, keys, key histogram
-    GridParams gp;
-    for (int a = 0; a < 3; ++a) { gp.min[a] = s->min[a]; gp.dims[a] = s->dims[a]; }
-    gp.inv = s->inv;
-    if (!ensure_buf(ctx->scratch[1], (nkeys + 2) * sizeof(uint32_t)) ||  // key counts + long-segment count
-        !ensure_buf(ctx->scratch[2], n * sizeof(uint32_t)) ||            // slots
-        !ensure_buf(ctx->scratch[3], n * sizeof(uint32_t)) ||            // long-segment sort temporaries
-        !ensure_buf(ctx->scratch[4], n * sizeof(uint32_t)) ||            // long-segment keys
-        !ensure_buf(ctx->scratch[6], scan_tmp_words(nkeys + 1) * sizeof(uint32_t)) ||
-        !ensure_buf(ctx->scratch[7], n * sizeof(uint32_t)))              // keys (input order)
-        return set_err(ctx, FM_ERR_OOM, "grid build scratch allocation failed");
+    const bool vec3 = stride == 3 && ((uintptr_t)d_xyz & 15u) == 0;
+    const uint64_t items = vec3 ? (3 * n) / 4 : n;
+    uint64_t blocks = std::min<uint64_t>((items + kBoundsThreads - 1) / kBoundsThreads, (uint64_t)ctx->sm_count * 8);
+    if (vec3) blocks = (std::max<uint64_t>(blocks, 1) + 2) / 3 * 3;  // grid stride a multiple of 3 float4s
+    blocks = std::max<uint64_t>(blocks, 1);
+    if (vec3)
+        k_grid_bounds<true><<<(unsigned)blocks, kBoundsThreads, 0, st>>>(d_xyz, n, stride, mm);
+    else
+        k_grid_bounds<false><<<(unsigned)blocks, kBoundsThreads, 0, st>>>(d_xyz, n, stride, mm);
+    k_grid_record<<<1, 1, 0, st>>>(mm, s->support, cap, info);
+    FM_CUDA(ctx, cudaGetLastError());
+    if (cap == 0) return FM_OK;
+    const uint64_t nkeys = 8 * cap;
     uint32_t* counts = (uint32_t*)ctx->scratch[1].p;
-    uint32_t* n_long = counts + nkeys + 1;
-    uint32_t* slots = (uint32_t*)ctx->scratch[2].p;
+    uint2* slots = (uint2*)ctx->scratch[2].p;
+    uint32_t* rank = (uint32_t*)ctx->scratch[3].p;  // read by k_scatter, then reused as tmp0 below
     uint32_t* keys0 = (uint32_t*)ctx->scratch[7].p;
-    FM_CUDA(ctx, cudaMemsetAsync(counts, 0, (nkeys + 2) * sizeof(uint32_t), st));
     const unsigned pblocks = (unsigned)((n + 255) / 256);
-    k_cells<<<pblocks, 256, 0, st>>>(d_xyz, n, stride, gp, s->d_cell, keys0, counts);
+    k_cells_info<<<pblocks, 256, 0, st>>>(d_xyz, n, stride, info, s->d_cell, keys0, rank, counts);
     FM_CUDA(ctx, cudaGetLastError());
-    uint32_t* tmp = (uint32_t*)ctx->scratch[6].p;
-    exclusive_scan(counts, s->d_sub, nkeys + 1, tmp, st);
+    exclusive_scan(counts, s->d_sub, nkeys + 1, (uint32_t*)ctx->scratch[6].p, st);
     FM_CUDA(ctx, cudaGetLastError());
-    // 4. counting sort: scatter into the key segments, sort each by input index, gather
-    k_scatter<<<pblocks, 256, 0, st>>>(keys0, n, s->d_sub, counts, slots);
-    k_segsort_gather<<<(unsigned)((nkeys * kWarp + 255) / 256), 256, 0, st>>>(d_xyz, stride, nkeys, s->d_sub, slots,
-                                                                      s->d_perm, s->d_pts,
-                                                                      (uint32_t*)ctx->scratch[4].p, n_long);
+    k_scatter<<<pblocks, 256, 0, st>>>(info, keys0, rank, n, s->d_sub, slots);
+    k_segsort_gather<<<pblocks, 256, 0, st>>>(info, d_xyz, stride, n, s->d_sub, slots, counts, s->d_perm, s->d_pts,
+                                              (uint32_t*)ctx->scratch[4].p);
     int ibits = 1;
     while (ibits < 32 && ((n - 1) >> ibits)) ++ibits;
     k_long_segsort<<<(unsigned)ctx->sm_count, kLongThreads, 0, st>>>(
-        d_xyz, stride, s->d_sub, slots, (uint32_t*)ctx->scratch[3].p, (const uint32_t*)ctx->scratch[4].p, n_long,
+        d_xyz, stride, s->d_sub, slots, rank, (uint32_t*)ctx->scratch[5].p, (const uint32_t*)ctx->scratch[4].p, info,
         (ibits + 7) / 8, s->d_perm, s->d_pts);
     FM_CUDA(ctx, cudaGetLastError());
     return FM_OK;
+}
+
+// The grid build, one host sync at its end.  The whole chain is launched for
+// the cell capacity the scene already has; the bounds pass computes the grid
+// on the device and the later passes read it there.  When the grid needs more
+// cells than that (the first build of a scene, or a frame whose AABB grew) the
+// passes after the bounds pass do nothing, the host grows the cell tables to
+// the size the record reports and launches the chain again.
+int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
+    cudaStream_t st = ctx->stream;
+    const uint64_t n = s->n;
+    s->bound_valid = false;
+    s->flag_valid = false;
+    s->occ_valid = false;
+    if (!ensure_buf(ctx->scratch[2], n * sizeof(uint2)) ||     // slots: (input index, key)
+        !ensure_buf(ctx->scratch[3], n * sizeof(uint32_t)) ||  // ranks, then long-segment sort temporaries
+        !ensure_buf(ctx->scratch[4], n * sizeof(uint32_t)) ||  // long-segment keys
+        !ensure_buf(ctx->scratch[5], n * sizeof(uint32_t)) ||  // long-segment sort temporaries
+        !ensure_buf(ctx->scratch[7], n * sizeof(uint32_t)))    // keys (input order)
+        return set_err(ctx, FM_ERR_OOM, "grid build scratch allocation failed");
+    for (int attempt = 0; attempt < 2; ++attempt) {
+        const uint64_t nkeys = 8 * s->cell_capacity;
+        const size_t b0 = ctx->scratch[0].bytes, b1 = ctx->scratch[1].bytes;  // a reallocation grows them
+        if (!ensure_buf(ctx->scratch[0], 128) ||                          // bounds words + grid record
+            !ensure_buf(ctx->scratch[1], (nkeys + 2) * sizeof(uint32_t)) ||  // key counts
+            !ensure_buf(ctx->scratch[6], scan_tmp_words(nkeys + 1) * sizeof(uint32_t)))
+            return set_err(ctx, FM_ERR_OOM, "grid build scratch allocation failed");
+        uint32_t* mm = (uint32_t*)ctx->scratch[0].p;
+        GridInfo* info = (GridInfo*)(mm + 16);
+        if (ctx->grid_scratch_dirty || ctx->scratch[0].bytes != b0 || ctx->scratch[1].bytes != b1) {
+            ctx->grid_scratch_dirty = true;
+            FM_CUDA(ctx, cudaMemsetAsync(mm, 0xff, 3 * sizeof(uint32_t), st));
+            FM_CUDA(ctx, cudaMemsetAsync(mm + 3, 0, 4 * sizeof(uint32_t), st));
+            FM_CUDA(ctx, cudaMemsetAsync(ctx->scratch[1].p, 0, ctx->scratch[1].bytes, st));
+        }
+        // a build that stops between its launches and the sync below leaves the
+        // counts and bounds words to be set again
+        ctx->grid_scratch_dirty = true;
+        int rc = launch_build(ctx, s, d_xyz, stride, info);
+        if (rc != FM_OK) return rc;
+        GridInfo* h = (GridInfo*)ctx->h_pinned_small;
+        FM_CUDA(ctx, cudaMemcpyAsync(h, info, sizeof(GridInfo), cudaMemcpyDeviceToHost, st));
+        FM_CUDA(ctx, cudaStreamSynchronize(st));
+        // every pass has run: the segment sort zeroed the counts (or the cell
+        // pass did not touch them) and the bounds words are back to their start
+        ctx->grid_scratch_dirty = false;
+        const GridInfo gi = *h;
+        if (gi.status == kGridNonFinite)
+            return set_err(ctx, FM_ERR_INVALID, "particle positions contain non-finite values");
+        if (gi.status == kGridExtent)
+            return set_err(ctx, FM_ERR_INVALID, "grid extent / support radius out of range");
+        if (gi.status == kGridTooMany)
+            return set_err(ctx, FM_ERR_INVALID, "grid would exceed 2^28 cells: support radius too small for the extent");
+        if (gi.status == kGridOverCapacity) {
+            if ((rc = grow_cell_tables(ctx, s, gi.ncells)) != FM_OK) return rc;
+            continue;
+        }
+        if (gi.status != kGridOk) return set_err(ctx, FM_ERR_CUDA, "grid build returned an unknown status");
+        for (int a = 0; a < 3; ++a) {
+            s->min[a] = gi.g.min[a];
+            s->max[a] = gi.max[a];
+            s->dims[a] = gi.g.dims[a];
+        }
+        s->inv = gi.g.inv;
+        s->ncells = gi.ncells;
+        return FM_OK;
+    }
+    return set_err(ctx, FM_ERR_CUDA, "grid build: cell capacity still short after growing the tables");
 }
 
 // The bound table stores +inf for the boxes of a cell once all their sums

@@ -572,7 +572,7 @@ def run_files(args, fm, torch, ctx, sc):
 
 
 def run_grid(args, fm, torch, ctx, ext, sc, flush, peak):
-    """The uniform-grid build (AABB, cell keys, radix sort, start tables, sorted gather) of the bench frame
+    """The uniform-grid build (AABB and grid, cell keys, counting sort, start tables, sorted gather) of the bench frame
     and of a 4M-particle frame of the same layout, from positions in device memory, L2 flushed before each
     build; algorithmic bytes 64 B per particle + 16 B per cell."""
     from fluidmarch import scenes
@@ -604,9 +604,9 @@ def run_grid(args, fm, torch, ctx, ext, sc, flush, peak):
         res[name] = {"particles": g["n_particles"], "cells": g["n_cells"], "ms": ms, "algorithmic_bytes": alg,
                      "achieved_gbs": alg / ms / 1e6, "frac_of_hbm_peak": alg / ms / 1e6 / peak}
         del xyz_d
-    res["note"] = ("fm_scene_update from device positions: k_aabb, read-back of the bounds for the grid size, "
+    res["note"] = ("fm_scene_update from device positions: bounds pass that also computes the grid on the device, "
                    "cell keys and key histogram, its scan, counting scatter, per-sub-cell sort by input index "
-                   "with the gather; median of the builds, each after an L2 flush")
+                   "with the gather, one host sync at the end; median of the builds, each after an L2 flush")
     return res
 
 

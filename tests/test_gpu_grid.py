@@ -64,8 +64,17 @@ def test_grid_many_cells(fmlib, ctx):
     assert g["n_cells"] > (1 << 16)
 
 
+def test_grid_over_a_million_cells(fmlib, ctx):
+    """1.4M cells: 11.5M sub-cell keys, more scan tiles than one add pass sums directly (the scan
+    takes its recursive path)."""
+    rng = np.random.default_rng(13)
+    xyz = rng.uniform(0.0, 1.0, size=(200000, 3)).astype(np.float32)
+    g = check_grid(fmlib, ctx, xyz, 0.009)
+    assert 8 * g["n_cells"] + 1 > 2048 * 4096
+
+
 def test_grid_segment_lengths(fmlib, ctx):
-    """Sub-cells holding 1 .. 32 particles (sorted by one thread), 33 .. 4,000 and 60,000 (sorted by a
+    """Sub-cells holding 1 .. 64 particles (sorted by one warp), 257, 4,000 and 60,000 (sorted by a
     block, radix passes over the input indices), in scrambled input order."""
     rng = np.random.default_rng(4)
     parts = [rng.uniform(0.0, 2.0, (20000, 3))]
@@ -76,7 +85,7 @@ def test_grid_segment_lengths(fmlib, ctx):
     rng.shuffle(xyz)
     fr = O.build_frame(xyz, 0.1)
     seg = np.diff(fr.sub_start)
-    assert seg.max() >= 60000 and np.sum((seg > 32) & (seg < 60000)) >= 4
+    assert seg.max() >= 60000 and np.sum((seg > 64) & (seg < 60000)) >= 2 and np.sum((seg > 32) & (seg <= 64)) >= 2
     check_grid(fmlib, ctx, xyz, 0.1)
 
 
@@ -88,6 +97,71 @@ def test_scene_update_rebuilds(fmlib, ctx):
     fr = O.build_frame(b.xyz, a.support)
     d = sc.download()
     assert np.array_equal(d["perm"], fr.perm) and np.array_equal(d["start"], fr.start)
+
+
+def _check_scene(sc, xyz, H):
+    fr = O.build_frame(xyz, H)
+    g = sc.grid()
+    assert g["dims"] == fr.dims and g["n_cells"] == int(np.prod(fr.dims))
+    assert np.array_equal(g["min"].view(np.uint32), np.array(fr.grid.min[:], np.float32).view(np.uint32))
+    assert np.array_equal(g["max"].view(np.uint32), np.array(fr.grid.max[:], np.float32).view(np.uint32))
+    d = sc.download()
+    assert np.array_equal(d["cell"], fr.cells)
+    assert np.array_equal(d["perm"], fr.perm)
+    assert np.array_equal(d["start"], fr.start)
+    assert np.array_equal(d["sorted"].view(np.uint32), fr.sorted.view(np.uint32))
+
+
+def test_scene_update_grow_shrink_and_failed_update(fmlib, ctx):
+    """One scene through updates whose grids need more cells than its tables hold (the build grows
+    them and runs again), fewer cells (the larger tables are reused), a rejected update (an infinite
+    coordinate) and valid updates after it, plus a second scene of the same context in between:
+    every build bit-exact to the oracle."""
+    rng = np.random.default_rng(11)
+    H = 0.05
+    small = rng.uniform(0.0, 0.5, (30000, 3)).astype(np.float32)  # the scene's particle capacity
+    big = rng.uniform(-0.5, 1.5, (30000, 3)).astype(np.float32)
+    mid = rng.uniform(0.2, 1.0, (25000, 3)).astype(np.float32)
+    sc = fmlib.Scene(ctx, small, H)
+    _check_scene(sc, small, H)
+    sc.update(big)  # more cells than the first build allocated
+    _check_scene(sc, big, H)
+    sc.update(mid)  # fewer cells
+    _check_scene(sc, mid, H)
+    bad = mid.copy()
+    bad[123, 2] = np.inf
+    with pytest.raises(fmlib.FmError) as e:
+        sc.update(bad)
+    assert e.value.code == fmlib.FM_ERR_INVALID
+    other = fmlib.Scene(ctx, big[:7000], 0.02)  # another scene on the same scratch
+    _check_scene(other, big[:7000], 0.02)
+    other.close()
+    sc.update(small)
+    _check_scene(sc, small, H)
+    sc.update(big[:29999])  # 3n not a multiple of 4: the float4 pass's tail
+    _check_scene(sc, big[:29999], H)
+    sc.close()
+
+
+def test_scene_update_unaligned_device_positions(fmlib, ctx):
+    """Device positions at an address that is not 16-byte aligned (one-float offset) take the
+    scalar bounds pass; the same positions aligned take the float4 pass; both bit-exact."""
+    torch = pytest.importorskip("torch")
+    sc0 = scenes.small_scene(seed=12, n=9000)
+    xyz = np.ascontiguousarray(sc0.xyz)
+    n = xyz.shape[0]
+    flat = torch.zeros(3 * n + 4, dtype=torch.float32, device="cuda")
+    flat[1:1 + 3 * n] = torch.from_numpy(xyz.reshape(-1)).cuda()
+    off = flat[1:1 + 3 * n].view(n, 3)
+    assert off.data_ptr() % 16 == 4
+    s = fmlib.Scene(ctx, off, sc0.support)
+    _check_scene(s, xyz, sc0.support)
+    al = torch.from_numpy(xyz).cuda()
+    s.update(al)
+    _check_scene(s, xyz, sc0.support)
+    s.update(off)
+    _check_scene(s, xyz, sc0.support)
+    s.close()
 
 
 def test_scene_from_device_memory(fmlib, ctx):
