@@ -236,8 +236,8 @@ int fm_scene_download(const fm_scene* scene, uint32_t* cell, uint32_t* sorted_in
  * calls: calls that overlap on the GPU race and must be serialised.  The
  * first call in a CUDA context looks up that array's address in the context
  * (a driver-API context of the host application works as well as the
- * device's primary context); make that first call before any stream
- * capture.  Each call synchronises `stream` once (to read the bounding box);
+ * device's primary context).  Each call synchronises `stream` once (to read
+ * the bounding box);
  * the rest is enqueued asynchronously.  Returns FM_OK, FM_ERR_INVALID or
  * FM_ERR_CUDA; there is no context and no message. */
 int fm_grid_build_noalloc(const float* xyz, uint64_t n, uint32_t stride, float support_radius, float* sorted_xyzw,
