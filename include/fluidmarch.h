@@ -299,7 +299,8 @@ typedef struct fm_tile_config {
     int32_t tiles_per_claim; /* tiles a warp takes at a time: 1..16 */
     int32_t defer_iters;     /* density sums a warp runs for one tile before the
                                 rays it still has go to the long-ray pass: 1..4096;
-                                0 = 15 */
+                                0 = 12 on a scene's refined exact-skip table (its
+                                second and later marches), else 15 */
     int32_t long_queue;      /* entries of the long-ray queue; 0 = pixels / 4 + 65536.
                                 Rays that find it full stay with their warp. */
     int32_t defer_lanes;     /* a warp also defers its rays once at most this many are
