@@ -214,7 +214,12 @@ int prepare(fm_batch* b) {
         o.depth = v.out.depth;
         o.col = (float4*)v.out.colour;
         o.start_depth = z;
-        MarchArgs a = march_view_args(v.scene, &v.camera, &v.params, o, b->cfg);
+        // a batch's long pass takes the deferred rays of every view: by default
+        // deferral after 15 sums (the 128-view 4K batch of 4M-particle scenes:
+        // 3.06 s per launch against 3.52 s after 12, the single-view default)
+        TileConfig vc = b->cfg;
+        if (vc.cap == 0) vc.cap = 15;
+        MarchArgs a = march_view_args(v.scene, &v.camera, &v.params, o, vc);
         a.tile_counter = cnt;
         a.q_tail = cnt + 1;
         a.q_head = cnt + 2;

@@ -138,12 +138,12 @@ __device__ __forceinline__ void for_packed_warp(const GridDev& g, const Loc& L, 
             if (y < 0 || y >= Hd) continue;
             const float dy2 = slab_d2(L.u[1], -1.0f + 0.5f * (float)(2 * dy + ((sb >> 1) & 1)));
             const bool reach = lane_ok && (dx2 + dy2 + dz2 < T);
-            if (!__any_sync(kFull, reach)) continue;
             const uint32_t row = ((uint32_t)z * (uint32_t)Hd + (uint32_t)y) * (uint32_t)W;
-            if (STATS && cnt) {
+            if (STATS && cnt) {  // every row of the 27 cells, reached or not: the reference's candidates
                 const int x0 = max(L.c[0] - 1, 0), x1 = min(L.c[0] + 1, W - 1);
                 if (x0 <= x1) acc.cand += __ldg(g.sub + 8u * (row + (uint32_t)x1) + 8u) - __ldg(g.sub + 8u * (row + (uint32_t)x0));
             }
+            if (!__any_sync(kFull, reach)) continue;
             // base wraps below 0 when row + cx == 0 (then lanes 0-7 are out of the grid);
             // indices are formed in uint32 and loads past the table are never made
             const uint32_t base = 8u * (row + (uint32_t)L.c[0]) - 8u;

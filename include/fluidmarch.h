@@ -237,9 +237,8 @@ int fm_scene_download(const fm_scene* scene, uint32_t* cell, uint32_t* sorted_in
  * first call in a CUDA context looks up that array's address in the context
  * (a driver-API context of the host application works as well as the
  * device's primary context).  Each call synchronises `stream` once (to read
- * the bounding box);
- * the rest is enqueued asynchronously.  Returns FM_OK, FM_ERR_INVALID or
- * FM_ERR_CUDA; there is no context and no message. */
+ * the bounding box); the rest is enqueued asynchronously.  Returns FM_OK,
+ * FM_ERR_INVALID or FM_ERR_CUDA; there is no context and no message. */
 int fm_grid_build_noalloc(const float* xyz, uint64_t n, uint32_t stride, float support_radius, float* sorted_xyzw,
                           uint32_t* cell, uint32_t* sorted_index, uint32_t* sub_start, uint64_t sub_start_capacity,
                           fm_grid_info* info, void* stream);
@@ -299,8 +298,9 @@ typedef struct fm_tile_config {
     int32_t tiles_per_claim; /* tiles a warp takes at a time: 1..16 */
     int32_t defer_iters;     /* density sums a warp runs for one tile before the
                                 rays it still has go to the long-ray pass: 1..4096;
-                                0 = 12 on a scene's refined exact-skip table (its
-                                second and later marches), else 15 */
+                                0 = 12 for fm_march on a scene's refined exact-skip
+                                table (its second and later marches), else 15
+                                (batches: 15) */
     int32_t long_queue;      /* entries of the long-ray queue; 0 = pixels / 4 + 65536.
                                 Rays that find it full stay with their warp. */
     int32_t defer_lanes;     /* a warp also defers its rays once at most this many are
