@@ -925,9 +925,9 @@ static int grow_cell_tables(fm_ctx* ctx, fm_scene* s, uint64_t ncells) {
     return FM_OK;
 }
 
-// One build, launched for the scene's current cell capacity: the bounds pass
-// (which writes the grid and its status to info) and, when the scene has cell
-// tables, the cell keys, their scan, the counting scatter and the segment
+// One build, launched for the scene's current cell capacity: the bounds pass,
+// the record pass (the grid and its status into info) and, when the scene has
+// cell tables, the cell keys, their scan, the counting scatter and the segment
 // sorts, every one of which does nothing unless the grid fits.  No host sync.
 static int launch_build(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride, GridInfo* info) {
     cudaStream_t st = ctx->stream;
@@ -969,11 +969,11 @@ static int launch_build(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t s
 }
 
 // The grid build, one host sync at its end.  The whole chain is launched for
-// the cell capacity the scene already has; the bounds pass computes the grid
-// on the device and the later passes read it there.  When the grid needs more
-// cells than that (the first build of a scene, or a frame whose AABB grew) the
-// passes after the bounds pass do nothing, the host grows the cell tables to
-// the size the record reports and launches the chain again.
+// the cell capacity the scene already has; the record pass computes the grid
+// from the bounds on the device and the later passes read it there.  When the
+// grid needs more cells than that (the first build of a scene, or a frame
+// whose AABB grew) the passes after the record pass do nothing, the host grows
+// the cell tables to the size the record reports and launches the chain again.
 int build_grid(fm_ctx* ctx, fm_scene* s, const float* d_xyz, uint32_t stride) {
     cudaStream_t st = ctx->stream;
     const uint64_t n = s->n;

@@ -604,9 +604,10 @@ def run_grid(args, fm, torch, ctx, ext, sc, flush, peak):
         res[name] = {"particles": g["n_particles"], "cells": g["n_cells"], "ms": ms, "algorithmic_bytes": alg,
                      "achieved_gbs": alg / ms / 1e6, "frac_of_hbm_peak": alg / ms / 1e6 / peak}
         del xyz_d
-    res["note"] = ("fm_scene_update from device positions: bounds pass that also computes the grid on the device, "
-                   "cell keys and key histogram, its scan, counting scatter, per-sub-cell sort by input index "
-                   "with the gather, one host sync at the end; median of the builds, each after an L2 flush")
+    res["note"] = ("fm_scene_update from device positions: bounds pass, a one-thread pass that computes the grid "
+                   "on the device, cell keys and key histogram with ranks, its scan, scatter, per-sub-cell sort "
+                   "by input index with the gather, one host sync at the end; median of the builds, each after "
+                   "an L2 flush")
     return res
 
 
