@@ -798,12 +798,23 @@ __device__ __forceinline__ float union_density(const MarchArgs& a, bool mine, co
                 if (d3 < k.h2) rho = rho + w_in(k, d3);
             }
         }
-        for (; j < e_; ++j) {
-            const float4 q = __ldg(a.g.pts + j);
+        if (j < e_) {
+            // the last 1-3 particles in one round: their loads issue together
+            // (the count is the same on every lane), the sums keep their order
+            const uint32_t r = e_ - j;
+            const float4 q0 = __ldg(a.g.pts + j);
+            const float4 q1 = r > 1u ? __ldg(a.g.pts + j + 1) : q0;
+            const float4 q2 = r > 2u ? __ldg(a.g.pts + j + 2) : q0;
             if (pred) {
-                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-                const float d = dot3(rx, ry, rz, rx, ry, rz);
-                if (d < k.h2) rho = rho + w_in(k, d);
+                const float r0x = q0.x - px, r0y = q0.y - py, r0z = q0.z - pz;
+                const float r1x = q1.x - px, r1y = q1.y - py, r1z = q1.z - pz;
+                const float r2x = q2.x - px, r2y = q2.y - py, r2z = q2.z - pz;
+                const float d0 = dot3(r0x, r0y, r0z, r0x, r0y, r0z);
+                const float d1 = dot3(r1x, r1y, r1z, r1x, r1y, r1z);
+                const float d2 = dot3(r2x, r2y, r2z, r2x, r2y, r2z);
+                if (d0 < k.h2) rho = rho + w_in(k, d0);
+                if (r > 1u && d1 < k.h2) rho = rho + w_in(k, d1);
+                if (r > 2u && d2 < k.h2) rho = rho + w_in(k, d2);
             }
         }
     });
