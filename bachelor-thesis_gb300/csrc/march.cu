@@ -828,13 +828,33 @@ __device__ __forceinline__ void union_grad(const MarchArgs& a, bool mine, const 
     const float px = e[0], py = e[1], pz = e[2];
     const KernelDev& k = a.k;
     gx = gy = gz = 0.0f;
+    // a particle's term when it lies within the support (and not at p), added in order
+    auto term = [&](const float4& q) {
+        const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
+        const float q2 = dot3(rx, ry, rz, rx, ry, rz);
+        if (q2 < k.h2 && q2 > 0.0f) gradw_acc(k, rx, ry, rz, q2, gx, gy, gz);
+    };
     union_stream<STATS>(a.g, mine, L, a.cull, acc, [&](bool pred, uint32_t b, uint32_t e_) {
-        for (uint32_t j = b; j < e_; ++j) {
-            const float4 q = __ldg(a.g.pts + j);
+        uint32_t j = b;
+        for (; j + 4 <= e_; j += 4) {  // four loads issued together
+            const float4 q0 = __ldg(a.g.pts + j), q1 = __ldg(a.g.pts + j + 1);
+            const float4 q2 = __ldg(a.g.pts + j + 2), q3 = __ldg(a.g.pts + j + 3);
             if (pred) {
-                const float rx = q.x - px, ry = q.y - py, rz = q.z - pz;
-                const float q2 = dot3(rx, ry, rz, rx, ry, rz);
-                if (q2 < k.h2 && q2 > 0.0f) gradw_acc(k, rx, ry, rz, q2, gx, gy, gz);
+                term(q0);
+                term(q1);
+                term(q2);
+                term(q3);
+            }
+        }
+        if (j < e_) {  // the last 1-3 (the count is the same on every lane)
+            const uint32_t r = e_ - j;
+            const float4 q0 = __ldg(a.g.pts + j);
+            const float4 q1 = r > 1u ? __ldg(a.g.pts + j + 1) : q0;
+            const float4 q2 = r > 2u ? __ldg(a.g.pts + j + 2) : q0;
+            if (pred) {
+                term(q0);
+                if (r > 1u) term(q1);
+                if (r > 2u) term(q2);
             }
         }
     });
