@@ -537,12 +537,6 @@ int fm_march(fm_ctx* ctx, const fm_scene* s, const fm_camera* cam, const fm_marc
     }
     o.start_depth = z;
     o.ivl = nullptr;
-    if (p->skip_mode == FM_SKIP_EXACT) {
-        // the table is built (on st, or on the side stream joined into st): one
-        // read a second time gets its shell boxes refined first
-        if (sm->bound_uses > 0 && (rc = refine_bound(ctx, sm, st)) != FM_OK) return rc;
-        sm->bound_uses++;
-    }
     if (p->flags & FM_MARCH_PROPOSAL) {
         if (p->skip_mode == FM_SKIP_REFERENCE)
             return set_err(ctx, FM_ERR_INVALID, "FM_MARCH_PROPOSAL marches the plain sample lattice: skip mode must be off or exact");

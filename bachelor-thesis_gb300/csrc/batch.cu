@@ -128,12 +128,6 @@ int prepare(fm_batch* b) {
         if (!rc && (v.params.flags & FM_MARCH_PROPOSAL)) rc = ensure_occupancy(ctx, s, ctx->stream);
         if (rc) return rc;
     }
-    // a batch is run many times: the scenes' tables get their refined shell boxes
-    for (const fm_view& v : b->views) {
-        if (v.params.skip_mode != FM_SKIP_EXACT) continue;
-        const int rc = refine_bound(ctx, const_cast<fm_scene*>(v.scene), ctx->stream);
-        if (rc) return rc;
-    }
     FM_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
     // prefix sums
     std::vector<uint64_t> px(n + 1, 0), smp(n + 1, 0), pn(n + 1, 0);

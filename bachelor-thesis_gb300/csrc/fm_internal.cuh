@@ -278,8 +278,7 @@ struct fm_scene {
     uint32_t* d_sub = nullptr;     // 8 * ncells + 1 sub-cell starts
     float* d_bound = nullptr;      // exact-skip bound table, 8x8x8 boxes per cell (lazy)
     fm::DevBuf coarse;             // its 4x4x4 first level (64 bounds per cell)
-    bool bound_fine = false;       // the shell boxes are refined (a second march of the same build)
-    uint32_t bound_uses = 0;       // marches that read the table since it was built
+    bool bound_fine = false;       // the shell boxes are refined (ensure_bound refines right after the first level)
     uint8_t* d_flag = nullptr;     // per-cell reference flag (lazy)
     bool bound_valid = false;      // built by the first exact-skip march after a build
     float bound_iso = 0.0f;        // the bound table holds +inf for boxes whose sum reached it

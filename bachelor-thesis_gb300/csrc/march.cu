@@ -1368,9 +1368,9 @@ MarchArgs march_view_args(const fm_scene* s, const fm_camera* cam, const fm_marc
     a.claim = cfg.claim;
     // measured optima at 1080p: 12 sums when the march reads the refined
     // (eighth-cell) bound table (7.51 ms against 8.23 ms at 15; the 640x480
-    // dam break 1.89 against 2.07 ms), 15 on the first level alone, which
-    // leaves more rays with long runs of sums (12 would defer 162k rays:
-    // 11.0 ms against 9.9 ms for the frame) and without the exact skip
+    // dam break 1.89 against 2.07 ms), 15 without the exact skip and on a
+    // first level alone, which leaves more rays with long runs of sums (12
+    // would defer 162k rays: 11.0 ms against 9.9 ms for the frame)
     a.cap = cfg.cap > 0 ? cfg.cap : ((p->skip_mode == FM_SKIP_EXACT && s->bound_fine) ? 12 : 15);
     a.defer_lanes = cfg.lanes;
     a.cap2 = cfg.cap2;

@@ -60,8 +60,8 @@ extern "C" {
 #define FM_SKIP_EXACT 1      /* skip samples whose bound box (an eighth of a cell per axis) has
                                 a density upper bound below iso; same results as FM_SKIP_OFF.
                                 The scene's bound table is built by its first such march
-                                (boxes of a quarter cell), refined where it lies near the iso
-                                surface by the second, and serves marches at that iso or a
+                                (boxes of a quarter cell, then those near the iso surface
+                                refined into eighths) and serves marches at that iso or a
                                 lower one; a march at a higher iso builds it again. */
 #define FM_SKIP_REFERENCE 2  /* the reference's skip: flag = own-cell count * W0 > 1, jump to the
                                 cell's exit plus one step (RayMarcher.cpp:281-306) */
@@ -298,8 +298,7 @@ typedef struct fm_tile_config {
     int32_t tiles_per_claim; /* tiles a warp takes at a time: 1..16 */
     int32_t defer_iters;     /* density sums a warp runs for one tile before the
                                 rays it still has go to the long-ray pass: 1..4096;
-                                0 = 12 for fm_march on a scene's refined exact-skip
-                                table (its second and later marches), else 15
+                                0 = 12 for fm_march with the exact skip, else 15
                                 (batches: 15) */
     int32_t long_queue;      /* entries of the long-ray queue; 0 = pixels / 4 + 65536.
                                 Rays that find it full stay with their warp. */

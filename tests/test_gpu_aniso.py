@@ -66,7 +66,7 @@ def test_aniso_march_vs_oracle(fmlib, ctx, n, w, h, bisect, skip):
 def test_aniso_exact_skip_equals_no_skip(fmlib, ctx, bisect):
     """FM_SKIP_EXACT steps over samples whose bound box has no particle within the support radius
     (anisotropic density exactly 0): every output equals the march without skipping, bit for bit,
-    when the march builds the bound table and when it refines it."""
+    when the march builds the bound table (both levels) and when a later march reuses it."""
     sc = scenes.small_scene(seed=8, n=12000, width=72, height=54, max_steps=160)
     cam = sc.cameras[0]
     fr = O.build_frame(sc.xyz, sc.support)
@@ -80,7 +80,7 @@ def test_aniso_exact_skip_equals_no_skip(fmlib, ctx, bisect):
     try:
         first = fmlib.render(s, cam, p)  # the scene's first exact march builds the table
         st_1 = ctx.stats()
-        again = fmlib.render(s, cam, p)  # the next one refines it (more boxes proven empty)
+        again = fmlib.render(s, cam, p)  # the next one reuses it
         st_2 = ctx.stats()
     finally:
         ctx.set_stats(False)
@@ -88,7 +88,7 @@ def test_aniso_exact_skip_equals_no_skip(fmlib, ctx, bisect):
         for k in ("position", "normal", "depth", "colour"):
             assert np.array_equal(got[k].view(np.uint32), off[k].view(np.uint32)), k
     assert (off["depth"] > 0).sum() > 200
-    assert st_1["skipped"] > 0 and st_2["skipped"] >= st_1["skipped"]
+    assert st_1["skipped"] > 0 and st_2["skipped"] == st_1["skipped"]
     s.close()
 
 

@@ -322,18 +322,22 @@ def test_density_probe_bitwise(fmlib, ctx):
 
 
 def test_bound_table_on_reuse(fmlib, ctx):
-    """The scene's first exact-skip march builds the bound table's 4x4x4 level, the second refines its
-    shell boxes into eighths and skips more samples, the third reuses the refined table: the oracle's
-    bits every time."""
+    """The scene's first exact-skip march builds both levels of the bound table (4x4x4 boxes, then the
+    shell boxes refined into eighths); later marches of the same build reuse it: the oracle's bits
+    every time, the same samples skipped and evaluated every time, and fewer evaluations than with the
+    skip off."""
     sc = scenes.small_scene(seed=23, n=20000, width=128, height=96)
     cam = sc.cameras[0]
     s = fmlib.Scene(ctx, sc.xyz, sc.support)
     p = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_EXACT)
+    p_off = fmlib.MarchParams(sc.iso, sc.step, sc.max_steps, 8, fmlib.FM_SKIP_OFF)
     ctx.set_stats(True)
     try:
         runs = []
         for _ in range(3):
             runs.append((fmlib.render(s, cam, p), ctx.stats()))
+        fmlib.render(s, cam, p_off)
+        st_off = ctx.stats()
     finally:
         ctx.set_stats(False)
     fr = O.build_frame(sc.xyz, sc.support)
@@ -342,9 +346,8 @@ def test_bound_table_on_reuse(fmlib, ctx):
         for k in ("position", "normal", "depth", "colour"):
             assert np.array_equal(bits(g[k]), bits(o[k])), k
     (_, st1), (_, st2), (_, st3) = runs
-    assert st1["skipped"] > 0
-    assert st2["skipped"] > st1["skipped"] and st2["evals"] < st1["evals"]
-    assert (st3["skipped"], st3["evals"]) == (st2["skipped"], st2["evals"])
+    assert st1["skipped"] > 0 and st1["evals"] < st_off["evals"]
+    assert (st1["skipped"], st1["evals"]) == (st2["skipped"], st2["evals"]) == (st3["skipped"], st3["evals"])
     s.close()
 
 
