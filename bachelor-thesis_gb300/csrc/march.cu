@@ -1878,7 +1878,7 @@ __global__ void __launch_bounds__(kThreads)
         unsigned k = 0;
         if (lane == 0) k = atomicAdd(a.tile_counter, 1u);
         k = __shfl_sync(kFull, k, 0);
-        if (BATCH) {
+        if constexpr (BATCH) {
             if (k >= nchunks) break;
             const int v = find_view(pfx, nviews, k);
             aniso_chunk<STATS>(views[v], aviews[v], (uint64_t)(k - __ldg(pfx + v)) * 32u, lane, c);
