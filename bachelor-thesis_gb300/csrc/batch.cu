@@ -209,10 +209,12 @@ int prepare(fm_batch* b) {
         o.col = (float4*)v.out.colour;
         o.start_depth = z;
         // a batch's long pass takes the deferred rays of every view: by default
-        // deferral after 15 sums (the 128-view 4K batch of 4M-particle scenes:
-        // 3.06 s per launch against 3.52 s after 12, the single-view default)
+        // deferral after 24 sums (the 128-view 4K batch of 4M-particle scenes,
+        // ms per launch: 3516 after 12 sums, the single-view default; 3029
+        // after 15, 2917 after 20, 2893 after 24, 2879 after 32; the 146-view
+        // batch's autotune picks 20-24)
         TileConfig vc = b->cfg;
-        if (vc.cap == 0) vc.cap = 15;
+        if (vc.cap == 0) vc.cap = 24;
         MarchArgs a = march_view_args(v.scene, &v.camera, &v.params, o, vc);
         a.tile_counter = cnt;
         a.q_tail = cnt + 1;

@@ -630,7 +630,7 @@ def run_batch(args, fm, torch, ctx, ext, dev):
             keep.append(o)
             views.append(fm.View(s, cam, p, **o))
     torch.cuda.synchronize()
-    b = fm.Batch(ctx, views)  # the context's work split (8x4 tiles, deferral after 15 sums in a batch)
+    b = fm.Batch(ctx, views)  # the context's work split (8x4 tiles, deferral after 24 sums in a batch)
     tuned = None
     if not args.no_autotune:
         # the batch's own autotuner picks tile shape, tiles per claim and deferral

@@ -299,7 +299,7 @@ typedef struct fm_tile_config {
     int32_t defer_iters;     /* density sums a warp runs for one tile before the
                                 rays it still has go to the long-ray pass: 1..4096;
                                 0 = 12 for fm_march with the exact skip, else 15
-                                (batches: 15) */
+                                (batches: 24) */
     int32_t long_queue;      /* entries of the long-ray queue; 0 = pixels / 4 + 65536.
                                 Rays that find it full stay with their warp. */
     int32_t defer_lanes;     /* a warp also defers its rays once at most this many are
