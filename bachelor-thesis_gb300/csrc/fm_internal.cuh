@@ -341,7 +341,7 @@ struct SplatBatch {
 };
 SplatArgs splat_args(const fm_scene* s, const fm_camera* cam);
 constexpr int kSplatHizTile = 8;
-constexpr uint64_t kSplatSample = 16;
+constexpr uint64_t kSplatSample = 24;
 int launch_splat_batch(fm_ctx* ctx, const SplatBatch& b, cudaStream_t st);
 
 // March (march.cu): all pointers device pointers.

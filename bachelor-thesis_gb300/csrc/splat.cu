@@ -17,7 +17,7 @@
 // at a time.  Three passes keep the work near the visible surface without
 // changing the result (the buffer is a minimum, so leaving out a particle that
 // cannot lower any pixel is exact):
-//   1. every 16th particle (in cell order) is splatted: the discs, about five
+//   1. every 24th particle (in cell order) is splatted: the discs, about five
 //      particle spacings wide, already form a nearly opaque cover of the front
 //      surface;
 //   2. a max-depth tile level (8x8 pixels) is built from the buffer, and every
