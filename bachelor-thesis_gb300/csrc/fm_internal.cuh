@@ -184,7 +184,7 @@ struct DevBuf {
 struct TileConfig {
     int tw_log2 = 3;  // 8x4 pixels
     int claim = 1;
-    int cap = 0;          // shared-stream sums before deferral; 0: 12 on a refined bound table (single views), else 15
+    int cap = 0;          // shared-stream sums before deferral; 0: 12 (single view, exact skip), 15, 24 (batches)
     int lanes = 2;        // a warp defers its rays once at most this many are active
     int cap2 = 0;         // iterations of the regrouped second pass (0: no second pass)
     uint32_t qlimit = 0;  // long-ray queue entries (0: long_queue_entries of the pixels)
